@@ -1,0 +1,64 @@
+"""ctypes binding of libbola_gb300.so (declared in include/bola_gb300.h).
+
+The library is loaded from bola_gb300/lib/ only; a missing library is an
+error, never a silent fallback.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libbola_gb300.so")
+
+_d = ctypes.c_double
+_i64 = ctypes.c_int64
+_i32 = ctypes.c_int32
+_c = ctypes.c_char
+_p = ctypes.c_void_p
+_int = ctypes.c_int
+
+# name -> (restype, argtypes); mirrors include/bola_gb300.h
+SIGNATURES = {
+    "bola_version": (ctypes.c_char_p, []),
+    "bola_last_error": (ctypes.c_char_p, []),
+    "bola_set_simd_lanes": (_int, [_int]),
+    "bola_get_simd_lanes": (_int, []),
+    "bola_idamax": (_int, [_i64, _p, _p, _p]),
+    "bola_dscal": (_int, [_i64, _d, _p, _i64, _p]),
+    "bola_dger": (_int, [_i64, _i64, _d, _p, _p, _i64, _p, _i64, _p]),
+    "bola_ddot": (_int, [_i64, _p, _i64, _p, _i64, _p, _p]),
+    "bola_daxpy": (_int, [_i64, _d, _p, _i64, _p, _i64, _p]),
+    "bola_dlaswp": (_int, [_i64, _p, _i64, _i32, _i32, _p, _i32, _p]),
+    "bola_dgemm": (_int, [_c, _c, _i64, _i64, _i64, _d, _p, _i64, _p, _i64, _d, _p, _i64, _p]),
+    "bola_dtrsm": (_int, [_c, _c, _c, _c, _i64, _i64, _d, _p, _i64, _p, _i64, _p]),
+    "bola_dsyrk": (_int, [_c, _c, _i64, _i64, _d, _p, _i64, _d, _p, _i64, _p]),
+    "bola_dgetrf": (_int, [_i64, _i64, _p, _i64, _p, _p, _p]),
+    "bola_dgetrf2": (_int, [_i64, _i64, _p, _i64, _p, _p, _p]),
+    "bola_dpotrf": (_int, [_c, _i64, _p, _i64, _p, _p]),
+    "bola_dpotrf2": (_int, [_c, _i64, _p, _i64, _p, _p]),
+    "bola_dgetrs": (_int, [_i64, _i64, _p, _i64, _p, _p, _i64, _p]),
+    "bola_dpotrs": (_int, [_c, _i64, _i64, _p, _i64, _p, _i64, _p]),
+}
+
+_lib = None
+
+
+class LibraryMissing(RuntimeError):
+    pass
+
+
+def load():
+    """Load (once) and return the CDLL with typed entry points."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise LibraryMissing(
+            f"{LIB_PATH} not found: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+            "(there is no CPU fallback)")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib

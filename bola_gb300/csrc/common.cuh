@@ -1,0 +1,255 @@
+// common.cuh — shared helpers of the FP64 path.
+//
+// Every kernel here reproduces BOLA's IEEE operation sequence, so these
+// translation units are compiled with -fmad=false: a product followed by a sum
+// is never contracted behind our back.  The only fused multiply-adds are the
+// explicit fused() calls, placed exactly where BOLA uses a vector FMA.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "bola_gb300.h"
+
+namespace bola {
+
+// ---- host side ------------------------------------------------------------
+int fail(int code, const char *fmt, ...);       // records the message, returns code
+int cuda_fail(cudaError_t e, const char *what);  // records the CUDA error text
+int lanes();                                     // SIMD width reproduced: 2 or 4
+int num_sms();                                   // SMs of the current device
+
+#define BOLA_TRY_CUDA(expr)                                   \
+  do {                                                        \
+    cudaError_t e_ = (expr);                                  \
+    if (e_ != cudaSuccess) return ::bola::cuda_fail(e_, #expr); \
+  } while (0)
+#define BOLA_CHECK_LAUNCH() BOLA_TRY_CUDA(cudaGetLastError())
+#define BOLA_TRY(expr)      \
+  do {                      \
+    int r_ = (expr);        \
+    if (r_ != 0) return r_; \
+  } while (0)
+
+inline char upc(char c) { return (c >= 'a' && c <= 'z') ? (char)(c - 32) : c; }
+__host__ __device__ inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+__host__ __device__ inline int64_t imin(int64_t a, int64_t b) { return a < b ? a : b; }
+__host__ __device__ inline int64_t imax(int64_t a, int64_t b) { return a > b ? a : b; }
+
+// Stream-ordered temporary device memory (cudaMallocAsync pool).
+class Scratch {
+ public:
+  Scratch() = default;
+  Scratch(const Scratch &) = delete;
+  Scratch &operator=(const Scratch &) = delete;
+  ~Scratch() { release(); }
+  int alloc(size_t bytes, cudaStream_t s) {
+    release();
+    stream_ = s;
+    if (bytes == 0) return 0;
+    cudaError_t e = cudaMallocAsync(&ptr_, bytes, s);
+    if (e != cudaSuccess) {
+      ptr_ = nullptr;
+      return cuda_fail(e, "cudaMallocAsync(scratch)");
+    }
+    return 0;
+  }
+  void release() {
+    if (ptr_) cudaFreeAsync(ptr_, stream_);
+    ptr_ = nullptr;
+  }
+  template <class T>
+  T *as() const { return static_cast<T *>(ptr_); }
+
+ private:
+  void *ptr_ = nullptr;
+  cudaStream_t stream_ = nullptr;
+};
+
+// ---- internal launchers shared between translation units -------------------
+// Exact DGEMM: per output element, K is walked in chunks of `kc`; each chunk is
+// accumulated from zero with fused multiply-adds in increasing k and added to C
+// as C = fma(alpha, acc, C) (BOLA's 8x4 micro-kernel, src/gemm.rs:228-336).
+// Elements in BOLA's partial 8x4 edge tiles use its unfused scalar kernel
+// (src/gemm.rs:357-377).  beta is applied first as BOLA does (src/gemm.rs:110-122).
+// tri: 0 = whole C; 1 / 2 = only elements whose 32-block lies strictly above /
+// below the block diagonal (the off-diagonal part of a blocked SYRK).
+// info: optional device flag; kernels return immediately when *info != 0.
+int dgemm_exact(cudaStream_t s, char ta, char tb, int64_t m, int64_t n, int64_t k, double alpha,
+                const double *A, int64_t lda, const double *B, int64_t ldb, double beta, double *C,
+                int64_t ldc, int kc, const int32_t *info, int tri);
+
+int trsm_exact(cudaStream_t s, char side, char uplo, char transa, char diag, int64_t m, int64_t n,
+               double alpha, const double *A, int64_t lda, double *B, int64_t ldb,
+               const int32_t *info);
+
+int syrk_exact(cudaStream_t s, char uplo, char trans, int64_t n, int64_t k, double alpha,
+               const double *A, int64_t lda, double beta, double *C, int64_t ldc,
+               const int32_t *info);
+
+int laswp_exact(cudaStream_t s, int64_t n, double *A, int64_t lda, int32_t k1, int32_t k2,
+                const int32_t *ipiv, int32_t incx, const int32_t *info);
+
+int getrf2_rec(cudaStream_t s, int64_t m, int64_t n, double *A, int64_t lda, int32_t *ipiv,
+               int32_t *info, int32_t col0);
+
+int potrf2_rec(cudaStream_t s, char uplo, int64_t n, double *A, int64_t lda, int32_t *info,
+               int32_t col0);
+
+// Adds `add` to ipiv[0..count) unless *info != 0.
+int ipiv_add(cudaStream_t s, int32_t *ipiv, int64_t count, int32_t add, const int32_t *info);
+
+// ---- device side -------------------------------------------------------------
+__device__ __forceinline__ double fused(double a, double b, double c) { return __fma_rn(a, b, c); }
+// c + t*x with two roundings (BOLA's scalar tails; Rust never contracts).
+__device__ __forceinline__ double add_prod(double c, double t, double x) {
+  return __dadd_rn(c, __dmul_rn(t, x));
+}
+__device__ __forceinline__ double sub_prod(double c, double t, double x) {
+  return __dsub_rn(c, __dmul_rn(t, x));
+}
+__device__ __forceinline__ bool stop_flag(const int32_t *info) {
+  return info != nullptr && *(volatile const int32_t *)info != 0;
+}
+
+// BOLA's daxpy(len, alpha, x, 1, y, 1) (src/utilities.rs:107-132 / :140-164):
+// element idx of the vector body (idx < len rounded down to `lanes`) is fused,
+// the scalar tail is not.
+__device__ __forceinline__ double daxpy_elem(double y, double alpha, double x, int64_t idx,
+                                             int64_t len, int lanes) {
+  const int64_t done = (len / lanes) * lanes;
+  return idx < done ? fused(alpha, x, y) : add_prod(y, alpha, x);
+}
+
+// BOLA's dot_product(n, x, 1, y, 1) (src/utilities.rs:22-54 / :62-92) with
+// element strides sx, sy (the unit-stride vector path applied to gathered
+// data).  Sequential per lane, then BOLA's horizontal sum and unfused tail.
+__device__ __forceinline__ double dot_exact(int64_t n, const double *x, int64_t sx, const double *y,
+                                            int64_t sy, int lanes) {
+  if (n == 0) return 0.0;
+  const int64_t nch = n / lanes;
+  double l0 = 0.0, l1 = 0.0, l2 = 0.0, l3 = 0.0;
+  for (int64_t i = 0; i < nch; ++i) {
+    const int64_t b = i * lanes;
+    l0 = fused(x[b * sx], y[b * sy], l0);
+    l1 = fused(x[(b + 1) * sx], y[(b + 1) * sy], l1);
+    if (lanes == 4) {
+      l2 = fused(x[(b + 2) * sx], y[(b + 2) * sy], l2);
+      l3 = fused(x[(b + 3) * sx], y[(b + 3) * sy], l3);
+    }
+  }
+  double s;
+  if (lanes == 4) {
+    double h = -0.0;
+    h = __dadd_rn(h, l0);
+    h = __dadd_rn(h, l1);
+    h = __dadd_rn(h, l2);
+    h = __dadd_rn(h, l3);
+    s = __dadd_rn(0.0, h);
+  } else {
+    s = __dadd_rn(l0, l1);
+  }
+  for (int64_t i = nch * lanes; i < n; ++i) s = add_prod(s, x[i * sx], y[i * sy]);
+  return s;
+}
+
+// Candidate of BOLA's idamax (src/idamax.rs): ordered by value, then by the
+// position BOLA's four lane-interleaved accumulators give it.  v = -1 marks
+// an element BOLA can never select (NaN; zero in the vector body or tail).
+struct Cand {
+  double v;
+  int64_t key;  // smaller wins among equal v
+  int64_t idx;  // 0-based index in the searched vector
+};
+__device__ __forceinline__ bool cand_better(const Cand &a, const Cand &b) {
+  return a.v > b.v || (a.v == b.v && a.key < b.key);
+}
+__device__ __forceinline__ Cand make_cand(double x, int64_t idx, int64_t n, int lanes) {
+  Cand c;
+  c.idx = idx;
+  const double ax = fabs(x);
+  const int64_t small = lanes == 4 ? 16 : 8;
+  if (n < small) {  // scalar path, starts from max = -1.0
+    c.v = (ax >= 0.0) ? ax : -1.0;
+    c.key = idx;
+    return c;
+  }
+  const int64_t chunk = 4 * lanes;
+  const int64_t nch = n / chunk;
+  const int64_t nv = nch * chunk;
+  c.v = (ax > 0.0) ? ax : -1.0;  // vector body and tail start from max = 0.0
+  if (idx < nv) {
+    const int64_t r = idx % chunk;
+    const int64_t lane = r % lanes, acc = r / lanes;
+    c.key = (lane * 4 + acc) * nch + idx / chunk;
+  } else {
+    c.key = idx;
+  }
+  return c;
+}
+__device__ __forceinline__ Cand cand_none() {
+  Cand c;
+  c.v = -2.0;
+  c.key = INT64_MAX;
+  c.idx = 0;
+  return c;
+}
+__device__ __forceinline__ Cand shfl_cand(const Cand &c, int src) {
+  Cand o;
+  o.v = __shfl_sync(0xffffffffu, c.v, src);
+  o.key = __shfl_sync(0xffffffffu, c.key, src);
+  o.idx = __shfl_sync(0xffffffffu, c.idx, src);
+  return o;
+}
+__device__ __forceinline__ Cand warp_best(Cand c) {
+  for (int off = 16; off > 0; off >>= 1) {
+    Cand o;
+    o.v = __shfl_down_sync(0xffffffffu, c.v, off);
+    o.key = __shfl_down_sync(0xffffffffu, c.key, off);
+    o.idx = __shfl_down_sync(0xffffffffu, c.idx, off);
+    if (cand_better(o, c)) c = o;
+  }
+  return c;
+}
+
+// An ordered list of row interchanges, walked as BOLA's laswp walks ipiv
+// (src/laswp.rs:30-37): i from i1 to i2 by i_inc, ipiv index from ix0 by incx.
+struct SwapPlan {
+  int64_t ix0;
+  int32_t i1, i2, i_inc, incx;
+};
+
+// Composes the interchanges into "row rows[t] takes the old value of row
+// src[t]" (at most 2 entries per interchange; the caller sizes the arrays).
+__device__ __forceinline__ int compose_swaps(const SwapPlan &p, const int32_t *ipiv, int64_t *rows,
+                                             int64_t *src) {
+  int cnt = 0;
+  int64_t ix = p.ix0;
+  for (int32_t i = p.i1; p.i_inc > 0 ? i <= p.i2 : i >= p.i2; i += p.i_inc, ix += p.incx) {
+    const int64_t ip = ipiv[ix];
+    if (ip == (int64_t)i) continue;
+    const int64_t r1 = (int64_t)i - 1, r2 = ip - 1;
+    int a = -1, b = -1;
+    for (int t = 0; t < cnt; ++t) {
+      if (rows[t] == r1) a = t;
+      if (rows[t] == r2) b = t;
+    }
+    if (a < 0) {
+      rows[cnt] = r1;
+      src[cnt] = r1;
+      a = cnt++;
+    }
+    if (b < 0) {
+      rows[cnt] = r2;
+      src[cnt] = r2;
+      b = cnt++;
+    }
+    const int64_t t = src[a];
+    src[a] = src[b];
+    src[b] = t;
+  }
+  return cnt;
+}
+
+}  // namespace bola

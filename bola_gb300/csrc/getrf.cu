@@ -1,0 +1,441 @@
+// getrf.cu — LU with partial pivoting, BOLA's blocking and rounding
+// (src/getrf.rs:37-101, src/getrf2.rs:39-185).
+//
+// Blocked right-looking LU with BOLA's NB = 32.  Per block column:
+//   1. panel_lu: one thread-block CLUSTER (up to 16 CTAs, the panel's rows
+//      spread over them and held in shared memory) factors the (m-j) x 32
+//      panel column by column: warp-shuffle idamax under BOLA's lane order,
+//      pivot-row exchange through distributed shared memory, reciprocal scale
+//      and BOLA's pairwise rank-1 update — one cluster barrier per column.
+//   2. step_swap_trsm: the 32 row interchanges applied to every other column
+//      (BOLA's two laswp calls) fused with BOLA's 32-row unit-lower trsm on
+//      the right block row.
+//   3. the exact DGEMM for the rank-32 trailing update.
+// Every element sees the same operation sequence as in BOLA, so A and ipiv
+// come out bit-identical (for the SIMD width selected).
+#include <cooperative_groups.h>
+
+#include "common.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace bola {
+namespace {
+
+constexpr int PNB = 32;   // panel width: BOLA's NB (src/getrf.rs:11) / recursion stop (src/getrf2.rs:11)
+constexpr int PT = 256;   // threads per CTA in the panel kernel
+constexpr int MAXC = 16;  // largest cluster (non-portable size on sm_103)
+constexpr size_t SMEM_DATA_LIMIT = 200 * 1024;
+
+struct PanelPub {  // what a CTA publishes to the rest of the cluster each column
+  double v;
+  int64_t key;
+  int64_t g;  // panel row of this CTA's best candidate, -1 if none
+  double best_row[PNB];
+  double row_j[PNB];  // the current pivot-position row, from the CTA that owns it
+};
+
+constexpr size_t panel_base_bytes() {
+  return 2 * sizeof(PanelPub) + (PT / 32) * sizeof(Cand) + PNB * sizeof(double) + 4 * sizeof(int64_t);
+}
+
+// Unblocked LU of an mp x nb panel (nb <= 32), iterative_getrf2 of
+// src/getrf2.rs:131-185.  SMEM: the CTA's rows live in shared memory
+// (column-major, ld R) while it works; otherwise they stay in global memory.
+template <bool SMEM>
+__global__ void __launch_bounds__(PT)
+panel_lu(double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_t *info, int32_t add_on_success,
+         int32_t col0, int lanes, int64_t R) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = (int)cluster.num_blocks();
+  const int cr = (int)cluster.block_rank();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  PanelPub *pub = reinterpret_cast<PanelPub *>(smem_raw);
+  Cand *red = reinterpret_cast<Cand *>(pub + 2);
+  double *prow = reinterpret_cast<double *>(red + PT / 32);
+  int64_t *bc = reinterpret_cast<int64_t *>(prow + PNB);
+  double *data = reinterpret_cast<double *>(bc + 4);
+
+  // Uniform across the cluster: the only writer of *info in this kernel acts
+  // after a cluster barrier that every CTA reaches after this read.
+  if (stop_flag(info)) return;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t r0 = (int64_t)cr * R;
+  const int64_t r1 = imin(mp, r0 + R);
+  const int64_t nr = r1 > r0 ? r1 - r0 : 0;
+  auto el = [&](int64_t il, int c) -> double & {
+    return SMEM ? data[(int64_t)c * R + il] : A[(r0 + il) + (int64_t)c * lda];
+  };
+  if (SMEM) {
+    for (int64_t e = tid; e < nr * nb; e += PT) {
+      const int64_t il = e % nr;
+      const int c = (int)(e / nr);
+      data[(int64_t)c * R + il] = A[(r0 + il) + (int64_t)c * lda];
+    }
+  }
+  __syncthreads();
+
+  const int steps = (int)imin(mp, nb);
+  bool failed = false;
+  for (int j = 0; j < steps; ++j) {
+    PanelPub *my = &pub[j & 1];
+    const int64_t nlen = mp - j;
+    // -- idamax over this CTA's rows >= j
+    Cand best = cand_none();
+    for (int64_t il = tid; il < nr; il += PT) {
+      const int64_t g = r0 + il;
+      if (g < j) continue;
+      const Cand c = make_cand(el(il, j), g - j, nlen, lanes);
+      if (cand_better(c, best)) best = c;
+    }
+    best = warp_best(best);
+    if (lane == 0) red[warp] = best;
+    __syncthreads();
+    if (tid == 0) {
+      Cand b = red[0];
+      for (int w = 1; w < PT / 32; ++w)
+        if (cand_better(red[w], b)) b = red[w];
+      my->v = b.v;
+      my->key = b.key;
+      my->g = (b.v > -2.0) ? j + b.idx : -1;
+      bc[0] = my->g;
+    }
+    __syncthreads();
+    const int64_t myg = bc[0];
+    if (tid < nb) {
+      if (myg >= 0) my->best_row[tid] = el(myg - r0, tid);
+      if (j >= r0 && j < r1) my->row_j[tid] = el(j - r0, tid);
+    }
+    cluster.sync();
+    // -- cluster-wide winner (same total order in every CTA)
+    if (warp == 0) {
+      Cand c = cand_none();
+      if (lane < C) {
+        const PanelPub *rp = cluster.map_shared_rank(my, lane);
+        c.v = rp->v;
+        c.key = rp->key;
+        c.idx = rp->g;
+      }
+      c = warp_best(c);
+      if (lane == 0) bc[1] = (c.v < 0.0) ? (int64_t)j : c.idx;  // idamax -> 0 when nothing qualifies
+    }
+    __syncthreads();
+    const int64_t jp = bc[1];
+    const int owner_j = (int)(j / R), owner_p = (int)(jp / R);
+    if (tid < nb) {
+      const PanelPub *src = cluster.map_shared_rank(my, jp == j ? owner_j : owner_p);
+      prow[tid] = (jp == j) ? src->row_j[tid] : src->best_row[tid];
+    }
+    __syncthreads();
+    const double pv = prow[j];
+    if (cr == 0 && tid == 0) ipiv[j] = (int32_t)(jp + 1);
+    if (!(pv != 0.0)) {  // exact zero pivot: BOLA's "Matrix is singular" (src/getrf2.rs:166-168)
+      if (cr == 0 && tid == 0) *info = col0 + j + 1;
+      failed = true;
+      break;
+    }
+    // -- row interchange across the whole panel width (src/getrf2.rs:144-150)
+    if (jp != j) {
+      if (cr == owner_j && tid < nb) el(j - r0, tid) = prow[tid];
+      if (cr == owner_p && tid < nb) {
+        const PanelPub *sj = cluster.map_shared_rank(my, owner_j);
+        el(jp - r0, tid) = sj->row_j[tid];
+      }
+    }
+    __syncthreads();
+    // -- reciprocal scale (src/getrf2.rs:152-164) and rank-1 update (ger, src/ger.rs:28-61)
+    if (j < mp - 1) {
+      const double inv = 1.0 / pv;
+      const int64_t mr = mp - j - 1;
+      const int64_t rows_vec = (mr / lanes) * lanes;
+      const int ncols = nb - j - 1;
+      const int n_unrolled = ncols - (ncols % 2);
+      const bool do_ger = j < steps - 1;
+      for (int64_t il = tid; il < nr; il += PT) {
+        const int64_t g = r0 + il;
+        if (g <= j) continue;
+        const double x = __dmul_rn(el(il, j), inv);
+        el(il, j) = x;
+        if (!do_ger) continue;
+        const bool vec = (g - j - 1) < rows_vec;
+        for (int t = 0; t < n_unrolled; t += 2) {
+          const int c0 = j + 1 + t;
+          const double t0 = -prow[c0], t1 = -prow[c0 + 1];
+          if (t0 == 0.0 && t1 == 0.0) continue;
+          double &a0 = el(il, c0);
+          double &a1 = el(il, c0 + 1);
+          a0 = vec ? fused(x, t0, a0) : add_prod(a0, t0, x);
+          a1 = vec ? fused(x, t1, a1) : add_prod(a1, t1, x);
+        }
+        if (ncols % 2) {
+          const int c = nb - 1;
+          const double t = -prow[c];
+          if (t != 0.0) el(il, c) = add_prod(el(il, c), t, x);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (!failed && cr == 0 && add_on_success != 0)
+    for (int t = tid; t < steps; t += PT) ipiv[t] += add_on_success;
+  if (SMEM) {
+    for (int64_t e = tid; e < nr * nb; e += PT) {
+      const int64_t il = e % nr;
+      const int c = (int)(e / nr);
+      A[(r0 + il) + (int64_t)c * lda] = data[(int64_t)c * R + il];
+    }
+  }
+  cluster.sync();  // no CTA may leave while another can still read its shared memory
+}
+
+// iterative_getrf2 for a short, wide matrix (m <= 32 rows, any n): one CTA,
+// data in global memory.
+__global__ void __launch_bounds__(PT)
+panel_lu_wide(double *A, int64_t lda, int64_t m, int64_t n, int32_t *ipiv, int32_t *info, int32_t col0,
+              int lanes) {
+  __shared__ Cand red[PT / 32];
+  __shared__ int64_t sjp;
+  if (stop_flag(info)) return;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t steps = imin(m, n);
+  for (int64_t j = 0; j < steps; ++j) {
+    Cand best = cand_none();
+    for (int64_t g = j + tid; g < m; g += PT) {
+      const Cand c = make_cand(A[g + j * lda], g - j, m - j, lanes);
+      if (cand_better(c, best)) best = c;
+    }
+    best = warp_best(best);
+    if (lane == 0) red[warp] = best;
+    __syncthreads();
+    if (tid == 0) {
+      Cand b = red[0];
+      for (int w = 1; w < PT / 32; ++w)
+        if (cand_better(red[w], b)) b = red[w];
+      sjp = (b.v < 0.0) ? j : j + b.idx;
+      ipiv[j] = (int32_t)(sjp + 1);
+    }
+    __syncthreads();
+    const int64_t jp = sjp;
+    const double pv = A[jp + j * lda];
+    if (!(pv != 0.0)) {
+      if (tid == 0) *info = col0 + (int32_t)j + 1;
+      return;
+    }
+    if (jp != j) {
+      for (int64_t c = tid; c < n; c += PT) {
+        const double t = A[j + c * lda];
+        A[j + c * lda] = A[jp + c * lda];
+        A[jp + c * lda] = t;
+      }
+    }
+    __syncthreads();
+    if (j < m - 1) {
+      const double inv = 1.0 / pv;
+      for (int64_t g = j + 1 + tid; g < m; g += PT) A[g + j * lda] = __dmul_rn(A[g + j * lda], inv);
+    }
+    __syncthreads();
+    if (j < steps - 1) {
+      const int64_t mr = m - j - 1, ncols = n - j - 1;
+      const int64_t rows_vec = (mr / lanes) * lanes, n_unrolled = ncols - (ncols % 2);
+      for (int64_t e = tid; e < mr * ncols; e += PT) {
+        const int64_t ri = e % mr, ci = e / mr;
+        const int64_t g = j + 1 + ri, c = j + 1 + ci;
+        const double x = A[g + j * lda];
+        double &a = A[g + c * lda];
+        if (ci < n_unrolled) {
+          const int64_t p0 = j + 1 + (ci & ~(int64_t)1);
+          const double t0 = -A[j + p0 * lda], t1 = -A[j + (p0 + 1) * lda];
+          if (t0 == 0.0 && t1 == 0.0) continue;
+          const double t = (c == p0) ? t0 : t1;
+          a = ri < rows_vec ? fused(x, t, a) : add_prod(a, t, x);
+        } else {
+          const double t = -A[j + c * lda];
+          if (t != 0.0) a = add_prod(a, t, x);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// One getrf block step after the panel: the panel's interchanges applied to
+// all other columns (src/getrf.rs:64-70) and, on the right block row, BOLA's
+// unit-lower trsm base case with its daxpy (src/getrf.rs:78, src/trsm.rs:96-109).
+// A warp per column.
+__global__ void __launch_bounds__(256)
+step_swap_trsm(double *A, int64_t lda, int64_t n, int64_t j, int jb, const int32_t *ipiv,
+               const int32_t *info, int lanes) {
+  __shared__ int64_t rows[2 * PNB], src[2 * PNB];
+  __shared__ double L[PNB * PNB];
+  __shared__ int cnt;
+  if (stop_flag(info)) return;
+  if (threadIdx.x == 0) {
+    SwapPlan p;
+    p.ix0 = j;
+    p.i1 = (int32_t)(j + 1);
+    p.i2 = (int32_t)(j + jb);
+    p.i_inc = 1;
+    p.incx = 1;
+    cnt = compose_swaps(p, ipiv, rows, src);
+  }
+  for (int e = threadIdx.x; e < jb * jb; e += blockDim.x) {
+    const int r = e % jb, c = e / jb;
+    L[r + c * PNB] = A[(j + r) + (j + c) * lda];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (w >= n - jb) return;
+  const int64_t col = w < j ? w : w + jb;
+  double *cp = A + col * lda;
+  const double v0 = lane < cnt ? cp[src[lane]] : 0.0;
+  const double v1 = lane + 32 < cnt ? cp[src[lane + 32]] : 0.0;
+  __syncwarp();
+  if (lane < cnt) cp[rows[lane]] = v0;
+  if (lane + 32 < cnt) cp[rows[lane + 32]] = v1;
+  __syncwarp();
+  if (col < j + jb) return;
+  double b = lane < jb ? cp[j + lane] : 0.0;
+  for (int k = 0; k < jb; ++k) {
+    const double bk = __shfl_sync(0xffffffffu, b, k);
+    if (bk == 0.0) continue;
+    if (lane > k && lane < jb)
+      b = daxpy_elem(b, -bk, L[lane + k * PNB], lane - k - 1, jb - k - 1, lanes);
+  }
+  if (lane < jb) cp[j + lane] = b;
+}
+
+__global__ void zero_i32(int32_t *p) { *p = 0; }
+
+// Launches panel_lu with the largest cluster (<= 16 CTAs, ~256 rows each)
+// the device can co-schedule.
+int launch_panel(cudaStream_t s, double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_t *info,
+                 int32_t add_on_success, int32_t col0) {
+  int C = (int)imin(MAXC, imax(1, cdiv(mp, 256)));
+  for (;; C = C > 1 ? (C + 1) / 2 : 0) {
+    if (C == 0) return fail(BOLA_ERR_CUDA, "panel_lu: no cluster size could be scheduled");
+    const int64_t R = cdiv(mp, C);
+    size_t smem = panel_base_bytes() + (size_t)R * nb * sizeof(double);
+    const bool use_smem = smem <= SMEM_DATA_LIMIT;
+    if (!use_smem) smem = panel_base_bytes();
+    void (*kern)(double *, int64_t, int64_t, int, int32_t *, int32_t *, int32_t, int32_t, int, int64_t) =
+        use_smem ? panel_lu<true> : panel_lu<false>;
+    BOLA_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_DATA_LIMIT + 4096));
+    BOLA_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)C, 1, 1);
+    cfg.blockDim = dim3(PT, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg) != cudaSuccess || nclusters < 1) {
+      cudaGetLastError();
+      continue;
+    }
+    const int lanes_v = lanes();
+    BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, kern, A, lda, mp, nb, ipiv, info, add_on_success, col0, lanes_v, R));
+    return 0;
+  }
+}
+
+// iterative_getrf2 dispatch: tall panels go to the cluster kernel, short wide
+// ones to the single-CTA kernel.
+int iterative(cudaStream_t s, int64_t m, int64_t n, double *A, int64_t lda, int32_t *ipiv, int32_t *info,
+              int32_t col0, int32_t add_on_success) {
+  if (n <= PNB) return launch_panel(s, A, lda, m, (int)n, ipiv, info, add_on_success, col0);
+  panel_lu_wide<<<1, PT, 0, s>>>(A, lda, m, n, ipiv, info, col0, lanes());
+  BOLA_CHECK_LAUNCH();
+  return ipiv_add(s, ipiv, imin(m, n), add_on_success, info);
+}
+
+}  // namespace
+
+// src/getrf2.rs:39-106; col0 is the global column of A's first column (for info).
+int getrf2_rec(cudaStream_t s, int64_t m, int64_t n, double *A, int64_t lda, int32_t *ipiv, int32_t *info,
+               int32_t col0) {
+  if (m == 0 || n == 0) return 0;
+  if (m <= PNB || n <= PNB) return iterative(s, m, n, A, lda, ipiv, info, col0, 0);
+  const int64_t n1 = imin(m, n) / 2, n2 = n - n1;
+  BOLA_TRY(getrf2_rec(s, m, n1, A, lda, ipiv, info, col0));
+  BOLA_TRY(laswp_exact(s, n2, A + n1 * lda, lda, 1, (int32_t)n1, ipiv, 1, info));
+  BOLA_TRY(trsm_exact(s, 'L', 'L', 'N', 'U', n1, n2, 1.0, A, lda, A + n1 * lda, lda, info));
+  if (n1 < m) {
+    BOLA_TRY(dgemm_exact(s, 'N', 'N', m - n1, n2, n1, -1.0, A + n1, lda, A + n1 * lda, lda, 1.0,
+                         A + n1 + n1 * lda, lda, 64, info, 0));
+    BOLA_TRY(getrf2_rec(s, m - n1, n2, A + n1 + n1 * lda, lda, ipiv + n1, info, col0 + (int32_t)n1));
+  }
+  BOLA_TRY(ipiv_add(s, ipiv + n1, imin(m, n) - n1, (int32_t)n1, info));
+  return laswp_exact(s, n1, A, lda, (int32_t)(n1 + 1), (int32_t)imin(m, n), ipiv, 1, info);
+}
+
+// src/getrf.rs:37-101
+int getrf_blocked(cudaStream_t s, int64_t m, int64_t n, double *A, int64_t lda, int32_t *ipiv, int32_t *info) {
+  zero_i32<<<1, 1, 0, s>>>(info);
+  BOLA_CHECK_LAUNCH();
+  if (m == 0 || n == 0) return 0;
+  const int64_t min_mn = imin(m, n);
+  if (PNB >= min_mn) return getrf2_rec(s, m, n, A, lda, ipiv, info, 0);
+  for (int64_t j = 0; j < min_mn; j += PNB) {
+    const int jb = (int)imin(PNB, min_mn - j);
+    BOLA_TRY(launch_panel(s, A + j + j * lda, lda, m - j, jb, ipiv + j, info, (int32_t)j, (int32_t)j));
+    const int64_t others = n - jb;
+    if (others > 0) {
+      step_swap_trsm<<<(unsigned)cdiv(others, 8), 256, 0, s>>>(A, lda, n, j, jb, ipiv, info, lanes());
+      BOLA_CHECK_LAUNCH();
+    }
+    if (j + jb < n && j + jb < m) {
+      BOLA_TRY(dgemm_exact(s, 'N', 'N', m - j - jb, n - j - jb, jb, -1.0, A + (j + jb) + j * lda, lda,
+                           A + j + (j + jb) * lda, lda, 1.0, A + (j + jb) + (j + jb) * lda, lda, 64, info, 0));
+    }
+  }
+  return 0;
+}
+
+}  // namespace bola
+
+using namespace bola;
+
+extern "C" {
+
+int bola_dgetrf(int64_t m, int64_t n, double *a, int64_t lda, int32_t *ipiv, int32_t *info,
+                bola_stream_t stream) {
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (lda < imax(m, 1)) return -4;  // "Argument 4 to getrf had an illegal value" (src/getrf.rs:41-43)
+  if (imin(m, n) > INT32_MAX - 1) return -1;
+  return getrf_blocked((cudaStream_t)stream, m, n, a, lda, ipiv, info);
+}
+
+int bola_dgetrf2(int64_t m, int64_t n, double *a, int64_t lda, int32_t *ipiv, int32_t *info,
+                 bola_stream_t stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (lda < imax(m, 1)) return -4;  // src/getrf2.rs:43-45
+  zero_i32<<<1, 1, 0, s>>>(info);
+  BOLA_CHECK_LAUNCH();
+  return getrf2_rec(s, m, n, a, lda, ipiv, info, 0);
+}
+
+int bola_dgetrs(int64_t n, int64_t nrhs, const double *lu, int64_t lda, const int32_t *ipiv, double *b,
+                int64_t ldb, bola_stream_t stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  if (n < 0) return -1;
+  if (nrhs < 0) return -2;
+  if (lda < imax(1, n)) return -4;
+  if (ldb < imax(1, n)) return -7;
+  if (n == 0 || nrhs == 0) return 0;
+  BOLA_TRY(laswp_exact(s, nrhs, b, ldb, 1, (int32_t)n, ipiv, 1, nullptr));
+  BOLA_TRY(trsm_exact(s, 'L', 'L', 'N', 'U', n, nrhs, 1.0, lu, lda, b, ldb, nullptr));
+  return trsm_exact(s, 'L', 'U', 'N', 'N', n, nrhs, 1.0, lu, lda, b, ldb, nullptr);
+}
+
+}  // extern "C"

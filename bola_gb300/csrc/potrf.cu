@@ -1,0 +1,269 @@
+// potrf.cu — SYRK and Cholesky with BOLA's blocking and rounding
+// (src/syrk.rs:17-249, src/potrf.rs:101-181, src/potrf2.rs:25-80).
+//
+// SYRK: BOLA walks 32x32 blocks of C and 32-deep blocks of K.  Off-diagonal
+// blocks go through its gemm with K = 32, i.e. exactly the exact DGEMM with a
+// 32-deep chunk, restricted to the strictly upper / lower block triangle.  The
+// diagonal blocks use BOLA's syrk_kernel: per element a chain of daxpy
+// updates ('N') or of 32-deep dot products ('T') — one thread per element.
+//
+// POTRF is BOLA's left-looking blocked Cholesky (NB = 32): diagonal SYRK,
+// the 32x32 recursive potrf2 inside one CTA's shared memory, the panel GEMM
+// (split-K when the panel is skinny) and the right/left triangular solve.
+#include "common.cuh"
+
+namespace bola {
+namespace {
+
+constexpr int NB = 32;  // src/syrk.rs:9, src/potrf.rs:8
+
+__global__ void syrk_beta(bool upper, int64_t n, double beta, double *C, int64_t ldc, const int32_t *info) {
+  if (stop_flag(info)) return;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n * n) return;
+  const int64_t i = e % n, j = e / n;
+  if (upper ? i > j : i < j) return;
+  double &c = C[i + j * ldc];
+  c = beta == 0.0 ? 0.0 : __dmul_rn(c, beta);
+}
+
+// Diagonal 32x32 blocks: blockIdx.y = block, blockIdx.x = column in block,
+// threadIdx.x = row in block.
+__global__ void __launch_bounds__(NB)
+syrk_diag(bool upper, bool trans_t, int64_t n, int64_t k, double alpha, const double *__restrict__ A,
+          int64_t lda, double *C, int64_t ldc, int lanes, const int32_t *info) {
+  if (stop_flag(info)) return;
+  const int64_t j0 = (int64_t)blockIdx.y * NB;
+  const int jb = (int)imin(NB, n - j0);
+  const int jj = blockIdx.x, ii = threadIdx.x;
+  if (jj >= jb || ii >= jb) return;
+  if (upper ? ii > jj : ii < jj) return;
+  double *cp = C + (j0 + ii) + (j0 + jj) * ldc;
+  double c = *cp;
+  for (int64_t p0 = 0; p0 < k; p0 += NB) {
+    const int pb = (int)imin(NB, k - p0);
+    if (!trans_t) {
+      // syrk_kernel 'N' (src/syrk.rs:201-222): C(:,jj) += (alpha*A(jj,l)) * A(:,l), BOLA's daxpy
+      const double *P = A + j0 + p0 * lda;
+      const int64_t len = upper ? jj + 1 : jb - jj;
+      const int64_t idx = upper ? ii : ii - jj;
+      for (int l = 0; l < pb; ++l) {
+        const double t = __dmul_rn(alpha, P[jj + l * lda]);
+        if (t != 0.0) c = daxpy_elem(c, t, P[ii + l * lda], idx, len, lanes);
+      }
+    } else {
+      // syrk_kernel 'T' (src/syrk.rs:223-247): C(ii,jj) += alpha * dot(A(:,ii), A(:,jj))
+      const double *P = A + p0 + j0 * lda;
+      const double t = dot_exact(pb, P + ii * lda, 1, P + jj * lda, 1, lanes);
+      c = add_prod(c, alpha, t);
+    }
+  }
+  *cp = c;
+}
+
+// ---- potrf2 on one <=32 x 32 block in shared memory (src/potrf2.rs:36-80) ----
+constexpr int LDS = NB;
+
+__device__ int p2_rec(bool upper, double *a, int n, int lanes) {
+  const int tid = threadIdx.x;
+  if (n == 0) return 0;
+  if (n == 1) {
+    const double a11 = a[0];
+    __syncthreads();
+    if (!(a11 > 0.0)) return 1;
+    if (tid == 0) a[0] = sqrt(a11);
+    __syncthreads();
+    return 0;
+  }
+  const int n1 = n / 2, n2 = n - n1;
+  int r = p2_rec(upper, a, n1, lanes);
+  if (r) return r;
+  double *a22 = a + n1 + n1 * LDS;
+  if (upper) {
+    double *a12 = a + n1 * LDS;
+    // trsm('L','U','T','N', n1, n2, 1, a11, a12): trsm_ltu base, a thread per column
+    if (tid < n2) {
+      for (int i = 0; i < n1; ++i) {
+        double t = a12[i + tid * LDS];
+        for (int k = 0; k < i; ++k) t = sub_prod(t, a[k + i * LDS], a12[k + tid * LDS]);
+        t = t / a[i + i * LDS];
+        a12[i + tid * LDS] = t;
+      }
+    }
+    __syncthreads();
+    // syrk('U','T', n2, n1, -1, a12, 1, a22): dot path
+    for (int e = tid; e < n2 * n2; e += blockDim.x) {
+      const int ii = e % n2, jj = e / n2;
+      if (ii > jj) continue;
+      const double t = dot_exact(n1, a12 + ii * LDS, 1, a12 + jj * LDS, 1, lanes);
+      a22[ii + jj * LDS] = add_prod(a22[ii + jj * LDS], -1.0, t);
+    }
+  } else {
+    double *a21 = a + n1;
+    // trsm('R','L','T','N', n2, n1, 1, a11, a21): trsm_rtl base, a thread per row
+    if (tid < n2) {
+      for (int j = 0; j < n1; ++j) {
+        double b = a21[tid + j * LDS];
+        for (int k = 0; k < j; ++k) {
+          const double ajk = a[j + k * LDS];
+          if (ajk != 0.0) b = sub_prod(b, ajk, a21[tid + k * LDS]);
+        }
+        b = __dmul_rn(b, 1.0 / a[j + j * LDS]);
+        a21[tid + j * LDS] = b;
+      }
+    }
+    __syncthreads();
+    // syrk('L','N', n2, n1, -1, a21, 1, a22): daxpy path
+    for (int e = tid; e < n2 * n2; e += blockDim.x) {
+      const int ii = e % n2, jj = e / n2;
+      if (ii < jj) continue;
+      double c = a22[ii + jj * LDS];
+      for (int l = 0; l < n1; ++l) {
+        const double t = -a21[jj + l * LDS];
+        if (t != 0.0) c = daxpy_elem(c, t, a21[ii + l * LDS], ii - jj, n2 - jj, lanes);
+      }
+      a22[ii + jj * LDS] = c;
+    }
+  }
+  __syncthreads();
+  r = p2_rec(upper, a22, n2, lanes);
+  return r ? r + n1 : 0;
+}
+
+__global__ void __launch_bounds__(256)
+potrf2_block(bool upper, int n, double *A, int64_t lda, int32_t *info, int32_t col0, int lanes) {
+  __shared__ double a[LDS * LDS];
+  if (stop_flag(info)) return;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) a[(e % n) + (e / n) * LDS] = A[(e % n) + (e / n) * lda];
+  __syncthreads();
+  const int r = p2_rec(upper, a, n, lanes);
+  __syncthreads();
+  // BOLA stops at the failing column with everything before it written back.
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) A[(e % n) + (e / n) * lda] = a[(e % n) + (e / n) * LDS];
+  if (r && threadIdx.x == 0) *info = col0 + r;
+}
+
+__global__ void zero_i32(int32_t *p) { *p = 0; }
+
+}  // namespace
+
+int syrk_exact(cudaStream_t s, char uplo, char trans, int64_t n, int64_t k, double alpha, const double *A,
+               int64_t lda, double beta, double *C, int64_t ldc, const int32_t *info) {
+  const bool upper = upc(uplo) == 'U', tt = upc(trans) != 'N';
+  if (n <= 0 || ((alpha == 0.0 || k <= 0) && beta == 1.0)) return 0;
+  if (beta != 1.0) {
+    syrk_beta<<<(unsigned)cdiv(n * n, 256), 256, 0, s>>>(upper, n, beta, C, ldc, info);
+    BOLA_CHECK_LAUNCH();
+  }
+  if (alpha == 0.0 || k <= 0) return 0;
+  if (n > NB) {
+    BOLA_TRY(dgemm_exact(s, tt ? 'T' : 'N', tt ? 'N' : 'T', n, n, k, alpha, A, lda, A, lda, 1.0, C, ldc, NB,
+                         info, upper ? 1 : 2));
+  }
+  syrk_diag<<<dim3(NB, (unsigned)cdiv(n, NB)), NB, 0, s>>>(upper, tt, n, k, alpha, A, lda, C, ldc, lanes(), info);
+  BOLA_CHECK_LAUNCH();
+  return 0;
+}
+
+int potrf2_rec(cudaStream_t s, char uplo, int64_t n, double *A, int64_t lda, int32_t *info, int32_t col0) {
+  const bool upper = upc(uplo) == 'U';
+  if (n == 0) return 0;
+  if (n <= NB) {
+    potrf2_block<<<1, 256, 0, s>>>(upper, (int)n, A, lda, info, col0, lanes());
+    BOLA_CHECK_LAUNCH();
+    return 0;
+  }
+  const int64_t n1 = n / 2, n2 = n - n1;
+  BOLA_TRY(potrf2_rec(s, uplo, n1, A, lda, info, col0));
+  double *a22 = A + n1 + n1 * lda;
+  if (upper) {
+    BOLA_TRY(trsm_exact(s, 'L', 'U', 'T', 'N', n1, n2, 1.0, A, lda, A + n1 * lda, lda, info));
+    BOLA_TRY(syrk_exact(s, 'U', 'T', n2, n1, -1.0, A + n1 * lda, lda, 1.0, a22, lda, info));
+  } else {
+    BOLA_TRY(trsm_exact(s, 'R', 'L', 'T', 'N', n2, n1, 1.0, A, lda, A + n1, lda, info));
+    BOLA_TRY(syrk_exact(s, 'L', 'N', n2, n1, -1.0, A + n1, lda, 1.0, a22, lda, info));
+  }
+  return potrf2_rec(s, uplo, n2, a22, lda, info, col0 + (int32_t)n1);
+}
+
+int potrf_blocked(cudaStream_t s, char uplo, int64_t n, double *A, int64_t lda, int32_t *info) {
+  zero_i32<<<1, 1, 0, s>>>(info);
+  BOLA_CHECK_LAUNCH();
+  if (NB >= n) return potrf2_rec(s, uplo, n, A, lda, info, 0);
+  const bool upper = uplo == 'U';
+  for (int64_t j = 0; j < n; j += NB) {
+    const int64_t jb = imin(NB, n - j);
+    double *ajj = A + j + j * lda;
+    const int64_t n_rem = n - j - jb;
+    if (upper) {
+      BOLA_TRY(syrk_exact(s, 'U', 'T', jb, j, -1.0, A + j * lda, lda, 1.0, ajj, lda, info));
+      BOLA_TRY(potrf2_rec(s, 'U', jb, ajj, lda, info, (int32_t)j));
+      if (n_rem > 0) {
+        BOLA_TRY(dgemm_exact(s, 'T', 'N', jb, n_rem, j, -1.0, A + j * lda, lda, A + (j + jb) * lda, lda, 1.0,
+                             A + j + (j + jb) * lda, lda, 64, info, 0));
+        BOLA_TRY(trsm_exact(s, 'L', 'U', 'T', 'N', jb, n_rem, 1.0, ajj, lda, A + j + (j + jb) * lda, lda, info));
+      }
+    } else {
+      BOLA_TRY(syrk_exact(s, 'L', 'N', jb, j, -1.0, A + j, lda, 1.0, ajj, lda, info));
+      BOLA_TRY(potrf2_rec(s, 'L', jb, ajj, lda, info, (int32_t)j));
+      if (n_rem > 0) {
+        BOLA_TRY(dgemm_exact(s, 'N', 'T', n_rem, jb, j, -1.0, A + j + jb, lda, A + j, lda, 1.0,
+                             A + j + jb + j * lda, lda, 64, info, 0));
+        BOLA_TRY(trsm_exact(s, 'R', 'L', 'T', 'N', n_rem, jb, 1.0, ajj, lda, A + j + jb + j * lda, lda, info));
+      }
+    }
+  }
+  return 0;
+}
+
+}  // namespace bola
+
+using namespace bola;
+
+extern "C" {
+
+int bola_dsyrk(char uplo, char trans, int64_t n, int64_t k, double alpha, const double *a, int64_t lda,
+               double beta, double *c, int64_t ldc, bola_stream_t stream) {
+  if (n < 0) return -3;
+  if (k < 0) return -4;
+  if (n == 0) return 0;
+  const bool tt = upc(trans) != 'N';
+  if (k > 0 && alpha != 0.0 && lda < imax(1, tt ? k : n)) return -7;
+  if (ldc < imax(1, n)) return -10;
+  return syrk_exact((cudaStream_t)stream, uplo, trans, n, k, alpha, a, lda, beta, c, ldc, nullptr);
+}
+
+int bola_dpotrf(char uplo, int64_t n, double *a, int64_t lda, int32_t *info, bola_stream_t stream) {
+  if (uplo != 'U' && uplo != 'L') return -1;  // "Argument 1 to potrf had an illegal value" (src/potrf.rs:105-107)
+  if (n < 0) return -2;
+  if (lda < imax(n, 1)) return -4;  // "Argument 4 to potrf had an illegal value" (src/potrf.rs:108-110)
+  return potrf_blocked((cudaStream_t)stream, uplo, n, a, lda, info);
+}
+
+int bola_dpotrf2(char uplo, int64_t n, double *a, int64_t lda, int32_t *info, bola_stream_t stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  if (n < 0) return -2;
+  if (lda < imax(n, 1)) return -4;
+  zero_i32<<<1, 1, 0, s>>>(info);
+  BOLA_CHECK_LAUNCH();
+  return potrf2_rec(s, uplo, n, a, lda, info, 0);
+}
+
+int bola_dpotrs(char uplo, int64_t n, int64_t nrhs, const double *fac, int64_t lda, double *b, int64_t ldb,
+                bola_stream_t stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  if (upc(uplo) != 'U' && upc(uplo) != 'L') return -1;
+  if (n < 0) return -2;
+  if (nrhs < 0) return -3;
+  if (lda < imax(1, n)) return -5;
+  if (ldb < imax(1, n)) return -7;
+  if (n == 0 || nrhs == 0) return 0;
+  if (upc(uplo) == 'L') {
+    BOLA_TRY(trsm_exact(s, 'L', 'L', 'N', 'N', n, nrhs, 1.0, fac, lda, b, ldb, nullptr));
+    return trsm_exact(s, 'L', 'L', 'T', 'N', n, nrhs, 1.0, fac, lda, b, ldb, nullptr);
+  }
+  BOLA_TRY(trsm_exact(s, 'L', 'U', 'T', 'N', n, nrhs, 1.0, fac, lda, b, ldb, nullptr));
+  return trsm_exact(s, 'L', 'U', 'N', 'N', n, nrhs, 1.0, fac, lda, b, ldb, nullptr);
+}
+
+}  // extern "C"

@@ -1,0 +1,136 @@
+/*
+ * bola_gb300.h — C ABI of the GB300 (sm_103a) implementation of BOLA's dense
+ * BLAS-3/LAPACK path.
+ *
+ * Conventions (those of BOLA, alexlovric/bola v0.1.2):
+ *   - column-major FP64 matrices, leading dimensions in elements;
+ *   - ipiv is 1-based int32 (row i was swapped with row ipiv[i]); idamax is 0-based;
+ *   - every matrix/vector pointer is a DEVICE pointer; scalars are host values;
+ *   - `stream` is a cudaStream_t (NULL = the legacy default stream); the call
+ *     enqueues its work on it and returns without waiting for the GPU;
+ *   - return value: 0 success; -i argument i is illegal (LAPACK numbering, the
+ *     arguments BOLA itself checks); values <= -1000 are BOLA_ERR_* below, with
+ *     a message from bola_last_error().  Factorisation failures that the GPU
+ *     discovers (zero pivot, matrix not positive definite) are written to the
+ *     device int32 *info as a 1-based global column, 0 when the factorisation
+ *     succeeded; the factorisation stops at that column as BOLA does.
+ *   - characters are accepted in either case with their BLAS meaning.
+ *
+ * Rounding: each routine performs, element for element, the same sequence of
+ * IEEE operations as BOLA's CPU code (same blocking, same fused/unfused
+ * multiply-adds), so results are bit-identical to BOLA's for the SIMD width
+ * selected by bola_set_simd_lanes (2 = BOLA built for aarch64/NEON, the
+ * default; 4 = BOLA built for x86_64/AVX2).
+ */
+#ifndef BOLA_GB300_H
+#define BOLA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef void *bola_stream_t; /* cudaStream_t */
+
+#define BOLA_OK 0
+#define BOLA_ERR_CUDA (-1000)        /* a CUDA runtime call failed */
+#define BOLA_ERR_NO_DEVICE (-1001)   /* no usable sm_103 device */
+#define BOLA_ERR_UNSUPPORTED (-1002) /* argument combination outside this library */
+
+/* Library identification and diagnostics. */
+const char *bola_version(void);
+const char *bola_last_error(void); /* message of this thread's last failing call */
+
+/* Which of BOLA's two SIMD builds to reproduce bit-for-bit: 2 (aarch64 NEON,
+ * default) or 4 (x86_64 AVX2).  Returns the previous value, or -1 if invalid. */
+int bola_set_simd_lanes(int lanes);
+int bola_get_simd_lanes(void);
+
+/* ---- Level 1 ---------------------------------------------------------- */
+
+/* Replaces idamax(n, x) -> usize, src/idamax.rs:23 (x86_64) / :141 (aarch64).
+ * Writes the 0-based index of the element of largest |x| (BOLA's lane-merge
+ * order on ties; NaN never selected) to the device int64 *result. */
+int bola_idamax(int64_t n, const double *x, int64_t *result, bola_stream_t stream);
+
+/* Replaces scal(n, alpha, x, incx), src/scal.rs:45. */
+int bola_dscal(int64_t n, double alpha, double *x, int64_t incx, bola_stream_t stream);
+
+/* Replaces ger(m, n, alpha, x, y, ldy, a, lda), src/ger.rs:28:  A += alpha x y^T,
+ * x contiguous, y with stride ldy. */
+int bola_dger(int64_t m, int64_t n, double alpha, const double *x, const double *y, int64_t ldy,
+              double *a, int64_t lda, bola_stream_t stream);
+
+/* Replaces dot_product(n, x, incx, y, incy) -> f64, src/utilities.rs:22 / :62.
+ * Writes the result to the device double *result. */
+int bola_ddot(int64_t n, const double *x, int64_t incx, const double *y, int64_t incy,
+              double *result, bola_stream_t stream);
+
+/* Replaces daxpy(n, alpha, x, incx, y, incy), src/utilities.rs:107 / :140. */
+int bola_daxpy(int64_t n, double alpha, const double *x, int64_t incx, double *y, int64_t incy,
+               bola_stream_t stream);
+
+/* Replaces laswp(n, a, lda, k1, k2, ipiv, incx), src/laswp.rs:22.  ipiv is a
+ * device int32 array indexed like BOLA's slice (k1, k2 1-based). */
+int bola_dlaswp(int64_t n, double *a, int64_t lda, int32_t k1, int32_t k2, const int32_t *ipiv,
+                int32_t incx, bola_stream_t stream);
+
+/* ---- BLAS 3 ----------------------------------------------------------- */
+
+/* Replaces gemm(transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc),
+ * src/gemm.rs:88:  C = alpha op(A) op(B) + beta C. */
+int bola_dgemm(char transa, char transb, int64_t m, int64_t n, int64_t k, double alpha,
+               const double *a, int64_t lda, const double *b, int64_t ldb, double beta, double *c,
+               int64_t ldc, bola_stream_t stream);
+
+/* Replaces trsm(side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb),
+ * src/trsm.rs:33:  op(A) X = alpha B (side 'L') or X op(A) = alpha B ('R'), X over B. */
+int bola_dtrsm(char side, char uplo, char transa, char diag, int64_t m, int64_t n, double alpha,
+               const double *a, int64_t lda, double *b, int64_t ldb, bola_stream_t stream);
+
+/* Replaces syrk(uplo, trans, n, k, alpha, a, lda, beta, c, ldc), src/syrk.rs:17:
+ * C = alpha A A^T + beta C ('N') or alpha A^T A + beta C ('T'), one triangle.
+ * (uplo,trans) = (L,N) and (U,T) are bit-identical to BOLA; (U,N) and (L,T)
+ * compute the BLAS definition (BOLA addresses A wrongly there once n or k
+ * exceeds 32, src/syrk.rs:80,139). */
+int bola_dsyrk(char uplo, char trans, int64_t n, int64_t k, double alpha, const double *a,
+               int64_t lda, double beta, double *c, int64_t ldc, bola_stream_t stream);
+
+/* ---- LAPACK ----------------------------------------------------------- */
+
+/* Replaces getrf(m, n, a, lda, ipiv) -> Result, src/getrf.rs:37.  Returns -4 for
+ * lda < max(1, m) (BOLA: "Argument 4 to getrf had an illegal value").  *info
+ * (device) = 0, or the 1-based column whose pivot is exactly zero (BOLA:
+ * "Matrix is singular..."), in which case A and ipiv stay as BOLA leaves them. */
+int bola_dgetrf(int64_t m, int64_t n, double *a, int64_t lda, int32_t *ipiv, int32_t *info,
+                bola_stream_t stream);
+
+/* Replaces getrf2(m, n, a, lda, ipiv) -> Result, src/getrf2.rs:39 (recursive LU). */
+int bola_dgetrf2(int64_t m, int64_t n, double *a, int64_t lda, int32_t *ipiv, int32_t *info,
+                 bola_stream_t stream);
+
+/* Replaces potrf(uplo, n, a, lda) -> Result, src/potrf.rs:101.  Returns -1 for
+ * uplo other than 'U'/'L' (BOLA requires upper case here), -4 for
+ * lda < max(1, n).  *info (device) = 0 or the 1-based column where A is found
+ * not positive definite. */
+int bola_dpotrf(char uplo, int64_t n, double *a, int64_t lda, int32_t *info, bola_stream_t stream);
+
+/* Replaces potrf2(uplo, n, a, lda) -> Result, src/potrf2.rs:25 (recursive Cholesky). */
+int bola_dpotrf2(char uplo, int64_t n, double *a, int64_t lda, int32_t *info, bola_stream_t stream);
+
+/* Solve with the LU factors of bola_dgetrf: laswp on B, then unit-lower and
+ * upper triangular solves — the composite BOLA users write by hand (BOLA has
+ * no getrs; src/laswp.rs:22 + src/trsm.rs:95,135).  B (n x nrhs) is overwritten. */
+int bola_dgetrs(int64_t n, int64_t nrhs, const double *lu, int64_t lda, const int32_t *ipiv,
+                double *b, int64_t ldb, bola_stream_t stream);
+
+/* Solve with the Cholesky factor of bola_dpotrf (uplo 'L': L then L^T solves,
+ * src/trsm.rs:95,174; 'U': U^T then U, src/trsm.rs:213,135). */
+int bola_dpotrs(char uplo, int64_t n, int64_t nrhs, const double *fac, int64_t lda, double *b,
+                int64_t ldb, bola_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BOLA_GB300_H */
