@@ -64,70 +64,96 @@ syrk_diag(bool upper, bool trans_t, int64_t n, int64_t k, double alpha, const do
 // ---- potrf2 on one <=32 x 32 block in shared memory (src/potrf2.rs:36-80) ----
 constexpr int LDS = NB;
 
-__device__ int p2_rec(bool upper, double *a, int n, int lanes) {
+// BOLA's recursion (halve, factor the leading half, trsm + syrk, factor the
+// trailing half) walked with an explicit stack: device recursion would need
+// more per-thread stack than the default.  Every thread runs the same walk.
+// Returns 0 or the 1-based failing column inside the block.
+__device__ int p2_walk(bool upper, double *a0, int n, int lanes) {
+  struct Frame {
+    int off, n, phase;
+  };
+  Frame st[8];
+  int sp = 0;
+  st[0] = {0, n, 0};
   const int tid = threadIdx.x;
-  if (n == 0) return 0;
-  if (n == 1) {
-    const double a11 = a[0];
-    __syncthreads();
-    if (!(a11 > 0.0)) return 1;
-    if (tid == 0) a[0] = sqrt(a11);
-    __syncthreads();
-    return 0;
-  }
-  const int n1 = n / 2, n2 = n - n1;
-  int r = p2_rec(upper, a, n1, lanes);
-  if (r) return r;
-  double *a22 = a + n1 + n1 * LDS;
-  if (upper) {
-    double *a12 = a + n1 * LDS;
-    // trsm('L','U','T','N', n1, n2, 1, a11, a12): trsm_ltu base, a thread per column
-    if (tid < n2) {
-      for (int i = 0; i < n1; ++i) {
-        double t = a12[i + tid * LDS];
-        for (int k = 0; k < i; ++k) t = sub_prod(t, a[k + i * LDS], a12[k + tid * LDS]);
-        t = t / a[i + i * LDS];
-        a12[i + tid * LDS] = t;
-      }
+  while (sp >= 0) {
+    Frame &f = st[sp];
+    double *a = a0 + f.off + f.off * LDS;
+    if (f.n == 0) {
+      --sp;
+      continue;
     }
-    __syncthreads();
-    // syrk('U','T', n2, n1, -1, a12, 1, a22): dot path
-    for (int e = tid; e < n2 * n2; e += blockDim.x) {
-      const int ii = e % n2, jj = e / n2;
-      if (ii > jj) continue;
-      const double t = dot_exact(n1, a12 + ii * LDS, 1, a12 + jj * LDS, 1, lanes);
-      a22[ii + jj * LDS] = add_prod(a22[ii + jj * LDS], -1.0, t);
+    if (f.n == 1) {  // src/potrf2.rs:41-48
+      const double a11 = a[0];
+      __syncthreads();
+      if (!(a11 > 0.0)) return f.off + 1;
+      if (tid == 0) a[0] = sqrt(a11);
+      __syncthreads();
+      --sp;
+      continue;
     }
-  } else {
-    double *a21 = a + n1;
-    // trsm('R','L','T','N', n2, n1, 1, a11, a21): trsm_rtl base, a thread per row
-    if (tid < n2) {
-      for (int j = 0; j < n1; ++j) {
-        double b = a21[tid + j * LDS];
-        for (int k = 0; k < j; ++k) {
-          const double ajk = a[j + k * LDS];
-          if (ajk != 0.0) b = sub_prod(b, ajk, a21[tid + k * LDS]);
+    const int n1 = f.n / 2, n2 = f.n - n1;
+    if (f.phase == 0) {
+      f.phase = 1;
+      st[++sp] = {f.off, n1, 0};
+      continue;
+    }
+    if (f.phase == 2) {
+      --sp;
+      continue;
+    }
+    double *a22 = a + n1 + n1 * LDS;
+    if (upper) {
+      double *a12 = a + n1 * LDS;
+      // trsm('L','U','T','N', n1, n2, 1, a11, a12): trsm_ltu base, a thread per column
+      if (tid < n2) {
+        for (int i = 0; i < n1; ++i) {
+          double t = a12[i + tid * LDS];
+          for (int k = 0; k < i; ++k) t = sub_prod(t, a[k + i * LDS], a12[k + tid * LDS]);
+          t = t / a[i + i * LDS];
+          a12[i + tid * LDS] = t;
         }
-        b = __dmul_rn(b, 1.0 / a[j + j * LDS]);
-        a21[tid + j * LDS] = b;
+      }
+      __syncthreads();
+      // syrk('U','T', n2, n1, -1, a12, 1, a22): dot path
+      for (int e = tid; e < n2 * n2; e += blockDim.x) {
+        const int ii = e % n2, jj = e / n2;
+        if (ii > jj) continue;
+        const double t = dot_exact(n1, a12 + ii * LDS, 1, a12 + jj * LDS, 1, lanes);
+        a22[ii + jj * LDS] = add_prod(a22[ii + jj * LDS], -1.0, t);
+      }
+    } else {
+      double *a21 = a + n1;
+      // trsm('R','L','T','N', n2, n1, 1, a11, a21): trsm_rtl base, a thread per row
+      if (tid < n2) {
+        for (int j = 0; j < n1; ++j) {
+          double b = a21[tid + j * LDS];
+          for (int k = 0; k < j; ++k) {
+            const double ajk = a[j + k * LDS];
+            if (ajk != 0.0) b = sub_prod(b, ajk, a21[tid + k * LDS]);
+          }
+          b = __dmul_rn(b, 1.0 / a[j + j * LDS]);
+          a21[tid + j * LDS] = b;
+        }
+      }
+      __syncthreads();
+      // syrk('L','N', n2, n1, -1, a21, 1, a22): daxpy path
+      for (int e = tid; e < n2 * n2; e += blockDim.x) {
+        const int ii = e % n2, jj = e / n2;
+        if (ii < jj) continue;
+        double c = a22[ii + jj * LDS];
+        for (int l = 0; l < n1; ++l) {
+          const double t = -a21[jj + l * LDS];
+          if (t != 0.0) c = daxpy_elem(c, t, a21[ii + l * LDS], ii - jj, n2 - jj, lanes);
+        }
+        a22[ii + jj * LDS] = c;
       }
     }
     __syncthreads();
-    // syrk('L','N', n2, n1, -1, a21, 1, a22): daxpy path
-    for (int e = tid; e < n2 * n2; e += blockDim.x) {
-      const int ii = e % n2, jj = e / n2;
-      if (ii < jj) continue;
-      double c = a22[ii + jj * LDS];
-      for (int l = 0; l < n1; ++l) {
-        const double t = -a21[jj + l * LDS];
-        if (t != 0.0) c = daxpy_elem(c, t, a21[ii + l * LDS], ii - jj, n2 - jj, lanes);
-      }
-      a22[ii + jj * LDS] = c;
-    }
+    f.phase = 2;
+    st[++sp] = {f.off + n1, n2, 0};
   }
-  __syncthreads();
-  r = p2_rec(upper, a22, n2, lanes);
-  return r ? r + n1 : 0;
+  return 0;
 }
 
 __global__ void __launch_bounds__(256)
@@ -136,7 +162,7 @@ potrf2_block(bool upper, int n, double *A, int64_t lda, int32_t *info, int32_t c
   if (stop_flag(info)) return;
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) a[(e % n) + (e / n) * LDS] = A[(e % n) + (e / n) * lda];
   __syncthreads();
-  const int r = p2_rec(upper, a, n, lanes);
+  const int r = p2_walk(upper, a, n, lanes);
   __syncthreads();
   // BOLA stops at the failing column with everything before it written back.
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) A[(e % n) + (e / n) * lda] = a[(e % n) + (e / n) * LDS];
