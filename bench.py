@@ -1,0 +1,401 @@
+#!/usr/bin/env python
+"""Dense LU solve throughput on one GB300 (the BOLA getrf + trsm solve path).
+
+Workload: n = 8192, 16 right-hand sides, A = Q1 diag(sigma) Q2 with Q1, Q2
+from the Householder QR of Gaussian matrices (seed 3), sigma geometric from 1
+to 1/kappa; the timed steps rotate over kappa = 1e2, 1e6, 1e10; b = A x_true,
+x_true uniform [-1, 1).  One step = one complete solve of A x = b (factor +
+solve), whose normwise backward error is checked to be <= 1e-14.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+ours       the C-ABI library on the GPU; `value` has inputs resident in HBM,
+           `e2e` copies A and b from pinned host memory every step and reads
+           x back.  The library's device profiler (CUDA events on the launching
+           stream) gives the per-kernel roofline numbers and the launch count.
+reference  BOLA's CPU algorithm (the C restatement under oracle/, all host
+           threads) on the same inputs.
+Under torchrun each rank solves its own systems (replicas, no collective);
+value = all ranks' solves / max rank time.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+import torch  # noqa: E402
+
+METRIC = "solves/s and p99 latency, mixed-prec IR vs plain FP64 at ≤1e-14 backward error"
+KAPPAS = (1e2, 1e6, 1e10)
+BERR_TARGET = 1e-14
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=8192)
+    ap.add_argument("--nrhs", type=int, default=16)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- inputs ----
+
+def make_systems(n, nrhs, device):
+    """Config-3 systems, built with torch on `device` (input preparation only)."""
+    from bola_gb300 import workloads as wl
+    g1 = torch.from_numpy(wl.gaussian_matrix(n, n, seed=3, stream="q1")).to(device)
+    g2 = torch.from_numpy(wl.gaussian_matrix(n, n, seed=3, stream="q2")).to(device)
+    q1, _ = torch.linalg.qr(g1)
+    del g1
+    q2, _ = torch.linalg.qr(g2)
+    del g2
+    x_true = torch.from_numpy(wl.uniform_matrix(n, nrhs, seed=3, lo=-1.0, hi=1.0, stream="x")).to(device)
+    systems = []
+    for kappa in KAPPAS:
+        sigma = torch.logspace(0.0, -np.log10(kappa), n, dtype=torch.float64, device=device)
+        A = (q1 * sigma) @ q2
+        b = A @ x_true
+        # column-major flat storage, as the C ABI takes it
+        systems.append({"kappa": kappa, "A": A.t().contiguous().reshape(-1), "b": b.t().contiguous().reshape(-1),
+                        "x_true": x_true})
+    del q1, q2
+    torch.cuda.synchronize(device)
+    return systems
+
+
+def backward_error(A_flat, x_flat, b_flat, n, nrhs):
+    """max over right-hand sides of ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf)."""
+    A = A_flat.reshape(n, n).t()
+    X = x_flat.reshape(nrhs, n).t()
+    B = b_flat.reshape(nrhs, n).t()
+    R = B - A @ X
+    a_inf = A.abs().sum(dim=1).max()
+    num = R.abs().max(dim=0).values
+    den = a_inf * X.abs().max(dim=0).values + B.abs().max(dim=0).values
+    return float((num / den).max())
+
+
+# ---------------------------------------------------------------- clocks ----
+
+class ClockSampler:
+    """nvidia-smi SM clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path:
+            return None
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v.lower().startswith("active")})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "power_w_max": max(r[2] for r in rows), "samples": len(rows), "reasons": reasons}
+
+
+# ---------------------------------------------------------------- ours ----
+
+class Solver:
+    """Plain FP64 solve through the C ABI: getrf (BOLA's blocked LU, exact)
+    then getrs (laswp + two trsm), on one stream."""
+
+    def __init__(self, n, nrhs, device):
+        from bola_gb300 import _lib
+        self.L = _lib.load()
+        self.n, self.nrhs = n, nrhs
+        self.work = torch.empty(n * n, dtype=torch.float64, device=device)
+        self.x = torch.empty(n * nrhs, dtype=torch.float64, device=device)
+        self.ipiv = torch.empty(n, dtype=torch.int32, device=device)
+        self.info = torch.zeros(1, dtype=torch.int32, device=device)
+        self.stream = torch.cuda.current_stream(device)
+        self.sp = ctypes.c_void_p(self.stream.cuda_stream)
+
+    def _p(self, t):
+        return ctypes.c_void_p(t.data_ptr())
+
+    def solve_device(self, A, b):
+        """A, b resident on the device; result in self.x (device)."""
+        self.work.copy_(A)
+        self.x.copy_(b)
+        self._factor_solve()
+
+    def solve_host(self, A_host, b_host, x_host):
+        """Pinned host A, b in; pinned host x out."""
+        self.work.copy_(A_host, non_blocking=True)
+        self.x.copy_(b_host, non_blocking=True)
+        self._factor_solve()
+        x_host.copy_(self.x, non_blocking=True)
+
+    def _factor_solve(self):
+        n, L = self.n, self.L
+        st = L.bola_dgetrf(n, n, self._p(self.work), n, self._p(self.ipiv), self._p(self.info), self.sp)
+        if st != 0:
+            raise RuntimeError(f"bola_dgetrf status {st}: {L.bola_last_error().decode()}")
+        st = L.bola_dgetrs(n, self.nrhs, self._p(self.work), n, self._p(self.ipiv), self._p(self.x), n, self.sp)
+        if st != 0:
+            raise RuntimeError(f"bola_dgetrs status {st}: {L.bola_last_error().decode()}")
+
+
+def time_steps(fn, steps, stream):
+    """CUDA-event time of each step on `stream`; synchronised on both sides."""
+    torch.cuda.synchronize()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    evs[0].record(stream)
+    for k in range(steps):
+        fn(k)
+        evs[k + 1].record(stream)
+    torch.cuda.synchronize()
+    per = [evs[k].elapsed_time(evs[k + 1]) for k in range(steps)]
+    total = evs[0].elapsed_time(evs[-1])
+    return total, per
+
+
+def run_ours(args, rank, world, device):
+    from bola_gb300 import api
+    torch.cuda.set_device(device)
+    n, nrhs = args.n, args.nrhs
+    systems = make_systems(n, nrhs, device)
+    solver = Solver(n, nrhs, device)
+    stream = solver.stream
+    peak_fp64 = api.measure_fp64_peak()
+
+    def step(k):
+        s = systems[k % len(systems)]
+        solver.solve_device(s["A"], s["b"])
+
+    for k in range(args.warmup):
+        step(k)
+    torch.cuda.synchronize()
+    # check every system once (outside the timed region)
+    berr = {}
+    for s in systems:
+        solver.solve_device(s["A"], s["b"])
+        torch.cuda.synchronize()
+        if int(solver.info.item()) != 0:
+            raise RuntimeError(f"getrf info {solver.info.item()} for kappa {s['kappa']}")
+        berr[f"{s['kappa']:.0e}"] = backward_error(s["A"], solver.x, s["b"], n, nrhs)
+
+    if world > 1:
+        torch.distributed.barrier()
+    api.profile_reset()
+    api.profile_enable(True)
+    with ClockSampler(device.index if device.index is not None else 0) as clk:
+        total_ms, per = time_steps(step, args.steps, stream)
+    api.profile_enable(False)
+    prof = api.profile_read()
+    if world > 1:
+        torch.distributed.barrier()
+
+    # end to end: pinned host buffers, copies inside the timed region
+    host = [{"A": s["A"].cpu().pin_memory(), "b": s["b"].cpu().pin_memory()} for s in systems]
+    x_host = torch.empty(n * nrhs, dtype=torch.float64).pin_memory()
+
+    def step_e2e(k):
+        h = host[k % len(host)]
+        solver.solve_host(h["A"], h["b"], x_host)
+
+    for k in range(min(args.warmup, 1)):
+        step_e2e(k)
+    e2e_total, e2e_per = time_steps(step_e2e, args.steps, stream)
+
+    t = torch.tensor([total_ms, e2e_total], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    total_ms, e2e_total = float(t[0]), float(t[1])
+    if rank != 0:
+        return None
+
+    # roofline of the dominant kernel (largest share of device time)
+    dom_name, dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    prof_total = sum(v["ms"] for v in prof.values())
+    achieved = dom["flops"] / (dom["ms"] * 1e-3) / 1e12  # TFLOP/s
+    peak = peak_fp64 / 1e3
+    kernels = {k: {"scopes": v["calls"], "launches": v["launches"], "ms": round(v["ms"], 3),
+                   "share": round(v["ms"] / prof_total, 4),
+                   "tflops": round(v["flops"] / max(v["ms"], 1e-9) / 1e9, 4) if v["flops"] else None}
+               for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])}
+    launches = int(sum(v["launches"] for v in prof.values()))
+
+    value = world * args.steps / (total_ms / 1e3)
+    out = {
+        "metric": METRIC, "value": round(value, 4), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: A = Q1 diag(sigma) Q2, Q from Householder QR of Gaussian matrices (seed 3), sigma "
+                "geometric 1..1/kappa, kappa in {1e2,1e6,1e10} rotating per step; b = A x_true, x_true U[-1,1)",
+        "config": {"workload": f"dense LU solve n={n} nrhs={nrhs} (BOLA getrf + laswp + 2 trsm), "
+                               f"backward error <= {BERR_TARGET:g}",
+                   "path": "plain FP64, BOLA-exact blocked LU (NB=32) + triangular solves",
+                   "replicas": "one independent solve stream per GPU (no collective)",
+                   "l2": "inputs larger than L2 (512 MiB matrix per step)"},
+        "latency_ms": {"p50": round(statistics.median(per), 3),
+                       "p99": round(float(np.percentile(per, 99)), 3)},
+        "backward_error": berr,
+        "backward_error_ok": all(v <= BERR_TARGET for v in berr.values()),
+        "e2e": {"value": round(world * args.steps / (e2e_total / 1e3), 4), "unit": "solves/s",
+                "h2d_bytes_per_step": 8 * (n * n + n * nrhs), "d2h_bytes_per_step": 8 * n * nrhs},
+        "roofline": {"kernel": dom_name, "bound": "fp64", "achieved": round(achieved, 4), "peak": round(peak, 4),
+                     "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
+                     "peak_source": "FP64 DFMA throughput measured in this run (bola_measure_fp64_peak); "
+                                    "GB300 FP64 runs on the DFMA pipe, not the tensor cores",
+                     "traffic": None},
+        "kernels": kernels,
+        "gpu_launches": launches,
+    }
+    clocks = clk.summary()
+    if clocks is not None:
+        out["clocks"] = clocks
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(systems[0], n, nrhs, budget_s=12.0)
+    return out
+
+
+# ---------------------------------------------------------------- CPU ----
+
+def cpu_solve_once(A_np, b_np):
+    import oracle
+    A = A_np.copy(order="F")
+    B = b_np.copy(order="F")
+    t0 = time.perf_counter()
+    info, _ = oracle.solve_lu(A, B)
+    dt = time.perf_counter() - t0
+    if info != 0:
+        raise RuntimeError(f"oracle getrf info {info}")
+    return dt, B
+
+
+def host_system(sysd, n, nrhs):
+    A = sysd["A"].cpu().numpy().reshape(n, n).T  # column-major view -> F-ordered array
+    b = sysd["b"].cpu().numpy().reshape(nrhs, n).T
+    return np.asfortranarray(A), np.asfortranarray(b)
+
+
+def cpu_baseline(sysd, n, nrhs, budget_s):
+    """BOLA restated in C (oracle/) on all host threads, a bounded sample of
+    complete n x n solves (at least one)."""
+    import oracle
+    oracle.lib()
+    threads = oracle.get_threads()
+    A, b = host_system(sysd, n, nrhs)
+    times = []
+    while True:
+        dt, _ = cpu_solve_once(A, b)
+        times.append(dt)
+        if sum(times) + dt > budget_s:
+            break
+    v = len(times) / sum(times)
+    return {"value": round(v, 5), "unit": "solves/s", "cores": threads, "kind": "port",
+            "sample": f"{len(times)} complete solve(s) n={n} nrhs={nrhs} (getrf + laswp + 2 trsm), kappa=1e2; "
+                      f"BOLA restated in C (Rust not available to build BOLA)"}
+
+
+def run_reference(args, device):
+    import oracle
+    n, nrhs = args.n, args.nrhs
+    oracle.lib()
+    systems = make_systems(n, nrhs, device)
+    host = [host_system(s, n, nrhs) for s in systems]
+    del systems
+    torch.cuda.empty_cache()
+    threads = oracle.get_threads()
+    # warm-up: one solve (bounds the rest of the run to a few minutes)
+    t_warm, _ = cpu_solve_once(*host[0])
+    steps = max(1, min(args.steps, int(150.0 / max(t_warm, 1e-3))))
+    per = []
+    for k in range(steps):
+        dt, _ = cpu_solve_once(*host[k % len(host)])
+        per.append(dt)
+    total = sum(per)
+    value = steps / total
+    sample = (f"{steps} complete solve(s) n={n} nrhs={nrhs} rotating kappa (getrf + laswp + 2 trsm) after 1 warm-up; "
+              f"BOLA restated in C on {threads} host threads")
+    return {
+        "metric": METRIC, "impl": "reference", "value": round(value, 5), "unit": "solves/s", "n_gpus": 1,
+        "steps": steps, "warmup": 1, "ms_per_step": round(1e3 * total / steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic, same systems as --impl ours",
+        "config": {"workload": f"dense LU solve n={n} nrhs={nrhs} (BOLA getrf + laswp + 2 trsm), "
+                               f"backward error <= {BERR_TARGET:g}",
+                   "path": "BOLA's CPU algorithm (C restatement, OpenMP in place of Rayon)"},
+        "latency_ms": {"p50": round(1e3 * statistics.median(per), 3),
+                       "p99": round(1e3 * float(np.percentile(per, 99)), 3)},
+        "cpu_baseline": {"value": round(value, 5), "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 5), "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        out = run_reference(args, torch.device("cuda", local))
+        print(json.dumps(out), flush=True)
+        return 0
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    if world > 1:
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        torch.distributed.init_process_group("nccl", device_id=device)
+    out = run_ours(args, rank, world, device)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -195,3 +195,52 @@ def potrs(uplo, n, nrhs, fac, lda, b, ldb):
     """Two triangular solves with potrf's factor."""
     _check(_lib.load().bola_dpotrs(_ch(uplo), n, nrhs, _ptr(fac), lda, _ptr(b), ldb, _stream()), "potrs")
     _sync()
+
+
+# ---- device-time profiler (BOLA's `profiling` feature, src/profiling.rs) ----
+
+def profile_enable(on=True):
+    return bool(_lib.load().bola_profile_enable(1 if on else 0))
+
+
+def profile_reset():
+    _check(_lib.load().bola_profile_reset(), "profile_reset")
+
+
+def profile_read():
+    """{name: {"calls", "ms", "flops", "bytes"}} accumulated since the last reset."""
+    L = _lib.load()
+    n = L.bola_profile_count()
+    if n < 0:
+        _check(n, "profile_count")
+    out = {}
+    for i in range(n):
+        name = ctypes.create_string_buffer(64)
+        calls, launches = ctypes.c_int64(), ctypes.c_int64()
+        ms, fl, by = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _check(L.bola_profile_read(i, name, 64, ctypes.byref(calls), ctypes.byref(launches), ctypes.byref(ms),
+                                   ctypes.byref(fl), ctypes.byref(by)), "profile_read")
+        out[name.value.decode()] = {"calls": calls.value, "launches": launches.value, "ms": ms.value,
+                                    "flops": fl.value, "bytes": by.value}
+    return out
+
+
+def measure_fp64_peak():
+    """FP64 DFMA throughput of this device in GFLOP/s (bola_measure_fp64_peak)."""
+    v = ctypes.c_double()
+    _check(_lib.load().bola_measure_fp64_peak(ctypes.byref(v)), "measure_fp64_peak")
+    return v.value
+
+
+def print_profile(prof=None):
+    """Report in the shape of BOLA's print_profile (src/profiling.rs:70-115)."""
+    prof = profile_read() if prof is None else prof
+    if not prof:
+        print("no profile data")
+        return
+    total = max(v["ms"] for v in prof.values())
+    print(f"{'routine':<20}{'calls':>8}{'ms total':>12}{'us/call':>12}{'GFLOP/s':>12}{'% of max':>10}")
+    for name, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"]):
+        gf = v["flops"] / (v["ms"] * 1e6) if v["ms"] > 0 else 0.0
+        print(f"{name:<20}{v['calls']:>8}{v['ms']:>12.3f}{1e3 * v['ms'] / max(v['calls'], 1):>12.1f}"
+              f"{gf:>12.1f}{100.0 * v['ms'] / total:>9.1f}%")

@@ -11,6 +11,7 @@
 #include <cstdint>
 
 #include "bola_gb300.h"
+#include "profile.cuh"
 
 namespace bola {
 
@@ -248,6 +249,63 @@ __device__ __forceinline__ int compose_swaps(const SwapPlan &p, const int32_t *i
     const int64_t t = src[a];
     src[a] = src[b];
     src[b] = t;
+  }
+  return cnt;
+}
+
+// Warp-cooperative compose_swaps for at most 32 interchanges (the getrf panel
+// case): lanes prefetch the pivots, each lane keeps entries lane and lane+32 in
+// registers, lookups are ballots.  Called by all 32 lanes of one warp; writes
+// rows/src (>= 64 entries) and returns the count on every lane.
+__device__ __forceinline__ int compose_swaps_warp(const SwapPlan &p, const int32_t *ipiv, int64_t *rows,
+                                                  int64_t *src) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int nsw = p.i_inc > 0 ? p.i2 - p.i1 + 1 : p.i1 - p.i2 + 1;
+  const int64_t my_ip = lane < nsw ? (int64_t)ipiv[p.ix0 + (int64_t)lane * p.incx] : 0;
+  int64_t R0 = -1, S0 = -1, R1 = -1, S1 = -1;
+  int cnt = 0;
+  for (int t = 0; t < nsw; ++t) {
+    const int32_t i = p.i1 + t * p.i_inc;
+    const int64_t ip = __shfl_sync(FULL, my_ip, t);
+    if (ip == (int64_t)i) continue;
+    const int64_t want[2] = {(int64_t)i - 1, ip - 1};
+    int slot[2];
+#pragma unroll
+    for (int w = 0; w < 2; ++w) {
+      const unsigned ma = __ballot_sync(FULL, lane < cnt && R0 == want[w]);
+      const unsigned mb = __ballot_sync(FULL, lane + 32 < cnt && R1 == want[w]);
+      int s = ma ? __ffs(ma) - 1 : (mb ? 32 + __ffs(mb) - 1 : -1);
+      if (s < 0) {
+        s = cnt++;
+        if (lane == (s & 31)) {
+          if (s < 32) {
+            R0 = want[w];
+            S0 = want[w];
+          } else {
+            R1 = want[w];
+            S1 = want[w];
+          }
+        }
+      }
+      slot[w] = s;
+    }
+    const int64_t sa = __shfl_sync(FULL, slot[0] < 32 ? S0 : S1, slot[0] & 31);
+    const int64_t sb = __shfl_sync(FULL, slot[1] < 32 ? S0 : S1, slot[1] & 31);
+    if (lane == (slot[0] & 31)) {
+      if (slot[0] < 32) S0 = sb; else S1 = sb;
+    }
+    if (lane == (slot[1] & 31)) {
+      if (slot[1] < 32) S0 = sa; else S1 = sa;
+    }
+  }
+  if (lane < cnt) {
+    rows[lane] = R0;
+    src[lane] = S0;
+  }
+  if (lane + 32 < cnt) {
+    rows[lane + 32] = R1;
+    src[lane + 32] = S1;
   }
   return cnt;
 }

@@ -305,6 +305,8 @@ int dgemm_exact(cudaStream_t s, char ta, char tb, int64_t m, int64_t n, int64_t 
       const double bytes = 8.0 * (double)nchunks * (double)m8 * (double)n4;
       partial = nsplit >= 2 && bytes <= (1u << 30);
     }
+    ProfScope prof(s, "dgemm", 2.0 * (double)m8 * (double)n4 * (double)K,
+                   8.0 * ((double)m8 * K + (double)K * n4 + 2.0 * (double)m8 * n4), partial ? 2 : 1);
     if (partial) {
       Scratch P;
       BOLA_TRY(P.alloc((size_t)(8 * nchunks * m8 * n4), s));
@@ -337,6 +339,7 @@ int dgemm_exact(cudaStream_t s, char ta, char tb, int64_t m, int64_t n, int64_t 
   }
   const int64_t ne = (m - m8) * n + m8 * (n - n4);
   if (ne > 0) {
+    ProfScope prof(s, "dgemm_edge", 2.0 * (double)ne * (double)K);
     const unsigned g = (unsigned)cdiv(ne, 128);
 #define BOLA_LE(a, b) \
   gemm_edge<a, b><<<g, 128, 0, s>>>(m, n, m8, n4, K, alpha, A, lda, B, ldb, beta, C, ldc, info, tri)

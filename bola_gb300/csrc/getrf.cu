@@ -270,14 +270,15 @@ step_swap_trsm(double *A, int64_t lda, int64_t n, int64_t j, int jb, const int32
   __shared__ double L[PNB * PNB];
   __shared__ int cnt;
   if (stop_flag(info)) return;
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 32) {
     SwapPlan p;
     p.ix0 = j;
     p.i1 = (int32_t)(j + 1);
     p.i2 = (int32_t)(j + jb);
     p.i_inc = 1;
     p.incx = 1;
-    cnt = compose_swaps(p, ipiv, rows, src);
+    const int c = compose_swaps_warp(p, ipiv, rows, src);
+    if (threadIdx.x == 0) cnt = c;
   }
   for (int e = threadIdx.x; e < jb * jb; e += blockDim.x) {
     const int r = e % jb, c = e / jb;
@@ -312,6 +313,9 @@ __global__ void zero_i32(int32_t *p) { *p = 0; }
 // the device can co-schedule.
 int launch_panel(cudaStream_t s, double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_t *info,
                  int32_t add_on_success, int32_t col0) {
+  double fl = 0.0;
+  for (int j = 0; j < nb && j < mp; ++j) fl += (double)(mp - j - 1) * (1.0 + 2.0 * (nb - j - 1));
+  ProfScope prof(s, "getrf_panel", fl, 16.0 * (double)mp * nb);
   int C = (int)imin(MAXC, imax(1, cdiv(mp, 256)));
   for (;; C = C > 1 ? (C + 1) / 2 : 0) {
     if (C == 0) return fail(BOLA_ERR_CUDA, "panel_lu: no cluster size could be scheduled");
@@ -351,6 +355,7 @@ int launch_panel(cudaStream_t s, double *A, int64_t lda, int64_t mp, int nb, int
 int iterative(cudaStream_t s, int64_t m, int64_t n, double *A, int64_t lda, int32_t *ipiv, int32_t *info,
               int32_t col0, int32_t add_on_success) {
   if (n <= PNB) return launch_panel(s, A, lda, m, (int)n, ipiv, info, add_on_success, col0);
+  ProfScope prof(s, "getrf_panel_wide", 2.0 * (double)m * m * n);
   panel_lu_wide<<<1, PT, 0, s>>>(A, lda, m, n, ipiv, info, col0, lanes());
   BOLA_CHECK_LAUNCH();
   return ipiv_add(s, ipiv, imin(m, n), add_on_success, info);
@@ -378,7 +383,10 @@ int getrf2_rec(cudaStream_t s, int64_t m, int64_t n, double *A, int64_t lda, int
 
 // src/getrf.rs:37-101
 int getrf_blocked(cudaStream_t s, int64_t m, int64_t n, double *A, int64_t lda, int32_t *ipiv, int32_t *info) {
-  zero_i32<<<1, 1, 0, s>>>(info);
+  {
+    ProfScope prof(s, "info_init");
+    zero_i32<<<1, 1, 0, s>>>(info);
+  }
   BOLA_CHECK_LAUNCH();
   if (m == 0 || n == 0) return 0;
   const int64_t min_mn = imin(m, n);
@@ -388,6 +396,7 @@ int getrf_blocked(cudaStream_t s, int64_t m, int64_t n, double *A, int64_t lda, 
     BOLA_TRY(launch_panel(s, A + j + j * lda, lda, m - j, jb, ipiv + j, info, (int32_t)j, (int32_t)j));
     const int64_t others = n - jb;
     if (others > 0) {
+      ProfScope prof(s, "getrf_swap_trsm", (double)jb * (jb - 1) * (double)(n - j - jb), 32.0 * jb * (double)others);
       step_swap_trsm<<<(unsigned)cdiv(others, 8), 256, 0, s>>>(A, lda, n, j, jb, ipiv, info, lanes());
       BOLA_CHECK_LAUNCH();
     }
@@ -420,7 +429,10 @@ int bola_dgetrf2(int64_t m, int64_t n, double *a, int64_t lda, int32_t *ipiv, in
   if (m < 0) return -1;
   if (n < 0) return -2;
   if (lda < imax(m, 1)) return -4;  // src/getrf2.rs:43-45
-  zero_i32<<<1, 1, 0, s>>>(info);
+  {
+    ProfScope prof(s, "info_init");
+    zero_i32<<<1, 1, 0, s>>>(info);
+  }
   BOLA_CHECK_LAUNCH();
   return getrf2_rec(s, m, n, a, lda, ipiv, info, 0);
 }

@@ -122,7 +122,10 @@ __global__ void laswp_short(int64_t n, double *A, int64_t lda, SwapPlan plan, co
   __shared__ int64_t rows[64], src[64];
   __shared__ int cnt;
   if (stop_flag(info)) return;
-  if (threadIdx.x == 0) cnt = compose_swaps(plan, ipiv, rows, src);
+  if (threadIdx.x < 32) {
+    const int c = compose_swaps_warp(plan, ipiv, rows, src);
+    if (threadIdx.x == 0) cnt = c;
+  }
   __syncthreads();
   const int warps = blockDim.x >> 5, lane = threadIdx.x & 31;
   const int64_t col = (int64_t)blockIdx.x * warps + (threadIdx.x >> 5);
@@ -176,6 +179,7 @@ int laswp_exact(cudaStream_t s, int64_t n, double *A, int64_t lda, int32_t k1, i
     p.i_inc = -1;
   }
   p.incx = incx;
+  ProfScope prof(s, "laswp", 0.0, 32.0 * (double)n * ((int64_t)k2 - k1 + 1));
   if ((int64_t)k2 - k1 + 1 <= 32) {
     const int warps = 8;
     laswp_short<<<(unsigned)cdiv(n, warps), 32 * warps, 0, s>>>(n, A, lda, p, ipiv, info);
@@ -188,6 +192,7 @@ int laswp_exact(cudaStream_t s, int64_t n, double *A, int64_t lda, int32_t k1, i
 
 int ipiv_add(cudaStream_t s, int32_t *ipiv, int64_t count, int32_t add, const int32_t *info) {
   if (count <= 0 || add == 0) return 0;
+  ProfScope prof(s, "ipiv_add");
   ipiv_add_kernel<<<(unsigned)cdiv(count, 256), 256, 0, s>>>(ipiv, count, add, info);
   BOLA_CHECK_LAUNCH();
   return 0;

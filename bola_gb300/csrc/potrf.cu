@@ -178,6 +178,7 @@ int syrk_exact(cudaStream_t s, char uplo, char trans, int64_t n, int64_t k, doub
   const bool upper = upc(uplo) == 'U', tt = upc(trans) != 'N';
   if (n <= 0 || ((alpha == 0.0 || k <= 0) && beta == 1.0)) return 0;
   if (beta != 1.0) {
+    ProfScope prof(s, "syrk_beta", (double)n * n);
     syrk_beta<<<(unsigned)cdiv(n * n, 256), 256, 0, s>>>(upper, n, beta, C, ldc, info);
     BOLA_CHECK_LAUNCH();
   }
@@ -186,6 +187,7 @@ int syrk_exact(cudaStream_t s, char uplo, char trans, int64_t n, int64_t k, doub
     BOLA_TRY(dgemm_exact(s, tt ? 'T' : 'N', tt ? 'N' : 'T', n, n, k, alpha, A, lda, A, lda, 1.0, C, ldc, NB,
                          info, upper ? 1 : 2));
   }
+  ProfScope prof(s, "syrk_diag", (double)imin(n, NB) * (imin(n, NB) + 1) * (double)k * (double)cdiv(n, NB));
   syrk_diag<<<dim3(NB, (unsigned)cdiv(n, NB)), NB, 0, s>>>(upper, tt, n, k, alpha, A, lda, C, ldc, lanes(), info);
   BOLA_CHECK_LAUNCH();
   return 0;
@@ -195,6 +197,7 @@ int potrf2_rec(cudaStream_t s, char uplo, int64_t n, double *A, int64_t lda, int
   const bool upper = upc(uplo) == 'U';
   if (n == 0) return 0;
   if (n <= NB) {
+    ProfScope prof(s, "potrf2_block", (double)n * n * n / 3.0);
     potrf2_block<<<1, 256, 0, s>>>(upper, (int)n, A, lda, info, col0, lanes());
     BOLA_CHECK_LAUNCH();
     return 0;
@@ -213,7 +216,10 @@ int potrf2_rec(cudaStream_t s, char uplo, int64_t n, double *A, int64_t lda, int
 }
 
 int potrf_blocked(cudaStream_t s, char uplo, int64_t n, double *A, int64_t lda, int32_t *info) {
-  zero_i32<<<1, 1, 0, s>>>(info);
+  {
+    ProfScope prof(s, "info_init");
+    zero_i32<<<1, 1, 0, s>>>(info);
+  }
   BOLA_CHECK_LAUNCH();
   if (NB >= n) return potrf2_rec(s, uplo, n, A, lda, info, 0);
   const bool upper = uplo == 'U';
@@ -270,7 +276,10 @@ int bola_dpotrf2(char uplo, int64_t n, double *a, int64_t lda, int32_t *info, bo
   cudaStream_t s = (cudaStream_t)stream;
   if (n < 0) return -2;
   if (lda < imax(n, 1)) return -4;
-  zero_i32<<<1, 1, 0, s>>>(info);
+  {
+    ProfScope prof(s, "info_init");
+    zero_i32<<<1, 1, 0, s>>>(info);
+  }
   BOLA_CHECK_LAUNCH();
   return potrf2_rec(s, uplo, n, a, lda, info, 0);
 }

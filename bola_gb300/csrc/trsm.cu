@@ -147,6 +147,7 @@ struct Ctx {
 
 int base_left_n(const Ctx &c, bool lower, int64_t m, int64_t n, const double *A, int64_t lda, double *B,
                 int64_t ldb) {
+  ProfScope prof(c.s, "trsm_base", (double)m * m * n);
   const int warps = 8;
   const unsigned g = (unsigned)cdiv(n, warps);
   if (lower)
@@ -159,6 +160,7 @@ int base_left_n(const Ctx &c, bool lower, int64_t m, int64_t n, const double *A,
 
 int base_left_t(const Ctx &c, bool lower, int64_t m, int64_t n, const double *A, int64_t lda, double *B,
                 int64_t ldb) {
+  ProfScope prof(c.s, "trsm_base", (double)m * m * n);
   const unsigned g = (unsigned)cdiv(n, TCOLS);
   if (lower)
     left_t_base<true><<<g, TCOLS, 0, c.s>>>((int)m, n, c.unit, A, lda, B, ldb, c.info);
@@ -170,6 +172,7 @@ int base_left_t(const Ctx &c, bool lower, int64_t m, int64_t n, const double *A,
 
 int base_right(const Ctx &c, int v, int64_t m, int64_t n, const double *A, int64_t lda, double *B,
                int64_t ldb) {
+  ProfScope prof(c.s, "trsm_base", (double)m * n * n);
   const unsigned g = (unsigned)cdiv(m, 128);
   switch (v) {
     case 0: right_base<0><<<g, 128, 0, c.s>>>(m, (int)n, c.unit, A, lda, B, ldb, c.info); break;
@@ -258,6 +261,7 @@ int trsm_exact(cudaStream_t s, char side, char uplo, char transa, char diag, int
                double alpha, const double *A, int64_t lda, double *B, int64_t ldb, const int32_t *info) {
   if (m <= 0 || n <= 0) return 0;
   if (alpha != 1.0) {
+    ProfScope prof(s, "scale", (double)m * n);
     scale_matrix<<<(unsigned)cdiv(m * n, 256), 256, 0, s>>>(m, n, alpha, B, ldb, info);
     BOLA_CHECK_LAUNCH();
   }

@@ -47,6 +47,24 @@ const char *bola_last_error(void); /* message of this thread's last failing call
 int bola_set_simd_lanes(int lanes);
 int bola_get_simd_lanes(void);
 
+/* Device-time profiler: the GPU counterpart of BOLA's `profiling` feature
+ * (src/profiling.rs:25-140).  While enabled, every kernel launch is bracketed
+ * by CUDA events on its stream and tagged with a routine name plus its
+ * algorithmic flop/byte counts.  bola_profile_count() waits for the recorded
+ * events and returns the number of routine names seen; bola_profile_read()
+ * returns one name's totals (scopes, kernel launches, device ms, flops, bytes). */
+int bola_profile_enable(int on); /* returns the previous setting */
+int bola_profile_reset(void);
+int bola_profile_count(void);
+int bola_profile_read(int index, char *name, int name_len, int64_t *calls, int64_t *launches, double *ms,
+                      double *flops, double *bytes);
+
+/* Measures this device's FP64 fused multiply-add throughput (GFLOP/s) with a
+ * ~20 ms register-resident DFMA loop over every SM, so that roofline
+ * fractions of the FP64 kernels are stated against a peak measured on the
+ * same device and clocks.  Synchronises the device. */
+int bola_measure_fp64_peak(double *gflops);
+
 /* ---- Level 1 ---------------------------------------------------------- */
 
 /* Replaces idamax(n, x) -> usize, src/idamax.rs:23 (x86_64) / :141 (aarch64).
