@@ -34,6 +34,7 @@ SIGNATURES = {
     "bola_daxpy": (_int, [_i64, _d, _p, _i64, _p, _i64, _p]),
     "bola_dlaswp": (_int, [_i64, _p, _i64, _i32, _i32, _p, _i32, _p]),
     "bola_dgemm": (_int, [_c, _c, _i64, _i64, _i64, _d, _p, _i64, _p, _i64, _d, _p, _i64, _p]),
+    "bola_dgemm_noalloc": (_int, [_c, _c, _i64, _i64, _i64, _d, _p, _i64, _p, _i64, _d, _p, _i64, _p]),
     "bola_dtrsm": (_int, [_c, _c, _c, _c, _i64, _i64, _d, _p, _i64, _p, _i64, _p]),
     "bola_dsyrk": (_int, [_c, _c, _i64, _i64, _d, _p, _i64, _d, _p, _i64, _p]),
     "bola_dgetrf": (_int, [_i64, _i64, _p, _i64, _p, _p, _p]),

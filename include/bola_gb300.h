@@ -115,6 +115,31 @@ int bola_dtrsm(char side, char uplo, char transa, char diag, int64_t m, int64_t 
 int bola_dsyrk(char uplo, char trans, int64_t n, int64_t k, double alpha, const double *a,
                int64_t lda, double beta, double *c, int64_t ldc, bola_stream_t stream);
 
+/* DGEMM that allocates no device memory.  No counterpart in BOLA: it exists
+ * for callers of this library that cannot allocate — code running where
+ * cudaMalloc and memory-pool calls are not allowed or not wanted (inside a
+ * real-time loop where an allocation could stall, under an application that
+ * owns all device memory through its own allocator, or with a memory budget
+ * that must not move).  Same arguments and bit-identical results as
+ * bola_dgemm.  Where bola_dgemm would borrow temporary memory for its split-K
+ * partial sums (outputs too small to fill the GPU), this call uses a fixed
+ * 64 MiB array compiled into the library instead; every GPU that loads the
+ * library holds that array until the process exits.
+ *   - Shapes whose split-K partial sums need more than 64 MiB (K/64 chunks x
+ *     m x n doubles, rounded as bola_dgemm rounds them) are rejected with
+ *     BOLA_ERR_UNSUPPORTED and a message in bola_last_error().
+ *   - The first call on each device looks up the array's device address
+ *     (cudaGetSymbolAddress) with that device current; make that first call
+ *     before any stream capture.
+ *   - All calls on a device share the one array: calls whose kernels can
+ *     overlap on the GPU (different streams, no ordering) race on it.  Calls
+ *     on one stream are safe; each call writes every scratch value it later
+ *     reads, so nothing carries over from the previous call. */
+#define BOLA_NOALLOC_SCRATCH_BYTES (64ull << 20)
+int bola_dgemm_noalloc(char transa, char transb, int64_t m, int64_t n, int64_t k, double alpha,
+                       const double *a, int64_t lda, const double *b, int64_t ldb, double beta,
+                       double *c, int64_t ldc, bola_stream_t stream);
+
 /* ---- LAPACK ----------------------------------------------------------- */
 
 /* Replaces getrf(m, n, a, lda, ipiv) -> Result, src/getrf.rs:37.  Returns -4 for
