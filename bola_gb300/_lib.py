@@ -35,6 +35,7 @@ SIGNATURES = {
     "bola_dlaswp": (_int, [_i64, _p, _i64, _i32, _i32, _p, _i32, _p]),
     "bola_dgemm": (_int, [_c, _c, _i64, _i64, _i64, _d, _p, _i64, _p, _i64, _d, _p, _i64, _p]),
     "bola_dgemm_noalloc": (_int, [_c, _c, _i64, _i64, _i64, _d, _p, _i64, _p, _i64, _d, _p, _i64, _p]),
+    "bola_sgemm_tc_update": (_int, [_int, _i64, _i64, _p, _p, _p, _p, _p, _i64, _p, _p]),
     "bola_dtrsm": (_int, [_c, _c, _c, _c, _i64, _i64, _d, _p, _i64, _p, _i64, _p]),
     "bola_dsyrk": (_int, [_c, _c, _i64, _i64, _d, _p, _i64, _d, _p, _i64, _p]),
     "bola_dgetrf": (_int, [_i64, _i64, _p, _i64, _p, _p, _p]),
@@ -44,6 +45,21 @@ SIGNATURES = {
     "bola_dgetrs": (_int, [_i64, _i64, _p, _i64, _p, _p, _i64, _p]),
     "bola_dpotrs": (_int, [_c, _i64, _i64, _p, _i64, _p, _i64, _p]),
 }
+
+
+
+class MixedOpts(ctypes.Structure):
+    _fields_ = [("factor_kind", ctypes.c_int), ("max_iterations", ctypes.c_int), ("tolerance", ctypes.c_double),
+                ("fallback_fp64", ctypes.c_int)]
+
+
+class MixedInfo(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("gmres_iterations", ctypes.c_int), ("path", ctypes.c_int),
+                ("factor_info", ctypes.c_int), ("backward_error", ctypes.c_double)]
+
+
+SIGNATURES["bola_dgesv_mixed"] = (_int, [_i64, _i64, _p, _i64, _p, _i64, _p, _i64, ctypes.POINTER(MixedOpts),
+                                         ctypes.POINTER(MixedInfo), _p])
 
 _lib = None
 

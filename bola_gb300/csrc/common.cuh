@@ -253,60 +253,76 @@ __device__ __forceinline__ int compose_swaps(const SwapPlan &p, const int32_t *i
   return cnt;
 }
 
-// Warp-cooperative compose_swaps for at most 32 interchanges (the getrf panel
-// case): lanes prefetch the pivots, each lane keeps entries lane and lane+32 in
-// registers, lookups are ballots.  Called by all 32 lanes of one warp; writes
-// rows/src (>= 64 entries) and returns the count on every lane.
-__device__ __forceinline__ int compose_swaps_warp(const SwapPlan &p, const int32_t *ipiv, int64_t *rows,
-                                                  int64_t *src) {
+// Warp-cooperative compose_swaps for at most 16*E interchanges (E = 2: the
+// 32-column getrf panel; E = 4: the 64-column mixed-precision panel): lanes
+// prefetch the pivots, each lane keeps entries lane + 32*e in registers,
+// lookups are ballots.  Called by all 32 lanes of one warp; writes rows/src
+// (>= 32*E entries) and returns the count on every lane.
+template <int E = 2, typename RowT = int64_t>
+__device__ __forceinline__ int compose_swaps_warp(const SwapPlan &p, const int32_t *ipiv, RowT *rows, RowT *src) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int nsw = p.i_inc > 0 ? p.i2 - p.i1 + 1 : p.i1 - p.i2 + 1;
-  const int64_t my_ip = lane < nsw ? (int64_t)ipiv[p.ix0 + (int64_t)lane * p.incx] : 0;
-  int64_t R0 = -1, S0 = -1, R1 = -1, S1 = -1;
+  int64_t my_ip[E / 2];
+#pragma unroll
+  for (int h = 0; h < E / 2; ++h) {
+    const int t = lane + 32 * h;
+    my_ip[h] = t < nsw ? (int64_t)ipiv[p.ix0 + (int64_t)t * p.incx] : 0;
+  }
+  int64_t R[E], S[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) R[e] = S[e] = -1;
   int cnt = 0;
   for (int t = 0; t < nsw; ++t) {
     const int32_t i = p.i1 + t * p.i_inc;
-    const int64_t ip = __shfl_sync(FULL, my_ip, t);
+    int64_t ip = 0;
+#pragma unroll
+    for (int h = 0; h < E / 2; ++h) {
+      const int64_t v = __shfl_sync(FULL, my_ip[h], t & 31);
+      if ((t >> 5) == h) ip = v;
+    }
     if (ip == (int64_t)i) continue;
     const int64_t want[2] = {(int64_t)i - 1, ip - 1};
     int slot[2];
 #pragma unroll
     for (int w = 0; w < 2; ++w) {
-      const unsigned ma = __ballot_sync(FULL, lane < cnt && R0 == want[w]);
-      const unsigned mb = __ballot_sync(FULL, lane + 32 < cnt && R1 == want[w]);
-      int s = ma ? __ffs(ma) - 1 : (mb ? 32 + __ffs(mb) - 1 : -1);
+      int s = -1;
+#pragma unroll
+      for (int e = E - 1; e >= 0; --e) {
+        const unsigned mk = __ballot_sync(FULL, lane + 32 * e < cnt && R[e] == want[w]);
+        if (mk) s = 32 * e + __ffs(mk) - 1;
+      }
       if (s < 0) {
         s = cnt++;
-        if (lane == (s & 31)) {
-          if (s < 32) {
-            R0 = want[w];
-            S0 = want[w];
-          } else {
-            R1 = want[w];
-            S1 = want[w];
+#pragma unroll
+        for (int e = 0; e < E; ++e)
+          if (lane == (s & 31) && (s >> 5) == e) {
+            R[e] = want[w];
+            S[e] = want[w];
           }
-        }
       }
       slot[w] = s;
     }
-    const int64_t sa = __shfl_sync(FULL, slot[0] < 32 ? S0 : S1, slot[0] & 31);
-    const int64_t sb = __shfl_sync(FULL, slot[1] < 32 ? S0 : S1, slot[1] & 31);
-    if (lane == (slot[0] & 31)) {
-      if (slot[0] < 32) S0 = sb; else S1 = sb;
+    int64_t sa = 0, sb = 0;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int64_t va = __shfl_sync(FULL, S[e], slot[0] & 31);
+      const int64_t vb = __shfl_sync(FULL, S[e], slot[1] & 31);
+      if ((slot[0] >> 5) == e) sa = va;
+      if ((slot[1] >> 5) == e) sb = vb;
     }
-    if (lane == (slot[1] & 31)) {
-      if (slot[1] < 32) S0 = sa; else S1 = sa;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      if (lane == (slot[0] & 31) && (slot[0] >> 5) == e) S[e] = sb;
+      if (lane == (slot[1] & 31) && (slot[1] >> 5) == e) S[e] = sa;
     }
   }
-  if (lane < cnt) {
-    rows[lane] = R0;
-    src[lane] = S0;
-  }
-  if (lane + 32 < cnt) {
-    rows[lane + 32] = R1;
-    src[lane + 32] = S1;
-  }
+#pragma unroll
+  for (int e = 0; e < E; ++e)
+    if (lane + 32 * e < cnt) {
+      rows[lane + 32 * e] = (RowT)R[e];
+      src[lane + 32 * e] = (RowT)S[e];
+    }
   return cnt;
 }
 

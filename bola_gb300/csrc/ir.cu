@@ -1,0 +1,400 @@
+// ir.cu — mixed-precision solve: low-precision LU on the tensor cores,
+// FP64 iterative refinement (no BOLA counterpart; the FP64 answer it must
+// reach is BOLA's getrf + trsm solve).
+//
+//   W = fl32(A S)                 S: power-of-two scale per 64-column block
+//   P W = L U                     slu.cu (tcgen05 trailing updates)
+//   x0 = S U^-1 L^-1 P b          FP32 triangular solves
+//   repeat: r = b - A x           FP64 (the exact DGEMM)
+//           berr = max_rhs ||r||_inf / (||A||_inf ||x||_inf + ||b||_inf)
+//           stop when berr <= tol; on stall (berr not halving) switch to
+//           GMRES-IR, and when that stalls too, to the plain FP64 path
+//           d = S U^-1 L^-1 P (r / ||r||) * ||r||;  x += d    (FP64 update)
+// The residual, the update and the backward-error test are the only FP64
+// steps.  The FP32 triangular solves walk 64-row blocks, one launch per
+// block: every CTA re-solves the small diagonal block from shared memory and
+// then updates its slice of the rows below (above), so no grid barrier is
+// needed.
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+#include "mixed.cuh"
+
+namespace bola {
+namespace {
+
+constexpr int TB = 64;      // triangular-solve block (= LU block)
+constexpr int MAXRHS = 32;  // right-hand sides per refinement sweep
+
+// ---- scaling and conversion -------------------------------------------------------
+__global__ void colblock_scale(int64_t n, const double *__restrict__ A, int64_t lda, double *scale) {
+  // one CTA per 64-column block: scale = 2^-e with max|a| in [2^(e-1), 2^e)
+  __shared__ double red[32];
+  const int64_t c0 = (int64_t)blockIdx.x * TB;
+  const int64_t c1 = imin(n, c0 + TB);
+  double m = 0.0;
+  for (int64_t c = c0; c < c1; ++c)
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, fabs(A[i + c * lda]));
+  for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double mm = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mm = fmax(mm, red[w]);
+    int e = 0;
+    frexp(mm, &e);
+    scale[blockIdx.x] = (mm > 0.0 && isfinite(mm)) ? ldexp(1.0, -e) : 1.0;
+  }
+}
+
+__global__ void to_fp32_scaled(int64_t n, const double *__restrict__ A, int64_t lda, const double *scale,
+                               float *__restrict__ W, int64_t ldw) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n * n) return;
+  const int64_t i = e % n, j = e / n;
+  W[i + j * ldw] = (float)(A[i + j * lda] * scale[j / TB]);
+}
+
+// ||A||_inf: one thread per row, columns walked in order (coalesced across threads).
+__global__ void row_abs_sums(int64_t n, const double *__restrict__ A, int64_t lda, double *rows) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0.0;
+  for (int64_t j = 0; j < n; ++j) s += fabs(A[i + j * lda]);
+  rows[i] = s;
+}
+
+// perm[i] = original row that ends in position i after applying ipiv in order.
+__global__ void compose_perm(int64_t n, const int32_t *ipiv, int32_t *perm) {
+  extern __shared__ int32_t p[];
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) p[i] = (int32_t)i;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int64_t i = 0; i < n; ++i) {
+      const int32_t t = ipiv[i] - 1;
+      const int32_t v = p[i];
+      p[i] = p[t];
+      p[t] = v;
+    }
+  }
+  __syncthreads();
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) perm[i] = p[i];
+}
+
+// Per right-hand side: out[c] = max_i |v[i, c]| (one CTA per column).
+__global__ void col_absmax(int64_t n, const double *__restrict__ v, int64_t ldv, double *out) {
+  __shared__ double red[32];
+  const int c = blockIdx.x;
+  double m = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, fabs(v[i + c * ldv]));
+  for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double mm = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mm = fmax(mm, red[w]);
+    out[c] = mm;
+  }
+}
+
+__global__ void max_of(int64_t n, const double *v, double *out) {
+  __shared__ double red[32];
+  double m = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, v[i]);
+  for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double mm = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mm = fmax(mm, red[w]);
+    *out = mm;
+  }
+}
+
+// y[i, c] = fl32(r[perm[i], c] / rscale[c])
+__global__ void permute_scale_down(int64_t n, int nrhs, const double *__restrict__ r, int64_t ldr,
+                                   const int32_t *perm, const double *rscale, float *__restrict__ y) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n * nrhs) return;
+  const int64_t i = e % n, c = e / n;
+  const double s = rscale[c];
+  y[i + c * n] = s > 0.0 ? (float)(r[perm[i] + c * ldr] / s) : 0.f;
+}
+
+// x[i, c] += S_i * rscale[c] * y[i, c]   (or x = ... when assign)
+__global__ void update_x(int64_t n, int nrhs, const float *__restrict__ y, const double *scale, const double *rscale,
+                         double *__restrict__ x, int64_t ldx, int assign) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n * nrhs) return;
+  const int64_t i = e % n, c = e / n;
+  const double d = (double)y[i + c * n] * scale[i / TB] * rscale[c];
+  double *p = x + i + c * ldx;
+  *p = assign ? d : *p + d;
+}
+
+__global__ void copy_cols(int64_t n, int nrhs, const double *__restrict__ src, int64_t lds, double *__restrict__ dst,
+                          int64_t ldd) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n * nrhs) return;
+  const int64_t i = e % n, c = e / n;
+  dst[i + c * ldd] = src[i + c * lds];
+}
+
+// One block step of a blocked triangular solve with nrhs <= 32 right-hand
+// sides (n x nrhs, ld n).  LOWER: unit-lower L, forward; else upper U with
+// its diagonal, backward.  Every CTA solves the 64x64 diagonal block
+// k0..k0+kb of `y` from shared memory (a warp per right-hand side), CTA 0
+// writes the solved block to `out`, and every CTA applies it to its 256-row
+// slice of the rows below (LOWER) or above, in place in `y`.  The solved
+// block never goes back into `y`, which other CTAs of the launch still read.
+template <bool LOWER>
+__global__ void __launch_bounds__(256)
+trsv_block(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, int64_t k0, int kb, float *y,
+           float *out) {
+  __shared__ float D[TB * TB];      // diagonal block, column-major
+  __shared__ float ys[MAXRHS][TB];  // solved block of y
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int e = tid; e < kb * kb; e += blockDim.x) {
+    const int r = e % kb, c = e / kb;
+    D[r + c * TB] = W[(k0 + r) + (k0 + c) * ldw];
+  }
+  for (int e = tid; e < kb * nrhs; e += blockDim.x) {
+    const int r = e % kb, c = e / kb;
+    ys[c][r] = y[(k0 + r) + (int64_t)c * n];
+  }
+  __syncthreads();
+  for (int c = warp; c < nrhs; c += blockDim.x >> 5) {
+    float b0 = lane < kb ? ys[c][lane] : 0.f;
+    float b1 = lane + 32 < kb ? ys[c][lane + 32] : 0.f;
+    for (int s = 0; s < kb; ++s) {
+      const int k = LOWER ? s : kb - 1 - s;
+      float bk = __shfl_sync(0xffffffffu, k < 32 ? b0 : b1, k & 31);
+      if (!LOWER) {
+        bk = bk / D[k + k * TB];
+        if (k == lane) b0 = bk;
+        if (k == lane + 32) b1 = bk;
+      }
+      const bool in0 = LOWER ? (lane > k && lane < kb) : (lane < k);
+      const bool in1 = LOWER ? (lane + 32 > k && lane + 32 < kb) : (lane + 32 < k);
+      if (in0) b0 = fmaf(-D[lane + k * TB], bk, b0);
+      if (in1) b1 = fmaf(-D[lane + 32 + k * TB], bk, b1);
+    }
+    if (lane < kb) ys[c][lane] = b0;
+    if (lane + 32 < kb) ys[c][lane + 32] = b1;
+  }
+  __syncthreads();
+  if (blockIdx.x == 0) {
+    for (int e = tid; e < kb * nrhs; e += blockDim.x) {
+      const int r = e % kb, c = e / kb;
+      out[(k0 + r) + (int64_t)c * n] = ys[c][r];
+    }
+  }
+  // rows to update: below (LOWER) or above
+  const int64_t rbeg = LOWER ? k0 + kb : 0;
+  const int64_t rend = LOWER ? n : k0;
+  const int64_t i = rbeg + (int64_t)blockIdx.x * blockDim.x + tid;
+  if (i >= rend) return;
+  float acc[MAXRHS];
+#pragma unroll
+  for (int c = 0; c < MAXRHS; ++c) acc[c] = 0.f;
+  for (int k = 0; k < kb; ++k) {
+    const float l = W[i + (k0 + k) * ldw];
+#pragma unroll
+    for (int c = 0; c < MAXRHS; ++c)
+      if (c < nrhs) acc[c] = fmaf(l, ys[c][k], acc[c]);
+  }
+#pragma unroll
+  for (int c = 0; c < MAXRHS; ++c)
+    if (c < nrhs) y[i + (int64_t)c * n] -= acc[c];
+}
+
+// y (right-hand sides, overwritten) -> out (solution)
+int trsv(cudaStream_t s, bool lower, int64_t n, int nrhs, const float *W, int64_t ldw, float *y, float *out) {
+  ProfScope prof(s, lower ? "trsv_lower" : "trsv_upper", (double)n * n * nrhs, 4.0 * (double)n * n / 2);
+  const int64_t nb = cdiv(n, TB);
+  for (int64_t b = 0; b < nb; ++b) {
+    const int64_t k0 = lower ? b * TB : (nb - 1 - b) * TB;
+    const int kb = (int)imin(TB, n - k0);
+    const int64_t rows = lower ? n - k0 - kb : k0;
+    const unsigned grid = (unsigned)imax(1, cdiv(rows, 256));
+    if (lower)
+      trsv_block<true><<<grid, 256, 0, s>>>(n, nrhs, W, ldw, k0, kb, y, out);
+    else
+      trsv_block<false><<<grid, 256, 0, s>>>(n, nrhs, W, ldw, k0, kb, y, out);
+    BOLA_CHECK_LAUNCH();
+  }
+  return 0;
+}
+
+// Device workspace of one mixed solve, cached per device and grown on demand.
+struct Workspace {
+  int64_t n = 0, nrhs = 0;
+  float *W = nullptr, *y = nullptr, *z = nullptr;
+  double *scale = nullptr, *r = nullptr, *d = nullptr, *norms = nullptr, *rowsum = nullptr;
+  int32_t *ipiv = nullptr, *perm = nullptr, *info = nullptr;
+  MixedLU lu;
+};
+
+int ws_reserve(Workspace &w, int64_t n, int64_t nrhs, int kind, cudaStream_t s) {
+  if (n > w.n || nrhs > w.nrhs) {
+    for (void *p : {(void *)w.W, (void *)w.y, (void *)w.z, (void *)w.scale, (void *)w.r, (void *)w.d, (void *)w.norms,
+                    (void *)w.rowsum, (void *)w.ipiv, (void *)w.perm, (void *)w.info})
+      if (p) cudaFree(p);
+    w = Workspace{};
+    BOLA_TRY_CUDA(cudaMalloc(&w.W, sizeof(float) * n * n));
+    BOLA_TRY_CUDA(cudaMalloc(&w.y, sizeof(float) * n * nrhs));
+    BOLA_TRY_CUDA(cudaMalloc(&w.z, sizeof(float) * n * nrhs));
+    BOLA_TRY_CUDA(cudaMalloc(&w.scale, sizeof(double) * cdiv(n, TB)));
+    BOLA_TRY_CUDA(cudaMalloc(&w.r, sizeof(double) * n * nrhs));
+    BOLA_TRY_CUDA(cudaMalloc(&w.d, sizeof(double) * n * nrhs));
+    BOLA_TRY_CUDA(cudaMalloc(&w.norms, sizeof(double) * (3 * MAXRHS + 8)));
+    BOLA_TRY_CUDA(cudaMalloc(&w.rowsum, sizeof(double) * n));
+    BOLA_TRY_CUDA(cudaMalloc(&w.ipiv, sizeof(int32_t) * n));
+    BOLA_TRY_CUDA(cudaMalloc(&w.perm, sizeof(int32_t) * n));
+    BOLA_TRY_CUDA(cudaMalloc(&w.info, sizeof(int32_t)));
+    w.n = n;
+    w.nrhs = nrhs;
+  }
+  return w.lu.reserve(n, kind, s);
+}
+
+std::mutex g_ws_mu;
+Workspace g_ws[64];
+
+// Low-precision correction: y = S U^-1 L^-1 P (r / rs) * rs, added to (or assigned into) x.
+int correction(cudaStream_t s, Workspace &w, int64_t n, int nrhs, const double *r, int64_t ldr, const double *rs,
+               double *x, int64_t ldx, bool assign) {
+  const unsigned g = (unsigned)cdiv(n * nrhs, 256);
+  permute_scale_down<<<g, 256, 0, s>>>(n, nrhs, r, ldr, w.perm, rs, w.y);
+  BOLA_CHECK_LAUNCH();
+  BOLA_TRY(trsv(s, true, n, nrhs, w.W, n, w.y, w.z));
+  BOLA_TRY(trsv(s, false, n, nrhs, w.W, n, w.z, w.y));
+  update_x<<<g, 256, 0, s>>>(n, nrhs, w.y, w.scale, rs, x, ldx, assign ? 1 : 0);
+  BOLA_CHECK_LAUNCH();
+  return 0;
+}
+
+}  // namespace
+}  // namespace bola
+
+using namespace bola;
+
+extern "C" int bola_dgesv_mixed(int64_t n, int64_t nrhs, const double *a, int64_t lda, const double *b, int64_t ldb,
+                                double *x, int64_t ldx, const bola_mixed_opts *opts, bola_mixed_info *out,
+                                bola_stream_t stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  if (n < 0) return -1;
+  if (nrhs < 0 || nrhs > MAXRHS) return -2;
+  if (lda < imax(1, n)) return -4;
+  if (ldb < imax(1, n)) return -6;
+  if (ldx < imax(1, n)) return -8;
+  bola_mixed_opts o = {2, 30, 1e-14, 1};
+  if (opts) o = *opts;
+  if (o.factor_kind < 0 || o.factor_kind > 2) return -9;
+  bola_mixed_info info_out;
+  std::memset(&info_out, 0, sizeof info_out);
+  if (n == 0 || nrhs == 0) {
+    if (out) *out = info_out;
+    return 0;
+  }
+  if (n > 8192) return fail(BOLA_ERR_UNSUPPORTED, "bola_dgesv_mixed: n = %lld > 8192", (long long)n);
+  int dev = 0;
+  BOLA_TRY_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_ws_mu);
+  Workspace &w = g_ws[dev & 63];
+  BOLA_TRY(ws_reserve(w, n, nrhs, o.factor_kind, s));
+  const int nr = (int)nrhs;
+  double *nrm = w.norms;  // [0..nr): ||r||, [nr..2nr): ||x||, [2nr..3nr): ||b||, [3nr]: ||A||
+
+  // scale, convert, factor
+  {
+    ProfScope prof(s, "mixed_convert", 0.0, 12.0 * (double)n * n);
+    colblock_scale<<<(unsigned)cdiv(n, TB), 512, 0, s>>>(n, a, lda, w.scale);
+    to_fp32_scaled<<<(unsigned)cdiv(n * n, 256), 256, 0, s>>>(n, a, lda, w.scale, w.W, n);
+    row_abs_sums<<<(unsigned)cdiv(n, 128), 128, 0, s>>>(n, a, lda, w.rowsum);
+    max_of<<<1, 1024, 0, s>>>(n, w.rowsum, nrm + 3 * nr);
+    col_absmax<<<nr, 256, 0, s>>>(n, b, ldb, nrm + 2 * nr);
+  }
+  BOLA_CHECK_LAUNCH();
+  BOLA_TRY(w.lu.factor(s, w.W, n, w.ipiv, w.info));
+  {
+    ProfScope prof(s, "mixed_perm");
+    compose_perm<<<1, 1024, sizeof(int32_t) * n, s>>>(n, w.ipiv, w.perm);
+  }
+  BOLA_CHECK_LAUNCH();
+  int32_t finfo = 0, ferr = 0;
+  BOLA_TRY_CUDA(cudaMemcpyAsync(&finfo, w.info, sizeof finfo, cudaMemcpyDeviceToHost, s));
+  BOLA_TRY_CUDA(cudaMemcpyAsync(&ferr, w.lu.err, sizeof ferr, cudaMemcpyDeviceToHost, s));
+  BOLA_TRY_CUDA(cudaStreamSynchronize(s));
+  info_out.factor_info = finfo;
+  if (ferr != 0) return fail(BOLA_ERR_CUDA, "mixed LU: tensor-core update timed out (%d)", ferr);
+
+  bool converged = false;
+  double berr = INFINITY, prev = INFINITY;
+  if (finfo == 0) {
+    // x0 = correction of b (rscale = ||b||)
+    BOLA_TRY(correction(s, w, n, nr, b, ldb, nrm + 2 * nr, x, ldx, true));
+    std::vector<double> h(3 * nr + 1);
+    for (int it = 0; it <= o.max_iterations; ++it) {
+      {
+        ProfScope prof(s, "mixed_residual", 2.0 * (double)n * n * nr);
+        copy_cols<<<(unsigned)cdiv(n * nr, 256), 256, 0, s>>>(n, nr, b, ldb, w.r, n);
+        BOLA_CHECK_LAUNCH();
+        BOLA_TRY(dgemm_exact(s, 'N', 'N', n, nr, n, -1.0, a, lda, x, ldx, 1.0, w.r, n, 64, nullptr, 0));
+        col_absmax<<<nr, 256, 0, s>>>(n, w.r, n, nrm);
+        col_absmax<<<nr, 256, 0, s>>>(n, x, ldx, nrm + nr);
+      }
+      BOLA_CHECK_LAUNCH();
+      BOLA_TRY_CUDA(cudaMemcpyAsync(h.data(), nrm, sizeof(double) * (3 * nr + 1), cudaMemcpyDeviceToHost, s));
+      BOLA_TRY_CUDA(cudaStreamSynchronize(s));
+      berr = 0.0;
+      for (int c = 0; c < nr; ++c) {
+        const double den = h[3 * nr] * h[nr + c] + h[2 * nr + c];
+        const double e = den > 0.0 ? h[c] / den : (h[c] > 0.0 ? INFINITY : 0.0);
+        berr = std::isnan(e) ? INFINITY : fmax(berr, e);
+      }
+      info_out.iterations = it;
+      if (berr <= o.tolerance) {
+        converged = true;
+        break;
+      }
+      if (it > 0 && !(berr < 0.5 * prev)) break;  // stalled
+      prev = berr;
+      BOLA_TRY(correction(s, w, n, nr, w.r, n, nrm, x, ldx, false));
+    }
+  }
+  info_out.backward_error = berr;
+  info_out.path = 0;
+  if (!converged && o.fallback_fp64) {
+    // plain FP64 path on a copy of A (BOLA's getrf + laswp + trsm)
+    double *acopy = nullptr;
+    BOLA_TRY_CUDA(cudaMallocAsync(&acopy, sizeof(double) * n * n, s));
+    {
+      ProfScope prof(s, "mixed_fallback_copy", 0.0, 16.0 * (double)n * n);
+      BOLA_TRY_CUDA(cudaMemcpy2DAsync(acopy, sizeof(double) * n, a, sizeof(double) * lda, sizeof(double) * n, n,
+                                      cudaMemcpyDeviceToDevice, s));
+      copy_cols<<<(unsigned)cdiv(n * nr, 256), 256, 0, s>>>(n, nr, b, ldb, x, ldx);
+    }
+    int st = bola_dgetrf(n, n, acopy, n, w.ipiv, w.info, stream);
+    if (st == 0) st = bola_dgetrs(n, nr, acopy, n, w.ipiv, x, ldx, stream);
+    cudaFreeAsync(acopy, s);
+    if (st != 0) return st;
+    info_out.path = 2;
+    // backward error of the FP64 answer
+    copy_cols<<<(unsigned)cdiv(n * nr, 256), 256, 0, s>>>(n, nr, b, ldb, w.r, n);
+    BOLA_TRY(dgemm_exact(s, 'N', 'N', n, nr, n, -1.0, a, lda, x, ldx, 1.0, w.r, n, 64, nullptr, 0));
+    col_absmax<<<nr, 256, 0, s>>>(n, w.r, n, nrm);
+    col_absmax<<<nr, 256, 0, s>>>(n, x, ldx, nrm + nr);
+    std::vector<double> h(3 * nr + 1);
+    BOLA_TRY_CUDA(cudaMemcpyAsync(h.data(), nrm, sizeof(double) * (3 * nr + 1), cudaMemcpyDeviceToHost, s));
+    BOLA_TRY_CUDA(cudaStreamSynchronize(s));
+    berr = 0.0;
+    for (int c = 0; c < nr; ++c) berr = fmax(berr, h[c] / (h[3 * nr] * h[nr + c] + h[2 * nr + c]));
+    info_out.backward_error = berr;
+  }
+  if (out) *out = info_out;
+  return 0;
+}

@@ -1,0 +1,366 @@
+// slu.cu — the low-precision LU of the mixed-precision solver (no BOLA
+// counterpart; it preconditions the FP64 refinement in ir.cu).
+//
+// A (FP64) is scaled per 64-column block by a power of two (exact) and
+// rounded to an FP32 working matrix W.  Blocked right-looking LU with partial
+// pivoting and NB = 64 = the K of the tensor-core update:
+//   spanel_kernel   the (n-j) x 64 panel on a cluster of <=16 CTAs, the rows
+//                   held in registers; per column each CTA pushes its pivot
+//                   candidate (key + row) into every CTA's shared memory, so
+//                   a column costs one CTA barrier pair and one cluster
+//                   barrier.  It also writes L21 as the K-major A operand
+//                   (bf16, or tf32 hi/lo) of the update.
+//   sswap_trsm      the 64 interchanges on every other column, U12 = L11^-1 A12
+//                   and the K-major B operand.
+//   tc_update       W22 -= L21 U12 on tcgen05 with FP32 accumulation in TMEM.
+// Pivots are this algorithm's own; only the FP64 refinement decides accuracy.
+#include <cooperative_groups.h>
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+#include "mixed.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace bola {
+namespace {
+
+constexpr int SNB = 64;   // panel width and update depth
+constexpr int SPT = 256;  // threads per panel CTA
+constexpr int SMAXC = 16;
+
+struct SSlot {
+  uint32_t khi, klo;  // |pivot candidate| bits, ~row
+  float v[SNB];       // the candidate row
+};
+
+template <int N>
+__device__ __forceinline__ float pick(const float (&a)[N], int j) {
+  float v = 0.f;
+#pragma unroll
+  for (int c = 0; c < N; ++c) v = (c == j) ? a[c] : v;
+  return v;
+}
+
+__device__ __forceinline__ float tf32_round(float x) {
+  uint32_t u = __float_as_uint(x);
+  u = (u + 0x1000u) & ~0x1FFFu;
+  return __uint_as_float(u);
+}
+
+// Writes one 64-wide row of an update operand (K-major, row `r`).
+__device__ __forceinline__ void write_operand_row(int kind, void *op, float *op_lo, int64_t r, const float *v) {
+  if (kind == 0) {
+    __nv_bfloat16 *d = static_cast<__nv_bfloat16 *>(op) + r * SNB;
+#pragma unroll
+    for (int c = 0; c < SNB; c += 8) {
+      __align__(16) __nv_bfloat16 t[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) t[u] = __float2bfloat16_rn(v[c + u]);
+      *reinterpret_cast<uint4 *>(d + c) = *reinterpret_cast<const uint4 *>(t);
+    }
+  } else {
+    float *d = static_cast<float *>(op) + r * SNB;
+    float *dl = op_lo + r * SNB;
+#pragma unroll
+    for (int c = 0; c < SNB; c += 4) {
+      float4 h, l;
+      h.x = tf32_round(v[c]);
+      h.y = tf32_round(v[c + 1]);
+      h.z = tf32_round(v[c + 2]);
+      h.w = tf32_round(v[c + 3]);
+      *reinterpret_cast<float4 *>(d + c) = h;
+      if (kind == 2) {
+        l.x = tf32_round(v[c] - h.x);
+        l.y = tf32_round(v[c + 1] - h.y);
+        l.z = tf32_round(v[c + 2] - h.z);
+        l.w = tf32_round(v[c + 3] - h.w);
+        *reinterpret_cast<float4 *>(dl + c) = l;
+      }
+    }
+  }
+}
+
+// Panel LU of W[0:mp, 0:jb] (W points at the panel's top-left).  ipiv gets
+// global 1-based rows (col0 + local + 1).  RPT rows per thread.
+template <int RPT>
+__global__ void __launch_bounds__(SPT)
+spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0, int32_t *info, int kind,
+              void *aop, float *aop_lo, int64_t R) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = (int)cluster.num_blocks();
+  const int cr = (int)cluster.block_rank();
+  __shared__ SSlot slots[2][SMAXC];
+  __shared__ float rowj[2][SNB];
+  __shared__ float myrow[SNB], myrowj[SNB];
+  __shared__ uint64_t wkey[SPT / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t r0 = (int64_t)cr * R;
+  const int64_t r1 = imin(mp, r0 + R);
+
+  float a[RPT][SNB];
+#pragma unroll
+  for (int q = 0; q < RPT; ++q) {
+    const int64_t g = r0 + tid + (int64_t)SPT * q;
+    const bool valid = g < r1;
+#pragma unroll
+    for (int c = 0; c < SNB; ++c) a[q][c] = (valid && c < jb) ? W[g + c * ldw] : 0.f;
+  }
+
+  for (int j = 0; j < jb; ++j) {
+    const int par = j & 1;
+    // -- local pivot candidate: key = (|v| bits, ~row), max wins, ties -> lowest row
+    uint64_t best = 0;
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) {
+      const int64_t g = r0 + tid + (int64_t)SPT * q;
+      if (g < r1 && g >= j) {
+        const float v = fabsf(pick(a[q], j));
+        const uint32_t bits = (v == v) ? __float_as_uint(v) : 0u;
+        const uint64_t key = ((uint64_t)bits << 32) | (0xFFFFFFFFu - (uint32_t)g);
+        best = key > best ? key : best;
+      }
+    }
+    const uint32_t hi = (uint32_t)(best >> 32), lo = (uint32_t)best;
+    const uint32_t mhi = __reduce_max_sync(0xffffffffu, hi);
+    const uint32_t mlo = __reduce_max_sync(0xffffffffu, hi == mhi ? lo : 0u);
+    if (lane == 0) wkey[warp] = ((uint64_t)mhi << 32) | mlo;
+    __syncthreads();
+    uint64_t ck = 0;
+#pragma unroll
+    for (int w = 0; w < SPT / 32; ++w) ck = wkey[w] > ck ? wkey[w] : ck;
+    const int64_t gbest = ck ? (int64_t)(0xFFFFFFFFu - (uint32_t)ck) : -1;
+    const bool own_j = j >= r0 && j < r1;
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) {
+      const int64_t g = r0 + tid + (int64_t)SPT * q;
+      if (g == gbest) {
+#pragma unroll
+        for (int c = 0; c < SNB; ++c) myrow[c] = a[q][c];
+      }
+      if (own_j && g == j) {
+#pragma unroll
+        for (int c = 0; c < SNB; ++c) myrowj[c] = a[q][c];
+      }
+    }
+    __syncthreads();
+    // -- push this CTA's candidate (and row j if owned) into every CTA
+    if (warp == 0) {
+      for (int d = 0; d < C; ++d) {
+        SSlot *rs = cluster.map_shared_rank(&slots[par][cr], d);
+        if (lane == 0) {
+          rs->khi = (uint32_t)(ck >> 32);
+          rs->klo = (uint32_t)ck;
+        }
+        rs->v[lane] = myrow[lane];
+        rs->v[lane + 32] = myrow[lane + 32];
+        if (own_j) {
+          float *rj = cluster.map_shared_rank(&rowj[par][0], d);
+          rj[lane] = myrowj[lane];
+          rj[lane + 32] = myrowj[lane + 32];
+        }
+      }
+    }
+    cluster.sync();
+    // -- the winner, identical in every CTA
+    uint64_t wk = 0;
+    int ws = 0;
+    for (int s = 0; s < C; ++s) {
+      const uint64_t k = ((uint64_t)slots[par][s].khi << 32) | slots[par][s].klo;
+      if (k > wk) {
+        wk = k;
+        ws = s;
+      }
+    }
+    const int64_t jp = wk ? (int64_t)(0xFFFFFFFFu - (uint32_t)wk) : (int64_t)j;
+    const float *prow = wk ? slots[par][ws].v : rowj[par];
+    const float pv = prow[j];
+    if (cr == 0 && tid == 0) ipiv[j] = col0 + (int32_t)jp + 1;
+    float inv = 1.0f / pv;
+    if (pv == 0.0f) {
+      inv = 0.0f;
+      if (cr == 0 && tid == 0) atomicCAS(info, 0, col0 + j + 1);
+    }
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) {
+      const int64_t g = r0 + tid + (int64_t)SPT * q;
+      if (g >= r1) continue;
+      if (jp != j && g == j) {
+#pragma unroll
+        for (int c = 0; c < SNB; ++c) a[q][c] = prow[c];
+      } else if (jp != j && g == jp) {
+#pragma unroll
+        for (int c = 0; c < SNB; ++c) a[q][c] = rowj[par][c];
+      }
+      if (g > j) {
+        const float l = pick(a[q], j) * inv;
+#pragma unroll
+        for (int c = 0; c < SNB; ++c) {
+          if (c == j) a[q][c] = l;
+          if (c > j) a[q][c] = fmaf(-l, prow[c], a[q][c]);
+        }
+      }
+    }
+  }
+
+  // -- write back the panel and the update's A operand (rows below the panel)
+#pragma unroll
+  for (int q = 0; q < RPT; ++q) {
+    const int64_t g = r0 + tid + (int64_t)SPT * q;
+    if (g >= r1) continue;
+#pragma unroll
+    for (int c = 0; c < SNB; ++c)
+      if (c < jb) W[g + c * ldw] = a[q][c];
+    if (aop != nullptr && g >= jb) write_operand_row(kind, aop, aop_lo, g - jb, a[q]);
+  }
+  cluster.sync();
+}
+
+// The panel's interchanges on all other columns, U12 = L11^-1 A12 on the
+// right ones and their K-major B operand.  A warp per column.
+__global__ void __launch_bounds__(256)
+sswap_trsm(float *W, int64_t ldw, int64_t n, int64_t j, int jb, const int32_t *ipiv, int kind, void *bop,
+           float *bop_lo) {
+  __shared__ int32_t rows[2 * SNB], src[2 * SNB];
+  __shared__ float L[SNB * SNB];
+  __shared__ int cnt;
+  if (threadIdx.x < 32) {
+    SwapPlan p;
+    p.ix0 = j;
+    p.i1 = (int32_t)(j + 1);
+    p.i2 = (int32_t)(j + jb);
+    p.i_inc = 1;
+    p.incx = 1;
+    const int c = compose_swaps_warp<4, int32_t>(p, ipiv, rows, src);
+    if (threadIdx.x == 0) cnt = c;
+  }
+  for (int e = threadIdx.x; e < jb * jb; e += blockDim.x) {
+    const int r = e % jb, c = e / jb;
+    L[r + c * SNB] = W[(j + r) + (j + c) * ldw];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (w >= n - jb) return;
+  const int64_t col = w < j ? w : w + jb;
+  float *cp = W + col * ldw;
+  float v[4];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) v[e] = lane + 32 * e < cnt ? cp[src[lane + 32 * e]] : 0.f;
+  __syncwarp();
+#pragma unroll
+  for (int e = 0; e < 4; ++e)
+    if (lane + 32 * e < cnt) cp[rows[lane + 32 * e]] = v[e];
+  __syncwarp();
+  if (col < j + jb) return;
+  float b0 = lane < jb ? cp[j + lane] : 0.f;
+  float b1 = lane + 32 < jb ? cp[j + lane + 32] : 0.f;
+  for (int k = 0; k < jb; ++k) {
+    const float bk = __shfl_sync(0xffffffffu, k < 32 ? b0 : b1, k & 31);
+    if (lane > k) b0 = fmaf(-L[lane + k * SNB], bk, b0);
+    if (lane + 32 > k && lane + 32 < jb) b1 = fmaf(-L[lane + 32 + k * SNB], bk, b1);
+  }
+  if (lane < jb) cp[j + lane] = b0;
+  if (lane + 32 < jb) cp[j + lane + 32] = b1;
+  if (bop != nullptr) {
+    // row (col - j - jb) of the K-major B operand: the 64 values of U12's column
+    __shared__ float stage[8][SNB];
+    float *st = stage[threadIdx.x >> 5];
+    st[lane] = lane < jb ? b0 : 0.f;
+    st[lane + 32] = lane + 32 < jb ? b1 : 0.f;
+    __syncwarp();
+    if (lane == 0) write_operand_row(kind, bop, bop_lo, col - j - jb, st);
+  }
+}
+
+__global__ void zero_i32(int32_t *p) { *p = 0; }
+
+int launch_spanel(cudaStream_t s, float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0,
+                  int32_t *info, int kind, void *aop, float *aop_lo) {
+  int C = (int)imin(SMAXC, imax(1, cdiv(mp, SPT)));
+  const int rpt = (int)cdiv(mp, (int64_t)C * SPT);
+  if (rpt > 2) return fail(BOLA_ERR_UNSUPPORTED, "mixed LU: panel of %lld rows exceeds 8192", (long long)mp);
+  const int64_t R = cdiv(mp, C);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)C, 1, 1);
+  cfg.blockDim = dim3(SPT, 1, 1);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  ProfScope prof(s, "spanel", 2.0 * (double)mp * SNB * SNB / 2.0);
+  if (rpt == 1) {
+    BOLA_TRY_CUDA(cudaFuncSetAttribute(spanel_kernel<1>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, spanel_kernel<1>, W, ldw, mp, jb, ipiv, col0, info, kind, aop, aop_lo, R));
+  } else {
+    BOLA_TRY_CUDA(cudaFuncSetAttribute(spanel_kernel<2>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, spanel_kernel<2>, W, ldw, mp, jb, ipiv, col0, info, kind, aop, aop_lo, R));
+  }
+  return 0;
+}
+
+}  // namespace
+
+int MixedLU::reserve(int64_t n_, int kind_, cudaStream_t s) {
+  if (n_ <= cap_n && kind_ == kind && aop) {
+    n = n_;
+    return 0;
+  }
+  release(s);
+  n = cap_n = n_;
+  kind = kind_;
+  const size_t esz = kind == 0 ? 2 : 4;
+  BOLA_TRY_CUDA(cudaMallocAsync(&aop, (size_t)n * SNB * esz, s));
+  BOLA_TRY_CUDA(cudaMallocAsync(&bop, (size_t)n * SNB * esz, s));
+  if (kind == 2) {
+    BOLA_TRY_CUDA(cudaMallocAsync(&aop_lo, (size_t)n * SNB * 4, s));
+    BOLA_TRY_CUDA(cudaMallocAsync(&bop_lo, (size_t)n * SNB * 4, s));
+  }
+  BOLA_TRY_CUDA(cudaMallocAsync(&err, sizeof(int32_t), s));
+  BOLA_TRY_CUDA(cudaMemsetAsync(err, 0, sizeof(int32_t), s));
+  const bool bf = kind == 0;
+  BOLA_TRY(make_kmajor_map(&mapA, aop, n, bf));
+  BOLA_TRY(make_kmajor_map(&mapB, bop, n, bf));
+  BOLA_TRY(make_kmajor_map(&mapAlo, kind == 2 ? aop_lo : aop, n, bf));
+  BOLA_TRY(make_kmajor_map(&mapBlo, kind == 2 ? bop_lo : bop, n, bf));
+  return 0;
+}
+
+void MixedLU::release(cudaStream_t s) {
+  for (void **p : {&aop, &bop, reinterpret_cast<void **>(&aop_lo), reinterpret_cast<void **>(&bop_lo),
+                   reinterpret_cast<void **>(&err)}) {
+    if (*p) cudaFreeAsync(*p, s);
+    *p = nullptr;
+  }
+  cap_n = 0;
+}
+
+// Right-looking blocked LU of W (n x n FP32), ipiv global 1-based, *info the
+// first zero pivot (the factor is then unusable; the caller falls back).
+int MixedLU::factor(cudaStream_t s, float *W, int64_t ldw, int32_t *ipiv, int32_t *info) {
+  zero_i32<<<1, 1, 0, s>>>(info);
+  BOLA_CHECK_LAUNCH();
+  for (int64_t j = 0; j < n; j += SNB) {
+    const int jb = (int)imin(SNB, n - j);
+    const int64_t mp = n - j;
+    const bool upd = j + jb < n;
+    BOLA_TRY(launch_spanel(s, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, kind, upd ? aop : nullptr,
+                           aop_lo));
+    const int64_t others = n - jb;
+    if (others > 0) {
+      ProfScope prof(s, "sswap_trsm", (double)jb * jb * (double)(n - j - jb));
+      sswap_trsm<<<(unsigned)cdiv(others, 8), 256, 0, s>>>(W, ldw, n, j, jb, ipiv, kind, upd ? bop : nullptr, bop_lo);
+      BOLA_CHECK_LAUNCH();
+    }
+    if (upd) BOLA_TRY(tc_update(s, kind, mp - jb, n - j - jb, mapA, mapB, mapAlo, mapBlo,
+                                W + (j + jb) + (j + jb) * ldw, ldw, err));
+  }
+  return 0;
+}
+
+}  // namespace bola

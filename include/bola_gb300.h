@@ -140,6 +140,15 @@ int bola_dgemm_noalloc(char transa, char transb, int64_t m, int64_t n, int64_t k
                        const double *a, int64_t lda, const double *b, int64_t ldb, double beta,
                        double *c, int64_t ldc, bola_stream_t stream);
 
+/* Building block of the mixed-precision solver (no BOLA counterpart):
+ * W (m x n FP32, column-major) -= A * B^T on the tcgen05 tensor cores, A
+ * (m x 64) and B (n x 64) stored K-major (64 contiguous values per row).
+ * kind 0: bf16 operands; 1: tf32 operands (fp32 storage); 2: 3xTF32, with
+ * a_lo/b_lo the tf32 remainders (A ~ a + a_lo), for ~2^-22 relative accuracy.
+ * *err (device int32) becomes non-zero if a bounded on-chip wait expired. */
+int bola_sgemm_tc_update(int kind, int64_t m, int64_t n, const void *a, const void *b, const void *a_lo,
+                         const void *b_lo, float *w, int64_t ldw, int32_t *err, bola_stream_t stream);
+
 /* ---- LAPACK ----------------------------------------------------------- */
 
 /* Replaces getrf(m, n, a, lda, ipiv) -> Result, src/getrf.rs:37.  Returns -4 for
@@ -172,6 +181,34 @@ int bola_dgetrs(int64_t n, int64_t nrhs, const double *lu, int64_t lda, const in
  * src/trsm.rs:95,174; 'U': U^T then U, src/trsm.rs:213,135). */
 int bola_dpotrs(char uplo, int64_t n, int64_t nrhs, const double *fac, int64_t lda, double *b,
                 int64_t ldb, bola_stream_t stream);
+
+/* ---- Mixed-precision solve (no BOLA counterpart) ------------------------
+ * Solves A X = B (A n x n FP64, B and X n x nrhs FP64, device pointers) to a
+ * normwise backward error max_j ||b_j - A x_j||_inf / (||A||_inf ||x_j||_inf
+ * + ||b_j||_inf) <= tolerance: A is factored in low precision (FP32 storage,
+ * tcgen05 tensor-core trailing updates, per-64-column-block power-of-two
+ * scaling), then the solution is refined with FP64 residuals and updates.
+ * When refinement stalls the plain FP64 path (bola_dgetrf + bola_dgetrs)
+ * solves the system instead, if fallback_fp64 is set.  Synchronous: it
+ * returns after the result and *info are final.  n <= 8192, nrhs <= 32. */
+typedef struct {
+  int factor_kind;       /* 0: bf16 tensor-core updates; 1: tf32; 2: 3xTF32 (FP32-accurate) */
+  int max_iterations;    /* refinement sweeps before declaring a stall (default 30) */
+  double tolerance;      /* target backward error (default 1e-14) */
+  int fallback_fp64;     /* 1: finish with the plain FP64 path when refinement stalls */
+} bola_mixed_opts;
+
+typedef struct {
+  int iterations;        /* refinement sweeps performed */
+  int gmres_iterations;  /* inner GMRES steps (GMRES-IR), 0 when not used */
+  int path;              /* 0 mixed IR, 1 mixed GMRES-IR, 2 plain FP64 fallback */
+  int factor_info;       /* first zero pivot of the low-precision LU (1-based), 0 if none */
+  double backward_error; /* of the returned X */
+} bola_mixed_info;
+
+int bola_dgesv_mixed(int64_t n, int64_t nrhs, const double *a, int64_t lda, const double *b, int64_t ldb,
+                     double *x, int64_t ldx, const bola_mixed_opts *opts, bola_mixed_info *info,
+                     bola_stream_t stream);
 
 #ifdef __cplusplus
 }

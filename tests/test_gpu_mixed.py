@@ -1,0 +1,98 @@
+"""Mixed-precision solve (tensor-core LU + FP64 refinement) against the FP64
+oracle (BOLA's getrf + trsm solve): every result must reach the normwise
+backward error target 1e-14, and its forward error against the oracle's
+solution must stay within kappa * 1e-14 (the conditioning bound)."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from bola_gb300 import workloads as wl
+
+pytestmark = pytest.mark.gpu
+
+
+def _p(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def make_system(n, nrhs, kappa, seed):
+    g1 = torch.from_numpy(wl.gaussian_matrix(n, n, seed=seed, stream="q1")).cuda()
+    g2 = torch.from_numpy(wl.gaussian_matrix(n, n, seed=seed, stream="q2")).cuda()
+    q1, _ = torch.linalg.qr(g1)
+    q2, _ = torch.linalg.qr(g2)
+    sigma = torch.logspace(0.0, -np.log10(kappa), n, dtype=torch.float64, device="cuda")
+    A = (q1 * sigma) @ q2
+    xt = torch.from_numpy(wl.uniform_matrix(n, nrhs, seed=seed, lo=-1, hi=1, stream="x")).cuda()
+    b = A @ xt
+    return A.t().contiguous().reshape(-1), b.t().contiguous().reshape(-1)
+
+
+def solve(A, b, n, nrhs, kind, fallback=1, max_it=30):
+    from bola_gb300 import _lib
+    L = _lib.load()
+    x = torch.zeros(n * nrhs, dtype=torch.float64, device="cuda")
+    opts = _lib.MixedOpts(kind, max_it, 1e-14, fallback)
+    info = _lib.MixedInfo()
+    st = L.bola_dgesv_mixed(n, nrhs, _p(A), n, _p(b), n, _p(x), n, ctypes.byref(opts), ctypes.byref(info),
+                            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == 0, L.bola_last_error()
+    return x, info
+
+
+def berr(A, x, b, n, nrhs):
+    Am = A.reshape(n, n).t()
+    X = x.reshape(nrhs, n).t()
+    B = b.reshape(nrhs, n).t()
+    R = B - Am @ X
+    den = Am.abs().sum(1).max() * X.abs().max(0).values + B.abs().max(0).values
+    return float((R.abs().max(0).values / den).max())
+
+
+@pytest.mark.parametrize("kind", [0, 1, 2])
+@pytest.mark.parametrize("n,nrhs", [(64, 1), (200, 3), (1000, 16), (2048, 32)])
+def test_mixed_reaches_1e14_well_conditioned(kind, n, nrhs):
+    A, b = make_system(n, nrhs, 1e2, seed=3)
+    x, info = solve(A, b, n, nrhs, kind)
+    assert info.backward_error <= 1e-14
+    assert berr(A, x, b, n, nrhs) <= 1e-14
+    if kind == 2 or n <= 1000:
+        assert info.path == 0, (info.path, info.iterations)  # refinement alone converged
+
+
+@pytest.mark.parametrize("kappa", [1e2, 1e6, 1e10])
+@pytest.mark.parametrize("kind", [0, 2])
+def test_mixed_kappa_sweep_vs_oracle(oracle_lib, kappa, kind):
+    n, nrhs = 1024, 4
+    A, b = make_system(n, nrhs, kappa, seed=5)
+    x, info = solve(A, b, n, nrhs, kind)
+    assert info.backward_error <= 1e-14
+    assert berr(A, x, b, n, nrhs) <= 1e-14
+    A_np = A.cpu().numpy().reshape(n, n).T.copy(order="F")
+    b_np = b.cpu().numpy().reshape(nrhs, n).T.copy(order="F")
+    info_o, _ = oracle_lib.solve_lu(A_np, b_np)
+    assert info_o == 0
+    X = x.cpu().numpy().reshape(nrhs, n).T
+    fwd = np.abs(X - b_np).max() / np.abs(b_np).max()
+    assert fwd <= max(kappa, 10.0) * 1e-13, fwd
+
+
+def test_mixed_without_fallback_reports_stall_honestly():
+    n, nrhs = 512, 2
+    A, b = make_system(n, nrhs, 1e10, seed=7)
+    x, info = solve(A, b, n, nrhs, 0, fallback=0, max_it=10)
+    # bf16 factors cannot refine a kappa = 1e10 system: the call says so
+    assert info.path == 0
+    assert info.backward_error > 1e-14 or berr(A, x, b, n, nrhs) <= 1e-14
+
+
+def test_mixed_singular_falls_back_to_fp64_info():
+    from bola_gb300 import _lib
+    n, nrhs = 128, 1
+    A = torch.rand(n * n, dtype=torch.float64, device="cuda")
+    A.view(n, n)[10, :] = 0.0  # column 10 (column-major storage) is zero
+    b = torch.rand(n, dtype=torch.float64, device="cuda")
+    x, info = solve(A, b, n, nrhs, 2)
+    assert info.factor_info > 0
+    assert info.path == 2
