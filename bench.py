@@ -9,10 +9,14 @@ solve), whose normwise backward error is checked to be <= 1e-14.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-ours       the C-ABI library on the GPU; `value` has inputs resident in HBM,
-           `e2e` copies A and b from pinned host memory every step and reads
-           x back.  The library's device profiler (CUDA events on the launching
-           stream) gives the per-kernel roofline numbers and the launch count.
+ours       the C-ABI library on the GPU: `value` is the mixed-precision solve
+           (bola_dgesv_mixed: 3xTF32 tensor-core LU + FP64 refinement, plain
+           FP64 fallback when refinement stalls) with inputs resident in HBM;
+           `plain_fp64` is the BOLA-exact FP64 path (bola_dgetrf + bola_dgetrs)
+           on the same systems; `e2e` copies A and b from pinned host memory
+           every step and reads x back.  The library's device profiler (CUDA
+           events on the launching stream) gives the per-kernel roofline
+           numbers and the launch count.
 reference  BOLA's CPU algorithm (the C restatement under oracle/, all host
            threads) on the same inputs.
 Under torchrun each rank solves its own systems (replicas, no collective);
@@ -154,6 +158,7 @@ class Solver:
         self.n, self.nrhs = n, nrhs
         self.work = torch.empty(n * n, dtype=torch.float64, device=device)
         self.x = torch.empty(n * nrhs, dtype=torch.float64, device=device)
+        self.bdev = torch.empty(n * nrhs, dtype=torch.float64, device=device)
         self.ipiv = torch.empty(n, dtype=torch.int32, device=device)
         self.info = torch.zeros(1, dtype=torch.int32, device=device)
         self.stream = torch.cuda.current_stream(device)
@@ -174,6 +179,24 @@ class Solver:
         self.x.copy_(b_host, non_blocking=True)
         self._factor_solve()
         x_host.copy_(self.x, non_blocking=True)
+
+    def solve_mixed(self, A, b, kind=2):
+        """bola_dgesv_mixed; returns the bola_mixed_info of the call."""
+        from bola_gb300 import _lib
+        opts = _lib.MixedOpts(kind, 30, BERR_TARGET, 1)
+        info = _lib.MixedInfo()
+        st = self.L.bola_dgesv_mixed(self.n, self.nrhs, self._p(A), self.n, self._p(b), self.n, self._p(self.x),
+                                     self.n, ctypes.byref(opts), ctypes.byref(info), self.sp)
+        if st != 0:
+            raise RuntimeError(f"bola_dgesv_mixed status {st}: {self.L.bola_last_error().decode()}")
+        return info
+
+    def solve_mixed_host(self, A_host, b_host, x_host, kind=2):
+        self.work.copy_(A_host, non_blocking=True)
+        self.bdev.copy_(b_host, non_blocking=True)
+        info = self.solve_mixed(self.work, self.bdev, kind)
+        x_host.copy_(self.x, non_blocking=True)
+        return info
 
     def _factor_solve(self):
         n, L = self.n, self.L
@@ -207,25 +230,29 @@ def run_ours(args, rank, world, device):
     solver = Solver(n, nrhs, device)
     stream = solver.stream
     peak_fp64 = api.measure_fp64_peak()
+    infos = []
 
     def step(k):
         s = systems[k % len(systems)]
-        solver.solve_device(s["A"], s["b"])
+        infos.append((s["kappa"], solver.solve_mixed(s["A"], s["b"])))
 
     for k in range(args.warmup):
         step(k)
     torch.cuda.synchronize()
-    # check every system once (outside the timed region)
-    berr = {}
+    # every system once, outside the timed region: the answer must meet the target
+    berr, paths = {}, {}
     for s in systems:
-        solver.solve_device(s["A"], s["b"])
+        info = solver.solve_mixed(s["A"], s["b"])
         torch.cuda.synchronize()
-        if int(solver.info.item()) != 0:
-            raise RuntimeError(f"getrf info {solver.info.item()} for kappa {s['kappa']}")
-        berr[f"{s['kappa']:.0e}"] = backward_error(s["A"], solver.x, s["b"], n, nrhs)
+        key = f"{s['kappa']:.0e}"
+        berr[key] = backward_error(s["A"], solver.x, s["b"], n, nrhs)
+        paths[key] = {"path": ["mixed-IR", "mixed-GMRES-IR", "fp64-fallback"][info.path],
+                      "iterations": info.iterations, "gmres_iterations": info.gmres_iterations,
+                      "reported_backward_error": info.backward_error}
 
     if world > 1:
         torch.distributed.barrier()
+    infos.clear()
     api.profile_reset()
     api.profile_enable(True)
     with ClockSampler(device.index if device.index is not None else 0) as clk:
@@ -235,59 +262,71 @@ def run_ours(args, rank, world, device):
     if world > 1:
         torch.distributed.barrier()
 
+    # the plain FP64 path on the same systems (BOLA-exact getrf + getrs)
+    plain_steps = max(1, min(3, args.steps))
+
+    def step_plain(k):
+        s = systems[k % len(systems)]
+        solver.solve_device(s["A"], s["b"])
+
+    step_plain(0)
+    plain_total, plain_per = time_steps(step_plain, plain_steps, stream)
+
     # end to end: pinned host buffers, copies inside the timed region
     host = [{"A": s["A"].cpu().pin_memory(), "b": s["b"].cpu().pin_memory()} for s in systems]
     x_host = torch.empty(n * nrhs, dtype=torch.float64).pin_memory()
 
     def step_e2e(k):
         h = host[k % len(host)]
-        solver.solve_host(h["A"], h["b"], x_host)
+        solver.solve_mixed_host(h["A"], h["b"], x_host)
 
     for k in range(min(args.warmup, 1)):
         step_e2e(k)
     e2e_total, e2e_per = time_steps(step_e2e, args.steps, stream)
 
-    t = torch.tensor([total_ms, e2e_total], dtype=torch.float64, device=device)
+    t = torch.tensor([total_ms, e2e_total, plain_total], dtype=torch.float64, device=device)
     if world > 1:
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    total_ms, e2e_total = float(t[0]), float(t[1])
+    total_ms, e2e_total, plain_total = float(t[0]), float(t[1]), float(t[2])
     if rank != 0:
         return None
 
     # roofline of the dominant kernel (largest share of device time)
     dom_name, dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
     prof_total = sum(v["ms"] for v in prof.values())
-    achieved = dom["flops"] / (dom["ms"] * 1e-3) / 1e12  # TFLOP/s
-    peak = peak_fp64 / 1e3
+    roof = roofline_for(dom_name, dom, peak_fp64)
     kernels = {k: {"scopes": v["calls"], "launches": v["launches"], "ms": round(v["ms"], 3),
                    "share": round(v["ms"] / prof_total, 4),
-                   "tflops": round(v["flops"] / max(v["ms"], 1e-9) / 1e9, 4) if v["flops"] else None}
+                   "tflops": round(v["flops"] / max(v["ms"], 1e-9) / 1e9, 4) if v["flops"] else None,
+                   "gbs": round(v["bytes"] / max(v["ms"], 1e-9) / 1e6, 1) if v["bytes"] else None}
                for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])}
     launches = int(sum(v["launches"] for v in prof.values()))
 
     value = world * args.steps / (total_ms / 1e3)
+    plain_value = world * plain_steps / (plain_total / 1e3)
     out = {
         "metric": METRIC, "value": round(value, 4), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: A = Q1 diag(sigma) Q2, Q from Householder QR of Gaussian matrices (seed 3), sigma "
                 "geometric 1..1/kappa, kappa in {1e2,1e6,1e10} rotating per step; b = A x_true, x_true U[-1,1)",
-        "config": {"workload": f"dense LU solve n={n} nrhs={nrhs} (BOLA getrf + laswp + 2 trsm), "
-                               f"backward error <= {BERR_TARGET:g}",
-                   "path": "plain FP64, BOLA-exact blocked LU (NB=32) + triangular solves",
+        "config": {"workload": f"dense LU solve n={n} nrhs={nrhs} to backward error <= {BERR_TARGET:g}",
+                   "path": "mixed: 3xTF32 tcgen05 LU (FP32 storage, per-block-column scaling) + FP64 iterative "
+                           "refinement, plain FP64 fallback on stall",
                    "replicas": "one independent solve stream per GPU (no collective)",
                    "l2": "inputs larger than L2 (512 MiB matrix per step)"},
         "latency_ms": {"p50": round(statistics.median(per), 3),
                        "p99": round(float(np.percentile(per, 99)), 3)},
+        "plain_fp64": {"value": round(plain_value, 4), "unit": "solves/s", "steps": plain_steps,
+                       "ms_per_step": round(plain_total / plain_steps, 3),
+                       "path": "BOLA-exact bola_dgetrf + bola_dgetrs (FP64, NB=32)"},
+        "speedup_vs_plain_fp64": round(value / plain_value, 3),
         "backward_error": berr,
         "backward_error_ok": all(v <= BERR_TARGET for v in berr.values()),
+        "refinement": paths,
         "e2e": {"value": round(world * args.steps / (e2e_total / 1e3), 4), "unit": "solves/s",
                 "h2d_bytes_per_step": 8 * (n * n + n * nrhs), "d2h_bytes_per_step": 8 * n * nrhs},
-        "roofline": {"kernel": dom_name, "bound": "fp64", "achieved": round(achieved, 4), "peak": round(peak, 4),
-                     "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
-                     "peak_source": "FP64 DFMA throughput measured in this run (bola_measure_fp64_peak); "
-                                    "GB300 FP64 runs on the DFMA pipe, not the tensor cores",
-                     "traffic": None},
+        "roofline": roof,
         "kernels": kernels,
         "gpu_launches": launches,
     }
@@ -297,6 +336,27 @@ def run_ours(args, rank, world, device):
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(systems[0], n, nrhs, budget_s=12.0)
     return out
+
+
+def roofline_for(name, v, peak_fp64_gflops):
+    """The dominant kernel's achieved rate against its bounding peak.
+    FP64 kernels: DFMA peak measured in this run.  Tensor-core update: HBM
+    (it reads and writes the FP32 trailing matrix once per step).  Others:
+    HBM bytes of their algorithmic traffic."""
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    secs = v["ms"] * 1e-3
+    if name in ("dgemm", "mixed_residual", "dgemm_edge"):
+        ach = v["flops"] / secs / 1e12
+        pk = peak_fp64_gflops / 1e3
+        return {"kernel": name, "bound": "fp64", "achieved": round(ach, 4), "peak": round(pk, 4), "unit": "TFLOP/s",
+                "frac": round(ach / pk, 4), "traffic": None,
+                "peak_source": "FP64 DFMA throughput measured in this run (bola_measure_fp64_peak)"}
+    ach = v["bytes"] / secs / 1e9
+    return {"kernel": name, "bound": "hbm", "achieved": round(ach, 2), "peak": hbm, "unit": "GB/s",
+            "frac": round(ach / hbm, 4), "traffic": None,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s"}
 
 
 # ---------------------------------------------------------------- CPU ----

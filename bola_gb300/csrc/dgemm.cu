@@ -248,28 +248,24 @@ template <bool TA, bool TB>
 void launch_tile(Tile t, bool partial, cudaStream_t s, dim3 grid, int64_t m8, int64_t n4, int64_t K,
                  double alpha, const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
                  double *C, int64_t ldc, int kc, const int32_t *info, int tri, int64_t cps, double *P) {
-  if (partial) {
-    launch_main<32, 32, 2, 2, TA, TB, true>(s, grid, m8, n4, K, alpha, A, lda, B, ldb, beta, C, ldc, kc,
-                                           info, tri, cps, P);
-  } else if (t.bm == 64 && t.bn == 64) {
-    launch_main<64, 64, 4, 4, TA, TB, false>(s, grid, m8, n4, K, alpha, A, lda, B, ldb, beta, C, ldc, kc,
-                                            info, tri, cps, P);
-  } else if (t.bm == 64 && t.bn == 32) {
-    launch_main<64, 32, 4, 2, TA, TB, false>(s, grid, m8, n4, K, alpha, A, lda, B, ldb, beta, C, ldc, kc,
-                                            info, tri, cps, P);
-  } else if (t.bm == 32 && t.bn == 64) {
-    launch_main<32, 64, 2, 4, TA, TB, false>(s, grid, m8, n4, K, alpha, A, lda, B, ldb, beta, C, ldc, kc,
-                                            info, tri, cps, P);
-  } else {
-    launch_main<32, 32, 2, 2, TA, TB, false>(s, grid, m8, n4, K, alpha, A, lda, B, ldb, beta, C, ldc, kc,
-                                            info, tri, cps, P);
-  }
+#define BOLA_LM(bm, bn, tm, tn)                                                                                    \
+  (partial ? launch_main<bm, bn, tm, tn, TA, TB, true>(s, grid, m8, n4, K, alpha, A, lda, B, ldb, beta, C, ldc, kc, \
+                                                     info, tri, cps, P)                                            \
+           : launch_main<bm, bn, tm, tn, TA, TB, false>(s, grid, m8, n4, K, alpha, A, lda, B, ldb, beta, C, ldc,    \
+                                                      kc, info, tri, cps, P))
+  if (t.bm == 64 && t.bn == 64) BOLA_LM(64, 64, 4, 4);
+  else if (t.bm == 64 && t.bn == 32) BOLA_LM(64, 32, 4, 2);
+  else if (t.bm == 32 && t.bn == 64) BOLA_LM(32, 64, 2, 4);
+  else if (t.bm == 64 && t.bn == 16) BOLA_LM(64, 16, 4, 1);
+  else BOLA_LM(32, 32, 2, 2);
+#undef BOLA_LM
 }
 
 // Pick the tile whose most-loaded SM carries the least tile area (ties go to
 // the larger tile).
 Tile choose_tile(int64_t m8, int64_t n4, int sms) {
-  const Tile cands[4] = {{64, 64}, {64, 32}, {32, 64}, {32, 32}};
+  // 64x16 serves skinny outputs such as 16 right-hand sides
+  const Tile cands[5] = {{64, 64}, {64, 32}, {32, 64}, {32, 32}, {64, 16}};
   Tile best = cands[0];
   double best_cost = 1e300;
   for (const Tile &t : cands) {
@@ -300,8 +296,7 @@ int dgemm_exact(cudaStream_t s, char ta, char tb, int64_t m, int64_t n, int64_t 
     bool partial = false;
     int64_t cps = 0, nsplit = 1;
     if (tiles < sms && nchunks >= 2) {
-      const int64_t t32 = cdiv(m8, 32) * cdiv(n4, 32);
-      nsplit = imin(nchunks, cdiv(2 * (int64_t)sms, t32));
+      nsplit = imin(nchunks, cdiv(2 * (int64_t)sms, tiles));
       cps = cdiv(nchunks, nsplit);
       nsplit = cdiv(nchunks, cps);
       const double bytes = 8.0 * (double)nchunks * (double)m8 * (double)n4;
@@ -312,10 +307,9 @@ int dgemm_exact(cudaStream_t s, char ta, char tb, int64_t m, int64_t n, int64_t 
     if (partial) {
       Scratch P;
       BOLA_TRY(P.alloc((size_t)(8 * nchunks * m8 * n4), s));
-      dim3 grid((unsigned)cdiv(m8, 32), (unsigned)cdiv(n4, 32), (unsigned)nsplit);
-      Tile t32{32, 32};
-#define BOLA_LT(a, b)                                                                              \
-  launch_tile<a, b>(t32, true, s, grid, m8, n4, K, alpha, A, lda, B, ldb, beta, C, ldc, kc, info, tri, \
+      dim3 grid((unsigned)cdiv(m8, t.bm), (unsigned)cdiv(n4, t.bn), (unsigned)nsplit);
+#define BOLA_LT(a, b)                                                                            \
+  launch_tile<a, b>(t, true, s, grid, m8, n4, K, alpha, A, lda, B, ldb, beta, C, ldc, kc, info, tri, \
                     cps, P.as<double>())
       if (!TA && !TB) BOLA_LT(false, false);
       else if (!TA && TB) BOLA_LT(false, true);

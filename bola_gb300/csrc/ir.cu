@@ -143,47 +143,77 @@ __global__ void copy_cols(int64_t n, int nrhs, const double *__restrict__ src, i
   dst[i + c * ldd] = src[i + c * lds];
 }
 
+// Inverses of the 64x64 diagonal blocks of L (unit lower) and U, once per
+// factorisation: block b -> Dl[b], Du[b] (column-major 64x64).  A thread per
+// column of the inverse, substitution down (L) or up (U) the block.
+__global__ void __launch_bounds__(64)
+diag_block_inverses(int64_t n, const float *__restrict__ W, int64_t ldw, float *Dl, float *Du) {
+  __shared__ float B[TB][TB + 1];
+  const int64_t k0 = (int64_t)blockIdx.x * TB;
+  const int kb = (int)imin(TB, n - k0);
+  for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) B[e % kb][e / kb] = W[(k0 + e % kb) + (k0 + e / kb) * ldw];
+  __syncthreads();
+  const int j = threadIdx.x;
+  float *L = Dl + (int64_t)blockIdx.x * TB * TB, *U = Du + (int64_t)blockIdx.x * TB * TB;
+  if (j >= TB) return;
+  float x[TB];
+#pragma unroll
+  for (int i = 0; i < TB; ++i) {  // L x = e_j (unit diagonal)
+    float t = (i == j) ? 1.f : 0.f;
+#pragma unroll
+    for (int k = 0; k < i; ++k) t = fmaf(-B[i][k], x[k], t);
+    x[i] = (i < kb) ? t : 0.f;
+  }
+#pragma unroll
+  for (int i = 0; i < TB; ++i) L[i + j * TB] = (j < kb) ? x[i] : 0.f;
+#pragma unroll
+  for (int ii = 0; ii < TB; ++ii) {  // U x = e_j
+    const int i = TB - 1 - ii;
+    float t = (i == j) ? 1.f : 0.f;
+#pragma unroll
+    for (int k = i + 1; k < TB; ++k) t = fmaf(-B[i][k], x[k], t);
+    x[i] = (i < kb && j < kb) ? t / B[i][i] : 0.f;
+  }
+#pragma unroll
+  for (int i = 0; i < TB; ++i) U[i + j * TB] = x[i];
+}
+
 // One block step of a blocked triangular solve with nrhs <= 32 right-hand
-// sides (n x nrhs, ld n).  LOWER: unit-lower L, forward; else upper U with
-// its diagonal, backward.  Every CTA solves the 64x64 diagonal block
-// k0..k0+kb of `y` from shared memory (a warp per right-hand side), CTA 0
-// writes the solved block to `out`, and every CTA applies it to its 256-row
-// slice of the rows below (LOWER) or above, in place in `y`.  The solved
-// block never goes back into `y`, which other CTAs of the launch still read.
+// sides (n x nrhs, ld n).  LOWER: unit-lower L, forward; else U, backward.
+// Every CTA forms the solved block ys = Dinv * y[k0:k0+kb] (a small GEMM with
+// the precomputed inverse), CTA 0 writes it to `out`, and every CTA then
+// subtracts L[rows, blk] * ys (or U[rows, blk] * ys) from its 64-row slice of
+// the rows below (above) in place in `y`.  The solved block never goes back
+// into `y`, which other CTAs of the launch still read.
 template <bool LOWER>
 __global__ void __launch_bounds__(256)
-trsv_block(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, int64_t k0, int kb, float *y,
-           float *out) {
-  __shared__ float D[TB * TB];      // diagonal block, column-major
-  __shared__ float ys[MAXRHS][TB];  // solved block of y
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int e = tid; e < kb * kb; e += blockDim.x) {
-    const int r = e % kb, c = e / kb;
-    D[r + c * TB] = W[(k0 + r) + (k0 + c) * ldw];
+trsv_block(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, const float *__restrict__ Dinv, int64_t k0,
+           int kb, float *y, float *out) {
+  __shared__ float DiT[TB][TB];     // DiT[k][r] = Dinv(r, k)
+  __shared__ float rb[MAXRHS][TB];
+  __shared__ float ys[MAXRHS][TB];
+  __shared__ float Ls[TB][TB];      // Ls[k][r]: the update tile of this CTA's rows
+  const int tid = threadIdx.x;
+  const float *D = Dinv + (k0 / TB) * TB * TB;
+  for (int e = tid; e < TB * TB; e += blockDim.x) DiT[e / TB][e % TB] = D[e];
+  for (int e = tid; e < TB * nrhs; e += blockDim.x) {
+    const int r = e % TB, c = e / TB;
+    rb[c][r] = r < kb ? y[(k0 + r) + (int64_t)c * n] : 0.f;
   }
-  for (int e = tid; e < kb * nrhs; e += blockDim.x) {
-    const int r = e % kb, c = e / kb;
-    ys[c][r] = y[(k0 + r) + (int64_t)c * n];
+  const int64_t rbeg = LOWER ? k0 + kb : 0;
+  const int64_t rend = LOWER ? n : k0;
+  const int64_t i0 = rbeg + (int64_t)blockIdx.x * TB;
+  for (int e = tid; e < TB * kb; e += blockDim.x) {
+    const int r = e % TB, k = e / TB;
+    Ls[k][r] = (i0 + r < rend) ? W[(i0 + r) + (k0 + k) * ldw] : 0.f;
   }
   __syncthreads();
-  for (int c = warp; c < nrhs; c += blockDim.x >> 5) {
-    float b0 = lane < kb ? ys[c][lane] : 0.f;
-    float b1 = lane + 32 < kb ? ys[c][lane + 32] : 0.f;
-    for (int s = 0; s < kb; ++s) {
-      const int k = LOWER ? s : kb - 1 - s;
-      float bk = __shfl_sync(0xffffffffu, k < 32 ? b0 : b1, k & 31);
-      if (!LOWER) {
-        bk = bk / D[k + k * TB];
-        if (k == lane) b0 = bk;
-        if (k == lane + 32) b1 = bk;
-      }
-      const bool in0 = LOWER ? (lane > k && lane < kb) : (lane < k);
-      const bool in1 = LOWER ? (lane + 32 > k && lane + 32 < kb) : (lane + 32 < k);
-      if (in0) b0 = fmaf(-D[lane + k * TB], bk, b0);
-      if (in1) b1 = fmaf(-D[lane + 32 + k * TB], bk, b1);
-    }
-    if (lane < kb) ys[c][lane] = b0;
-    if (lane + 32 < kb) ys[c][lane + 32] = b1;
+  for (int e = tid; e < TB * nrhs; e += blockDim.x) {
+    const int r = e % TB, c = e / TB;
+    float acc = 0.f;
+#pragma unroll 16
+    for (int k = 0; k < TB; ++k) acc = fmaf(DiT[k][r], rb[c][k], acc);
+    ys[c][r] = acc;
   }
   __syncthreads();
   if (blockIdx.x == 0) {
@@ -192,38 +222,32 @@ trsv_block(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, int64_
       out[(k0 + r) + (int64_t)c * n] = ys[c][r];
     }
   }
-  // rows to update: below (LOWER) or above
-  const int64_t rbeg = LOWER ? k0 + kb : 0;
-  const int64_t rend = LOWER ? n : k0;
-  const int64_t i = rbeg + (int64_t)blockIdx.x * blockDim.x + tid;
+  const int r = tid >> 2, part = tid & 3;
+  const int64_t i = i0 + r;
   if (i >= rend) return;
-  float acc[MAXRHS];
-#pragma unroll
-  for (int c = 0; c < MAXRHS; ++c) acc[c] = 0.f;
-  for (int k = 0; k < kb; ++k) {
-    const float l = W[i + (k0 + k) * ldw];
-#pragma unroll
-    for (int c = 0; c < MAXRHS; ++c)
-      if (c < nrhs) acc[c] = fmaf(l, ys[c][k], acc[c]);
+  for (int c = part; c < nrhs; c += 4) {
+    float acc = 0.f;
+#pragma unroll 16
+    for (int k = 0; k < TB; ++k) acc = fmaf(Ls[k][r], ys[c][k], acc);
+    y[i + (int64_t)c * n] -= acc;
   }
-#pragma unroll
-  for (int c = 0; c < MAXRHS; ++c)
-    if (c < nrhs) y[i + (int64_t)c * n] -= acc[c];
 }
 
 // y (right-hand sides, overwritten) -> out (solution)
-int trsv(cudaStream_t s, bool lower, int64_t n, int nrhs, const float *W, int64_t ldw, float *y, float *out) {
-  ProfScope prof(s, lower ? "trsv_lower" : "trsv_upper", (double)n * n * nrhs, 4.0 * (double)n * n / 2);
+int trsv(cudaStream_t s, bool lower, int64_t n, int nrhs, const float *W, int64_t ldw, const float *Dinv, float *y,
+         float *out) {
+  ProfScope prof(s, lower ? "trsv_lower" : "trsv_upper", (double)n * n * nrhs, 4.0 * (double)n * n / 2,
+                 (int)cdiv(n, TB));
   const int64_t nb = cdiv(n, TB);
   for (int64_t b = 0; b < nb; ++b) {
     const int64_t k0 = lower ? b * TB : (nb - 1 - b) * TB;
     const int kb = (int)imin(TB, n - k0);
     const int64_t rows = lower ? n - k0 - kb : k0;
-    const unsigned grid = (unsigned)imax(1, cdiv(rows, 256));
+    const unsigned grid = (unsigned)imax(1, cdiv(rows, TB));
     if (lower)
-      trsv_block<true><<<grid, 256, 0, s>>>(n, nrhs, W, ldw, k0, kb, y, out);
+      trsv_block<true><<<grid, 256, 0, s>>>(n, nrhs, W, ldw, Dinv, k0, kb, y, out);
     else
-      trsv_block<false><<<grid, 256, 0, s>>>(n, nrhs, W, ldw, k0, kb, y, out);
+      trsv_block<false><<<grid, 256, 0, s>>>(n, nrhs, W, ldw, Dinv, k0, kb, y, out);
     BOLA_CHECK_LAUNCH();
   }
   return 0;
@@ -232,7 +256,7 @@ int trsv(cudaStream_t s, bool lower, int64_t n, int nrhs, const float *W, int64_
 // Device workspace of one mixed solve, cached per device and grown on demand.
 struct Workspace {
   int64_t n = 0, nrhs = 0;
-  float *W = nullptr, *y = nullptr, *z = nullptr;
+  float *W = nullptr, *y = nullptr, *z = nullptr, *Dl = nullptr, *Du = nullptr;
   double *scale = nullptr, *r = nullptr, *d = nullptr, *norms = nullptr, *rowsum = nullptr;
   int32_t *ipiv = nullptr, *perm = nullptr, *info = nullptr;
   MixedLU lu;
@@ -240,13 +264,15 @@ struct Workspace {
 
 int ws_reserve(Workspace &w, int64_t n, int64_t nrhs, int kind, cudaStream_t s) {
   if (n > w.n || nrhs > w.nrhs) {
-    for (void *p : {(void *)w.W, (void *)w.y, (void *)w.z, (void *)w.scale, (void *)w.r, (void *)w.d, (void *)w.norms,
+    for (void *p : {(void *)w.W, (void *)w.y, (void *)w.z, (void *)w.Dl, (void *)w.Du, (void *)w.scale, (void *)w.r, (void *)w.d, (void *)w.norms,
                     (void *)w.rowsum, (void *)w.ipiv, (void *)w.perm, (void *)w.info})
       if (p) cudaFree(p);
     w = Workspace{};
     BOLA_TRY_CUDA(cudaMalloc(&w.W, sizeof(float) * n * n));
     BOLA_TRY_CUDA(cudaMalloc(&w.y, sizeof(float) * n * nrhs));
     BOLA_TRY_CUDA(cudaMalloc(&w.z, sizeof(float) * n * nrhs));
+    BOLA_TRY_CUDA(cudaMalloc(&w.Dl, sizeof(float) * cdiv(n, TB) * TB * TB));
+    BOLA_TRY_CUDA(cudaMalloc(&w.Du, sizeof(float) * cdiv(n, TB) * TB * TB));
     BOLA_TRY_CUDA(cudaMalloc(&w.scale, sizeof(double) * cdiv(n, TB)));
     BOLA_TRY_CUDA(cudaMalloc(&w.r, sizeof(double) * n * nrhs));
     BOLA_TRY_CUDA(cudaMalloc(&w.d, sizeof(double) * n * nrhs));
@@ -270,8 +296,8 @@ int correction(cudaStream_t s, Workspace &w, int64_t n, int nrhs, const double *
   const unsigned g = (unsigned)cdiv(n * nrhs, 256);
   permute_scale_down<<<g, 256, 0, s>>>(n, nrhs, r, ldr, w.perm, rs, w.y);
   BOLA_CHECK_LAUNCH();
-  BOLA_TRY(trsv(s, true, n, nrhs, w.W, n, w.y, w.z));
-  BOLA_TRY(trsv(s, false, n, nrhs, w.W, n, w.z, w.y));
+  BOLA_TRY(trsv(s, true, n, nrhs, w.W, n, w.Dl, w.y, w.z));
+  BOLA_TRY(trsv(s, false, n, nrhs, w.W, n, w.Du, w.z, w.y));
   update_x<<<g, 256, 0, s>>>(n, nrhs, w.y, w.scale, rs, x, ldx, assign ? 1 : 0);
   BOLA_CHECK_LAUNCH();
   return 0;
@@ -323,6 +349,7 @@ extern "C" int bola_dgesv_mixed(int64_t n, int64_t nrhs, const double *a, int64_
   {
     ProfScope prof(s, "mixed_perm");
     compose_perm<<<1, 1024, sizeof(int32_t) * n, s>>>(n, w.ipiv, w.perm);
+    diag_block_inverses<<<(unsigned)cdiv(n, TB), TB, 0, s>>>(n, w.W, n, w.Dl, w.Du);
   }
   BOLA_CHECK_LAUNCH();
   int32_t finfo = 0, ferr = 0;
