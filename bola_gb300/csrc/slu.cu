@@ -5,7 +5,7 @@
 // rounded to an FP32 working matrix W.  Blocked right-looking LU with partial
 // pivoting and NB = 64 = the K of the tensor-core update:
 //   spanel_kernel   the (n-j) x 64 panel on a cluster of <=16 CTAs, the rows
-//                   held in registers; per column each CTA pushes its pivot
+//                   held in shared memory; per column each CTA pushes its pivot
 //                   candidate (key + row) into every CTA's shared memory, so
 //                   a column costs one CTA barrier pair and one cluster
 //                   barrier.  It also writes L21 as the K-major A operand
@@ -33,14 +33,6 @@ struct SSlot {
   uint32_t khi, klo;  // |pivot candidate| bits, ~row
   float v[SNB];       // the candidate row
 };
-
-template <int N>
-__device__ __forceinline__ float pick(const float (&a)[N], int j) {
-  float v = 0.f;
-#pragma unroll
-  for (int c = 0; c < N; ++c) v = (c == j) ? a[c] : v;
-  return v;
-}
 
 __device__ __forceinline__ float tf32_round(float x) {
   uint32_t u = __float_as_uint(x);
@@ -82,8 +74,13 @@ __device__ __forceinline__ void write_operand_row(int kind, void *op, float *op_
 }
 
 // Panel LU of W[0:mp, 0:jb] (W points at the panel's top-left).  ipiv gets
-// global 1-based rows (col0 + local + 1).  RPT rows per thread.
-template <int RPT>
+// global 1-based rows (col0 + local + 1).  CTA cr of the cluster owns panel
+// rows [cr*R, cr*R + R), kept in shared memory column-major with an odd
+// pitch (R + 1) so that both a thread walking its row and a warp walking a
+// column are conflict-free.  Per column: warp-redux pivot search, one CTA
+// barrier, warp 0 pushes the CTA's candidate row (and row j if it owns it)
+// into every CTA, one cluster barrier, every CTA picks the same winner from
+// its own slots, swaps, one CTA barrier, rank-1 update of the active columns.
 __global__ void __launch_bounds__(SPT)
 spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0, int32_t *info, int kind,
               void *aop, float *aop_lo, int64_t R) {
@@ -92,72 +89,66 @@ spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
   const int cr = (int)cluster.block_rank();
   __shared__ SSlot slots[2][SMAXC];
   __shared__ float rowj[2][SNB];
-  __shared__ float myrow[SNB], myrowj[SNB];
   __shared__ uint64_t wkey[SPT / 32];
+  extern __shared__ float sp[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t RP = R + 1;
   const int64_t r0 = (int64_t)cr * R;
   const int64_t r1 = imin(mp, r0 + R);
+  const int64_t nr = r1 > r0 ? r1 - r0 : 0;
 
-  float a[RPT][SNB];
-#pragma unroll
-  for (int q = 0; q < RPT; ++q) {
-    const int64_t g = r0 + tid + (int64_t)SPT * q;
-    const bool valid = g < r1;
-#pragma unroll
-    for (int c = 0; c < SNB; ++c) a[q][c] = (valid && c < jb) ? W[g + c * ldw] : 0.f;
+  for (int64_t e = tid; e < nr * jb; e += SPT) {
+    const int64_t il = e % nr;
+    const int c = (int)(e / nr);
+    sp[c * RP + il] = W[(r0 + il) + c * ldw];
   }
+  __syncthreads();
 
   for (int j = 0; j < jb; ++j) {
     const int par = j & 1;
-    // -- local pivot candidate: key = (|v| bits, ~row), max wins, ties -> lowest row
+    // -- pivot candidate of this CTA: key = (|v| bits, ~row), max wins, ties -> lowest row
     uint64_t best = 0;
-#pragma unroll
-    for (int q = 0; q < RPT; ++q) {
-      const int64_t g = r0 + tid + (int64_t)SPT * q;
-      if (g < r1 && g >= j) {
-        const float v = fabsf(pick(a[q], j));
-        const uint32_t bits = (v == v) ? __float_as_uint(v) : 0u;
-        const uint64_t key = ((uint64_t)bits << 32) | (0xFFFFFFFFu - (uint32_t)g);
-        best = key > best ? key : best;
-      }
+    for (int64_t il = tid; il < nr; il += SPT) {
+      const int64_t g = r0 + il;
+      if (g < j) continue;
+      const float v = fabsf(sp[j * RP + il]);
+      const uint32_t bits = (v == v) ? __float_as_uint(v) : 0u;
+      const uint64_t key = ((uint64_t)bits << 32) | (0xFFFFFFFFu - (uint32_t)g);
+      best = key > best ? key : best;
     }
     const uint32_t hi = (uint32_t)(best >> 32), lo = (uint32_t)best;
     const uint32_t mhi = __reduce_max_sync(0xffffffffu, hi);
     const uint32_t mlo = __reduce_max_sync(0xffffffffu, hi == mhi ? lo : 0u);
     if (lane == 0) wkey[warp] = ((uint64_t)mhi << 32) | mlo;
     __syncthreads();
-    uint64_t ck = 0;
-#pragma unroll
-    for (int w = 0; w < SPT / 32; ++w) ck = wkey[w] > ck ? wkey[w] : ck;
-    const int64_t gbest = ck ? (int64_t)(0xFFFFFFFFu - (uint32_t)ck) : -1;
-    const bool own_j = j >= r0 && j < r1;
-#pragma unroll
-    for (int q = 0; q < RPT; ++q) {
-      const int64_t g = r0 + tid + (int64_t)SPT * q;
-      if (g == gbest) {
-#pragma unroll
-        for (int c = 0; c < SNB; ++c) myrow[c] = a[q][c];
-      }
-      if (own_j && g == j) {
-#pragma unroll
-        for (int c = 0; c < SNB; ++c) myrowj[c] = a[q][c];
-      }
-    }
-    __syncthreads();
-    // -- push this CTA's candidate (and row j if owned) into every CTA
+    // -- warp 0 pushes the candidate (and row j if owned) into every CTA
     if (warp == 0) {
+      uint64_t ck = 0;
+#pragma unroll
+      for (int w = 0; w < SPT / 32; ++w) ck = wkey[w] > ck ? wkey[w] : ck;
+      const int64_t gbest = ck ? (int64_t)(0xFFFFFFFFu - (uint32_t)ck) : -1;
+      float c0 = 0.f, c1 = 0.f, j0v = 0.f, j1v = 0.f;
+      if (gbest >= 0) {
+        c0 = lane < jb ? sp[lane * RP + (gbest - r0)] : 0.f;
+        c1 = lane + 32 < jb ? sp[(lane + 32) * RP + (gbest - r0)] : 0.f;
+      }
+      const bool own_j = j >= r0 && j < r1;
+      if (own_j) {
+        j0v = lane < jb ? sp[lane * RP + (j - r0)] : 0.f;
+        j1v = lane + 32 < jb ? sp[(lane + 32) * RP + (j - r0)] : 0.f;
+      }
       for (int d = 0; d < C; ++d) {
         SSlot *rs = cluster.map_shared_rank(&slots[par][cr], d);
         if (lane == 0) {
           rs->khi = (uint32_t)(ck >> 32);
           rs->klo = (uint32_t)ck;
         }
-        rs->v[lane] = myrow[lane];
-        rs->v[lane + 32] = myrow[lane + 32];
+        rs->v[lane] = c0;
+        rs->v[lane + 32] = c1;
         if (own_j) {
           float *rj = cluster.map_shared_rank(&rowj[par][0], d);
-          rj[lane] = myrowj[lane];
-          rj[lane + 32] = myrowj[lane + 32];
+          rj[lane] = j0v;
+          rj[lane + 32] = j1v;
         }
       }
     }
@@ -165,11 +156,11 @@ spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
     // -- the winner, identical in every CTA
     uint64_t wk = 0;
     int ws = 0;
-    for (int s = 0; s < C; ++s) {
-      const uint64_t k = ((uint64_t)slots[par][s].khi << 32) | slots[par][s].klo;
+    for (int s2 = 0; s2 < C; ++s2) {
+      const uint64_t k = ((uint64_t)slots[par][s2].khi << 32) | slots[par][s2].klo;
       if (k > wk) {
         wk = k;
-        ws = s;
+        ws = s2;
       }
     }
     const int64_t jp = wk ? (int64_t)(0xFFFFFFFFu - (uint32_t)wk) : (int64_t)j;
@@ -181,37 +172,36 @@ spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
       inv = 0.0f;
       if (cr == 0 && tid == 0) atomicCAS(info, 0, col0 + j + 1);
     }
-#pragma unroll
-    for (int q = 0; q < RPT; ++q) {
-      const int64_t g = r0 + tid + (int64_t)SPT * q;
-      if (g >= r1) continue;
-      if (jp != j && g == j) {
-#pragma unroll
-        for (int c = 0; c < SNB; ++c) a[q][c] = prow[c];
-      } else if (jp != j && g == jp) {
-#pragma unroll
-        for (int c = 0; c < SNB; ++c) a[q][c] = rowj[par][c];
-      }
-      if (g > j) {
-        const float l = pick(a[q], j) * inv;
-#pragma unroll
-        for (int c = 0; c < SNB; ++c) {
-          if (c == j) a[q][c] = l;
-          if (c > j) a[q][c] = fmaf(-l, prow[c], a[q][c]);
-        }
-      }
+    if (jp != j && tid < jb) {
+      if (j >= r0 && j < r1) sp[tid * RP + (j - r0)] = prow[tid];
+      if (jp >= r0 && jp < r1) sp[tid * RP + (jp - r0)] = rowj[par][tid];
+    }
+    __syncthreads();
+    for (int64_t il = tid; il < nr; il += SPT) {
+      const int64_t g = r0 + il;
+      if (g <= j) continue;
+      const float l = sp[j * RP + il] * inv;
+      sp[j * RP + il] = l;
+      for (int c = j + 1; c < jb; ++c) sp[c * RP + il] = fmaf(-l, prow[c], sp[c * RP + il]);
     }
   }
+  __syncthreads();
 
   // -- write back the panel and the update's A operand (rows below the panel)
+  for (int64_t e = tid; e < nr * jb; e += SPT) {
+    const int64_t il = e % nr;
+    const int c = (int)(e / nr);
+    W[(r0 + il) + c * ldw] = sp[c * RP + il];
+  }
+  if (aop != nullptr) {
+    for (int64_t il = tid; il < nr; il += SPT) {
+      const int64_t g = r0 + il;
+      if (g < jb) continue;
+      float v[SNB];
 #pragma unroll
-  for (int q = 0; q < RPT; ++q) {
-    const int64_t g = r0 + tid + (int64_t)SPT * q;
-    if (g >= r1) continue;
-#pragma unroll
-    for (int c = 0; c < SNB; ++c)
-      if (c < jb) W[g + c * ldw] = a[q][c];
-    if (aop != nullptr && g >= jb) write_operand_row(kind, aop, aop_lo, g - jb, a[q]);
+      for (int c = 0; c < SNB; ++c) v[c] = c < jb ? sp[c * RP + il] : 0.f;
+      write_operand_row(kind, aop, aop_lo, g - jb, v);
+    }
   }
   cluster.sync();
 }
@@ -277,30 +267,30 @@ __global__ void zero_i32(int32_t *p) { *p = 0; }
 
 int launch_spanel(cudaStream_t s, float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0,
                   int32_t *info, int kind, void *aop, float *aop_lo) {
-  int C = (int)imin(SMAXC, imax(1, cdiv(mp, SPT)));
-  const int rpt = (int)cdiv(mp, (int64_t)C * SPT);
-  if (rpt > 2) return fail(BOLA_ERR_UNSUPPORTED, "mixed LU: panel of %lld rows exceeds 8192", (long long)mp);
+  const int C = (int)imin(SMAXC, imax(1, cdiv(mp, SPT)));
   const int64_t R = cdiv(mp, C);
+  const size_t smem = sizeof(float) * SNB * (size_t)(R + 1);
+  if (smem > 200 * 1024) return fail(BOLA_ERR_UNSUPPORTED, "mixed LU: panel of %lld rows too tall", (long long)mp);
+  static bool attr = false;
+  if (!attr) {
+    BOLA_TRY_CUDA(cudaFuncSetAttribute(spanel_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    BOLA_TRY_CUDA(cudaFuncSetAttribute(spanel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr = true;
+  }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)C, 1, 1);
   cfg.blockDim = dim3(SPT, 1, 1);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = (unsigned)C;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
+  cudaLaunchAttribute attr1[1];
+  attr1[0].id = cudaLaunchAttributeClusterDimension;
+  attr1[0].val.clusterDim.x = (unsigned)C;
+  attr1[0].val.clusterDim.y = 1;
+  attr1[0].val.clusterDim.z = 1;
+  cfg.attrs = attr1;
   cfg.numAttrs = 1;
-  ProfScope prof(s, "spanel", 2.0 * (double)mp * SNB * SNB / 2.0);
-  if (rpt == 1) {
-    BOLA_TRY_CUDA(cudaFuncSetAttribute(spanel_kernel<1>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, spanel_kernel<1>, W, ldw, mp, jb, ipiv, col0, info, kind, aop, aop_lo, R));
-  } else {
-    BOLA_TRY_CUDA(cudaFuncSetAttribute(spanel_kernel<2>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, spanel_kernel<2>, W, ldw, mp, jb, ipiv, col0, info, kind, aop, aop_lo, R));
-  }
+  ProfScope prof(s, "spanel", (double)mp * SNB * SNB, 8.0 * (double)mp * SNB);
+  BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, spanel_kernel, W, ldw, mp, jb, ipiv, col0, info, kind, aop, aop_lo, R));
   return 0;
 }
 
