@@ -183,7 +183,7 @@ class Solver:
     def solve_mixed(self, A, b, kind=2):
         """bola_dgesv_mixed; returns the bola_mixed_info of the call."""
         from bola_gb300 import _lib
-        opts = _lib.MixedOpts(kind, 30, BERR_TARGET, 1)
+        opts = _lib.MixedOpts(kind, 30, BERR_TARGET, 1, 1)
         info = _lib.MixedInfo()
         st = self.L.bola_dgesv_mixed(self.n, self.nrhs, self._p(A), self.n, self._p(b), self.n, self._p(self.x),
                                      self.n, ctypes.byref(opts), ctypes.byref(info), self.sp)

@@ -195,17 +195,35 @@ trsv_block(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, const 
   __shared__ float Ls[TB][TB];      // Ls[k][r]: the update tile of this CTA's rows
   const int tid = threadIdx.x;
   const float *D = Dinv + (k0 / TB) * TB * TB;
-  for (int e = tid; e < TB * TB; e += blockDim.x) DiT[e / TB][e % TB] = D[e];
-  for (int e = tid; e < TB * nrhs; e += blockDim.x) {
-    const int r = e % TB, c = e / TB;
-    rb[c][r] = r < kb ? y[(k0 + r) + (int64_t)c * n] : 0.f;
-  }
   const int64_t rbeg = LOWER ? k0 + kb : 0;
   const int64_t rend = LOWER ? n : k0;
   const int64_t i0 = rbeg + (int64_t)blockIdx.x * TB;
-  for (int e = tid; e < TB * kb; e += blockDim.x) {
+  // fixed-count loads, all issued before any shared-memory store
+  constexpr int PER = TB * TB / 256;  // 16 per thread
+  float dv[PER], lv[PER], bv[MAXRHS * TB / 256];
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int e = tid + 256 * q;
     const int r = e % TB, k = e / TB;
-    Ls[k][r] = (i0 + r < rend) ? W[(i0 + r) + (k0 + k) * ldw] : 0.f;
+    dv[q] = D[e];
+    lv[q] = (k < kb && i0 + r < rend) ? W[(i0 + r) + (k0 + k) * ldw] : 0.f;
+  }
+#pragma unroll
+  for (int q = 0; q < MAXRHS * TB / 256; ++q) {
+    const int e = tid + 256 * q;
+    const int r = e % TB, c = e / TB;
+    bv[q] = (c < nrhs && r < kb) ? y[(k0 + r) + (int64_t)c * n] : 0.f;
+  }
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int e = tid + 256 * q;
+    DiT[e / TB][e % TB] = dv[q];
+    Ls[e / TB][e % TB] = lv[q];
+  }
+#pragma unroll
+  for (int q = 0; q < MAXRHS * TB / 256; ++q) {
+    const int e = tid + 256 * q;
+    rb[e / TB][e % TB] = bv[q];
   }
   __syncthreads();
   for (int e = tid; e < TB * nrhs; e += blockDim.x) {
@@ -253,11 +271,86 @@ int trsv(cudaStream_t s, bool lower, int64_t n, int nrhs, const float *W, int64_
   return 0;
 }
 
+// ---- GMRES-IR (flexible GMRES on A d = r, preconditioned by the LU) -------------
+// Basis layout: V[(k * nrhs + c) * n + row] (column k of right-hand side c).
+constexpr int GM_M = 24;  // restart length
+
+// H[i + c * ldh] = <V_i,c , w_c> for i < kk (one CTA per (i, c), fixed-order reduction)
+__global__ void gm_dots(int64_t n, int nrhs, const double *__restrict__ V, const double *__restrict__ w, double *H,
+                        int ldh) {
+  __shared__ double red[32];
+  const int i = blockIdx.x, c = blockIdx.y;
+  const double *v = V + ((int64_t)i * nrhs + c) * n;
+  const double *ww = w + (int64_t)c * n;
+  double acc = 0.0;
+  for (int64_t r = threadIdx.x; r < n; r += blockDim.x) acc = fma(v[r], ww[r], acc);
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[q];
+    H[i + c * ldh] = t;
+  }
+}
+
+// w_c -= sum_{i<kk} V_i,c * H[i + c*ldh]
+__global__ void gm_sub(int64_t n, int nrhs, int kk, const double *__restrict__ V, const double *__restrict__ H,
+                       int ldh, double *w) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n * nrhs) return;
+  const int64_t r = e % n;
+  const int c = (int)(e / n);
+  double acc = w[r + (int64_t)c * n];
+  for (int i = 0; i < kk; ++i) acc = fma(-V[((int64_t)i * nrhs + c) * n + r], H[i + c * ldh], acc);
+  w[r + (int64_t)c * n] = acc;
+}
+
+// out[c] = ||w_c||_2 (one CTA per column)
+__global__ void gm_norm2(int64_t n, const double *__restrict__ w, double *out) {
+  __shared__ double red[32];
+  const int c = blockIdx.x;
+  const double *ww = w + (int64_t)c * n;
+  double acc = 0.0;
+  for (int64_t r = threadIdx.x; r < n; r += blockDim.x) acc = fma(ww[r], ww[r], acc);
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[q];
+    out[c] = sqrt(t);
+  }
+}
+
+// V_k,c = w_c / nrm[c]  (zero when the norm is zero)
+__global__ void gm_scale_into(int64_t n, int nrhs, const double *__restrict__ w, const double *nrm, double *Vk) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n * nrhs) return;
+  const int c = (int)(e / n);
+  const double s = nrm[c];
+  Vk[e] = s > 0.0 ? w[e] / s : 0.0;
+}
+
+// x[r, c] += sum_{i<kk} Z_i,c[r] * y[i + c*ldy]
+__global__ void gm_add_zy(int64_t n, int nrhs, int kk, const double *__restrict__ Z, const double *__restrict__ y,
+                          int ldy, double *x, int64_t ldx) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n * nrhs) return;
+  const int64_t r = e % n;
+  const int c = (int)(e / n);
+  double acc = 0.0;
+  for (int i = 0; i < kk; ++i) acc = fma(Z[((int64_t)i * nrhs + c) * n + r], y[i + c * ldy], acc);
+  x[r + c * ldx] += acc;
+}
+
 // Device workspace of one mixed solve, cached per device and grown on demand.
 struct Workspace {
   int64_t n = 0, nrhs = 0;
   float *W = nullptr, *y = nullptr, *z = nullptr, *Dl = nullptr, *Du = nullptr;
   double *scale = nullptr, *r = nullptr, *d = nullptr, *norms = nullptr, *rowsum = nullptr;
+  double *V = nullptr, *Z = nullptr, *H = nullptr;  // GMRES basis, preconditioned basis, Hessenberg column
+  double *hn = nullptr;                              // per-column 2-norms (GMRES)
   int32_t *ipiv = nullptr, *perm = nullptr, *info = nullptr;
   MixedLU lu;
 };
@@ -265,7 +358,8 @@ struct Workspace {
 int ws_reserve(Workspace &w, int64_t n, int64_t nrhs, int kind, cudaStream_t s) {
   if (n > w.n || nrhs > w.nrhs) {
     for (void *p : {(void *)w.W, (void *)w.y, (void *)w.z, (void *)w.Dl, (void *)w.Du, (void *)w.scale, (void *)w.r, (void *)w.d, (void *)w.norms,
-                    (void *)w.rowsum, (void *)w.ipiv, (void *)w.perm, (void *)w.info})
+                    (void *)w.rowsum, (void *)w.ipiv, (void *)w.perm, (void *)w.info, (void *)w.V, (void *)w.Z,
+                    (void *)w.H, (void *)w.hn})
       if (p) cudaFree(p);
     w = Workspace{};
     BOLA_TRY_CUDA(cudaMalloc(&w.W, sizeof(float) * n * n));
@@ -276,11 +370,15 @@ int ws_reserve(Workspace &w, int64_t n, int64_t nrhs, int kind, cudaStream_t s) 
     BOLA_TRY_CUDA(cudaMalloc(&w.scale, sizeof(double) * cdiv(n, TB)));
     BOLA_TRY_CUDA(cudaMalloc(&w.r, sizeof(double) * n * nrhs));
     BOLA_TRY_CUDA(cudaMalloc(&w.d, sizeof(double) * n * nrhs));
-    BOLA_TRY_CUDA(cudaMalloc(&w.norms, sizeof(double) * (3 * MAXRHS + 8)));
+    BOLA_TRY_CUDA(cudaMalloc(&w.norms, sizeof(double) * 6 * MAXRHS));  // [r | x | b | A, ... | v scales]
     BOLA_TRY_CUDA(cudaMalloc(&w.rowsum, sizeof(double) * n));
     BOLA_TRY_CUDA(cudaMalloc(&w.ipiv, sizeof(int32_t) * n));
     BOLA_TRY_CUDA(cudaMalloc(&w.perm, sizeof(int32_t) * n));
     BOLA_TRY_CUDA(cudaMalloc(&w.info, sizeof(int32_t)));
+    BOLA_TRY_CUDA(cudaMalloc(&w.V, sizeof(double) * (GM_M + 1) * nrhs * n));
+    BOLA_TRY_CUDA(cudaMalloc(&w.Z, sizeof(double) * GM_M * nrhs * n));
+    BOLA_TRY_CUDA(cudaMalloc(&w.H, sizeof(double) * (GM_M + 2) * MAXRHS * 2));
+    BOLA_TRY_CUDA(cudaMalloc(&w.hn, sizeof(double) * MAXRHS));
     w.n = n;
     w.nrhs = nrhs;
   }
@@ -303,6 +401,118 @@ int correction(cudaStream_t s, Workspace &w, int64_t n, int nrhs, const double *
   return 0;
 }
 
+// r = b - A x in FP64, then the backward error over all right-hand sides.
+int residual_berr(cudaStream_t s, Workspace &w, int64_t n, int nr, const double *a, int64_t lda, const double *b,
+                  int64_t ldb, const double *x, int64_t ldx, double *berr) {
+  double *nrm = w.norms;
+  {
+    ProfScope prof(s, "mixed_residual", 2.0 * (double)n * n * nr, 8.0 * (double)n * n, 4);
+    copy_cols<<<(unsigned)cdiv(n * nr, 256), 256, 0, s>>>(n, nr, b, ldb, w.r, n);
+    BOLA_CHECK_LAUNCH();
+    BOLA_TRY(dgemm_exact(s, 'N', 'N', n, nr, n, -1.0, a, lda, x, ldx, 1.0, w.r, n, 64, nullptr, 0));
+    col_absmax<<<nr, 256, 0, s>>>(n, w.r, n, nrm);
+    col_absmax<<<nr, 256, 0, s>>>(n, x, ldx, nrm + nr);
+  }
+  BOLA_CHECK_LAUNCH();
+  std::vector<double> h(3 * nr + 1);
+  BOLA_TRY_CUDA(cudaMemcpyAsync(h.data(), nrm, sizeof(double) * (3 * nr + 1), cudaMemcpyDeviceToHost, s));
+  BOLA_TRY_CUDA(cudaStreamSynchronize(s));
+  double e = 0.0;
+  for (int c = 0; c < nr; ++c) {
+    const double den = h[3 * nr] * h[nr + c] + h[2 * nr + c];
+    const double v = den > 0.0 ? h[c] / den : (h[c] > 0.0 ? INFINITY : 0.0);
+    e = std::isnan(v) ? INFINITY : fmax(e, v);
+  }
+  *berr = e;
+  return 0;
+}
+
+// One GMRES-IR step: flexible GMRES (restart GM_M) on A d = r for the residual
+// in w.r, right-preconditioned by the low-precision LU (z = M^-1 v through
+// the FP32 triangular solves), FP64 matrix products (the exact DGEMM) and
+// classical Gram-Schmidt with one reorthogonalisation; then x += Z y.
+// Each right-hand side runs its own Krylov process; they advance together.
+int gmres_step(cudaStream_t s, Workspace &w, int64_t n, int nr, const double *a, int64_t lda, double *x,
+               int64_t ldx, double inner_tol, int *inner_iters) {
+  const int ldh = GM_M + 2;
+  double *H1 = w.H, *H2 = w.H + ldh * MAXRHS;  // device Hessenberg columns (two CGS passes)
+  double *beta_d = w.norms + 4 * MAXRHS;       // per-column max |v| for the FP32 scaling
+  const unsigned g = (unsigned)cdiv(n * nr, 256);
+  gm_norm2<<<nr, 256, 0, s>>>(n, w.r, w.hn);
+  gm_scale_into<<<g, 256, 0, s>>>(n, nr, w.r, w.hn, w.V);
+  BOLA_CHECK_LAUNCH();
+  std::vector<double> beta(nr), hd(2 * ldh * MAXRHS), hnh(MAXRHS);
+  BOLA_TRY_CUDA(cudaMemcpyAsync(beta.data(), w.hn, sizeof(double) * nr, cudaMemcpyDeviceToHost, s));
+  BOLA_TRY_CUDA(cudaStreamSynchronize(s));
+  // per right-hand side: R (upper, column-major ldh), Givens cs/sn, rhs gvec
+  std::vector<double> R((size_t)ldh * GM_M * nr, 0.0), cs((size_t)GM_M * nr), sn((size_t)GM_M * nr),
+      gv((size_t)ldh * nr, 0.0);
+  for (int c = 0; c < nr; ++c) gv[(size_t)c * ldh] = beta[c];
+  int kk = 0;
+  for (int k = 0; k < GM_M; ++k) {
+    double *Vk = w.V + (int64_t)k * nr * n, *Zk = w.Z + (int64_t)k * nr * n;
+    col_absmax<<<nr, 256, 0, s>>>(n, Vk, n, beta_d);
+    BOLA_CHECK_LAUNCH();
+    BOLA_TRY(correction(s, w, n, nr, Vk, n, beta_d, Zk, n, true));
+    {
+      ProfScope prof(s, "gmres_matvec", 2.0 * (double)n * n * nr, 8.0 * (double)n * n);
+      BOLA_TRY(dgemm_exact(s, 'N', 'N', n, nr, n, 1.0, a, lda, Zk, n, 0.0, w.d, n, 64, nullptr, 0));
+    }
+    {
+      ProfScope prof(s, "gmres_orth", 8.0 * (double)n * nr * (k + 1), 0.0, 6);
+      gm_dots<<<dim3(k + 1, nr), 256, 0, s>>>(n, nr, w.V, w.d, H1, ldh);
+      gm_sub<<<g, 256, 0, s>>>(n, nr, k + 1, w.V, H1, ldh, w.d);
+      gm_dots<<<dim3(k + 1, nr), 256, 0, s>>>(n, nr, w.V, w.d, H2, ldh);
+      gm_sub<<<g, 256, 0, s>>>(n, nr, k + 1, w.V, H2, ldh, w.d);
+      gm_norm2<<<nr, 256, 0, s>>>(n, w.d, w.hn);
+      gm_scale_into<<<g, 256, 0, s>>>(n, nr, w.d, w.hn, w.V + (int64_t)(k + 1) * nr * n);
+    }
+    BOLA_CHECK_LAUNCH();
+    BOLA_TRY_CUDA(cudaMemcpyAsync(hd.data(), w.H, sizeof(double) * 2 * ldh * MAXRHS, cudaMemcpyDeviceToHost, s));
+    BOLA_TRY_CUDA(cudaMemcpyAsync(hnh.data(), w.hn, sizeof(double) * nr, cudaMemcpyDeviceToHost, s));
+    BOLA_TRY_CUDA(cudaStreamSynchronize(s));
+    kk = k + 1;
+    bool done = true;
+    for (int c = 0; c < nr; ++c) {
+      double *col = &R[((size_t)c * GM_M + k) * ldh];
+      for (int i = 0; i <= k; ++i) col[i] = hd[i + c * ldh] + hd[ldh * MAXRHS + i + c * ldh];
+      col[k + 1] = hnh[c];
+      double *csc = &cs[(size_t)c * GM_M], *snc = &sn[(size_t)c * GM_M], *gc = &gv[(size_t)c * ldh];
+      for (int i = 0; i < k; ++i) {  // previous rotations
+        const double t = csc[i] * col[i] + snc[i] * col[i + 1];
+        col[i + 1] = -snc[i] * col[i] + csc[i] * col[i + 1];
+        col[i] = t;
+      }
+      const double den = hypot(col[k], col[k + 1]);
+      csc[k] = den > 0.0 ? col[k] / den : 1.0;
+      snc[k] = den > 0.0 ? col[k + 1] / den : 0.0;
+      col[k] = den;
+      col[k + 1] = 0.0;
+      gc[k + 1] = -snc[k] * gc[k];
+      gc[k] = csc[k] * gc[k];
+      if (beta[c] > 0.0 && fabs(gc[k + 1]) > inner_tol * beta[c]) done = false;
+    }
+    if (done) break;
+  }
+  *inner_iters += kk;
+  // y = R^-1 g per right-hand side, then x += Z y
+  std::vector<double> y((size_t)ldh * MAXRHS, 0.0);
+  for (int c = 0; c < nr; ++c) {
+    if (!(beta[c] > 0.0)) continue;
+    for (int i = kk - 1; i >= 0; --i) {
+      double t = gv[(size_t)c * ldh + i];
+      for (int j = i + 1; j < kk; ++j) t -= R[((size_t)c * GM_M + j) * ldh + i] * y[(size_t)c * ldh + j];
+      const double d = R[((size_t)c * GM_M + i) * ldh + i];
+      y[(size_t)c * ldh + i] = d != 0.0 ? t / d : 0.0;
+    }
+  }
+  BOLA_TRY_CUDA(cudaMemcpyAsync(H2, y.data(), sizeof(double) * ldh * MAXRHS, cudaMemcpyHostToDevice, s));
+  gm_add_zy<<<g, 256, 0, s>>>(n, nr, kk, w.Z, H2, ldh, x, ldx);
+  BOLA_CHECK_LAUNCH();
+  BOLA_TRY_CUDA(cudaStreamSynchronize(s));  // y lives on this host stack frame
+  return 0;
+}
+
 }  // namespace
 }  // namespace bola
 
@@ -317,7 +527,7 @@ extern "C" int bola_dgesv_mixed(int64_t n, int64_t nrhs, const double *a, int64_
   if (lda < imax(1, n)) return -4;
   if (ldb < imax(1, n)) return -6;
   if (ldx < imax(1, n)) return -8;
-  bola_mixed_opts o = {2, 30, 1e-14, 1};
+  bola_mixed_opts o = {2, 30, 1e-14, 1, 1};
   if (opts) o = *opts;
   if (o.factor_kind < 0 || o.factor_kind > 2) return -9;
   bola_mixed_info info_out;
@@ -361,40 +571,52 @@ extern "C" int bola_dgesv_mixed(int64_t n, int64_t nrhs, const double *a, int64_
 
   bool converged = false;
   double berr = INFINITY, prev = INFINITY;
+  int path = 0;
   if (finfo == 0) {
     // x0 = correction of b (rscale = ||b||)
     BOLA_TRY(correction(s, w, n, nr, b, ldb, nrm + 2 * nr, x, ldx, true));
-    std::vector<double> h(3 * nr + 1);
+    bool to_gmres = false;
     for (int it = 0; it <= o.max_iterations; ++it) {
-      {
-        ProfScope prof(s, "mixed_residual", 2.0 * (double)n * n * nr);
-        copy_cols<<<(unsigned)cdiv(n * nr, 256), 256, 0, s>>>(n, nr, b, ldb, w.r, n);
-        BOLA_CHECK_LAUNCH();
-        BOLA_TRY(dgemm_exact(s, 'N', 'N', n, nr, n, -1.0, a, lda, x, ldx, 1.0, w.r, n, 64, nullptr, 0));
-        col_absmax<<<nr, 256, 0, s>>>(n, w.r, n, nrm);
-        col_absmax<<<nr, 256, 0, s>>>(n, x, ldx, nrm + nr);
-      }
-      BOLA_CHECK_LAUNCH();
-      BOLA_TRY_CUDA(cudaMemcpyAsync(h.data(), nrm, sizeof(double) * (3 * nr + 1), cudaMemcpyDeviceToHost, s));
-      BOLA_TRY_CUDA(cudaStreamSynchronize(s));
-      berr = 0.0;
-      for (int c = 0; c < nr; ++c) {
-        const double den = h[3 * nr] * h[nr + c] + h[2 * nr + c];
-        const double e = den > 0.0 ? h[c] / den : (h[c] > 0.0 ? INFINITY : 0.0);
-        berr = std::isnan(e) ? INFINITY : fmax(berr, e);
-      }
+      BOLA_TRY(residual_berr(s, w, n, nr, a, lda, b, ldb, x, ldx, &berr));
       info_out.iterations = it;
       if (berr <= o.tolerance) {
         converged = true;
         break;
       }
-      if (it > 0 && !(berr < 0.5 * prev)) break;  // stalled
+      if (it > 0) {
+        const double rate = berr / prev;
+        if (!(rate < 0.5)) {  // stalled or diverging
+          to_gmres = o.gmres != 0;
+          break;
+        }
+        if (o.gmres && rate > 0.05) {  // converging slowly: Krylov acceleration pays
+          to_gmres = true;
+          break;
+        }
+      }
       prev = berr;
       BOLA_TRY(correction(s, w, n, nr, w.r, n, nrm, x, ldx, false));
     }
+    if (!converged && to_gmres) {
+      // a stalled sweep may have made x worse than the previous one; GMRES-IR
+      // starts from the current x and its residual (w.r)
+      path = 1;
+      double gprev = berr;
+      for (int outer = 0; outer < 10; ++outer) {
+        BOLA_TRY(gmres_step(s, w, n, nr, a, lda, x, ldx, 1e-8, &info_out.gmres_iterations));
+        BOLA_TRY(residual_berr(s, w, n, nr, a, lda, b, ldb, x, ldx, &berr));
+        info_out.iterations += 1;
+        if (berr <= o.tolerance) {
+          converged = true;
+          break;
+        }
+        if (!(berr < 0.5 * gprev)) break;
+        gprev = berr;
+      }
+    }
   }
   info_out.backward_error = berr;
-  info_out.path = 0;
+  info_out.path = path;
   if (!converged && o.fallback_fp64) {
     // plain FP64 path on a copy of A (BOLA's getrf + laswp + trsm)
     double *acopy = nullptr;
@@ -411,15 +633,7 @@ extern "C" int bola_dgesv_mixed(int64_t n, int64_t nrhs, const double *a, int64_
     if (st != 0) return st;
     info_out.path = 2;
     // backward error of the FP64 answer
-    copy_cols<<<(unsigned)cdiv(n * nr, 256), 256, 0, s>>>(n, nr, b, ldb, w.r, n);
-    BOLA_TRY(dgemm_exact(s, 'N', 'N', n, nr, n, -1.0, a, lda, x, ldx, 1.0, w.r, n, 64, nullptr, 0));
-    col_absmax<<<nr, 256, 0, s>>>(n, w.r, n, nrm);
-    col_absmax<<<nr, 256, 0, s>>>(n, x, ldx, nrm + nr);
-    std::vector<double> h(3 * nr + 1);
-    BOLA_TRY_CUDA(cudaMemcpyAsync(h.data(), nrm, sizeof(double) * (3 * nr + 1), cudaMemcpyDeviceToHost, s));
-    BOLA_TRY_CUDA(cudaStreamSynchronize(s));
-    berr = 0.0;
-    for (int c = 0; c < nr; ++c) berr = fmax(berr, h[c] / (h[3 * nr] * h[nr + c] + h[2 * nr + c]));
+    BOLA_TRY(residual_berr(s, w, n, nr, a, lda, b, ldb, x, ldx, &berr));
     info_out.backward_error = berr;
   }
   if (out) *out = info_out;

@@ -25,6 +25,7 @@ struct MixedLU {
   void *aop = nullptr, *bop = nullptr;
   float *aop_lo = nullptr, *bop_lo = nullptr;
   int32_t *err = nullptr;
+  int32_t *plan = nullptr;  // the current panel's composed interchanges: count, rows[128], src[128]
   CUtensorMap mapA, mapB, mapAlo, mapBlo;
   int reserve(int64_t n, int kind, cudaStream_t s);
   void release(cudaStream_t s);

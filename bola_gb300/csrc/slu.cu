@@ -83,7 +83,7 @@ __device__ __forceinline__ void write_operand_row(int kind, void *op, float *op_
 // its own slots, swaps, one CTA barrier, rank-1 update of the active columns.
 __global__ void __launch_bounds__(SPT)
 spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0, int32_t *info, int kind,
-              void *aop, float *aop_lo, int64_t R) {
+              void *aop, float *aop_lo, int64_t R, int32_t *plan) {
   cg::cluster_group cluster = cg::this_cluster();
   const int C = (int)cluster.num_blocks();
   const int cr = (int)cluster.block_rank();
@@ -92,7 +92,7 @@ spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
   __shared__ uint64_t wkey[SPT / 32];
   extern __shared__ float sp[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int64_t RP = R + 1;
+  const int RP = (int)R + 1;
   const int64_t r0 = (int64_t)cr * R;
   const int64_t r1 = imin(mp, r0 + R);
   const int64_t nr = r1 > r0 ? r1 - r0 : 0;
@@ -121,23 +121,24 @@ spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
     const uint32_t mlo = __reduce_max_sync(0xffffffffu, hi == mhi ? lo : 0u);
     if (lane == 0) wkey[warp] = ((uint64_t)mhi << 32) | mlo;
     __syncthreads();
-    // -- warp 0 pushes the candidate (and row j if owned) into every CTA
-    if (warp == 0) {
+    // -- every warp pushes the candidate (and row j if owned) to its share of the CTAs
+    {
       uint64_t ck = 0;
 #pragma unroll
       for (int w = 0; w < SPT / 32; ++w) ck = wkey[w] > ck ? wkey[w] : ck;
-      const int64_t gbest = ck ? (int64_t)(0xFFFFFFFFu - (uint32_t)ck) : -1;
-      float c0 = 0.f, c1 = 0.f, j0v = 0.f, j1v = 0.f;
-      if (gbest >= 0) {
-        c0 = lane < jb ? sp[lane * RP + (gbest - r0)] : 0.f;
-        c1 = lane + 32 < jb ? sp[(lane + 32) * RP + (gbest - r0)] : 0.f;
-      }
+      const int gl = ck ? (int)(0xFFFFFFFFu - (uint32_t)ck) - (int)r0 : -1;  // local row of the candidate
       const bool own_j = j >= r0 && j < r1;
-      if (own_j) {
-        j0v = lane < jb ? sp[lane * RP + (j - r0)] : 0.f;
-        j1v = lane + 32 < jb ? sp[(lane + 32) * RP + (j - r0)] : 0.f;
+      const int jl = (int)(j - r0);
+      float c0 = 0.f, c1 = 0.f, j0v = 0.f, j1v = 0.f;
+      if (gl >= 0) {
+        c0 = lane < jb ? sp[lane * RP + gl] : 0.f;
+        c1 = lane + 32 < jb ? sp[(lane + 32) * RP + gl] : 0.f;
       }
-      for (int d = 0; d < C; ++d) {
+      if (own_j) {
+        j0v = lane < jb ? sp[lane * RP + jl] : 0.f;
+        j1v = lane + 32 < jb ? sp[(lane + 32) * RP + jl] : 0.f;
+      }
+      for (int d = warp; d < C; d += SPT / 32) {
         SSlot *rs = cluster.map_shared_rank(&slots[par][cr], d);
         if (lane == 0) {
           rs->khi = (uint32_t)(ck >> 32);
@@ -153,15 +154,20 @@ spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
       }
     }
     cluster.sync();
-    // -- the winner, identical in every CTA
+    // -- the winner, identical in every CTA: lane s reads slot s, warp max
     uint64_t wk = 0;
+    {
+      const uint64_t k = lane < C ? (((uint64_t)slots[par][lane].khi << 32) | slots[par][lane].klo) : 0ull;
+      const uint32_t khi = (uint32_t)(k >> 32);
+      const uint32_t mh = __reduce_max_sync(0xffffffffu, khi);
+      const uint32_t ml = __reduce_max_sync(0xffffffffu, khi == mh ? (uint32_t)k : 0u);
+      wk = ((uint64_t)mh << 32) | ml;
+    }
     int ws = 0;
-    for (int s2 = 0; s2 < C; ++s2) {
-      const uint64_t k = ((uint64_t)slots[par][s2].khi << 32) | slots[par][s2].klo;
-      if (k > wk) {
-        wk = k;
-        ws = s2;
-      }
+    {
+      const uint64_t k = lane < C ? (((uint64_t)slots[par][lane].khi << 32) | slots[par][lane].klo) : 0ull;
+      const unsigned m = __ballot_sync(0xffffffffu, k == wk && lane < C);
+      ws = m ? __ffs(m) - 1 : 0;
     }
     const int64_t jp = wk ? (int64_t)(0xFFFFFFFFu - (uint32_t)wk) : (int64_t)j;
     const float *prow = wk ? slots[par][ws].v : rowj[par];
@@ -177,12 +183,15 @@ spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
       if (jp >= r0 && jp < r1) sp[tid * RP + (jp - r0)] = rowj[par][tid];
     }
     __syncthreads();
-    for (int64_t il = tid; il < nr; il += SPT) {
-      const int64_t g = r0 + il;
-      if (g <= j) continue;
-      const float l = sp[j * RP + il] * inv;
-      sp[j * RP + il] = l;
-      for (int c = j + 1; c < jb; ++c) sp[c * RP + il] = fmaf(-l, prow[c], sp[c * RP + il]);
+    for (int il = tid; il < (int)nr; il += SPT) {
+      if (r0 + il <= j) continue;
+      float *col = sp + j * RP + il;
+      const float l = *col * inv;
+      *col = l;
+      for (int c = j + 1; c < jb; ++c) {
+        col += RP;
+        *col = fmaf(-l, prow[c], *col);
+      }
     }
   }
   __syncthreads();
@@ -192,6 +201,19 @@ spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
     const int64_t il = e % nr;
     const int c = (int)(e / nr);
     W[(r0 + il) + c * ldw] = sp[c * RP + il];
+  }
+  if (plan != nullptr && cr == 0 && warp == 0) {
+    // the panel's interchanges as "row rows[t] takes the old row src[t]",
+    // composed once here for the swap kernel that follows
+    __syncwarp();
+    SwapPlan p;
+    p.ix0 = 0;
+    p.i1 = col0 + 1;
+    p.i2 = col0 + jb;
+    p.i_inc = 1;
+    p.incx = 1;
+    const int cnt = compose_swaps_warp<4, int32_t>(p, ipiv, plan + 1, plan + 1 + 2 * SNB);
+    if (lane == 0) plan[0] = cnt;
   }
   if (aop != nullptr) {
     for (int64_t il = tid; il < nr; il += SPT) {
@@ -209,20 +231,16 @@ spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
 // The panel's interchanges on all other columns, U12 = L11^-1 A12 on the
 // right ones and their K-major B operand.  A warp per column.
 __global__ void __launch_bounds__(256)
-sswap_trsm(float *W, int64_t ldw, int64_t n, int64_t j, int jb, const int32_t *ipiv, int kind, void *bop,
+sswap_trsm(float *W, int64_t ldw, int64_t n, int64_t j, int jb, const int32_t *plan, int kind, void *bop,
            float *bop_lo) {
   __shared__ int32_t rows[2 * SNB], src[2 * SNB];
   __shared__ float L[SNB * SNB];
   __shared__ int cnt;
-  if (threadIdx.x < 32) {
-    SwapPlan p;
-    p.ix0 = j;
-    p.i1 = (int32_t)(j + 1);
-    p.i2 = (int32_t)(j + jb);
-    p.i_inc = 1;
-    p.incx = 1;
-    const int c = compose_swaps_warp<4, int32_t>(p, ipiv, rows, src);
-    if (threadIdx.x == 0) cnt = c;
+  // the interchanges, composed once by the panel kernel
+  if (threadIdx.x == 0) cnt = plan[0];
+  for (int t = threadIdx.x; t < 2 * SNB; t += blockDim.x) {
+    rows[t] = plan[1 + t];
+    src[t] = plan[1 + 2 * SNB + t];
   }
   for (int e = threadIdx.x; e < jb * jb; e += blockDim.x) {
     const int r = e % jb, c = e / jb;
@@ -266,7 +284,7 @@ sswap_trsm(float *W, int64_t ldw, int64_t n, int64_t j, int jb, const int32_t *i
 __global__ void zero_i32(int32_t *p) { *p = 0; }
 
 int launch_spanel(cudaStream_t s, float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0,
-                  int32_t *info, int kind, void *aop, float *aop_lo) {
+                  int32_t *info, int kind, void *aop, float *aop_lo, int32_t *plan) {
   const int C = (int)imin(SMAXC, imax(1, cdiv(mp, SPT)));
   const int64_t R = cdiv(mp, C);
   const size_t smem = sizeof(float) * SNB * (size_t)(R + 1);
@@ -290,7 +308,7 @@ int launch_spanel(cudaStream_t s, float *W, int64_t ldw, int64_t mp, int jb, int
   cfg.attrs = attr1;
   cfg.numAttrs = 1;
   ProfScope prof(s, "spanel", (double)mp * SNB * SNB, 8.0 * (double)mp * SNB);
-  BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, spanel_kernel, W, ldw, mp, jb, ipiv, col0, info, kind, aop, aop_lo, R));
+  BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, spanel_kernel, W, ldw, mp, jb, ipiv, col0, info, kind, aop, aop_lo, R, plan));
   return 0;
 }
 
@@ -312,6 +330,7 @@ int MixedLU::reserve(int64_t n_, int kind_, cudaStream_t s) {
     BOLA_TRY_CUDA(cudaMallocAsync(&bop_lo, (size_t)n * SNB * 4, s));
   }
   BOLA_TRY_CUDA(cudaMallocAsync(&err, sizeof(int32_t), s));
+  BOLA_TRY_CUDA(cudaMallocAsync(&plan, sizeof(int32_t) * (1 + 4 * SNB), s));
   BOLA_TRY_CUDA(cudaMemsetAsync(err, 0, sizeof(int32_t), s));
   const bool bf = kind == 0;
   BOLA_TRY(make_kmajor_map(&mapA, aop, n, bf));
@@ -323,7 +342,7 @@ int MixedLU::reserve(int64_t n_, int kind_, cudaStream_t s) {
 
 void MixedLU::release(cudaStream_t s) {
   for (void **p : {&aop, &bop, reinterpret_cast<void **>(&aop_lo), reinterpret_cast<void **>(&bop_lo),
-                   reinterpret_cast<void **>(&err)}) {
+                   reinterpret_cast<void **>(&err), reinterpret_cast<void **>(&plan)}) {
     if (*p) cudaFreeAsync(*p, s);
     *p = nullptr;
   }
@@ -340,11 +359,11 @@ int MixedLU::factor(cudaStream_t s, float *W, int64_t ldw, int32_t *ipiv, int32_
     const int64_t mp = n - j;
     const bool upd = j + jb < n;
     BOLA_TRY(launch_spanel(s, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, kind, upd ? aop : nullptr,
-                           aop_lo));
+                           aop_lo, plan));
     const int64_t others = n - jb;
     if (others > 0) {
       ProfScope prof(s, "sswap_trsm", (double)jb * jb * (double)(n - j - jb));
-      sswap_trsm<<<(unsigned)cdiv(others, 8), 256, 0, s>>>(W, ldw, n, j, jb, ipiv, kind, upd ? bop : nullptr, bop_lo);
+      sswap_trsm<<<(unsigned)cdiv(others, 8), 256, 0, s>>>(W, ldw, n, j, jb, plan, kind, upd ? bop : nullptr, bop_lo);
       BOLA_CHECK_LAUNCH();
     }
     if (upd) BOLA_TRY(tc_update(s, kind, mp - jb, n - j - jb, mapA, mapB, mapAlo, mapBlo,

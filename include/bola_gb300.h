@@ -188,14 +188,18 @@ int bola_dpotrs(char uplo, int64_t n, int64_t nrhs, const double *fac, int64_t l
  * + ||b_j||_inf) <= tolerance: A is factored in low precision (FP32 storage,
  * tcgen05 tensor-core trailing updates, per-64-column-block power-of-two
  * scaling), then the solution is refined with FP64 residuals and updates.
- * When refinement stalls the plain FP64 path (bola_dgetrf + bola_dgetrs)
- * solves the system instead, if fallback_fp64 is set.  Synchronous: it
+ * Plain refinement runs while each sweep cuts the backward error by 20x or
+ * more; otherwise flexible GMRES on the correction equation, preconditioned
+ * by the low-precision LU, takes over (GMRES-IR); if that stalls too, the
+ * plain FP64 path (bola_dgetrf + bola_dgetrs) solves the system, when
+ * fallback_fp64 is set.  Synchronous: it
  * returns after the result and *info are final.  n <= 8192, nrhs <= 32. */
 typedef struct {
   int factor_kind;       /* 0: bf16 tensor-core updates; 1: tf32; 2: 3xTF32 (FP32-accurate) */
   int max_iterations;    /* refinement sweeps before declaring a stall (default 30) */
   double tolerance;      /* target backward error (default 1e-14) */
   int fallback_fp64;     /* 1: finish with the plain FP64 path when refinement stalls */
+  int gmres;             /* 1: switch to GMRES-IR when plain refinement is slow (< 20x per sweep) or stalls */
 } bola_mixed_opts;
 
 typedef struct {

@@ -29,11 +29,11 @@ def make_system(n, nrhs, kappa, seed):
     return A.t().contiguous().reshape(-1), b.t().contiguous().reshape(-1)
 
 
-def solve(A, b, n, nrhs, kind, fallback=1, max_it=30):
+def solve(A, b, n, nrhs, kind, fallback=1, max_it=30, gmres=1):
     from bola_gb300 import _lib
     L = _lib.load()
     x = torch.zeros(n * nrhs, dtype=torch.float64, device="cuda")
-    opts = _lib.MixedOpts(kind, max_it, 1e-14, fallback)
+    opts = _lib.MixedOpts(kind, max_it, 1e-14, fallback, gmres)
     info = _lib.MixedInfo()
     st = L.bola_dgesv_mixed(n, nrhs, _p(A), n, _p(b), n, _p(x), n, ctypes.byref(opts), ctypes.byref(info),
                             ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
@@ -81,10 +81,25 @@ def test_mixed_kappa_sweep_vs_oracle(oracle_lib, kappa, kind):
 def test_mixed_without_fallback_reports_stall_honestly():
     n, nrhs = 512, 2
     A, b = make_system(n, nrhs, 1e10, seed=7)
-    x, info = solve(A, b, n, nrhs, 0, fallback=0, max_it=10)
-    # bf16 factors cannot refine a kappa = 1e10 system: the call says so
+    x, info = solve(A, b, n, nrhs, 0, fallback=0, max_it=10, gmres=0)
+    # bf16 factors cannot refine a kappa = 1e10 system by plain IR: the call says so
     assert info.path == 0
-    assert info.backward_error > 1e-14 or berr(A, x, b, n, nrhs) <= 1e-14
+    measured = berr(A, x, b, n, nrhs)
+    assert (info.backward_error > 1e-14) == (measured > 1e-14)
+
+
+@pytest.mark.parametrize("kind", [0, 2])
+def test_gmres_ir_recovers_kappa_1e10_without_fp64(kind):
+    n, nrhs = 1024, 4
+    A, b = make_system(n, nrhs, 1e10, seed=9)
+    x, info = solve(A, b, n, nrhs, kind, fallback=0)
+    if kind == 2:
+        assert info.path == 1 and info.gmres_iterations > 0
+        assert info.backward_error <= 1e-14
+        assert berr(A, x, b, n, nrhs) <= 1e-14
+    else:
+        # bf16 factors: GMRES-IR may or may not get there; the report must match the truth
+        assert (info.backward_error <= 1e-14) == (berr(A, x, b, n, nrhs) <= 1e-14)
 
 
 def test_mixed_singular_falls_back_to_fp64_info():
