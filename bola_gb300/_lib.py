@@ -61,6 +61,22 @@ class MixedInfo(ctypes.Structure):
 SIGNATURES["bola_dgesv_mixed"] = (_int, [_i64, _i64, _p, _i64, _p, _i64, _p, _i64, ctypes.POINTER(MixedOpts),
                                          ctypes.POINTER(MixedInfo), _p])
 
+
+
+class System(ctypes.Structure):
+    """bola_system (include/bola_gb300.h)."""
+    _fields_ = [("n", ctypes.c_int32), ("nrhs", ctypes.c_int32), ("kind", ctypes.c_int32), ("lda", ctypes.c_int32),
+                ("ldb", ctypes.c_int32), ("reserved", ctypes.c_int32), ("a", ctypes.c_void_p), ("b", ctypes.c_void_p)]
+
+
+SIGNATURES.update({
+    "bola_batch_plan_create": (_int, [_i32, _p, _p, _p, _p]),
+    "bola_batch_solve": (_int, [_p, _p, _p, _p]),
+    "bola_batch_solve_graph": (_int, [_p, _p, _p, _p]),
+    "bola_batch_plan_info": (_int, [_p, _p, _p, _p]),
+    "bola_batch_plan_destroy": (_int, [_p]),
+})
+
 _lib = None
 
 

@@ -1,0 +1,109 @@
+"""Batches of small independent systems for bola_batch_* (include/bola_gb300.h).
+
+`Batch` packs the systems' matrices and right-hand sides into two device
+buffers, builds the device array of `bola_system` descriptors, and owns the
+plan (bucketing, group sizes, work order) created by the C library.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+
+
+class Batch:
+    """A batch of systems A_i X_i = B_i on one device.
+
+    ns, nrhs, kinds: per-system order, right-hand-side count and kind (0 LU,
+    1 Cholesky).  group_size: optional 8-entry table of threads per system for
+    the size buckets (the autotuner's output); None = library defaults.
+    """
+
+    def __init__(self, ns, nrhs, kinds, device="cuda", group_size=None):
+        self.L = _lib.load()
+        self.ns = np.asarray(ns, dtype=np.int32)
+        self.nrhs = np.asarray(nrhs, dtype=np.int32)
+        self.kinds = np.asarray(kinds, dtype=np.int32)
+        self.count = len(self.ns)
+        self.a_off = np.zeros(self.count + 1, dtype=np.int64)
+        self.a_off[1:] = np.cumsum(self.ns.astype(np.int64) ** 2)
+        self.b_off = np.zeros(self.count + 1, dtype=np.int64)
+        self.b_off[1:] = np.cumsum(self.ns.astype(np.int64) * self.nrhs)
+        self.A = torch.empty(int(self.a_off[-1]), dtype=torch.float64, device=device)
+        self.B = torch.empty(int(self.b_off[-1]), dtype=torch.float64, device=device)
+        self.info = torch.zeros(self.count, dtype=torch.int32, device=device)
+        desc = (_lib.System * max(self.count, 1))()
+        a0, b0 = self.A.data_ptr(), self.B.data_ptr()
+        for i in range(self.count):
+            n = int(self.ns[i])
+            desc[i] = _lib.System(n, int(self.nrhs[i]), int(self.kinds[i]), n, n, 0, a0 + 8 * int(self.a_off[i]),
+                                  b0 + 8 * int(self.b_off[i]))
+        raw = np.frombuffer(desc, dtype=np.uint8)
+        self.desc = torch.from_numpy(raw.copy()).to(device)
+        self.plan = ctypes.c_void_p()
+        gs = None
+        if group_size is not None:
+            gs = (ctypes.c_int32 * 8)(*[int(v) for v in group_size])
+        st = self.L.bola_batch_plan_create(self.count, self.ns.ctypes.data_as(ctypes.c_void_p),
+                                           self.kinds.ctypes.data_as(ctypes.c_void_p),
+                                           ctypes.cast(gs, ctypes.c_void_p) if gs is not None else None,
+                                           ctypes.byref(self.plan))
+        if st != 0:
+            raise RuntimeError(f"bola_batch_plan_create: {st} {self.L.bola_last_error().decode()}")
+
+    def a_view(self, i):
+        n = int(self.ns[i])
+        return self.A[int(self.a_off[i]):int(self.a_off[i + 1])].view(n, n).t()  # column-major n x n
+
+    def b_view(self, i):
+        n, r = int(self.ns[i]), int(self.nrhs[i])
+        return self.B[int(self.b_off[i]):int(self.b_off[i + 1])].view(r, n).t()
+
+    def flops(self):
+        f = ctypes.c_double()
+        self.L.bola_batch_plan_info(self.plan, None, None, ctypes.byref(f))
+        return f.value
+
+    def solve(self, graph=False, stream=None):
+        s = ctypes.c_void_p((stream or torch.cuda.current_stream()).cuda_stream)
+        fn = self.L.bola_batch_solve_graph if graph else self.L.bola_batch_solve
+        st = fn(self.plan, ctypes.c_void_p(self.desc.data_ptr()), ctypes.c_void_p(self.info.data_ptr()), s)
+        if st != 0:
+            raise RuntimeError(f"bola_batch_solve: {st} {self.L.bola_last_error().decode()}")
+
+    def close(self):
+        if self.plan:
+            self.L.bola_batch_plan_destroy(self.plan)
+            self.plan = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def config4_batch(count, seed=4, device="cuda", nmin=8, nmax=256, rmax=8):
+    """The batched-solve workload: n uniform-integer in [nmin, nmax], even ids
+    LU on uniform[-1,1) + n*I, odd ids Cholesky on B B^T / n + I (B uniform
+    [-1,1)), nrhs uniform in [1, rmax], right-hand sides uniform [-1,1).
+    Returns (ns, nrhs, kinds, fill) where fill(batch) writes the matrices."""
+    rng = np.random.default_rng(seed)
+    ns = rng.integers(nmin, nmax + 1, size=count).astype(np.int32)
+    nrhs = rng.integers(1, rmax + 1, size=count).astype(np.int32)
+    kinds = (np.arange(count) % 2).astype(np.int32)
+
+    def fill(batch):
+        g = torch.Generator(device=device)
+        g.manual_seed(seed)
+        for i in range(count):
+            n = int(ns[i])
+            M = torch.rand(n, n, dtype=torch.float64, device=device, generator=g) * 2 - 1
+            if kinds[i] == 0:
+                M += n * torch.eye(n, dtype=torch.float64, device=device)
+            else:
+                M = M @ M.t() / n + torch.eye(n, dtype=torch.float64, device=device)
+            batch.a_view(i).copy_(M)
+            batch.b_view(i).copy_(torch.rand(n, int(nrhs[i]), dtype=torch.float64, device=device, generator=g) * 2 - 1)
+    return ns, nrhs, kinds, fill

@@ -1,0 +1,363 @@
+// batched.cu — many small independent solves of uneven size in one persistent
+// launch (no BOLA counterpart; each system's answer must match BOLA's FP64
+// getrf/potrf + trsm solve within rounding).
+//
+// Plan (host, once per batch shape): systems are bucketed by order n; each
+// bucket has a group size G (threads per system: 32, 64, 128 or 256, from the
+// autotuned table) and work items of 256/G systems of that bucket, ordered by
+// decreasing cost (largest first, for load balance).  Solve (device): a grid
+// of persistent 256-thread CTAs pulls items from an atomic counter; the CTA
+// splits into 256/G groups, each factoring one system in place in global
+// memory (L2-resident: at most 512 KB per system) with partial pivoting (LU)
+// or Cholesky, and then solving its right-hand sides.  A group synchronises
+// with its own named barrier, so a system's arithmetic never depends on which
+// systems share its CTA: every result is the same alone and in any mix.
+// FP64 throughout; all waits are barriers (no spin loops).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+
+namespace bola {
+namespace {
+
+constexpr int BT = 256;         // threads per CTA
+constexpr int MAXG = BT / 32;   // groups per CTA at most
+constexpr int ITEM = 2 + MAXG;  // ints per work item: G, count, system ids
+constexpr int NBUCKET = 8;
+// upper n of each bucket (inclusive)
+constexpr int BUCKET_N[NBUCKET] = {16, 32, 48, 64, 96, 128, 192, 1 << 30};
+
+struct SystemDesc {
+  int32_t n, nrhs, kind, lda, ldb, pad;
+  double *a, *b;
+};
+static_assert(sizeof(SystemDesc) == sizeof(bola_system), "bola_system layout");
+
+__device__ __forceinline__ void group_sync(int G, int g) {
+  if (G == 32) {
+    __syncwarp();
+  } else if (G == BT) {
+    __syncthreads();
+  } else {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "r"(G) : "memory");
+  }
+}
+
+// argmax |A[k:n, k]| within a group; ties -> lowest row.  red: 2*MAXG scratch per group.
+__device__ int group_argmax(const double *col, int k, int n, int t, int G, int g, double *redv, int *redi) {
+  double best = -1.0;
+  int bi = k;
+  for (int i = k + t; i < n; i += G) {
+    const double v = fabs(col[i]);
+    if (v > best) {
+      best = v;
+      bi = i;
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    const double ov = __shfl_down_sync(0xffffffffu, best, off);
+    const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+    if (ov > best || (ov == best && oi < bi)) {
+      best = ov;
+      bi = oi;
+    }
+  }
+  const int w = t >> 5, nw = G >> 5;
+  if ((t & 31) == 0) {
+    redv[w] = best;
+    redi[w] = bi;
+  }
+  group_sync(G, g);
+  double b = redv[0];
+  int r = redi[0];
+  for (int q = 1; q < nw; ++q)
+    if (redv[q] > b || (redv[q] == b && redi[q] < r)) {
+      b = redv[q];
+      r = redi[q];
+    }
+  group_sync(G, g);
+  return r;
+}
+
+// LU with partial pivoting of one system by a group; the row interchanges are
+// applied to B as they happen, then L y = P b and U x = y.
+__device__ int group_lu_solve(const SystemDesc &S, int t, int G, int g, double *redv, int *redi) {
+  const int n = S.n, lda = S.lda, ldb = S.ldb, nr = S.nrhs;
+  double *A = S.a, *B = S.b;
+  int info = 0;
+  for (int k = 0; k < n; ++k) {
+    const int p = group_argmax(A + (int64_t)k * lda, k, n, t, G, g, redv, redi);
+    const double piv = A[p + (int64_t)k * lda];
+    if (piv == 0.0) {
+      info = k + 1;
+      break;
+    }
+    if (p != k) {
+      for (int j = t; j < n; j += G) {
+        const double tmp = A[k + (int64_t)j * lda];
+        A[k + (int64_t)j * lda] = A[p + (int64_t)j * lda];
+        A[p + (int64_t)j * lda] = tmp;
+      }
+      for (int c = t; c < nr; c += G) {
+        const double tmp = B[k + (int64_t)c * ldb];
+        B[k + (int64_t)c * ldb] = B[p + (int64_t)c * ldb];
+        B[p + (int64_t)c * ldb] = tmp;
+      }
+    }
+    group_sync(G, g);
+    const double inv = 1.0 / piv;
+    for (int i = k + 1 + t; i < n; i += G) A[i + (int64_t)k * lda] *= inv;
+    group_sync(G, g);
+    const int m = n - k - 1;
+    for (int e = t; e < m * m; e += G) {
+      const int i = k + 1 + e % m, j = k + 1 + e / m;
+      A[i + (int64_t)j * lda] = fma(-A[i + (int64_t)k * lda], A[k + (int64_t)j * lda], A[i + (int64_t)j * lda]);
+    }
+    group_sync(G, g);
+  }
+  if (info) return info;
+  // forward: unit lower
+  for (int k = 0; k < n; ++k) {
+    for (int e = t; e < (n - k - 1) * nr; e += G) {
+      const int i = k + 1 + e % (n - k - 1), c = e / (n - k - 1);
+      B[i + (int64_t)c * ldb] = fma(-A[i + (int64_t)k * lda], B[k + (int64_t)c * ldb], B[i + (int64_t)c * ldb]);
+    }
+    group_sync(G, g);
+  }
+  // backward: upper
+  for (int k = n - 1; k >= 0; --k) {
+    for (int c = t; c < nr; c += G) B[k + (int64_t)c * ldb] /= A[k + (int64_t)k * lda];
+    group_sync(G, g);
+    for (int e = t; e < k * nr; e += G) {
+      const int i = e % k, c = e / k;
+      B[i + (int64_t)c * ldb] = fma(-A[i + (int64_t)k * lda], B[k + (int64_t)c * ldb], B[i + (int64_t)c * ldb]);
+    }
+    group_sync(G, g);
+  }
+  return 0;
+}
+
+// Cholesky A = L L^T (lower) of one system by a group, then L y = b, L^T x = y.
+__device__ int group_chol_solve(const SystemDesc &S, int t, int G, int g) {
+  const int n = S.n, lda = S.lda, ldb = S.ldb, nr = S.nrhs;
+  double *A = S.a, *B = S.b;
+  for (int k = 0; k < n; ++k) {
+    const double d = A[k + (int64_t)k * lda];
+    if (!(d > 0.0)) return k + 1;
+    const double r = sqrt(d);
+    group_sync(G, g);
+    if (t == 0) A[k + (int64_t)k * lda] = r;
+    const double inv = 1.0 / r;
+    for (int i = k + 1 + t; i < n; i += G) A[i + (int64_t)k * lda] *= inv;
+    group_sync(G, g);
+    const int m = n - k - 1;
+    for (int e = t; e < m * m; e += G) {
+      const int i = k + 1 + e % m, j = k + 1 + e / m;
+      if (j <= i)
+        A[i + (int64_t)j * lda] = fma(-A[i + (int64_t)k * lda], A[j + (int64_t)k * lda], A[i + (int64_t)j * lda]);
+    }
+    group_sync(G, g);
+  }
+  for (int k = 0; k < n; ++k) {  // L y = b
+    for (int c = t; c < nr; c += G) B[k + (int64_t)c * ldb] /= A[k + (int64_t)k * lda];
+    group_sync(G, g);
+    for (int e = t; e < (n - k - 1) * nr; e += G) {
+      const int i = k + 1 + e % (n - k - 1), c = e / (n - k - 1);
+      B[i + (int64_t)c * ldb] = fma(-A[i + (int64_t)k * lda], B[k + (int64_t)c * ldb], B[i + (int64_t)c * ldb]);
+    }
+    group_sync(G, g);
+  }
+  for (int k = n - 1; k >= 0; --k) {  // L^T x = y
+    for (int c = t; c < nr; c += G) B[k + (int64_t)c * ldb] /= A[k + (int64_t)k * lda];
+    group_sync(G, g);
+    for (int e = t; e < k * nr; e += G) {
+      const int i = e % k, c = e / k;
+      B[i + (int64_t)c * ldb] = fma(-A[k + (int64_t)i * lda], B[k + (int64_t)c * ldb], B[i + (int64_t)c * ldb]);
+    }
+    group_sync(G, g);
+  }
+  return 0;
+}
+
+__global__ void __launch_bounds__(BT)
+batched_solve_kernel(const SystemDesc *__restrict__ sys, const int32_t *__restrict__ items, int32_t nitems,
+                     int32_t *counter, int32_t *info) {
+  __shared__ int32_t cur[ITEM];
+  __shared__ double redv[MAXG][MAXG];
+  __shared__ int redi[MAXG][MAXG];
+  const int tid = threadIdx.x;
+  for (;;) {
+    if (tid == 0) {
+      const int it = atomicAdd(counter, 1);
+      cur[0] = it < nitems ? items[(int64_t)it * ITEM] : 0;
+      for (int q = 1; q < ITEM; ++q) cur[q] = it < nitems ? items[(int64_t)it * ITEM + q] : 0;
+    }
+    __syncthreads();
+    const int G = cur[0];
+    if (G == 0) break;
+    const int g = tid / G, t = tid % G;
+    if (g < cur[1]) {
+      const int id = cur[2 + g];
+      const SystemDesc S = sys[id];
+      const int r = S.kind == 1 ? group_chol_solve(S, t, G, g) : group_lu_solve(S, t, G, g, redv[g], redi[g]);
+      if (t == 0) info[id] = r;
+    }
+    __syncthreads();
+  }
+}
+
+struct Plan {
+  int32_t count = 0, nitems = 0;
+  int32_t *items = nullptr;    // device
+  int32_t *counter = nullptr;  // device
+  int grid = 0;
+  double flops = 0.0;
+  int group[NBUCKET];
+  cudaGraphExec_t exec = nullptr;
+  const void *g_sys = nullptr;
+  const void *g_info = nullptr;
+};
+
+int bucket_of(int n) {
+  int b = 0;
+  while (n > BUCKET_N[b]) ++b;
+  return b;
+}
+
+}  // namespace
+}  // namespace bola
+
+using namespace bola;
+
+extern "C" {
+
+int bola_batch_plan_create(int32_t count, const int32_t *n, const int32_t *kind, const int32_t *group_size,
+                           bola_batch_plan *plan_out) {
+  if (count < 0) return -1;
+  if (!plan_out) return -5;
+  Plan *P = new Plan();
+  P->count = count;
+  static const int kDefault[NBUCKET] = {32, 32, 64, 64, 128, 128, 256, 256};
+  for (int b = 0; b < NBUCKET; ++b) {
+    int gsz = group_size ? group_size[b] : kDefault[b];
+    if (gsz != 32 && gsz != 64 && gsz != 128 && gsz != 256) gsz = kDefault[b];
+    P->group[b] = gsz;
+  }
+  // per bucket, systems by decreasing n; items of BT/G systems; items by decreasing cost
+  std::vector<std::vector<int>> byb(NBUCKET);
+  for (int i = 0; i < count; ++i) {
+    if (n[i] < 1 || n[i] > 256) {
+      delete P;
+      return fail(-2, "bola_batch_plan_create: system %d has n = %d (supported 1..256)", i, n[i]);
+    }
+    byb[bucket_of(n[i])].push_back(i);
+    const double nn = n[i];
+    P->flops += (kind && kind[i] == 1) ? nn * nn * nn / 3.0 : 2.0 * nn * nn * nn / 3.0;
+  }
+  struct It {
+    double cost;
+    std::vector<int32_t> v;
+  };
+  std::vector<It> its;
+  for (int b = 0; b < NBUCKET; ++b) {
+    auto &ids = byb[b];
+    std::sort(ids.begin(), ids.end(), [&](int x, int y) { return n[x] > n[y] || (n[x] == n[y] && x < y); });
+    const int G = P->group[b], per = BT / G;
+    for (size_t s = 0; s < ids.size(); s += per) {
+      It it;
+      it.v.assign(ITEM, 0);
+      it.v[0] = G;
+      int c = 0;
+      double cost = 0.0;
+      for (size_t q = s; q < ids.size() && c < per; ++q, ++c) {
+        it.v[2 + c] = ids[q];
+        cost = std::max(cost, (double)n[ids[q]] * n[ids[q]] * n[ids[q]] / G);
+      }
+      it.v[1] = c;
+      it.cost = cost;
+      its.push_back(std::move(it));
+    }
+  }
+  std::stable_sort(its.begin(), its.end(), [](const It &x, const It &y) { return x.cost > y.cost; });
+  P->nitems = (int32_t)its.size();
+  std::vector<int32_t> flat((size_t)its.size() * ITEM);
+  for (size_t i = 0; i < its.size(); ++i) std::memcpy(&flat[i * ITEM], its[i].v.data(), sizeof(int32_t) * ITEM);
+  if (cudaMalloc(&P->items, sizeof(int32_t) * std::max<size_t>(flat.size(), 1)) != cudaSuccess ||
+      cudaMalloc(&P->counter, sizeof(int32_t)) != cudaSuccess) {
+    delete P;
+    return fail(BOLA_ERR_CUDA, "bola_batch_plan_create: device allocation failed");
+  }
+  if (!flat.empty()) cudaMemcpy(P->items, flat.data(), sizeof(int32_t) * flat.size(), cudaMemcpyHostToDevice);
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batched_solve_kernel, BT, 0);
+  P->grid = std::max(1, std::min(P->nitems, num_sms() * std::max(occ, 1)));
+  *plan_out = reinterpret_cast<bola_batch_plan>(P);
+  return 0;
+}
+
+int bola_batch_solve(bola_batch_plan plan, const bola_system *systems, int32_t *info, bola_stream_t stream) {
+  Plan *P = reinterpret_cast<Plan *>(plan);
+  if (!P) return -1;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (P->nitems == 0) return 0;
+  ProfScope prof(s, "batched_solve", P->flops, 0.0, 2);
+  BOLA_TRY_CUDA(cudaMemsetAsync(P->counter, 0, sizeof(int32_t), s));
+  batched_solve_kernel<<<P->grid, BT, 0, s>>>(reinterpret_cast<const SystemDesc *>(systems), P->items, P->nitems,
+                                              P->counter, info);
+  BOLA_CHECK_LAUNCH();
+  return 0;
+}
+
+int bola_batch_solve_graph(bola_batch_plan plan, const bola_system *systems, int32_t *info, bola_stream_t stream) {
+  Plan *P = reinterpret_cast<Plan *>(plan);
+  if (!P) return -1;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (P->nitems == 0) return 0;
+  if (P->exec && (P->g_sys != systems || P->g_info != info)) {
+    cudaGraphExecDestroy(P->exec);
+    P->exec = nullptr;
+  }
+  if (!P->exec) {
+    cudaStream_t cap;
+    BOLA_TRY_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaGraph_t g;
+    BOLA_TRY_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    cudaMemsetAsync(P->counter, 0, sizeof(int32_t), cap);
+    batched_solve_kernel<<<P->grid, BT, 0, cap>>>(reinterpret_cast<const SystemDesc *>(systems), P->items,
+                                                  P->nitems, P->counter, info);
+    BOLA_TRY_CUDA(cudaStreamEndCapture(cap, &g));
+    BOLA_TRY_CUDA(cudaGraphInstantiate(&P->exec, g, 0));
+    cudaGraphDestroy(g);
+    cudaStreamDestroy(cap);
+    P->g_sys = systems;
+    P->g_info = info;
+  }
+  ProfScope prof(s, "batched_solve", P->flops, 0.0, 2);
+  BOLA_TRY_CUDA(cudaGraphLaunch(P->exec, s));
+  return 0;
+}
+
+int bola_batch_plan_info(bola_batch_plan plan, int32_t *nitems, int32_t *grid, double *flops) {
+  Plan *P = reinterpret_cast<Plan *>(plan);
+  if (!P) return -1;
+  if (nitems) *nitems = P->nitems;
+  if (grid) *grid = P->grid;
+  if (flops) *flops = P->flops;
+  return 0;
+}
+
+int bola_batch_plan_destroy(bola_batch_plan plan) {
+  Plan *P = reinterpret_cast<Plan *>(plan);
+  if (!P) return 0;
+  if (P->exec) cudaGraphExecDestroy(P->exec);
+  if (P->items) cudaFree(P->items);
+  if (P->counter) cudaFree(P->counter);
+  delete P;
+  return 0;
+}
+
+}  // extern "C"

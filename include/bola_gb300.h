@@ -214,6 +214,38 @@ int bola_dgesv_mixed(int64_t n, int64_t nrhs, const double *a, int64_t lda, cons
                      double *x, int64_t ldx, const bola_mixed_opts *opts, bola_mixed_info *info,
                      bola_stream_t stream);
 
+/* ---- Batched solves of many small systems (no BOLA counterpart) --------
+ * Each system: A X = B with A n x n (1 <= n <= 256), kind 0 = general (LU
+ * with partial pivoting), kind 1 = symmetric positive definite (Cholesky,
+ * lower triangle used); A is overwritten by its factors and B by X.  All
+ * systems of a batch are solved in ONE persistent kernel launch: a plan
+ * buckets the systems by n, gives each bucket a group size (threads per
+ * system, from an autotuned table or the built-in defaults) and orders the
+ * work largest first.  Results do not depend on which other systems are in
+ * the batch.  info[i] (device) = 0, or the 1-based column of a zero pivot
+ * (kind 0) or of the first non-positive pivot (kind 1). */
+typedef struct {
+  int32_t n, nrhs, kind, lda, ldb, reserved;
+  double *a; /* device, n x n column-major */
+  double *b; /* device, n x nrhs column-major */
+} bola_system;
+
+typedef struct bola_batch_plan_st *bola_batch_plan;
+
+/* n, kind: host arrays of `count`.  group_size: host array of 8 group sizes
+ * (32/64/128/256) for the buckets n <= 16, 32, 48, 64, 96, 128, 192, 256;
+ * NULL = built-in defaults.  Returns -2 for an n outside 1..256. */
+int bola_batch_plan_create(int32_t count, const int32_t *n, const int32_t *kind, const int32_t *group_size,
+                           bola_batch_plan *plan);
+/* systems: device array of `count` descriptors; info: device int32[count]. */
+int bola_batch_solve(bola_batch_plan plan, const bola_system *systems, int32_t *info, bola_stream_t stream);
+/* Same solve through a CUDA graph captured on first use for these pointers
+ * and replayed afterwards (one graph launch per batch). */
+int bola_batch_solve_graph(bola_batch_plan plan, const bola_system *systems, int32_t *info,
+                           bola_stream_t stream);
+int bola_batch_plan_info(bola_batch_plan plan, int32_t *nitems, int32_t *grid, double *flops);
+int bola_batch_plan_destroy(bola_batch_plan plan);
+
 #ifdef __cplusplus
 }
 #endif

@@ -58,7 +58,8 @@ def test_mixed_reaches_1e14_well_conditioned(kind, n, nrhs):
     assert info.backward_error <= 1e-14
     assert berr(A, x, b, n, nrhs) <= 1e-14
     if kind == 2 or n <= 1000:
-        assert info.path == 0, (info.path, info.iterations)  # refinement alone converged
+        # refinement (plain, or GMRES-IR for the slower bf16 factors) converged without the FP64 path
+        assert info.path in (0, 1), (info.path, info.iterations)
 
 
 @pytest.mark.parametrize("kappa", [1e2, 1e6, 1e10])
