@@ -55,7 +55,8 @@ class MixedOpts(ctypes.Structure):
 
 class MixedInfo(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("gmres_iterations", ctypes.c_int), ("path", ctypes.c_int),
-                ("factor_info", ctypes.c_int), ("backward_error", ctypes.c_double)]
+                ("factor_info", ctypes.c_int), ("backward_error", ctypes.c_double),
+                ("condition_estimate", ctypes.c_double)]
 
 
 SIGNATURES["bola_dgesv_mixed"] = (_int, [_i64, _i64, _p, _i64, _p, _i64, _p, _i64, ctypes.POINTER(MixedOpts),
@@ -70,11 +71,40 @@ class System(ctypes.Structure):
 
 
 SIGNATURES.update({
+    "bola_mixed_ctx_create": (_int, [_p]),
+    "bola_mixed_ctx_destroy": (_int, [_p]),
+    "bola_mixed_ctx_bytes": (_i64, [_p]),
+    "bola_dgesv_mixed_ctx": (_int, [_p, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, ctypes.POINTER(MixedOpts),
+                                    ctypes.POINTER(MixedInfo), _p]),
     "bola_batch_plan_create": (_int, [_i32, _p, _p, _p, _p]),
     "bola_batch_solve": (_int, [_p, _p, _p, _p]),
     "bola_batch_solve_graph": (_int, [_p, _p, _p, _p]),
     "bola_batch_plan_info": (_int, [_p, _p, _p, _p]),
     "bola_batch_plan_destroy": (_int, [_p]),
+})
+
+
+
+class ServerOpts(ctypes.Structure):
+    """bola_server_opts (include/bola_gb300.h)."""
+    _fields_ = [("slots", ctypes.c_int32), ("small_n", ctypes.c_int32), ("max_batch", ctypes.c_int32),
+                ("mode", ctypes.c_int32), ("factor_kind", ctypes.c_int32), ("group_size", ctypes.c_int32 * 8),
+                ("reserved", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_int64)]
+
+
+class RequestInfo(ctypes.Structure):
+    """bola_request_info (include/bola_gb300.h)."""
+    _fields_ = [("status", ctypes.c_int32), ("path", ctypes.c_int32), ("iterations", ctypes.c_int32),
+                ("info", ctypes.c_int32), ("backward_error", ctypes.c_double), ("t_submit", ctypes.c_double),
+                ("t_admit", ctypes.c_double), ("t_done", ctypes.c_double)]
+
+
+SIGNATURES.update({
+    "bola_server_create": (_int, [ctypes.POINTER(ServerOpts), _p]),
+    "bola_server_submit": (_int, [_p, _i64, _i64, _i32, _p, _p, _p]),
+    "bola_server_wait": (_int, [_p, _i64, _p, ctypes.POINTER(RequestInfo)]),
+    "bola_server_stats": (_int, [_p, _p, _p, _p]),
+    "bola_server_destroy": (_int, [_p]),
 })
 
 _lib = None

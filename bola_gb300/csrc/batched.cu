@@ -229,34 +229,25 @@ int bucket_of(int n) {
 }
 
 }  // namespace
-}  // namespace bola
 
-using namespace bola;
-
-extern "C" {
-
-int bola_batch_plan_create(int32_t count, const int32_t *n, const int32_t *kind, const int32_t *group_size,
-                           bola_batch_plan *plan_out) {
-  if (count < 0) return -1;
-  if (!plan_out) return -5;
-  Plan *P = new Plan();
-  P->count = count;
+// Work items of a batch: per size bucket, systems by decreasing n, BT/G
+// systems per item; items by decreasing cost.  flat holds ITEM int32 per item.
+int batch_items(int32_t count, const int32_t *n, const int32_t *kind, const int32_t *group_size,
+                std::vector<int32_t> &flat, int32_t *nitems, int *group, double *flops) {
   static const int kDefault[NBUCKET] = {32, 32, 64, 64, 128, 128, 256, 256};
   for (int b = 0; b < NBUCKET; ++b) {
     int gsz = group_size ? group_size[b] : kDefault[b];
     if (gsz != 32 && gsz != 64 && gsz != 128 && gsz != 256) gsz = kDefault[b];
-    P->group[b] = gsz;
+    group[b] = gsz;
   }
-  // per bucket, systems by decreasing n; items of BT/G systems; items by decreasing cost
+  double fl = 0.0;
   std::vector<std::vector<int>> byb(NBUCKET);
   for (int i = 0; i < count; ++i) {
-    if (n[i] < 1 || n[i] > 256) {
-      delete P;
+    if (n[i] < 1 || n[i] > 256)
       return fail(-2, "bola_batch_plan_create: system %d has n = %d (supported 1..256)", i, n[i]);
-    }
     byb[bucket_of(n[i])].push_back(i);
     const double nn = n[i];
-    P->flops += (kind && kind[i] == 1) ? nn * nn * nn / 3.0 : 2.0 * nn * nn * nn / 3.0;
+    fl += (kind && kind[i] == 1) ? nn * nn * nn / 3.0 : 2.0 * nn * nn * nn / 3.0;
   }
   struct It {
     double cost;
@@ -266,7 +257,7 @@ int bola_batch_plan_create(int32_t count, const int32_t *n, const int32_t *kind,
   for (int b = 0; b < NBUCKET; ++b) {
     auto &ids = byb[b];
     std::sort(ids.begin(), ids.end(), [&](int x, int y) { return n[x] > n[y] || (n[x] == n[y] && x < y); });
-    const int G = P->group[b], per = BT / G;
+    const int G = group[b], per = BT / G;
     for (size_t s = 0; s < ids.size(); s += per) {
       It it;
       it.v.assign(ITEM, 0);
@@ -283,18 +274,59 @@ int bola_batch_plan_create(int32_t count, const int32_t *n, const int32_t *kind,
     }
   }
   std::stable_sort(its.begin(), its.end(), [](const It &x, const It &y) { return x.cost > y.cost; });
-  P->nitems = (int32_t)its.size();
-  std::vector<int32_t> flat((size_t)its.size() * ITEM);
+  flat.assign(its.size() * ITEM, 0);
   for (size_t i = 0; i < its.size(); ++i) std::memcpy(&flat[i * ITEM], its[i].v.data(), sizeof(int32_t) * ITEM);
+  if (flops) *flops = fl;
+  if (nitems) *nitems = (int32_t)its.size();
+  return 0;
+}
+
+int batch_grid(int32_t nitems) {
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batched_solve_kernel, BT, 0);
+  return std::max(1, std::min((int)nitems, num_sms() * std::max(occ, 1)));
+}
+
+// One persistent launch over nitems work items (device array); *counter is
+// the work queue's head and is reset here.
+int batch_launch(cudaStream_t s, const bola_system *systems, const int32_t *items, int32_t nitems, int32_t *counter,
+                 int32_t *info) {
+  if (nitems == 0) return 0;
+  BOLA_TRY_CUDA(cudaMemsetAsync(counter, 0, sizeof(int32_t), s));
+  batched_solve_kernel<<<batch_grid(nitems), BT, 0, s>>>(reinterpret_cast<const SystemDesc *>(systems), items,
+                                                         nitems, counter, info);
+  BOLA_CHECK_LAUNCH();
+  return 0;
+}
+
+namespace {
+
+}  // namespace
+}  // namespace bola
+
+using namespace bola;
+
+extern "C" {
+
+int bola_batch_plan_create(int32_t count, const int32_t *n, const int32_t *kind, const int32_t *group_size,
+                           bola_batch_plan *plan_out) {
+  if (count < 0) return -1;
+  if (!plan_out) return -5;
+  Plan *P = new Plan();
+  P->count = count;
+  std::vector<int32_t> flat;
+  const int st = batch_items(count, n, kind, group_size, flat, &P->nitems, P->group, &P->flops);
+  if (st != 0) {
+    delete P;
+    return st;
+  }
   if (cudaMalloc(&P->items, sizeof(int32_t) * std::max<size_t>(flat.size(), 1)) != cudaSuccess ||
       cudaMalloc(&P->counter, sizeof(int32_t)) != cudaSuccess) {
     delete P;
     return fail(BOLA_ERR_CUDA, "bola_batch_plan_create: device allocation failed");
   }
   if (!flat.empty()) cudaMemcpy(P->items, flat.data(), sizeof(int32_t) * flat.size(), cudaMemcpyHostToDevice);
-  int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batched_solve_kernel, BT, 0);
-  P->grid = std::max(1, std::min(P->nitems, num_sms() * std::max(occ, 1)));
+  P->grid = batch_grid(P->nitems);
   *plan_out = reinterpret_cast<bola_batch_plan>(P);
   return 0;
 }

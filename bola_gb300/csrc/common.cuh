@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <vector>
 
 #include "bola_gb300.h"
 #include "profile.cuh"
@@ -100,6 +101,14 @@ int potrf2_rec(cudaStream_t s, char uplo, int64_t n, double *A, int64_t lda, int
 
 // Adds `add` to ipiv[0..count) unless *info != 0.
 int ipiv_add(cudaStream_t s, int32_t *ipiv, int64_t count, int32_t add, const int32_t *info);
+
+// Batched small-system solver pieces (batched.cu): the work items of a batch
+// (flat int32 records, *nitems of them; group = the 8 per-bucket group sizes
+// used) and one persistent launch over items already on the device.
+int batch_items(int32_t count, const int32_t *n, const int32_t *kind, const int32_t *group_size,
+                std::vector<int32_t> &flat, int32_t *nitems, int *group, double *flops);
+int batch_launch(cudaStream_t s, const bola_system *systems, const int32_t *items, int32_t nitems, int32_t *counter,
+                 int32_t *info);
 
 // ---- device side -------------------------------------------------------------
 __device__ __forceinline__ double fused(double a, double b, double c) { return __fma_rn(a, b, c); }

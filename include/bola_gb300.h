@@ -192,7 +192,10 @@ int bola_dpotrs(char uplo, int64_t n, int64_t nrhs, const double *fac, int64_t l
  * more; otherwise flexible GMRES on the correction equation, preconditioned
  * by the low-precision LU, takes over (GMRES-IR); if that stalls too, the
  * plain FP64 path (bola_dgetrf + bola_dgetrs) solves the system, when
- * fallback_fp64 is set.  Synchronous: it
+ * fallback_fp64 is set.  The FP64 path is taken at once when the spread
+ * max|u_ii| / min|u_ii| of the low-precision U exceeds a per-kind limit
+ * (bf16 175, tf32 1100, 3xTF32 4.5e4), beyond which refinement was measured
+ * not to converge.  Synchronous: it
  * returns after the result and *info are final.  n <= 8192, nrhs <= 32. */
 typedef struct {
   int factor_kind;       /* 0: bf16 tensor-core updates; 1: tf32; 2: 3xTF32 (FP32-accurate) */
@@ -208,11 +211,24 @@ typedef struct {
   int path;              /* 0 mixed IR, 1 mixed GMRES-IR, 2 plain FP64 fallback */
   int factor_info;       /* first zero pivot of the low-precision LU (1-based), 0 if none */
   double backward_error; /* of the returned X */
+  double condition_estimate; /* max|u_ii| / min|u_ii| of the low-precision factor */
 } bola_mixed_info;
 
 int bola_dgesv_mixed(int64_t n, int64_t nrhs, const double *a, int64_t lda, const double *b, int64_t ldb,
                      double *x, int64_t ldx, const bola_mixed_opts *opts, bola_mixed_info *info,
                      bola_stream_t stream);
+
+/* The same solve with caller-owned device workspace, so that several solves
+ * can run at once on different streams and host threads (bola_dgesv_mixed
+ * shares one workspace per device and serialises).  A context grows to the
+ * largest (n, nrhs) it has served; bola_mixed_ctx_bytes reports its size. */
+typedef struct bola_mixed_ctx_st *bola_mixed_ctx;
+int bola_mixed_ctx_create(bola_mixed_ctx *ctx);
+int bola_mixed_ctx_destroy(bola_mixed_ctx ctx);
+int64_t bola_mixed_ctx_bytes(bola_mixed_ctx ctx);
+int bola_dgesv_mixed_ctx(bola_mixed_ctx ctx, int64_t n, int64_t nrhs, const double *a, int64_t lda, const double *b,
+                         int64_t ldb, double *x, int64_t ldx, const bola_mixed_opts *opts, bola_mixed_info *info,
+                         bola_stream_t stream);
 
 /* ---- Batched solves of many small systems (no BOLA counterpart) --------
  * Each system: A X = B with A n x n (1 <= n <= 256), kind 0 = general (LU
@@ -245,6 +261,58 @@ int bola_batch_solve_graph(bola_batch_plan plan, const bola_system *systems, int
                            bola_stream_t stream);
 int bola_batch_plan_info(bola_batch_plan plan, int32_t *nitems, int32_t *grid, double *flops);
 int bola_batch_plan_destroy(bola_batch_plan plan);
+
+/* ---- Solve server (no BOLA counterpart) --------------------------------
+ * Accepts solve requests A X = B (host buffers, column-major, ld = n;
+ * 1 <= n <= 8192, 1 <= nrhs <= 32; kind 0 general, 1 SPD) from any host
+ * thread and serves them on the current device.  Requests are admitted in
+ * arrival order while the device bytes held by admitted requests stay within
+ * hbm_budget_bytes.  Requests with n > small_n run on `slots` workers, each
+ * with its own stream and mixed-solver context (several run at once); in
+ * mode 0 they take bola_dgesv_mixed_ctx (tensor-core LU, FP64 refinement,
+ * FP64 fallback; SPD systems are solved by the same LU), in mode 1 the plain
+ * FP64 path (bola_dgetrf/bola_dgetrs, or bola_dpotrf/bola_dpotrs for SPD).
+ * Requests with n <= small_n (at most 256) are gathered continuously: every
+ * admitted small request waiting when the previous batch ends goes into the
+ * next persistent batched launch (bola_batch_solve, FP64).  Every result's
+ * normwise backward error is measured in FP64 on the device against the
+ * request's original A and B.  A result does not depend on the other
+ * requests in flight.  The caller keeps a and b alive until the request's
+ * bola_server_wait returns. */
+typedef struct {
+  int32_t slots;        /* concurrent large-request workers (>= 1) */
+  int32_t small_n;      /* largest n sent to the batcher (0..256) */
+  int32_t max_batch;    /* most small requests in one batched launch */
+  int32_t mode;         /* 0 mixed precision, 1 plain FP64 per request */
+  int32_t factor_kind;  /* mode 0: factor kind as in bola_mixed_opts */
+  int32_t group_size[8];/* batched group sizes per bucket; all 0 = defaults */
+  int32_t reserved;
+  int64_t hbm_budget_bytes; /* admission budget for requests' device buffers */
+} bola_server_opts;
+
+typedef struct {
+  int32_t status;        /* 0 queued, 1 running, 2 done; < 0 error code */
+  int32_t path;          /* 0 mixed IR, 1 GMRES-IR, 2 FP64, 3 batched FP64 */
+  int32_t iterations;    /* refinement sweeps (mixed paths) */
+  int32_t info;          /* factorisation info (0 = success) */
+  double backward_error; /* max over right-hand sides */
+  double t_submit, t_admit, t_done; /* seconds since the server was created */
+} bola_request_info;
+
+typedef struct bola_server_st *bola_server;
+int bola_server_create(const bola_server_opts *opts, bola_server *server);
+/* Returns -2 for n outside 1..8192, -3 for nrhs outside 1..32, -4 for a kind
+ * other than 0/1, -5 when the request alone needs more device bytes than
+ * the budget.  *id identifies the request for bola_server_wait. */
+int bola_server_submit(bola_server server, int64_t n, int64_t nrhs, int32_t kind, const double *a,
+                       const double *b, int64_t *id);
+/* Blocks until request `id` is done, copies X (n x nrhs) into x (host, may
+ * be NULL) and its record into *info; the id is then released.  Returns the
+ * request's error status (0 on success), -2 for an unknown id. */
+int bola_server_wait(bola_server server, int64_t id, double *x, bola_request_info *info);
+int bola_server_stats(bola_server server, int64_t *bytes_in_use, int32_t *pending, int32_t *running);
+/* Serves every request already submitted, then stops the workers. */
+int bola_server_destroy(bola_server server);
 
 #ifdef __cplusplus
 }
