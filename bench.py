@@ -52,6 +52,12 @@ def parse():
     ap.add_argument("--n", type=int, default=8192)
     ap.add_argument("--nrhs", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-systems", type=int, default=20000)
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[25.0, 50.0, 100.0, 200.0])
+    ap.add_argument("--serve-requests", type=int, default=300)
+    ap.add_argument("--serve-pool", type=int, default=48)
+    ap.add_argument("--no-serve", action="store_true")
     return ap.parse_args()
 
 
@@ -333,8 +339,81 @@ def run_ours(args, rank, world, device):
     clocks = clk.summary()
     if clocks is not None:
         out["clocks"] = clocks
+    if not args.no_batched:
+        out["batched"] = run_batched(args, device, peak_fp64)
+    if not args.no_serve:
+        out["serve"] = run_serve(args, device)
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(systems[0], n, nrhs, budget_s=12.0)
+    return out
+
+
+def run_batched(args, device, peak_fp64):
+    """20,000 independent systems (n uniform in [8, 256], half LU on
+    diagonally dominant, half Cholesky on SPD matrices, nrhs uniform in
+    [1, 8], seed 4) solved in one persistent launch replayed from a CUDA
+    graph; group sizes autotuned per size bucket in this run."""
+    from bola_gb300.batch import Batch, autotune, config4_batch, time_solve
+    count = args.batch_systems
+    ns, nrhs, kinds, fill = config4_batch(count, seed=4, device=device)
+    b = Batch(ns, nrhs, kinds, device=device)
+    fill(b)
+    A0, B0 = b.A.clone(), b.B.clone()
+    table, trials = autotune(b)
+    b.replan(table)
+    b.solve(graph=True)
+    torch.cuda.synchronize()
+    ok_info = int((b.info != 0).sum()) == 0
+    # accuracy on a sample of systems
+    rng = np.random.default_rng(4)
+    worst = 0.0
+    for i in rng.choice(count, size=min(200, count), replace=False):
+        n, r = int(ns[i]), int(nrhs[i])
+        A = A0[int(b.a_off[i]):int(b.a_off[i + 1])].view(n, n).t()
+        B = B0[int(b.b_off[i]):int(b.b_off[i + 1])].view(r, n).t()
+        X = b.b_view(int(i))
+        R = B - A @ X
+        den = A.abs().sum(1).max() * X.abs().max(0).values + B.abs().max(0).values
+        worst = max(worst, float((R.abs().max(0).values / den).max()))
+    steps = max(3, args.steps)
+    times = []
+    for _ in range(steps):
+        times.append(time_solve(b, A0, B0, 1, graph=True))
+    n64 = ns.astype(np.float64)
+    flops = float(np.sum(np.where(kinds == 1, n64 ** 3 / 3, 2 * n64 ** 3 / 3) + 2 * n64 ** 2 * nrhs))
+    ms = statistics.median(times)
+    b.close()
+    return {"workload": f"{count} systems, n U[8,256], nrhs U[1,8], half LU / half Cholesky, seed 4",
+            "systems_per_s": round(count / (ms / 1e3), 1), "ms_per_batch": round(ms, 3),
+            "ms_min": round(min(times), 3), "steps": steps, "launches_per_batch": 1, "graph": True,
+            "gflops": round(flops / (ms / 1e3) / 1e9, 1),
+            "fp64_peak_frac": round(flops / (ms / 1e3) / 1e9 / peak_fp64, 4) if peak_fp64 else None,
+            "group_sizes": table,
+            "autotune_ms": {str(k): {str(g): round(t, 3) for g, t in v.items()} for k, v in trials.items()},
+            "info_all_zero": ok_info, "max_backward_error_sample": worst}
+
+
+def run_serve(args, device):
+    """The serving loop: Poisson arrivals (seed 5) at swept rates of requests
+    with n log-uniform in [16, 4096], nrhs U[1, 32], 70 % LU / 30 % SPD,
+    kappa in {1e2, 1e6, 1e10}; mixed server (tensor-core LU + FP64
+    refinement, small requests batched) against the plain FP64 per-request
+    server; inputs from pinned host memory, results copied back."""
+    from bola_gb300.serve import Server, poisson_trace, request_pool, run_trace, summarize
+    pool = request_pool(args.serve_pool, seed=5, device=device)
+    out = {"workload": f"{args.serve_requests} requests per rate from a pool of {args.serve_pool} seeded systems "
+                       f"(mean n {np.mean([p['n'] for p in pool]):.0f}), 4 slots, admission budget 120 GB",
+           "rates": list(args.serve_rates), "mixed": {}, "fp64": {}}
+    for mode, small in (("mixed", 256), ("fp64", 0)):
+        with Server(slots=4, small_n=small, mode=mode) as srv:
+            # warm-up: one request of every pool entry
+            for k in range(len(pool)):
+                p = pool[k]
+                srv.wait(srv.submit_raw(p["n"], 4, p["kind"], p["A"].data_ptr(), p["B"].data_ptr()), want_x=False)
+            for rate in args.serve_rates:
+                tr = poisson_trace(rate, args.serve_requests, len(pool), seed=5)
+                recs, _ = run_trace(srv, pool, tr)
+                out[mode][str(rate)] = summarize(recs)
     return out
 
 

@@ -42,9 +42,15 @@ class Batch:
         raw = np.frombuffer(desc, dtype=np.uint8)
         self.desc = torch.from_numpy(raw.copy()).to(device)
         self.plan = ctypes.c_void_p()
+        self.replan(group_size)
+
+    def replan(self, group_size=None):
+        """(Re)build the plan with an 8-entry group-size table (None = defaults)."""
+        self.close()
         gs = None
         if group_size is not None:
             gs = (ctypes.c_int32 * 8)(*[int(v) for v in group_size])
+        self.group_size = None if group_size is None else [int(v) for v in group_size]
         st = self.L.bola_batch_plan_create(self.count, self.ns.ctypes.data_as(ctypes.c_void_p),
                                            self.kinds.ctypes.data_as(ctypes.c_void_p),
                                            ctypes.cast(gs, ctypes.c_void_p) if gs is not None else None,
@@ -107,3 +113,59 @@ def config4_batch(count, seed=4, device="cuda", nmin=8, nmax=256, rmax=8):
             batch.a_view(i).copy_(M)
             batch.b_view(i).copy_(torch.rand(n, int(nrhs[i]), dtype=torch.float64, device=device, generator=g) * 2 - 1)
     return ns, nrhs, kinds, fill
+
+
+BUCKET_N = (16, 32, 48, 64, 96, 128, 192, 256)
+DEFAULT_GROUPS = (32, 32, 64, 64, 128, 128, 256, 256)
+GROUP_CHOICES = (32, 64, 128, 256)
+
+
+def bucket_of(n):
+    for b, top in enumerate(BUCKET_N):
+        if n <= top:
+            return b
+    raise ValueError(n)
+
+
+def time_solve(batch, A0, B0, reps, graph=True):
+    """Minimum CUDA-event time (ms) of one batched solve over `reps` runs, the
+    inputs restored from A0/B0 before each (outside the timed region)."""
+    stream = torch.cuda.current_stream()
+    best = float("inf")
+    for _ in range(reps):
+        batch.A.copy_(A0)
+        batch.B.copy_(B0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        batch.solve(graph=graph)
+        e1.record(stream)
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return best
+
+
+def autotune(batch, reps=3):
+    """Per size bucket, the group size (threads per system) with the shortest
+    solve of that bucket's systems of `batch` (measured on a sub-batch holding
+    copies of them).  Returns (table of 8 group sizes, {bucket: {G: ms}})."""
+    buckets = np.array([bucket_of(int(n)) for n in batch.ns])
+    table, trials = list(DEFAULT_GROUPS), {}
+    for b in range(len(BUCKET_N)):
+        idx = np.nonzero(buckets == b)[0]
+        if len(idx) == 0:
+            continue
+        sub = Batch(batch.ns[idx], batch.nrhs[idx], batch.kinds[idx], device=batch.A.device)
+        for j, i in enumerate(idx):
+            sub.a_view(j).copy_(batch.a_view(int(i)))
+            sub.b_view(j).copy_(batch.b_view(int(i)))
+        A0, B0 = sub.A.clone(), sub.B.clone()
+        trials[b] = {}
+        for g in GROUP_CHOICES:
+            t = list(DEFAULT_GROUPS)
+            t[b] = g
+            sub.replan(t)
+            sub.solve(graph=False)  # warm-up
+            trials[b][g] = time_solve(sub, A0, B0, reps, graph=False)
+        table[b] = min(trials[b], key=trials[b].get)
+        sub.close()
+    return table, trials

@@ -113,18 +113,22 @@ __global__ void compose_perm(int64_t n, const int32_t *ipiv, int32_t *perm) {
   for (int64_t i = threadIdx.x; i < n; i += blockDim.x) perm[i] = p[i];
 }
 
+// max that keeps a NaN (fmax would drop it): the norms below feed the
+// backward-error test, which must fail on a NaN anywhere in x or r
+__device__ __forceinline__ double nan_max(double a, double b) { return (b > a || b != b) ? b : a; }
+
 // Per right-hand side: out[c] = max_i |v[i, c]| (one CTA per column).
 __global__ void col_absmax(int64_t n, const double *__restrict__ v, int64_t ldv, double *out) {
   __shared__ double red[32];
   const int c = blockIdx.x;
   double m = 0.0;
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, fabs(v[i + c * ldv]));
-  for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) m = nan_max(m, fabs(v[i + c * ldv]));
+  for (int off = 16; off > 0; off >>= 1) m = nan_max(m, __shfl_xor_sync(0xffffffffu, m, off));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x == 0) {
     double mm = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mm = fmax(mm, red[w]);
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mm = nan_max(mm, red[w]);
     out[c] = mm;
   }
 }
@@ -132,13 +136,13 @@ __global__ void col_absmax(int64_t n, const double *__restrict__ v, int64_t ldv,
 __global__ void max_of(int64_t n, const double *v, double *out) {
   __shared__ double red[32];
   double m = 0.0;
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, v[i]);
-  for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) m = nan_max(m, v[i]);
+  for (int off = 16; off > 0; off >>= 1) m = nan_max(m, __shfl_xor_sync(0xffffffffu, m, off));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x == 0) {
     double mm = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mm = fmax(mm, red[w]);
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mm = nan_max(mm, red[w]);
     *out = mm;
   }
 }
@@ -180,7 +184,12 @@ diag_block_inverses(int64_t n, const float *__restrict__ W, int64_t ldw, float *
   __shared__ float B[TB][TB + 1];
   const int64_t k0 = (int64_t)blockIdx.x * TB;
   const int kb = (int)imin(TB, n - k0);
-  for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) B[e % kb][e / kb] = W[(k0 + e % kb) + (k0 + e / kb) * ldw];
+  // the whole tile is written: the substitutions below multiply entries
+  // outside the kb x kb block by zeros, and 0 * (stale NaN) would be NaN
+  for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
+    const int r = e % TB, c = e / TB;
+    B[r][c] = (r < kb && c < kb) ? W[(k0 + r) + (k0 + c) * ldw] : 0.f;
+  }
   __syncthreads();
   const int j = threadIdx.x;
   float *L = Dl + (int64_t)blockIdx.x * TB * TB, *U = Du + (int64_t)blockIdx.x * TB * TB;
