@@ -11,10 +11,10 @@
 //           GMRES-IR, and when that stalls too, to the plain FP64 path
 //           d = S U^-1 L^-1 P (r / ||r||) * ||r||;  x += d    (FP64 update)
 // The residual, the update and the backward-error test are the only FP64
-// steps.  The FP32 triangular solves walk 64-row blocks, one launch per
-// block: every CTA re-solves the small diagonal block from shared memory and
-// then updates its slice of the rows below (above), so no grid barrier is
-// needed.
+// steps.  Each FP32 triangular solve is one launch: a dataflow over 64-row
+// blocks in which a CTA per block folds in the blocks solved before it as
+// their flags appear, then applies the precomputed inverse of its diagonal
+// block.
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -216,96 +216,137 @@ diag_block_inverses(int64_t n, const float *__restrict__ W, int64_t ldw, float *
   for (int i = 0; i < TB; ++i) U[i + j * TB] = x[i];
 }
 
-// One block step of a blocked triangular solve with nrhs <= 32 right-hand
-// sides (n x nrhs, ld n).  LOWER: unit-lower L, forward; else U, backward.
-// Every CTA forms the solved block ys = Dinv * y[k0:k0+kb] (a small GEMM with
-// the precomputed inverse), CTA 0 writes it to `out`, and every CTA then
-// subtracts L[rows, blk] * ys (or U[rows, blk] * ys) from its 64-row slice of
-// the rows below (above) in place in `y`.  The solved block never goes back
-// into `y`, which other CTAs of the launch still read.
-template <bool LOWER>
-__global__ void __launch_bounds__(256)
-trsv_block(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, const float *__restrict__ Dinv, int64_t k0,
-           int kb, float *y, float *out) {
-  __shared__ float DiT[TB][TB];     // DiT[k][r] = Dinv(r, k)
-  __shared__ float rb[MAXRHS][TB];
-  __shared__ float ys[MAXRHS][TB];
-  __shared__ float Ls[TB][TB];      // Ls[k][r]: the update tile of this CTA's rows
-  const int tid = threadIdx.x;
-  const float *D = Dinv + (k0 / TB) * TB * TB;
-  const int64_t rbeg = LOWER ? k0 + kb : 0;
-  const int64_t rend = LOWER ? n : k0;
-  const int64_t i0 = rbeg + (int64_t)blockIdx.x * TB;
-  // fixed-count loads, all issued before any shared-memory store
-  constexpr int PER = TB * TB / 256;  // 16 per thread
-  float dv[PER], lv[PER], bv[MAXRHS * TB / 256];
-#pragma unroll
-  for (int q = 0; q < PER; ++q) {
-    const int e = tid + 256 * q;
-    const int r = e % TB, k = e / TB;
-    dv[q] = D[e];
-    lv[q] = (k < kb && i0 + r < rend) ? W[(i0 + r) + (k0 + k) * ldw] : 0.f;
-  }
-#pragma unroll
-  for (int q = 0; q < MAXRHS * TB / 256; ++q) {
-    const int e = tid + 256 * q;
-    const int r = e % TB, c = e / TB;
-    bv[q] = (c < nrhs && r < kb) ? y[(k0 + r) + (int64_t)c * n] : 0.f;
-  }
-#pragma unroll
-  for (int q = 0; q < PER; ++q) {
-    const int e = tid + 256 * q;
-    DiT[e / TB][e % TB] = dv[q];
-    Ls[e / TB][e % TB] = lv[q];
-  }
-#pragma unroll
-  for (int q = 0; q < MAXRHS * TB / 256; ++q) {
-    const int e = tid + 256 * q;
-    rb[e / TB][e % TB] = bv[q];
-  }
-  __syncthreads();
-  for (int e = tid; e < TB * nrhs; e += blockDim.x) {
-    const int r = e % TB, c = e / TB;
-    float acc = 0.f;
-#pragma unroll 16
-    for (int k = 0; k < TB; ++k) acc = fmaf(DiT[k][r], rb[c][k], acc);
-    ys[c][r] = acc;
-  }
-  __syncthreads();
-  if (blockIdx.x == 0) {
-    for (int e = tid; e < kb * nrhs; e += blockDim.x) {
-      const int r = e % kb, c = e / kb;
-      out[(k0 + r) + (int64_t)c * n] = ys[c][r];
-    }
-  }
-  const int r = tid >> 2, part = tid & 3;
-  const int64_t i = i0 + r;
-  if (i >= rend) return;
-  for (int c = part; c < nrhs; c += 4) {
-    float acc = 0.f;
-#pragma unroll 16
-    for (int k = 0; k < TB; ++k) acc = fmaf(Ls[k][r], ys[c][k], acc);
-    y[i + (int64_t)c * n] -= acc;
-  }
+// Blocked triangular solve with nrhs <= 32 right-hand sides (n x nrhs, ld n)
+// in ONE launch, as a dataflow over the 64-row blocks.  LOWER: unit-lower L,
+// blocks solved top to bottom; else U, bottom to top.  Each CTA takes the
+// next block in solve order from an atomic ticket, so it only ever waits for
+// blocks held by CTAs that started before it (no co-residency assumption).
+// It folds in the blocks solved before its own, in solve order, each as soon
+// as that block's flag carries this launch's epoch:
+//   acc -= L[blk, k] x_k      (the tile of W is loaded before the wait)
+// then solves its own block with the precomputed inverse of the diagonal
+// block, x_blk = Dinv acc, writes it to `out` and publishes its flag.  Waits
+// are bounded: on expiry *err is set (the host fails the solve) and the CTA
+// goes on, so that every later wait still ends.
+__device__ __forceinline__ int ld_acquire(const int32_t *p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
 }
 
-// y (right-hand sides, overwritten) -> out (solution)
-int trsv(cudaStream_t s, bool lower, int64_t n, int nrhs, const float *W, int64_t ldw, const float *Dinv, float *y,
-         float *out) {
-  ProfScope prof(s, lower ? "trsv_lower" : "trsv_upper", (double)n * n * nrhs, 4.0 * (double)n * n / 2,
-                 (int)cdiv(n, TB));
-  const int64_t nb = cdiv(n, TB);
-  for (int64_t b = 0; b < nb; ++b) {
-    const int64_t k0 = lower ? b * TB : (nb - 1 - b) * TB;
-    const int kb = (int)imin(TB, n - k0);
-    const int64_t rows = lower ? n - k0 - kb : k0;
-    const unsigned grid = (unsigned)imax(1, cdiv(rows, TB));
-    if (lower)
-      trsv_block<true><<<grid, 256, 0, s>>>(n, nrhs, W, ldw, Dinv, k0, kb, y, out);
-    else
-      trsv_block<false><<<grid, 256, 0, s>>>(n, nrhs, W, ldw, Dinv, k0, kb, y, out);
-    BOLA_CHECK_LAUNCH();
+__device__ __forceinline__ void st_release(int32_t *p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+template <bool LOWER>
+__global__ void __launch_bounds__(256)
+trsv_dataflow(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, const float *__restrict__ Dinv,
+              const float *__restrict__ y, float *out, int32_t *flags, int32_t *ticket, int32_t epoch, int32_t *err) {
+  __shared__ float Ls[TB][TB + 1];  // Ls[k][r] = tile(r, k)
+  __shared__ float xs[MAXRHS][TB];
+  __shared__ int sb;
+  const int tid = threadIdx.x;
+  const int nb = (int)((n + TB - 1) / TB);
+  if (tid == 0) sb = atomicAdd(ticket, 1);
+  __syncthreads();
+  const int t = sb;
+  const int b = LOWER ? t : nb - 1 - t;
+  const int64_t i0 = (int64_t)b * TB;
+  const int kb = (int)imin(TB, n - i0);
+  const int r = tid & (TB - 1), cg = tid >> 6;  // row of the block, right-hand-side group (4 groups)
+  constexpr int NQ = MAXRHS / 4;
+  float acc[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    const int c = cg + 4 * q;
+    acc[q] = (c < nrhs && r < kb) ? y[i0 + r + (int64_t)c * n] : 0.f;
   }
+  constexpr int PER = TB * TB / 256;
+  for (int sidx = 0; sidx < t; ++sidx) {
+    const int k = LOWER ? sidx : nb - 1 - sidx;
+    const int64_t k0 = (int64_t)k * TB;
+    const int kbk = (int)imin(TB, n - k0);
+    float lv[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int e = tid + 256 * q;
+      const int rr = e % TB, kk = e / TB;
+      lv[q] = (rr < kb && kk < kbk) ? W[(i0 + rr) + (k0 + kk) * ldw] : 0.f;
+    }
+    if (tid == 0) {
+      int polls = 0;
+      while (ld_acquire(flags + k) != epoch) {
+        if (++polls > (1 << 21)) {
+          atomicExch(err, 3);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int e = tid + 256 * q;
+      Ls[e / TB][e % TB] = lv[q];
+    }
+    for (int e = tid; e < TB * nrhs; e += 256) {
+      const int kk = e % TB, c = e / TB;
+      xs[c][kk] = kk < kbk ? __ldcg(out + k0 + kk + (int64_t)c * n) : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < TB; ++kk) {
+      const float a = Ls[kk][r];
+#pragma unroll
+      for (int q = 0; q < NQ; ++q)
+        if (cg + 4 * q < nrhs) acc[q] = fmaf(-a, xs[cg + 4 * q][kk], acc[q]);
+    }
+    __syncthreads();
+  }
+  // the diagonal block: x = Dinv acc
+  const float *D = Dinv + (int64_t)b * TB * TB;
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int e = tid + 256 * q;
+    Ls[e / TB][e % TB] = D[e];
+  }
+#pragma unroll
+  for (int q = 0; q < NQ; ++q)
+    if (cg + 4 * q < nrhs) xs[cg + 4 * q][r] = acc[q];
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    const int c = cg + 4 * q;
+    if (c >= nrhs) continue;
+    float v = 0.f;
+#pragma unroll 8
+    for (int kk = 0; kk < TB; ++kk) v = fmaf(Ls[kk][r], xs[c][kk], v);
+    if (r < kb) out[i0 + r + (int64_t)c * n] = v;
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) st_release(flags + b, epoch);
+}
+
+// Sequencing state of the dataflow solves: flags (one per 64-row block,
+// zeroed once), the ticket, the wait-expiry flag and the launch epoch.
+struct TrsvSync {
+  int32_t *flags = nullptr, *ticket = nullptr, *err = nullptr;
+  int32_t epoch = 0;
+};
+
+// y (right-hand sides) -> out (solution); y is not modified.
+int trsv(cudaStream_t s, bool lower, int64_t n, int nrhs, const float *W, int64_t ldw, const float *Dinv,
+         const float *y, float *out, TrsvSync &sync) {
+  ProfScope prof(s, lower ? "trsv_lower" : "trsv_upper", (double)n * n * nrhs, 4.0 * (double)n * n / 2, 1);
+  const unsigned nb = (unsigned)cdiv(n, TB);
+  const int32_t epoch = ++sync.epoch;
+  BOLA_TRY_CUDA(cudaMemsetAsync(sync.ticket, 0, sizeof(int32_t), s));
+  if (lower)
+    trsv_dataflow<true><<<nb, 256, 0, s>>>(n, nrhs, W, ldw, Dinv, y, out, sync.flags, sync.ticket, epoch, sync.err);
+  else
+    trsv_dataflow<false><<<nb, 256, 0, s>>>(n, nrhs, W, ldw, Dinv, y, out, sync.flags, sync.ticket, epoch, sync.err);
+  BOLA_CHECK_LAUNCH();
   return 0;
 }
 
@@ -390,14 +431,16 @@ struct Workspace {
   double *V = nullptr, *Z = nullptr, *H = nullptr;  // GMRES basis, preconditioned basis, Hessenberg column
   double *hn = nullptr;                              // per-column 2-norms (GMRES)
   int32_t *ipiv = nullptr, *perm = nullptr, *info = nullptr;
+  TrsvSync ts;  // dataflow triangular solves
   MixedLU lu;
 };
 
 void ws_free(Workspace &w) {
   for (void *p : {(void *)w.W, (void *)w.y, (void *)w.z, (void *)w.Dl, (void *)w.Du, (void *)w.scale, (void *)w.r,
                   (void *)w.d, (void *)w.norms, (void *)w.rowsum, (void *)w.ipiv, (void *)w.perm, (void *)w.info,
-                  (void *)w.V, (void *)w.Z, (void *)w.H, (void *)w.hn})
+                  (void *)w.V, (void *)w.Z, (void *)w.H, (void *)w.hn, (void *)w.ts.flags, (void *)w.ts.ticket})
     if (p) cudaFree(p);
+  w.ts.flags = w.ts.ticket = w.ts.err = nullptr;
   w.lu.release(nullptr);
   w.W = w.y = w.z = w.Dl = w.Du = nullptr;
   w.scale = w.r = w.d = w.norms = w.rowsum = w.V = w.Z = w.H = w.hn = nullptr;
@@ -437,6 +480,12 @@ int ws_reserve(Workspace &w, int64_t n, int64_t nrhs, int kind, cudaStream_t s) 
     BOLA_TRY(alloc(&w.Z, sizeof(double) * GM_M * nrhs * n));
     BOLA_TRY(alloc(&w.H, sizeof(double) * (GM_M + 2) * MAXRHS * 2));
     BOLA_TRY(alloc(&w.hn, sizeof(double) * MAXRHS));
+    BOLA_TRY(alloc(&w.ts.flags, sizeof(int32_t) * cdiv(n, TB)));
+    BOLA_TRY(alloc(&w.ts.ticket, sizeof(int32_t) * 2));
+    w.ts.err = w.ts.ticket + 1;
+    BOLA_TRY_CUDA(cudaMemset(w.ts.flags, 0, sizeof(int32_t) * cdiv(n, TB)));
+    BOLA_TRY_CUDA(cudaMemset(w.ts.ticket, 0, sizeof(int32_t) * 2));
+    w.ts.epoch = 0;
     w.n = n;
     w.nrhs = nrhs;
     w.bytes = bytes + (int64_t)n * 64 * 4 * 4;  // plus the update operands of the LU
@@ -453,8 +502,8 @@ int correction(cudaStream_t s, Workspace &w, int64_t n, int nrhs, const double *
   const unsigned g = (unsigned)cdiv(n * nrhs, 256);
   permute_scale_down<<<g, 256, 0, s>>>(n, nrhs, r, ldr, w.perm, rs, w.y);
   BOLA_CHECK_LAUNCH();
-  BOLA_TRY(trsv(s, true, n, nrhs, w.W, n, w.Dl, w.y, w.z));
-  BOLA_TRY(trsv(s, false, n, nrhs, w.W, n, w.Du, w.z, w.y));
+  BOLA_TRY(trsv(s, true, n, nrhs, w.W, n, w.Dl, w.y, w.z, w.ts));
+  BOLA_TRY(trsv(s, false, n, nrhs, w.W, n, w.Du, w.z, w.y, w.ts));
   update_x<<<g, 256, 0, s>>>(n, nrhs, w.y, w.scale, rs, x, ldx, assign ? 1 : 0);
   BOLA_CHECK_LAUNCH();
   return 0;
@@ -474,8 +523,14 @@ int residual_berr(cudaStream_t s, Workspace &w, int64_t n, int nr, const double 
   }
   BOLA_CHECK_LAUNCH();
   std::vector<double> h(3 * nr + 1);
+  int32_t terr = 0;
   BOLA_TRY_CUDA(cudaMemcpyAsync(h.data(), nrm, sizeof(double) * (3 * nr + 1), cudaMemcpyDeviceToHost, s));
+  BOLA_TRY_CUDA(cudaMemcpyAsync(&terr, w.ts.err, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
   BOLA_TRY_CUDA(cudaStreamSynchronize(s));
+  if (terr != 0) {
+    cudaMemsetAsync(w.ts.err, 0, sizeof(int32_t), s);
+    return fail(BOLA_ERR_CUDA, "mixed: a triangular-solve wait expired (%d)", terr);
+  }
   double e = 0.0;
   for (int c = 0; c < nr; ++c) {
     const double den = h[3 * nr] * h[nr + c] + h[2 * nr + c];

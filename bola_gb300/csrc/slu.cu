@@ -77,10 +77,24 @@ __device__ __forceinline__ void write_operand_row(int kind, void *op, float *op_
 // global 1-based rows (col0 + local + 1).  CTA cr of the cluster owns panel
 // rows [cr*R, cr*R + R), kept in shared memory column-major with an odd
 // pitch (R + 1) so that both a thread walking its row and a warp walking a
-// column are conflict-free.  Per column: warp-redux pivot search, one CTA
-// barrier, warp 0 pushes the CTA's candidate row (and row j if it owns it)
-// into every CTA, one cluster barrier, every CTA picks the same winner from
-// its own slots, swaps, one CTA barrier, rank-1 update of the active columns.
+// column are conflict-free.
+//
+// Per column j: pivot search in column j, one CTA barrier, every warp pushes
+// the CTA's candidate row (and row j if the CTA owns it) into its share of
+// the CTAs, cluster-barrier ARRIVE; then, while the other CTAs catch up, the
+// rank-1 update of pivot j-1 on columns j+1.. (deferred from the previous
+// column); cluster-barrier WAIT; every CTA picks the same winner from its own
+// slots and brings the pushed rows up to date (they left before pivot j-1's
+// deferred update reached their columns > j: the same fmaf the owner does);
+// swap; one CTA barrier; the update of column j+1 only (the next pivot
+// column).  Multipliers of column j are scaled when column j+1 is searched.
+__device__ __forceinline__ void cluster_arrive() {
+  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() {
+  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 __global__ void __launch_bounds__(SPT)
 spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0, int32_t *info, int kind,
               void *aop, float *aop_lo, int64_t R, int32_t *plan) {
@@ -89,27 +103,34 @@ spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
   const int cr = (int)cluster.block_rank();
   __shared__ SSlot slots[2][SMAXC];
   __shared__ float rowj[2][SNB];
+  __shared__ float piv[2][SNB];   // pivot rows, up to date (piv[par] = column j's)
+  __shared__ float oldj[SNB];     // the old row j, up to date (goes to the pivot's place)
   __shared__ uint64_t wkey[SPT / 32];
   extern __shared__ float sp[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int RP = (int)R + 1;
-  const int64_t r0 = (int64_t)cr * R;
-  const int64_t r1 = imin(mp, r0 + R);
-  const int64_t nr = r1 > r0 ? r1 - r0 : 0;
+  const int r0 = (int)(cr * R);
+  const int r1 = (int)imin(mp, r0 + R);
+  const int nr = r1 > r0 ? r1 - r0 : 0;
 
-  for (int64_t e = tid; e < nr * jb; e += SPT) {
-    const int64_t il = e % nr;
+  for (int64_t e = tid; e < (int64_t)nr * jb; e += SPT) {
+    const int il = (int)(e % nr);
     const int c = (int)(e / nr);
     sp[c * RP + il] = W[(r0 + il) + c * ldw];
   }
   __syncthreads();
+  cluster.sync();  // every CTA of the cluster is running before the first push
 
+  float inv = 0.f;  // 1 / pivot of the previous column
   for (int j = 0; j < jb; ++j) {
     const int par = j & 1;
-    // -- pivot candidate of this CTA: key = (|v| bits, ~row), max wins, ties -> lowest row
+    const float *pprev = piv[par ^ 1];
+    // -- the multipliers of column j-1, then this CTA's pivot candidate in
+    // column j: key = (|v| bits, ~row), max wins, ties -> lowest row
     uint64_t best = 0;
-    for (int64_t il = tid; il < nr; il += SPT) {
-      const int64_t g = r0 + il;
+    for (int il = tid; il < nr; il += SPT) {
+      const int g = r0 + il;
+      if (j > 0 && g >= j) sp[(j - 1) * RP + il] *= inv;
       if (g < j) continue;
       const float v = fabsf(sp[j * RP + il]);
       const uint32_t bits = (v == v) ? __float_as_uint(v) : 0u;
@@ -126,9 +147,9 @@ spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
       uint64_t ck = 0;
 #pragma unroll
       for (int w = 0; w < SPT / 32; ++w) ck = wkey[w] > ck ? wkey[w] : ck;
-      const int gl = ck ? (int)(0xFFFFFFFFu - (uint32_t)ck) - (int)r0 : -1;  // local row of the candidate
+      const int gl = ck ? (int)(0xFFFFFFFFu - (uint32_t)ck) - r0 : -1;  // local row of the candidate
       const bool own_j = j >= r0 && j < r1;
-      const int jl = (int)(j - r0);
+      const int jl = j - r0;
       float c0 = 0.f, c1 = 0.f, j0v = 0.f, j1v = 0.f;
       if (gl >= 0) {
         c0 = lane < jb ? sp[lane * RP + gl] : 0.f;
@@ -153,7 +174,37 @@ spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
         }
       }
     }
-    cluster.sync();
+    __syncthreads();  // the rows are read before the deferred update changes them
+    cluster_arrive();
+    // -- the deferred rank-1 update of pivot j-1 on columns j+1..jb-1, rows >= j:
+    // lanes walk rows, warps take every 8th column; the pivot-row values sit
+    // in registers, so a thread's 8 loads are all in flight together
+    if (j > 0 && j + 1 < jb) {
+      float pr[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int c = j + 1 + warp + 8 * q;
+        pr[q] = c < jb ? pprev[c] : 0.f;
+      }
+      const int ib = j > r0 ? j - r0 : 0;
+      for (int il = ib + lane; il < nr; il += 32) {
+        const float l = sp[(j - 1) * RP + il];
+        float v[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int c = j + 1 + warp + 8 * q;
+          v[q] = c < jb ? sp[c * RP + il] : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = fmaf(-l, pr[q], v[q]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int c = j + 1 + warp + 8 * q;
+          if (c < jb) sp[c * RP + il] = v[q];
+        }
+      }
+    }
+    cluster_wait();
     // -- the winner, identical in every CTA: lane s reads slot s, warp max
     uint64_t wk = 0;
     {
@@ -169,36 +220,51 @@ spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
       const unsigned m = __ballot_sync(0xffffffffu, k == wk && lane < C);
       ws = m ? __ffs(m) - 1 : 0;
     }
-    const int64_t jp = wk ? (int64_t)(0xFFFFFFFFu - (uint32_t)wk) : (int64_t)j;
-    const float *prow = wk ? slots[par][ws].v : rowj[par];
-    const float pv = prow[j];
-    if (cr == 0 && tid == 0) ipiv[j] = col0 + (int32_t)jp + 1;
-    float inv = 1.0f / pv;
+    const int jp = wk ? (int)(0xFFFFFFFFu - (uint32_t)wk) : j;
+    const float *raw = wk ? slots[par][ws].v : rowj[par];
+    float *pcur = piv[par];
+    // the pushed rows, brought up to date: columns > j still lack pivot j-1
+    if (tid < jb) {
+      float pv_ = raw[tid], ov = rowj[par][tid];
+      if (j > 0 && tid > j) {
+        pv_ = fmaf(-raw[j - 1], pprev[tid], pv_);
+        ov = fmaf(-rowj[par][j - 1], pprev[tid], ov);
+      }
+      pcur[tid] = pv_;
+      oldj[tid] = ov;
+    }
+    __syncthreads();
+    const float pv = pcur[j];
+    if (cr == 0 && tid == 0) ipiv[j] = col0 + jp + 1;
+    inv = 1.0f / pv;
     if (pv == 0.0f) {
       inv = 0.0f;
       if (cr == 0 && tid == 0) atomicCAS(info, 0, col0 + j + 1);
     }
     if (jp != j && tid < jb) {
-      if (j >= r0 && j < r1) sp[tid * RP + (j - r0)] = prow[tid];
-      if (jp >= r0 && jp < r1) sp[tid * RP + (jp - r0)] = rowj[par][tid];
+      if (j >= r0 && j < r1) sp[tid * RP + (j - r0)] = pcur[tid];
+      if (jp >= r0 && jp < r1) sp[tid * RP + (jp - r0)] = oldj[tid];
     }
     __syncthreads();
-    for (int il = tid; il < (int)nr; il += SPT) {
-      if (r0 + il <= j) continue;
-      float *col = sp + j * RP + il;
-      const float l = *col * inv;
-      *col = l;
-      for (int c = j + 1; c < jb; ++c) {
-        col += RP;
-        *col = fmaf(-l, prow[c], *col);
+    // -- the next pivot column now (the rest of this update is deferred);
+    // same row-to-thread map as the search, so no barrier before it
+    if (j + 1 < jb) {
+      const float pj1 = pcur[j + 1];
+      for (int il = tid; il < nr; il += SPT) {
+        if (r0 + il <= j) continue;
+        float *x = sp + (j + 1) * RP + il;
+        *x = fmaf(-(sp[j * RP + il] * inv), pj1, *x);
       }
     }
   }
+  // the last column's multipliers
+  for (int il = tid; il < nr; il += SPT)
+    if (r0 + il >= jb) sp[(jb - 1) * RP + il] *= inv;
   __syncthreads();
 
   // -- write back the panel and the update's A operand (rows below the panel)
-  for (int64_t e = tid; e < nr * jb; e += SPT) {
-    const int64_t il = e % nr;
+  for (int64_t e = tid; e < (int64_t)nr * jb; e += SPT) {
+    const int il = (int)(e % nr);
     const int c = (int)(e / nr);
     W[(r0 + il) + c * ldw] = sp[c * RP + il];
   }
@@ -216,8 +282,8 @@ spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
     if (lane == 0) plan[0] = cnt;
   }
   if (aop != nullptr) {
-    for (int64_t il = tid; il < nr; il += SPT) {
-      const int64_t g = r0 + il;
+    for (int il = tid; il < nr; il += SPT) {
+      const int g = r0 + il;
       if (g < jb) continue;
       float v[SNB];
 #pragma unroll
