@@ -36,6 +36,7 @@ SIGNATURES = {
     "bola_dgemm": (_int, [_c, _c, _i64, _i64, _i64, _d, _p, _i64, _p, _i64, _d, _p, _i64, _p]),
     "bola_dgemm_noalloc": (_int, [_c, _c, _i64, _i64, _i64, _d, _p, _i64, _p, _i64, _d, _p, _i64, _p]),
     "bola_sgemm_tc_update": (_int, [_int, _i64, _i64, _p, _p, _p, _p, _p, _i64, _p, _p]),
+    "bola_dgemm_oz_update": (_int, [_i64, _i64, _p, _p, _p, _i64, _p, _p]),
     "bola_dtrsm": (_int, [_c, _c, _c, _c, _i64, _i64, _d, _p, _i64, _p, _i64, _p]),
     "bola_dsyrk": (_int, [_c, _c, _i64, _i64, _d, _p, _i64, _d, _p, _i64, _p]),
     "bola_dgetrf": (_int, [_i64, _i64, _p, _i64, _p, _p, _p]),

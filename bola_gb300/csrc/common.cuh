@@ -102,6 +102,10 @@ int potrf2_rec(cudaStream_t s, char uplo, int64_t n, double *A, int64_t lda, int
 // Adds `add` to ipiv[0..count) unless *info != 0.
 int ipiv_add(cudaStream_t s, int32_t *ipiv, int64_t count, int32_t add, const int32_t *info);
 
+// Fused multiply-add of the operands' own precision (templated kernels).
+__device__ __forceinline__ float fmaT(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fmaT(double a, double b, double c) { return fma(a, b, c); }
+
 // Batched small-system solver pieces (batched.cu): the work items of a batch
 // (flat int32 records, *nitems of them; group = the 8 per-bucket group sizes
 // used) and one persistent launch over items already on the device.

@@ -50,12 +50,14 @@ __global__ void colblock_scale(int64_t n, const double *__restrict__ A, int64_t 
   }
 }
 
-__global__ void to_fp32_scaled(int64_t n, const double *__restrict__ A, int64_t lda, const double *scale,
-                               float *__restrict__ W, int64_t ldw) {
+// W = A S rounded to T (exact for T = double: S is a power of two per block).
+template <typename T>
+__global__ void convert_scaled(int64_t n, const double *__restrict__ A, int64_t lda, const double *scale,
+                               T *__restrict__ W, int64_t ldw) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n * n) return;
   const int64_t i = e % n, j = e / n;
-  W[i + j * ldw] = (float)(A[i + j * lda] * scale[j / TB]);
+  W[i + j * ldw] = (T)(A[i + j * lda] * scale[j / TB]);
 }
 
 // ||A||_inf: one thread per row, columns walked in order (coalesced across threads).
@@ -69,7 +71,8 @@ __global__ void row_abs_sums(int64_t n, const double *__restrict__ A, int64_t ld
 
 // max|u_ii| and min|u_ii| of the low-precision U (one CTA): a cheap lower
 // bound on the conditioning the refinement will face.
-__global__ void diag_extent(int64_t n, const float *__restrict__ W, int64_t ldw, double *out) {
+template <typename T>
+__global__ void diag_extent(int64_t n, const T *__restrict__ W, int64_t ldw, double *out) {
   __shared__ double mx[32], mn[32];
   double a = 0.0, b = INFINITY;
   for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
@@ -148,17 +151,19 @@ __global__ void max_of(int64_t n, const double *v, double *out) {
 }
 
 // y[i, c] = fl32(r[perm[i], c] / rscale[c])
+template <typename T>
 __global__ void permute_scale_down(int64_t n, int nrhs, const double *__restrict__ r, int64_t ldr,
-                                   const int32_t *perm, const double *rscale, float *__restrict__ y) {
+                                   const int32_t *perm, const double *rscale, T *__restrict__ y) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n * nrhs) return;
   const int64_t i = e % n, c = e / n;
   const double s = rscale[c];
-  y[i + c * n] = s > 0.0 ? (float)(r[perm[i] + c * ldr] / s) : 0.f;
+  y[i + c * n] = s > 0.0 ? (T)(r[perm[i] + c * ldr] / s) : T(0);
 }
 
 // x[i, c] += S_i * rscale[c] * y[i, c]   (or x = ... when assign)
-__global__ void update_x(int64_t n, int nrhs, const float *__restrict__ y, const double *scale, const double *rscale,
+template <typename T>
+__global__ void update_x(int64_t n, int nrhs, const T *__restrict__ y, const double *scale, const double *rscale,
                          double *__restrict__ x, int64_t ldx, int assign) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n * nrhs) return;
@@ -179,38 +184,39 @@ __global__ void copy_cols(int64_t n, int nrhs, const double *__restrict__ src, i
 // Inverses of the 64x64 diagonal blocks of L (unit lower) and U, once per
 // factorisation: block b -> Dl[b], Du[b] (column-major 64x64).  A thread per
 // column of the inverse, substitution down (L) or up (U) the block.
+template <typename T>
 __global__ void __launch_bounds__(64)
-diag_block_inverses(int64_t n, const float *__restrict__ W, int64_t ldw, float *Dl, float *Du) {
-  __shared__ float B[TB][TB + 1];
+diag_block_inverses(int64_t n, const T *__restrict__ W, int64_t ldw, T *Dl, T *Du) {
+  __shared__ T B[TB][TB + 1];
   const int64_t k0 = (int64_t)blockIdx.x * TB;
   const int kb = (int)imin(TB, n - k0);
   // the whole tile is written: the substitutions below multiply entries
   // outside the kb x kb block by zeros, and 0 * (stale NaN) would be NaN
   for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
     const int r = e % TB, c = e / TB;
-    B[r][c] = (r < kb && c < kb) ? W[(k0 + r) + (k0 + c) * ldw] : 0.f;
+    B[r][c] = (r < kb && c < kb) ? W[(k0 + r) + (k0 + c) * ldw] : T(0);
   }
   __syncthreads();
   const int j = threadIdx.x;
-  float *L = Dl + (int64_t)blockIdx.x * TB * TB, *U = Du + (int64_t)blockIdx.x * TB * TB;
+  T *L = Dl + (int64_t)blockIdx.x * TB * TB, *U = Du + (int64_t)blockIdx.x * TB * TB;
   if (j >= TB) return;
-  float x[TB];
+  T x[TB];
 #pragma unroll
   for (int i = 0; i < TB; ++i) {  // L x = e_j (unit diagonal)
-    float t = (i == j) ? 1.f : 0.f;
+    T t = (i == j) ? T(1) : T(0);
 #pragma unroll
-    for (int k = 0; k < i; ++k) t = fmaf(-B[i][k], x[k], t);
-    x[i] = (i < kb) ? t : 0.f;
+    for (int k = 0; k < i; ++k) t = fmaT(-B[i][k], x[k], t);
+    x[i] = (i < kb) ? t : T(0);
   }
 #pragma unroll
-  for (int i = 0; i < TB; ++i) L[i + j * TB] = (j < kb) ? x[i] : 0.f;
+  for (int i = 0; i < TB; ++i) L[i + j * TB] = (j < kb) ? x[i] : T(0);
 #pragma unroll
   for (int ii = 0; ii < TB; ++ii) {  // U x = e_j
     const int i = TB - 1 - ii;
-    float t = (i == j) ? 1.f : 0.f;
+    T t = (i == j) ? T(1) : T(0);
 #pragma unroll
-    for (int k = i + 1; k < TB; ++k) t = fmaf(-B[i][k], x[k], t);
-    x[i] = (i < kb && j < kb) ? t / B[i][i] : 0.f;
+    for (int k = i + 1; k < TB; ++k) t = fmaT(-B[i][k], x[k], t);
+    x[i] = (i < kb && j < kb) ? t / B[i][i] : T(0);
   }
 #pragma unroll
   for (int i = 0; i < TB; ++i) U[i + j * TB] = x[i];
@@ -328,14 +334,91 @@ trsv_dataflow(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, con
   if (tid == 0) st_release(flags + b, epoch);
 }
 
-// Sequencing state of the dataflow solves: flags (one per 64-row block,
-// zeroed once), the ticket, the wait-expiry flag and the launch epoch.
+// The FP64 form of the same dataflow, for the FP64-storage factor.  GB300's
+// FP64 pipe retires about two FMAs per clock per SM, so one CTA per block
+// would make each block's work a long serial chain; here a CTA of 64
+// threads owns one (block, right-hand side) pair: thread r keeps row r's
+// accumulator, prefetches its row of each L (U) tile before waiting for the
+// tile's solved block, and the 64 x 64 diagonal inverse finishes the block.
+// Flags are per (block, right-hand side); tickets run block-major, so a CTA
+// again only waits for CTAs that started before it.
+template <bool LOWER>
+__global__ void __launch_bounds__(64)
+trsv_dataflow64(int64_t n, int nrhs, const double *__restrict__ W, int64_t ldw, const double *__restrict__ Dinv,
+                const double *__restrict__ y, double *out, int32_t *flags, int32_t *ticket, int32_t epoch,
+                int32_t *err) {
+  __shared__ double xs[TB];
+  __shared__ int sb;
+  const int r = threadIdx.x;
+  const int nb = (int)((n + TB - 1) / TB);
+  if (r == 0) sb = atomicAdd(ticket, 1);
+  __syncthreads();
+  const int sidx = sb / nrhs, c = sb % nrhs;  // position in solve order, right-hand side
+  const int b = LOWER ? sidx : nb - 1 - sidx;
+  const int64_t i0 = (int64_t)b * TB;
+  const int kb = (int)imin(TB, n - i0);
+  double acc = r < kb ? y[i0 + r + (int64_t)c * n] : 0.0;
+  for (int q = 0; q < sidx; ++q) {
+    const int k = LOWER ? q : nb - 1 - q;
+    const int64_t k0 = (int64_t)k * TB;
+    const int kbk = (int)imin(TB, n - k0);
+    double lv[TB];
+    const double *Lr = W + (i0 + (r < kb ? r : 0)) + k0 * ldw;
+#pragma unroll
+    for (int kk = 0; kk < TB; ++kk) lv[kk] = (r < kb && kk < kbk) ? Lr[(int64_t)kk * ldw] : 0.0;
+    if (r == 0) {
+      int polls = 0;
+      while (ld_acquire(flags + (int64_t)k * MAXRHS + c) != epoch) {
+        if (++polls > (1 << 21)) {
+          atomicExch(err, 3);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __syncthreads();
+    xs[r] = r < kbk ? __ldcg(out + k0 + r + (int64_t)c * n) : 0.0;
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < TB; ++kk) acc = fma(-lv[kk], xs[kk], acc);
+    __syncthreads();
+  }
+  xs[r] = acc;
+  __syncthreads();
+  const double *D = Dinv + (int64_t)b * TB * TB;
+  double v = 0.0;
+#pragma unroll 8
+  for (int kk = 0; kk < TB; ++kk) v = fma(D[r + kk * TB], xs[kk], v);
+  if (r < kb) out[i0 + r + (int64_t)c * n] = v;
+  __threadfence();
+  __syncthreads();
+  if (r == 0) st_release(flags + (int64_t)b * MAXRHS + c, epoch);
+}
+
+// Sequencing state of the dataflow solves: flags (one per 64-row block and
+// right-hand side, zeroed once), the ticket, the wait-expiry flag and the
+// launch epoch.
 struct TrsvSync {
   int32_t *flags = nullptr, *ticket = nullptr, *err = nullptr;
   int32_t epoch = 0;
 };
 
 // y (right-hand sides) -> out (solution); y is not modified.
+int trsv(cudaStream_t s, bool lower, int64_t n, int nrhs, const float *W, int64_t ldw, const float *Dinv,
+         const float *y, float *out, TrsvSync &sync);
+int trsv(cudaStream_t s, bool lower, int64_t n, int nrhs, const double *W, int64_t ldw, const double *Dinv,
+         const double *y, double *out, TrsvSync &sync) {
+  ProfScope prof(s, lower ? "trsv64_lower" : "trsv64_upper", (double)n * n * nrhs, 8.0 * (double)n * n / 2, 1);
+  const unsigned grid = (unsigned)(cdiv(n, TB) * nrhs);
+  const int32_t epoch = ++sync.epoch;
+  BOLA_TRY_CUDA(cudaMemsetAsync(sync.ticket, 0, sizeof(int32_t), s));
+  if (lower)
+    trsv_dataflow64<true><<<grid, TB, 0, s>>>(n, nrhs, W, ldw, Dinv, y, out, sync.flags, sync.ticket, epoch, sync.err);
+  else
+    trsv_dataflow64<false><<<grid, TB, 0, s>>>(n, nrhs, W, ldw, Dinv, y, out, sync.flags, sync.ticket, epoch, sync.err);
+  BOLA_CHECK_LAUNCH();
+  return 0;
+}
 int trsv(cudaStream_t s, bool lower, int64_t n, int nrhs, const float *W, int64_t ldw, const float *Dinv,
          const float *y, float *out, TrsvSync &sync) {
   ProfScope prof(s, lower ? "trsv_lower" : "trsv_upper", (double)n * n * nrhs, 4.0 * (double)n * n / 2, 1);
@@ -426,7 +509,11 @@ __global__ void gm_add_zy(int64_t n, int nrhs, int kk, const double *__restrict_
 // Device workspace of one mixed solve, cached per device and grown on demand.
 struct Workspace {
   int64_t n = 0, nrhs = 0, bytes = 0;
-  float *W = nullptr, *y = nullptr, *z = nullptr, *Dl = nullptr, *Du = nullptr;
+  int fkind = 2;        // factor kind of the current solve (3: FP64 W, y, z, Dl, Du)
+  int64_t ldW = 0;      // leading dimension of W (FP64: padded to 32 for the TMA tiles)
+  size_t wbytes = 0;    // bytes held by W
+  void *W = nullptr;    // the working matrix, then its LU factors (FP32, or FP64 for kind 3)
+  void *y = nullptr, *z = nullptr, *Dl = nullptr, *Du = nullptr;  // 8-byte elements, used as FP32 or FP64
   double *scale = nullptr, *r = nullptr, *d = nullptr, *norms = nullptr, *rowsum = nullptr;
   double *V = nullptr, *Z = nullptr, *H = nullptr;  // GMRES basis, preconditioned basis, Hessenberg column
   double *hn = nullptr;                              // per-column 2-norms (GMRES)
@@ -443,6 +530,7 @@ void ws_free(Workspace &w) {
   w.ts.flags = w.ts.ticket = w.ts.err = nullptr;
   w.lu.release(nullptr);
   w.W = w.y = w.z = w.Dl = w.Du = nullptr;
+  w.wbytes = 0;
   w.scale = w.r = w.d = w.norms = w.rowsum = w.V = w.Z = w.H = w.hn = nullptr;
   w.ipiv = w.perm = w.info = nullptr;
   w.n = w.nrhs = w.bytes = 0;
@@ -463,11 +551,12 @@ int ws_reserve(Workspace &w, int64_t n, int64_t nrhs, int kind, cudaStream_t s) 
       bytes += (int64_t)sz;
       return cudaMalloc(reinterpret_cast<void **>(p), sz) == cudaSuccess ? 0 : fail(BOLA_ERR_CUDA, "mixed: out of memory");
     };
-    BOLA_TRY(alloc(&w.W, sizeof(float) * n * n));
-    BOLA_TRY(alloc(&w.y, sizeof(float) * n * nrhs));
-    BOLA_TRY(alloc(&w.z, sizeof(float) * n * nrhs));
-    BOLA_TRY(alloc(&w.Dl, sizeof(float) * cdiv(n, TB) * TB * TB));
-    BOLA_TRY(alloc(&w.Du, sizeof(float) * cdiv(n, TB) * TB * TB));
+    w.wbytes = (size_t)(kind == 3 ? cdiv(n, 32) * 32 : n) * n * (kind == 3 ? 8 : 4);
+    BOLA_TRY(alloc(&w.W, w.wbytes));
+    BOLA_TRY(alloc(&w.y, sizeof(double) * n * nrhs));
+    BOLA_TRY(alloc(&w.z, sizeof(double) * n * nrhs));
+    BOLA_TRY(alloc(&w.Dl, sizeof(double) * cdiv(n, TB) * TB * TB));
+    BOLA_TRY(alloc(&w.Du, sizeof(double) * cdiv(n, TB) * TB * TB));
     BOLA_TRY(alloc(&w.scale, sizeof(double) * cdiv(n, TB)));
     BOLA_TRY(alloc(&w.r, sizeof(double) * n * nrhs));
     BOLA_TRY(alloc(&w.d, sizeof(double) * n * nrhs));
@@ -480,15 +569,26 @@ int ws_reserve(Workspace &w, int64_t n, int64_t nrhs, int kind, cudaStream_t s) 
     BOLA_TRY(alloc(&w.Z, sizeof(double) * GM_M * nrhs * n));
     BOLA_TRY(alloc(&w.H, sizeof(double) * (GM_M + 2) * MAXRHS * 2));
     BOLA_TRY(alloc(&w.hn, sizeof(double) * MAXRHS));
-    BOLA_TRY(alloc(&w.ts.flags, sizeof(int32_t) * cdiv(n, TB)));
+    BOLA_TRY(alloc(&w.ts.flags, sizeof(int32_t) * cdiv(n, TB) * MAXRHS));
     BOLA_TRY(alloc(&w.ts.ticket, sizeof(int32_t) * 2));
     w.ts.err = w.ts.ticket + 1;
-    BOLA_TRY_CUDA(cudaMemset(w.ts.flags, 0, sizeof(int32_t) * cdiv(n, TB)));
+    BOLA_TRY_CUDA(cudaMemset(w.ts.flags, 0, sizeof(int32_t) * cdiv(n, TB) * MAXRHS));
     BOLA_TRY_CUDA(cudaMemset(w.ts.ticket, 0, sizeof(int32_t) * 2));
     w.ts.epoch = 0;
     w.n = n;
     w.nrhs = nrhs;
     w.bytes = bytes + (int64_t)n * 64 * 4 * 4;  // plus the update operands of the LU
+  }
+  const size_t wneed = (size_t)(kind == 3 ? cdiv(n_req, 32) * 32 : n_req) * n_req * (kind == 3 ? 8 : 4);
+  if (w.wbytes < wneed) {  // an FP64 factor in a workspace sized for FP32 ones
+    cudaStreamSynchronize(s);
+    cudaFree(w.W);
+    w.W = nullptr;
+    w.bytes -= (int64_t)w.wbytes;
+    w.wbytes = 0;
+    if (cudaMalloc(&w.W, wneed) != cudaSuccess) return fail(BOLA_ERR_CUDA, "mixed: out of memory");
+    w.wbytes = wneed;
+    w.bytes += (int64_t)wneed;
   }
   return w.lu.reserve(n_req, kind, s);
 }
@@ -500,11 +600,23 @@ Workspace g_ws[64];
 int correction(cudaStream_t s, Workspace &w, int64_t n, int nrhs, const double *r, int64_t ldr, const double *rs,
                double *x, int64_t ldx, bool assign) {
   const unsigned g = (unsigned)cdiv(n * nrhs, 256);
-  permute_scale_down<<<g, 256, 0, s>>>(n, nrhs, r, ldr, w.perm, rs, w.y);
-  BOLA_CHECK_LAUNCH();
-  BOLA_TRY(trsv(s, true, n, nrhs, w.W, n, w.Dl, w.y, w.z, w.ts));
-  BOLA_TRY(trsv(s, false, n, nrhs, w.W, n, w.Du, w.z, w.y, w.ts));
-  update_x<<<g, 256, 0, s>>>(n, nrhs, w.y, w.scale, rs, x, ldx, assign ? 1 : 0);
+  if (w.fkind == 3) {
+    double *y = static_cast<double *>(w.y), *z = static_cast<double *>(w.z);
+    const double *W = static_cast<const double *>(w.W);
+    permute_scale_down<double><<<g, 256, 0, s>>>(n, nrhs, r, ldr, w.perm, rs, y);
+    BOLA_CHECK_LAUNCH();
+    BOLA_TRY(trsv(s, true, n, nrhs, W, w.ldW, static_cast<const double *>(w.Dl), y, z, w.ts));
+    BOLA_TRY(trsv(s, false, n, nrhs, W, w.ldW, static_cast<const double *>(w.Du), z, y, w.ts));
+    update_x<double><<<g, 256, 0, s>>>(n, nrhs, y, w.scale, rs, x, ldx, assign ? 1 : 0);
+  } else {
+    float *y = static_cast<float *>(w.y), *z = static_cast<float *>(w.z);
+    const float *W = static_cast<const float *>(w.W);
+    permute_scale_down<float><<<g, 256, 0, s>>>(n, nrhs, r, ldr, w.perm, rs, y);
+    BOLA_CHECK_LAUNCH();
+    BOLA_TRY(trsv(s, true, n, nrhs, W, n, static_cast<const float *>(w.Dl), y, z, w.ts));
+    BOLA_TRY(trsv(s, false, n, nrhs, W, n, static_cast<const float *>(w.Du), z, y, w.ts));
+    update_x<float><<<g, 256, 0, s>>>(n, nrhs, y, w.scale, rs, x, ldx, assign ? 1 : 0);
+  }
   BOLA_CHECK_LAUNCH();
   return 0;
 }
@@ -690,7 +802,7 @@ int dgesv_mixed_ws(Workspace &w, int64_t n, int64_t nrhs, const double *a, int64
   if (ldx < imax(1, n)) return -8;
   bola_mixed_opts o = {2, 30, 1e-14, 1, 1};
   if (opts) o = *opts;
-  if (o.factor_kind < 0 || o.factor_kind > 2) return -9;
+  if (o.factor_kind < 0 || o.factor_kind > 3) return -9;
   bola_mixed_info info_out;
   std::memset(&info_out, 0, sizeof info_out);
   if (n == 0 || nrhs == 0) {
@@ -699,6 +811,10 @@ int dgesv_mixed_ws(Workspace &w, int64_t n, int64_t nrhs, const double *a, int64
   }
   if (n > 8192) return fail(BOLA_ERR_UNSUPPORTED, "bola_dgesv_mixed: n = %lld > 8192", (long long)n);
   BOLA_TRY(ws_reserve(w, n, nrhs, o.factor_kind, s));
+  w.fkind = o.factor_kind;
+  const bool fp64 = o.factor_kind == 3;
+  const int64_t ldW = fp64 ? cdiv(n, 32) * 32 : n;
+  w.ldW = ldW;
   const int nr = (int)nrhs;
   double *nrm = w.norms;  // [0..nr): ||r||, [nr..2nr): ||x||, [2nr..3nr): ||b||, [3nr]: ||A||
 
@@ -706,18 +822,30 @@ int dgesv_mixed_ws(Workspace &w, int64_t n, int64_t nrhs, const double *a, int64
   {
     ProfScope prof(s, "mixed_convert", 0.0, 12.0 * (double)n * n);
     colblock_scale<<<(unsigned)cdiv(n, TB), 512, 0, s>>>(n, a, lda, w.scale);
-    to_fp32_scaled<<<(unsigned)cdiv(n * n, 256), 256, 0, s>>>(n, a, lda, w.scale, w.W, n);
+    if (fp64)
+      convert_scaled<double><<<(unsigned)cdiv(n * n, 256), 256, 0, s>>>(n, a, lda, w.scale, (double *)w.W, ldW);
+    else
+      convert_scaled<float><<<(unsigned)cdiv(n * n, 256), 256, 0, s>>>(n, a, lda, w.scale, (float *)w.W, n);
     row_abs_sums<<<(unsigned)cdiv(n, 128), 128, 0, s>>>(n, a, lda, w.rowsum);
     max_of<<<1, 1024, 0, s>>>(n, w.rowsum, nrm + 3 * nr);
     col_absmax<<<nr, 256, 0, s>>>(n, b, ldb, nrm + 2 * nr);
   }
   BOLA_CHECK_LAUNCH();
-  BOLA_TRY(w.lu.factor(s, w.W, n, w.ipiv, w.info));
+  if (fp64)
+    BOLA_TRY(w.lu.factor64(s, (double *)w.W, ldW, w.ipiv, w.info));
+  else
+    BOLA_TRY(w.lu.factor(s, (float *)w.W, n, w.ipiv, w.info));
   {
     ProfScope prof(s, "mixed_perm");
     compose_perm<<<1, 1024, sizeof(int32_t) * n, s>>>(n, w.ipiv, w.perm);
-    diag_block_inverses<<<(unsigned)cdiv(n, TB), TB, 0, s>>>(n, w.W, n, w.Dl, w.Du);
-    diag_extent<<<1, 1024, 0, s>>>(n, w.W, n, w.norms + 5 * MAXRHS);
+    const unsigned nb = (unsigned)cdiv(n, TB);
+    if (fp64) {
+      diag_block_inverses<double><<<nb, TB, 0, s>>>(n, (const double *)w.W, ldW, (double *)w.Dl, (double *)w.Du);
+      diag_extent<double><<<1, 1024, 0, s>>>(n, (const double *)w.W, ldW, w.norms + 5 * MAXRHS);
+    } else {
+      diag_block_inverses<float><<<nb, TB, 0, s>>>(n, (const float *)w.W, n, (float *)w.Dl, (float *)w.Du);
+      diag_extent<float><<<1, 1024, 0, s>>>(n, (const float *)w.W, n, w.norms + 5 * MAXRHS);
+    }
   }
   BOLA_CHECK_LAUNCH();
   double ext[2] = {0.0, 0.0};
@@ -740,8 +868,9 @@ int dgesv_mixed_ws(Workspace &w, int64_t n, int64_t nrhs, const double *a, int64
   // n = 1024 and 4096 systems with geometric spectra and kappa 1e2/1e6/1e10:
   // bf16 55 | 560, tf32 93 | 1.3e4, 3xTF32 3.6e3 | 5.5e5.  A wrong call costs
   // time only: the refinement attempt before the fallback, or an FP64 solve
-  // where the mixed one would have done.
-  const double limit = o.factor_kind == 0 ? 175.0 : o.factor_kind == 1 ? 1100.0 : 4.5e4;
+  // where the mixed one would have done.  The FP64-accurate factor (kind 3)
+  // refines anything its pivots leave below ~1e13.
+  const double limit = o.factor_kind == 0 ? 175.0 : o.factor_kind == 1 ? 1100.0 : o.factor_kind == 2 ? 4.5e4 : 1e13;
   const double spread = ext[1] > 0.0 ? ext[0] / ext[1] : INFINITY;
   info_out.condition_estimate = spread;
   const bool hopeless = o.fallback_fp64 && !(spread < limit);

@@ -17,6 +17,8 @@
 #include <cooperative_groups.h>
 #include <cuda_bf16.h>
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "mixed.cuh"
 
@@ -29,10 +31,37 @@ constexpr int SNB = 64;   // panel width and update depth
 constexpr int SPT = 256;  // threads per panel CTA
 constexpr int SMAXC = 16;
 
+template <typename T>
 struct SSlot {
-  uint32_t khi, klo;  // |pivot candidate| bits, ~row
-  float v[SNB];       // the candidate row
+  uint32_t k0, k1, k2, pad;  // pivot key (see PKey)
+  T v[SNB];                  // the candidate row
 };
+
+// Pivot key, compared lexicographically: the bits of |v| (high word, low
+// word; the low word is 0 for FP32) and ~row, so the largest magnitude wins
+// and ties go to the lowest row; a NaN never wins.
+struct PKey {
+  uint32_t a, b, c;
+};
+__device__ __forceinline__ bool pk_less(const PKey &x, const PKey &y) {
+  return x.a != y.a ? x.a < y.a : (x.b != y.b ? x.b < y.b : x.c < y.c);
+}
+__device__ __forceinline__ PKey pk_make(float v, int g) {
+  v = fabsf(v);
+  return PKey{v == v ? __float_as_uint(v) : 0u, 0u, 0xFFFFFFFFu - (uint32_t)g};
+}
+__device__ __forceinline__ PKey pk_make(double v, int g) {
+  v = fabs(v);
+  const uint64_t u = v == v ? (uint64_t)__double_as_longlong(v) : 0ull;
+  return PKey{(uint32_t)(u >> 32), (uint32_t)u, 0xFFFFFFFFu - (uint32_t)g};
+}
+__device__ __forceinline__ PKey pk_warp_max(const PKey &k) {
+  const uint32_t a = __reduce_max_sync(0xffffffffu, k.a);
+  const uint32_t b = __reduce_max_sync(0xffffffffu, k.a == a ? k.b : 0u);
+  const uint32_t c = __reduce_max_sync(0xffffffffu, (k.a == a && k.b == b) ? k.c : 0u);
+  return PKey{a, b, c};
+}
+
 
 __device__ __forceinline__ float tf32_round(float x) {
   uint32_t u = __float_as_uint(x);
@@ -95,80 +124,83 @@ __device__ __forceinline__ void cluster_wait() {
   asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
+template <typename T>
 __global__ void __launch_bounds__(SPT)
-spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0, int32_t *info, int kind,
-              void *aop, float *aop_lo, int64_t R, int32_t *plan) {
+spanel_kernel(T *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0, int32_t *info, int kind,
+              void *aop, float *aop_lo, int32_t *aexp, int64_t cap, int64_t R, int32_t *plan) {
   cg::cluster_group cluster = cg::this_cluster();
   const int C = (int)cluster.num_blocks();
   const int cr = (int)cluster.block_rank();
-  __shared__ SSlot slots[2][SMAXC];
-  __shared__ float rowj[2][SNB];
-  __shared__ float piv[2][SNB];   // pivot rows, up to date (piv[par] = column j's)
-  __shared__ float oldj[SNB];     // the old row j, up to date (goes to the pivot's place)
-  __shared__ uint64_t wkey[SPT / 32];
-  extern __shared__ float sp[];
+  __shared__ SSlot<T> slots[2][SMAXC];
+  __shared__ T rowj[2][SNB];
+  __shared__ T piv[2][SNB];   // pivot rows, up to date (piv[par] = column j's)
+  __shared__ T oldj[SNB];     // the old row j, up to date (goes to the pivot's place)
+  __shared__ PKey wkey[SPT / 32];
+  extern __shared__ __align__(16) unsigned char sp_raw[];
+  T *sp = reinterpret_cast<T *>(sp_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int RP = (int)R + 1;
   const int r0 = (int)(cr * R);
   const int r1 = (int)imin(mp, r0 + R);
   const int nr = r1 > r0 ? r1 - r0 : 0;
+  // element (row il, column c) of this CTA's rows, in shared memory
+  auto PE = [&](int c, int il) -> T & { return sp[c * RP + il]; };
+  const int ns = nr;
 
-  for (int64_t e = tid; e < (int64_t)nr * jb; e += SPT) {
-    const int il = (int)(e % nr);
-    const int c = (int)(e / nr);
+  for (int64_t e = tid; e < (int64_t)ns * jb; e += SPT) {
+    const int il = (int)(e % ns);
+    const int c = (int)(e / ns);
     sp[c * RP + il] = W[(r0 + il) + c * ldw];
   }
   __syncthreads();
   cluster.sync();  // every CTA of the cluster is running before the first push
 
-  float inv = 0.f;  // 1 / pivot of the previous column
+  T inv = T(0);  // 1 / pivot of the previous column
   for (int j = 0; j < jb; ++j) {
     const int par = j & 1;
-    const float *pprev = piv[par ^ 1];
+    const T *pprev = piv[par ^ 1];
     // -- the multipliers of column j-1, then this CTA's pivot candidate in
     // column j: key = (|v| bits, ~row), max wins, ties -> lowest row
-    uint64_t best = 0;
+    PKey best = PKey{0u, 0u, 0u};
     for (int il = tid; il < nr; il += SPT) {
       const int g = r0 + il;
-      if (j > 0 && g >= j) sp[(j - 1) * RP + il] *= inv;
+      if (j > 0 && g >= j) PE(j - 1, il) *= inv;
       if (g < j) continue;
-      const float v = fabsf(sp[j * RP + il]);
-      const uint32_t bits = (v == v) ? __float_as_uint(v) : 0u;
-      const uint64_t key = ((uint64_t)bits << 32) | (0xFFFFFFFFu - (uint32_t)g);
-      best = key > best ? key : best;
+      const PKey k = pk_make(PE(j, il), g);
+      if (pk_less(best, k)) best = k;
     }
-    const uint32_t hi = (uint32_t)(best >> 32), lo = (uint32_t)best;
-    const uint32_t mhi = __reduce_max_sync(0xffffffffu, hi);
-    const uint32_t mlo = __reduce_max_sync(0xffffffffu, hi == mhi ? lo : 0u);
-    if (lane == 0) wkey[warp] = ((uint64_t)mhi << 32) | mlo;
+    best = pk_warp_max(best);
+    if (lane == 0) wkey[warp] = best;
     __syncthreads();
     // -- every warp pushes the candidate (and row j if owned) to its share of the CTAs
     {
-      uint64_t ck = 0;
+      PKey ck = wkey[0];
 #pragma unroll
-      for (int w = 0; w < SPT / 32; ++w) ck = wkey[w] > ck ? wkey[w] : ck;
-      const int gl = ck ? (int)(0xFFFFFFFFu - (uint32_t)ck) - r0 : -1;  // local row of the candidate
+      for (int w = 1; w < SPT / 32; ++w)
+        if (pk_less(ck, wkey[w])) ck = wkey[w];
+      const int gl = ck.c ? (int)(0xFFFFFFFFu - ck.c) - r0 : -1;  // local row of the candidate
       const bool own_j = j >= r0 && j < r1;
       const int jl = j - r0;
-      float c0 = 0.f, c1 = 0.f, j0v = 0.f, j1v = 0.f;
+      T c0 = T(0), c1 = T(0), j0v = T(0), j1v = T(0);
       if (gl >= 0) {
-        c0 = lane < jb ? sp[lane * RP + gl] : 0.f;
-        c1 = lane + 32 < jb ? sp[(lane + 32) * RP + gl] : 0.f;
+        c0 = lane < jb ? PE(lane, gl) : T(0);
+        c1 = lane + 32 < jb ? PE(lane + 32, gl) : T(0);
       }
       if (own_j) {
-        j0v = lane < jb ? sp[lane * RP + jl] : 0.f;
-        j1v = lane + 32 < jb ? sp[(lane + 32) * RP + jl] : 0.f;
+        j0v = lane < jb ? PE(lane, jl) : T(0);
+        j1v = lane + 32 < jb ? PE(lane + 32, jl) : T(0);
       }
       for (int d = warp; d < C; d += SPT / 32) {
-        SSlot *rs = cluster.map_shared_rank(&slots[par][cr], d);
+        SSlot<T> *rs = cluster.map_shared_rank(&slots[par][cr], d);
         if (lane == 0) {
-          rs->khi = (uint32_t)(ck >> 32);
-          rs->klo = (uint32_t)ck;
+          rs->k0 = ck.a;
+          rs->k1 = ck.b;
+          rs->k2 = ck.c;
         }
         rs->v[lane] = c0;
         rs->v[lane + 32] = c1;
         if (own_j) {
-          float *rj = cluster.map_shared_rank(&rowj[par][0], d);
+          T *rj = cluster.map_shared_rank(&rowj[par][0], d);
           rj[lane] = j0v;
           rj[lane + 32] = j1v;
         }
@@ -180,92 +212,86 @@ spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
     // lanes walk rows, warps take every 8th column; the pivot-row values sit
     // in registers, so a thread's 8 loads are all in flight together
     if (j > 0 && j + 1 < jb) {
-      float pr[8];
+      T pr[8];
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
         const int c = j + 1 + warp + 8 * q;
-        pr[q] = c < jb ? pprev[c] : 0.f;
+        pr[q] = c < jb ? pprev[c] : T(0);
       }
       const int ib = j > r0 ? j - r0 : 0;
       for (int il = ib + lane; il < nr; il += 32) {
-        const float l = sp[(j - 1) * RP + il];
-        float v[8];
+        const T l = PE(j - 1, il);
+        T v[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
           const int c = j + 1 + warp + 8 * q;
-          v[q] = c < jb ? sp[c * RP + il] : 0.f;
+          v[q] = c < jb ? PE(c, il) : T(0);
         }
 #pragma unroll
-        for (int q = 0; q < 8; ++q) v[q] = fmaf(-l, pr[q], v[q]);
+        for (int q = 0; q < 8; ++q) v[q] = fmaT(-l, pr[q], v[q]);
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
           const int c = j + 1 + warp + 8 * q;
-          if (c < jb) sp[c * RP + il] = v[q];
+          if (c < jb) PE(c, il) = v[q];
         }
       }
     }
     cluster_wait();
     // -- the winner, identical in every CTA: lane s reads slot s, warp max
-    uint64_t wk = 0;
-    {
-      const uint64_t k = lane < C ? (((uint64_t)slots[par][lane].khi << 32) | slots[par][lane].klo) : 0ull;
-      const uint32_t khi = (uint32_t)(k >> 32);
-      const uint32_t mh = __reduce_max_sync(0xffffffffu, khi);
-      const uint32_t ml = __reduce_max_sync(0xffffffffu, khi == mh ? (uint32_t)k : 0u);
-      wk = ((uint64_t)mh << 32) | ml;
-    }
+    PKey wk;
     int ws = 0;
     {
-      const uint64_t k = lane < C ? (((uint64_t)slots[par][lane].khi << 32) | slots[par][lane].klo) : 0ull;
-      const unsigned m = __ballot_sync(0xffffffffu, k == wk && lane < C);
+      const PKey k = lane < C ? PKey{slots[par][lane].k0, slots[par][lane].k1, slots[par][lane].k2} : PKey{0u, 0u, 0u};
+      wk = pk_warp_max(k);
+      const unsigned m = __ballot_sync(0xffffffffu, lane < C && k.a == wk.a && k.b == wk.b && k.c == wk.c);
       ws = m ? __ffs(m) - 1 : 0;
     }
-    const int jp = wk ? (int)(0xFFFFFFFFu - (uint32_t)wk) : j;
-    const float *raw = wk ? slots[par][ws].v : rowj[par];
-    float *pcur = piv[par];
+    const int jp = wk.c ? (int)(0xFFFFFFFFu - wk.c) : j;
+    const T *raw = wk.c ? slots[par][ws].v : rowj[par];
+    T *pcur = piv[par];
     // the pushed rows, brought up to date: columns > j still lack pivot j-1
     if (tid < jb) {
-      float pv_ = raw[tid], ov = rowj[par][tid];
+      T pv_ = raw[tid], ov = rowj[par][tid];
       if (j > 0 && tid > j) {
-        pv_ = fmaf(-raw[j - 1], pprev[tid], pv_);
-        ov = fmaf(-rowj[par][j - 1], pprev[tid], ov);
+        pv_ = fmaT(-raw[j - 1], pprev[tid], pv_);
+        ov = fmaT(-rowj[par][j - 1], pprev[tid], ov);
       }
       pcur[tid] = pv_;
       oldj[tid] = ov;
     }
     __syncthreads();
-    const float pv = pcur[j];
+    const T pv = pcur[j];
     if (cr == 0 && tid == 0) ipiv[j] = col0 + jp + 1;
-    inv = 1.0f / pv;
-    if (pv == 0.0f) {
-      inv = 0.0f;
+    inv = T(1) / pv;
+    if (pv == T(0)) {
+      inv = T(0);
       if (cr == 0 && tid == 0) atomicCAS(info, 0, col0 + j + 1);
     }
     if (jp != j && tid < jb) {
-      if (j >= r0 && j < r1) sp[tid * RP + (j - r0)] = pcur[tid];
-      if (jp >= r0 && jp < r1) sp[tid * RP + (jp - r0)] = oldj[tid];
+      if (j >= r0 && j < r1) PE(tid, j - r0) = pcur[tid];
+      if (jp >= r0 && jp < r1) PE(tid, jp - r0) = oldj[tid];
     }
     __syncthreads();
     // -- the next pivot column now (the rest of this update is deferred);
     // same row-to-thread map as the search, so no barrier before it
     if (j + 1 < jb) {
-      const float pj1 = pcur[j + 1];
+      const T pj1 = pcur[j + 1];
       for (int il = tid; il < nr; il += SPT) {
         if (r0 + il <= j) continue;
-        float *x = sp + (j + 1) * RP + il;
-        *x = fmaf(-(sp[j * RP + il] * inv), pj1, *x);
+        T &x = PE(j + 1, il);
+        x = fmaT(-(PE(j, il) * inv), pj1, x);
       }
     }
   }
   // the last column's multipliers
   for (int il = tid; il < nr; il += SPT)
-    if (r0 + il >= jb) sp[(jb - 1) * RP + il] *= inv;
+    if (r0 + il >= jb) PE(jb - 1, il) *= inv;
   __syncthreads();
 
   // -- write back the panel and the update's A operand (rows below the panel)
-  for (int64_t e = tid; e < (int64_t)nr * jb; e += SPT) {
-    const int il = (int)(e % nr);
-    const int c = (int)(e / nr);
+  for (int64_t e = tid; e < (int64_t)ns * jb; e += SPT) {
+    const int il = (int)(e % ns);
+    const int c = (int)(e / ns);
     W[(r0 + il) + c * ldw] = sp[c * RP + il];
   }
   if (plan != nullptr && cr == 0 && warp == 0) {
@@ -285,10 +311,36 @@ spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
     for (int il = tid; il < nr; il += SPT) {
       const int g = r0 + il;
       if (g < jb) continue;
-      float v[SNB];
+      if constexpr (std::is_same<T, float>::value) {
+        float v[SNB];
 #pragma unroll
-      for (int c = 0; c < SNB; ++c) v[c] = c < jb ? sp[c * RP + il] : 0.f;
-      write_operand_row(kind, aop, aop_lo, g - jb, v);
+        for (int c = 0; c < SNB; ++c) v[c] = c < jb ? PE(c, il) : 0.f;
+        write_operand_row(kind, aop, aop_lo, g - jb, v);
+      } else {
+        // exact bf16 slices of the row (FP64 factor): exponent, then 8 K values at a time
+        uint64_t mb = 0;
+        for (int c = 0; c < jb; ++c) {
+          const uint64_t mc = oz_mag((double)PE(c, il));
+          mb = mc > mb ? mc : mb;
+        }
+        const int e = oz_exponent(mb);
+        aexp[g - jb] = e;
+        __nv_bfloat16 *out = static_cast<__nv_bfloat16 *>(aop);
+        for (int c0 = 0; c0 < SNB; c0 += 8) {
+          __align__(16) __nv_bfloat16 q[OZ_SLICES][8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            __nv_bfloat16 t8[OZ_SLICES];
+            oz_slices(c0 + u < jb ? (double)PE(c0 + u, il) : 0.0, e, t8);
+#pragma unroll
+            for (int t = 0; t < OZ_SLICES; ++t) q[t][u] = t8[t];
+          }
+#pragma unroll
+          for (int t = 0; t < OZ_SLICES; ++t)
+            *reinterpret_cast<uint4 *>(out + ((int64_t)t * cap + (g - jb)) * SNB + c0) =
+                *reinterpret_cast<const uint4 *>(q[t]);
+        }
+      }
     }
   }
   cluster.sync();
@@ -296,11 +348,12 @@ spanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
 
 // The panel's interchanges on all other columns, U12 = L11^-1 A12 on the
 // right ones and their K-major B operand.  A warp per column.
+template <typename T>
 __global__ void __launch_bounds__(256)
-sswap_trsm(float *W, int64_t ldw, int64_t n, int64_t j, int jb, const int32_t *plan, int kind, void *bop,
-           float *bop_lo) {
+sswap_trsm(T *W, int64_t ldw, int64_t n, int64_t j, int jb, const int32_t *plan, int kind, void *bop,
+           float *bop_lo, int32_t *bexp, int64_t cap) {
   __shared__ int32_t rows[2 * SNB], src[2 * SNB];
-  __shared__ float L[SNB * SNB];
+  __shared__ T L[SNB * SNB];
   __shared__ int cnt;
   // the interchanges, composed once by the panel kernel
   if (threadIdx.x == 0) cnt = plan[0];
@@ -317,48 +370,54 @@ sswap_trsm(float *W, int64_t ldw, int64_t n, int64_t j, int jb, const int32_t *p
   const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (w >= n - jb) return;
   const int64_t col = w < j ? w : w + jb;
-  float *cp = W + col * ldw;
-  float v[4];
+  T *cp = W + col * ldw;
+  T v[4];
 #pragma unroll
-  for (int e = 0; e < 4; ++e) v[e] = lane + 32 * e < cnt ? cp[src[lane + 32 * e]] : 0.f;
+  for (int e = 0; e < 4; ++e) v[e] = lane + 32 * e < cnt ? cp[src[lane + 32 * e]] : T(0);
   __syncwarp();
 #pragma unroll
   for (int e = 0; e < 4; ++e)
     if (lane + 32 * e < cnt) cp[rows[lane + 32 * e]] = v[e];
   __syncwarp();
   if (col < j + jb) return;
-  float b0 = lane < jb ? cp[j + lane] : 0.f;
-  float b1 = lane + 32 < jb ? cp[j + lane + 32] : 0.f;
+  T b0 = lane < jb ? cp[j + lane] : T(0);
+  T b1 = lane + 32 < jb ? cp[j + lane + 32] : T(0);
   for (int k = 0; k < jb; ++k) {
-    const float bk = __shfl_sync(0xffffffffu, k < 32 ? b0 : b1, k & 31);
-    if (lane > k) b0 = fmaf(-L[lane + k * SNB], bk, b0);
-    if (lane + 32 > k && lane + 32 < jb) b1 = fmaf(-L[lane + 32 + k * SNB], bk, b1);
+    const T bk = __shfl_sync(0xffffffffu, k < 32 ? b0 : b1, k & 31);
+    if (lane > k) b0 = fmaT(-L[lane + k * SNB], bk, b0);
+    if (lane + 32 > k && lane + 32 < jb) b1 = fmaT(-L[lane + 32 + k * SNB], bk, b1);
   }
   if (lane < jb) cp[j + lane] = b0;
   if (lane + 32 < jb) cp[j + lane + 32] = b1;
   if (bop != nullptr) {
     // row (col - j - jb) of the K-major B operand: the 64 values of U12's column
-    __shared__ float stage[8][SNB];
-    float *st = stage[threadIdx.x >> 5];
-    st[lane] = lane < jb ? b0 : 0.f;
-    st[lane + 32] = lane + 32 < jb ? b1 : 0.f;
-    __syncwarp();
-    if (lane == 0) write_operand_row(kind, bop, bop_lo, col - j - jb, st);
+    if constexpr (std::is_same<T, float>::value) {
+      __shared__ float stage[8][SNB];
+      float *st = stage[threadIdx.x >> 5];
+      st[lane] = lane < jb ? b0 : 0.f;
+      st[lane + 32] = lane + 32 < jb ? b1 : 0.f;
+      __syncwarp();
+      if (lane == 0) write_operand_row(kind, bop, bop_lo, col - j - jb, st);
+    } else {
+      oz_split_pair(lane < jb ? (double)b0 : 0.0, lane + 32 < jb ? (double)b1 : 0.0, lane, col - j - jb, cap,
+                    static_cast<__nv_bfloat16 *>(bop), bexp);
+    }
   }
 }
 
 __global__ void zero_i32(int32_t *p) { *p = 0; }
 
-int launch_spanel(cudaStream_t s, float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0,
-                  int32_t *info, int kind, void *aop, float *aop_lo, int32_t *plan) {
+template <typename T>
+int launch_spanel(cudaStream_t s, T *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0,
+                  int32_t *info, int kind, void *aop, float *aop_lo, int32_t *aexp, int64_t cap, int32_t *plan) {
   const int C = (int)imin(SMAXC, imax(1, cdiv(mp, SPT)));
   const int64_t R = cdiv(mp, C);
-  const size_t smem = sizeof(float) * SNB * (size_t)(R + 1);
+  const size_t smem = sizeof(T) * (size_t)jb * (size_t)(R + 1);
   if (smem > 200 * 1024) return fail(BOLA_ERR_UNSUPPORTED, "mixed LU: panel of %lld rows too tall", (long long)mp);
   static bool attr = false;
   if (!attr) {
-    BOLA_TRY_CUDA(cudaFuncSetAttribute(spanel_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    BOLA_TRY_CUDA(cudaFuncSetAttribute(spanel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    BOLA_TRY_CUDA(cudaFuncSetAttribute(spanel_kernel<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    BOLA_TRY_CUDA(cudaFuncSetAttribute(spanel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     attr = true;
   }
   cudaLaunchConfig_t cfg = {};
@@ -373,8 +432,9 @@ int launch_spanel(cudaStream_t s, float *W, int64_t ldw, int64_t mp, int jb, int
   attr1[0].val.clusterDim.z = 1;
   cfg.attrs = attr1;
   cfg.numAttrs = 1;
-  ProfScope prof(s, "spanel", (double)mp * SNB * SNB, 8.0 * (double)mp * SNB);
-  BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, spanel_kernel, W, ldw, mp, jb, ipiv, col0, info, kind, aop, aop_lo, R, plan));
+  ProfScope prof(s, "spanel", (double)mp * jb * jb, 2.0 * sizeof(T) * (double)mp * jb);
+  BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, spanel_kernel<T>, W, ldw, mp, jb, ipiv, col0, info, kind, aop, aop_lo, aexp,
+                                   cap, R, plan));
   return 0;
 }
 
@@ -388,6 +448,19 @@ int MixedLU::reserve(int64_t n_, int kind_, cudaStream_t s) {
   release(s);
   n = cap_n = n_;
   kind = kind_;
+  BOLA_TRY_CUDA(cudaMallocAsync(&err, sizeof(int32_t), s));
+  BOLA_TRY_CUDA(cudaMallocAsync(&plan, sizeof(int32_t) * (1 + 4 * SNB), s));
+  BOLA_TRY_CUDA(cudaMemsetAsync(err, 0, sizeof(int32_t), s));
+  if (kind == 3) {
+    // exact bf16 slices of L21 and U12^T (OZ_SLICES planes of n rows) and their row exponents
+    BOLA_TRY_CUDA(cudaMallocAsync(&aop, (size_t)OZ_SLICES * n * SNB * 2, s));
+    BOLA_TRY_CUDA(cudaMallocAsync(&bop, (size_t)OZ_SLICES * n * SNB * 2, s));
+    BOLA_TRY_CUDA(cudaMallocAsync(&ea, sizeof(int32_t) * n, s));
+    BOLA_TRY_CUDA(cudaMallocAsync(&eb, sizeof(int32_t) * n, s));
+    BOLA_TRY(make_kmajor_map(&mapA, aop, OZ_SLICES * n, true, 128));
+    BOLA_TRY(make_kmajor_map(&mapB, bop, OZ_SLICES * n, true, 64));
+    return 0;
+  }
   const size_t esz = kind == 0 ? 2 : 4;
   BOLA_TRY_CUDA(cudaMallocAsync(&aop, (size_t)n * SNB * esz, s));
   BOLA_TRY_CUDA(cudaMallocAsync(&bop, (size_t)n * SNB * esz, s));
@@ -395,9 +468,6 @@ int MixedLU::reserve(int64_t n_, int kind_, cudaStream_t s) {
     BOLA_TRY_CUDA(cudaMallocAsync(&aop_lo, (size_t)n * SNB * 4, s));
     BOLA_TRY_CUDA(cudaMallocAsync(&bop_lo, (size_t)n * SNB * 4, s));
   }
-  BOLA_TRY_CUDA(cudaMallocAsync(&err, sizeof(int32_t), s));
-  BOLA_TRY_CUDA(cudaMallocAsync(&plan, sizeof(int32_t) * (1 + 4 * SNB), s));
-  BOLA_TRY_CUDA(cudaMemsetAsync(err, 0, sizeof(int32_t), s));
   const bool bf = kind == 0;
   BOLA_TRY(make_kmajor_map(&mapA, aop, n, bf));
   BOLA_TRY(make_kmajor_map(&mapB, bop, n, bf));
@@ -408,7 +478,8 @@ int MixedLU::reserve(int64_t n_, int kind_, cudaStream_t s) {
 
 void MixedLU::release(cudaStream_t s) {
   for (void **p : {&aop, &bop, reinterpret_cast<void **>(&aop_lo), reinterpret_cast<void **>(&bop_lo),
-                   reinterpret_cast<void **>(&err), reinterpret_cast<void **>(&plan)}) {
+                   reinterpret_cast<void **>(&err), reinterpret_cast<void **>(&plan), reinterpret_cast<void **>(&ea),
+                   reinterpret_cast<void **>(&eb)}) {
     if (*p) cudaFreeAsync(*p, s);
     *p = nullptr;
   }
@@ -424,15 +495,43 @@ int MixedLU::factor(cudaStream_t s, float *W, int64_t ldw, int32_t *ipiv, int32_
     const int jb = (int)imin(SNB, n - j);
     const int64_t mp = n - j;
     const bool upd = j + jb < n;
-    BOLA_TRY(launch_spanel(s, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, kind, upd ? aop : nullptr,
-                           aop_lo, plan));
+    BOLA_TRY(launch_spanel<float>(s, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, kind,
+                                  upd ? aop : nullptr, aop_lo, nullptr, 0, plan));
     const int64_t others = n - jb;
     if (others > 0) {
       ProfScope prof(s, "sswap_trsm", (double)jb * jb * (double)(n - j - jb));
-      sswap_trsm<<<(unsigned)cdiv(others, 8), 256, 0, s>>>(W, ldw, n, j, jb, plan, kind, upd ? bop : nullptr, bop_lo);
+      sswap_trsm<float><<<(unsigned)cdiv(others, 8), 256, 0, s>>>(W, ldw, n, j, jb, plan, kind, upd ? bop : nullptr,
+                                                                   bop_lo, nullptr, 0);
       BOLA_CHECK_LAUNCH();
     }
     if (upd) BOLA_TRY(tc_update(s, kind, mp - jb, n - j - jb, mapA, mapB, mapAlo, mapBlo,
+                                W + (j + jb) + (j + jb) * ldw, ldw, err));
+  }
+  return 0;
+}
+
+// The same LU of an FP64 W with FP64 panels and swaps and the exact-split
+// tensor-core update (kind 3).  An FP64 panel of 64 columns fits the
+// cluster's shared memory up to 16 x 399 rows; taller panels (n > 6384) take
+// 48 columns (16 x 532 rows), whose update runs with K = 64 zero-padded.
+int MixedLU::factor64(cudaStream_t s, double *W, int64_t ldw, int32_t *ipiv, int32_t *info) {
+  zero_i32<<<1, 1, 0, s>>>(info);
+  BOLA_CHECK_LAUNCH();
+  int jb = 0;
+  for (int64_t j = 0; j < n; j += jb) {
+    const int64_t mp = n - j;
+    jb = (int)imin(mp > SMAXC * 399 ? 48 : SNB, mp);
+    const bool upd = j + jb < n;
+    BOLA_TRY(launch_spanel<double>(s, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, 3,
+                                   upd ? aop : nullptr, nullptr, ea, cap_n, plan));
+    const int64_t others = n - jb;
+    if (others > 0) {
+      ProfScope prof(s, "sswap_trsm64", (double)jb * jb * (double)(n - j - jb));
+      sswap_trsm<double><<<(unsigned)cdiv(others, 8), 256, 0, s>>>(W, ldw, n, j, jb, plan, 3, upd ? bop : nullptr,
+                                                                    nullptr, eb, cap_n);
+      BOLA_CHECK_LAUNCH();
+    }
+    if (upd) BOLA_TRY(oz_update(s, mp - jb, n - j - jb, mapA, mapB, cap_n, cap_n, ea, eb,
                                 W + (j + jb) + (j + jb) * ldw, ldw, err));
   }
   return 0;

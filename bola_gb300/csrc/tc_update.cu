@@ -159,19 +159,36 @@ EncodeFn encode_fn() {
 
 }  // namespace
 
-// K-major operand: `rows` rows of 64 K values (bf16: 128 B per row; fp32: 256 B).
-int make_kmajor_map(CUtensorMap *map, const void *ptr, int64_t rows, bool bf16) {
+// K-major operand: `rows` rows of 64 K values (bf16: 128 B per row; fp32: 256 B), boxes of box_rows rows.
+int make_kmajor_map(CUtensorMap *map, const void *ptr, int64_t rows, bool bf16, int box_rows) {
   EncodeFn enc = encode_fn();
   if (!enc) return fail(BOLA_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
   const cuuint64_t dims[2] = {(cuuint64_t)KDIM, (cuuint64_t)rows};
   const cuuint64_t strides[1] = {(cuuint64_t)KDIM * (bf16 ? 2 : 4)};
-  const cuuint32_t box[2] = {bf16 ? 64u : 32u, 128u};
+  const cuuint32_t box[2] = {bf16 ? 64u : 32u, (cuuint32_t)box_rows};
   const cuuint32_t estr[2] = {1, 1};
   const CUresult r = enc(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
                          const_cast<void *>(ptr), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                          CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(BOLA_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return 0;
+}
+
+// FP64 column-major matrix (rows x cols, ld), boxes of box_rows x box_cols,
+// no swizzle (ld * 8 and the origin must be multiples of 16 bytes).
+int make_fp64_tile_map(CUtensorMap *map, const double *ptr, int64_t rows, int64_t cols, int64_t ld, int box_rows,
+                       int box_cols) {
+  EncodeFn enc = encode_fn();
+  if (!enc) return fail(BOLA_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  const cuuint64_t dims[2] = {(cuuint64_t)rows, (cuuint64_t)cols};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * 8};
+  const cuuint32_t box[2] = {(cuuint32_t)box_rows, (cuuint32_t)box_cols};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<double *>(ptr), dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(BOLA_ERR_CUDA, "cuTensorMapEncodeTiled (fp64 tile) failed (%d)", (int)r);
   return 0;
 }
 

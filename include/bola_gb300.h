@@ -149,6 +149,18 @@ int bola_dgemm_noalloc(char transa, char transb, int64_t m, int64_t n, int64_t k
 int bola_sgemm_tc_update(int kind, int64_t m, int64_t n, const void *a, const void *b, const void *a_lo,
                          const void *b_lo, float *w, int64_t ldw, int32_t *err, bola_stream_t stream);
 
+/* FP64-accurate update on the bf16 tensor cores (no BOLA counterpart; the
+ * trailing update of factor_kind 3 of bola_dgesv_mixed, exposed for
+ * testing):  W (m x n, FP64, column-major, ld ldw) -= A B^T with A (m x 64)
+ * and B (n x 64) FP64, stored K-major (64 contiguous K values per row).
+ * Each row of A and B is split exactly into six 8-bit integer slices under a
+ * power-of-two scale; slice products accumulate exactly in FP32 on the
+ * tensor cores and are combined in FP64.  Error per element about
+ * 2^-46 * 64 * max|A row| * max|B row|.  *err (device) is set non-zero if a
+ * bounded wait inside the kernel expired. */
+int bola_dgemm_oz_update(int64_t m, int64_t n, const double *a, const double *b, double *w, int64_t ldw,
+                         int32_t *err, bola_stream_t stream);
+
 /* ---- LAPACK ----------------------------------------------------------- */
 
 /* Replaces getrf(m, n, a, lda, ipiv) -> Result, src/getrf.rs:37.  Returns -4 for
@@ -198,7 +210,8 @@ int bola_dpotrs(char uplo, int64_t n, int64_t nrhs, const double *fac, int64_t l
  * not to converge.  Synchronous: it
  * returns after the result and *info are final.  n <= 8192, nrhs <= 32. */
 typedef struct {
-  int factor_kind;       /* 0: bf16 tensor-core updates; 1: tf32; 2: 3xTF32 (FP32-accurate) */
+  int factor_kind;       /* 0: bf16 tensor-core updates; 1: tf32; 2: 3xTF32 (FP32-accurate);
+                            3: FP64 storage, exact-split bf16 tensor-core updates (FP64-accurate) */
   int max_iterations;    /* refinement sweeps before declaring a stall (default 30) */
   double tolerance;      /* target backward error (default 1e-14) */
   int fallback_fp64;     /* 1: finish with the plain FP64 path when refinement stalls */

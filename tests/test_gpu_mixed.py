@@ -50,14 +50,14 @@ def berr(A, x, b, n, nrhs):
     return float((R.abs().max(0).values / den).max())
 
 
-@pytest.mark.parametrize("kind", [0, 1, 2])
+@pytest.mark.parametrize("kind", [0, 1, 2, 3])
 @pytest.mark.parametrize("n,nrhs", [(64, 1), (200, 3), (1000, 16), (2048, 32)])
 def test_mixed_reaches_1e14_well_conditioned(kind, n, nrhs):
     A, b = make_system(n, nrhs, 1e2, seed=3)
     x, info = solve(A, b, n, nrhs, kind)
     assert info.backward_error <= 1e-14
     assert berr(A, x, b, n, nrhs) <= 1e-14
-    if kind == 2 or n <= 1000:
+    if kind >= 2 or n <= 1000:
         # refinement (plain, or GMRES-IR for the slower bf16 factors) converged without the FP64 path
         assert info.path in (0, 1), (info.path, info.iterations)
 
@@ -121,3 +121,17 @@ def test_gmres_ir_handles_kappa_1e6(kind):
     assert berr(A, x, b, n, nrhs) <= 1e-14
     if kind == 2:
         assert info.path in (0, 1)
+
+
+@pytest.mark.parametrize("kappa", [1e6, 1e10])
+@pytest.mark.parametrize("n,nrhs", [(1024, 4), (777, 3), (6500, 2)])
+def test_fp64_factor_refines_ill_conditioned(kappa, n, nrhs):
+    """Factor kind 3 (FP64 storage, exact-split tensor-core updates) is
+    FP64-accurate: refinement reaches 1e-14 at kappa 1e10 without the FP64
+    fallback, in a few sweeps.  n = 6500 takes 32-column FP64 panels first."""
+    A, b = make_system(n, nrhs, kappa, seed=9)
+    x, info = solve(A, b, n, nrhs, 3, fallback=0)
+    assert info.path in (0, 1) and info.factor_info == 0
+    assert info.backward_error <= 1e-14
+    assert berr(A, x, b, n, nrhs) <= 1e-14
+    assert info.iterations <= 6
