@@ -10,8 +10,10 @@ solve), whose normwise backward error is checked to be <= 1e-14.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 ours       the C-ABI library on the GPU: `value` is the mixed-precision solve
-           (bola_dgesv_mixed: 3xTF32 tensor-core LU + FP64 refinement, plain
-           FP64 fallback when refinement stalls) with inputs resident in HBM;
+           (bola_dgesv_mixed: 3xTF32 tensor-core LU + FP64 refinement; a system
+           that factor cannot refine is solved again with the FP64-accurate
+           factor: FP64 panels, exact bf16 slicing of the trailing update on the
+           tensor cores; plain FP64 as the last resort) with inputs in HBM;
            `plain_fp64` is the BOLA-exact FP64 path (bola_dgetrf + bola_dgetrs)
            on the same systems; `e2e` copies A and b from pinned host memory
            every step and reads x back.  The library's device profiler (CUDA
@@ -189,7 +191,7 @@ class Solver:
     def solve_mixed(self, A, b, kind=2):
         """bola_dgesv_mixed; returns the bola_mixed_info of the call."""
         from bola_gb300 import _lib
-        opts = _lib.MixedOpts(kind, 30, BERR_TARGET, 1, 1)
+        opts = _lib.MixedOpts(kind, 30, BERR_TARGET, 1, 1, 1)
         info = _lib.MixedInfo()
         st = self.L.bola_dgesv_mixed(self.n, self.nrhs, self._p(A), self.n, self._p(b), self.n, self._p(self.x),
                                      self.n, ctypes.byref(opts), ctypes.byref(info), self.sp)
@@ -252,7 +254,7 @@ def run_ours(args, rank, world, device):
         torch.cuda.synchronize()
         key = f"{s['kappa']:.0e}"
         berr[key] = backward_error(s["A"], solver.x, s["b"], n, nrhs)
-        paths[key] = {"path": ["mixed-IR", "mixed-GMRES-IR", "fp64-fallback"][info.path],
+        paths[key] = {"path": ["mixed-IR", "mixed-GMRES-IR", "fp64-fallback", "fp64-accurate-factor-IR"][info.path],
                       "iterations": info.iterations, "gmres_iterations": info.gmres_iterations,
                       "reported_backward_error": info.backward_error}
 
@@ -318,7 +320,8 @@ def run_ours(args, rank, world, device):
                 "geometric 1..1/kappa, kappa in {1e2,1e6,1e10} rotating per step; b = A x_true, x_true U[-1,1)",
         "config": {"workload": f"dense LU solve n={n} nrhs={nrhs} to backward error <= {BERR_TARGET:g}",
                    "path": "mixed: 3xTF32 tcgen05 LU (FP32 storage, per-block-column scaling) + FP64 iterative "
-                           "refinement, plain FP64 fallback on stall",
+                           "refinement; escalation to the FP64-accurate factor (exact-split bf16 tcgen05 "
+                           "updates) when refinement cannot converge; plain FP64 last",
                    "replicas": "one independent solve stream per GPU (no collective)",
                    "l2": "inputs larger than L2 (512 MiB matrix per step)"},
         "latency_ms": {"p50": round(statistics.median(per), 3),

@@ -51,7 +51,7 @@ SIGNATURES = {
 
 class MixedOpts(ctypes.Structure):
     _fields_ = [("factor_kind", ctypes.c_int), ("max_iterations", ctypes.c_int), ("tolerance", ctypes.c_double),
-                ("fallback_fp64", ctypes.c_int), ("gmres", ctypes.c_int)]
+                ("fallback_fp64", ctypes.c_int), ("gmres", ctypes.c_int), ("escalate", ctypes.c_int)]
 
 
 class MixedInfo(ctypes.Structure):

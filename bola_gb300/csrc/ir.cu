@@ -800,7 +800,7 @@ int dgesv_mixed_ws(Workspace &w, int64_t n, int64_t nrhs, const double *a, int64
   if (lda < imax(1, n)) return -4;
   if (ldb < imax(1, n)) return -6;
   if (ldx < imax(1, n)) return -8;
-  bola_mixed_opts o = {2, 30, 1e-14, 1, 1};
+  bola_mixed_opts o = {2, 30, 1e-14, 1, 1, 1};
   if (opts) o = *opts;
   if (o.factor_kind < 0 || o.factor_kind > 3) return -9;
   bola_mixed_info info_out;
@@ -873,7 +873,7 @@ int dgesv_mixed_ws(Workspace &w, int64_t n, int64_t nrhs, const double *a, int64
   const double limit = o.factor_kind == 0 ? 175.0 : o.factor_kind == 1 ? 1100.0 : o.factor_kind == 2 ? 4.5e4 : 1e13;
   const double spread = ext[1] > 0.0 ? ext[0] / ext[1] : INFINITY;
   info_out.condition_estimate = spread;
-  const bool hopeless = o.fallback_fp64 && !(spread < limit);
+  const bool hopeless = (o.fallback_fp64 || o.escalate) && !(spread < limit);
   if (finfo == 0 && !hopeless) {
     // x0 = correction of b (rscale = ||b||)
     BOLA_TRY(correction(s, w, n, nr, b, ldb, nrm + 2 * nr, x, ldx, true));
@@ -919,6 +919,19 @@ int dgesv_mixed_ws(Workspace &w, int64_t n, int64_t nrhs, const double *a, int64
   }
   info_out.backward_error = berr;
   info_out.path = path;
+  if (!converged && o.escalate && o.factor_kind < 3) {
+    // the FP64-accurate factor: its own refinement, and its own FP64 fallback
+    bola_mixed_opts o3 = o;
+    o3.factor_kind = 3;
+    o3.escalate = 0;
+    bola_mixed_info i3;
+    BOLA_TRY(dgesv_mixed_ws(w, n, nrhs, a, lda, b, ldb, x, ldx, &o3, &i3, s));
+    i3.iterations += info_out.iterations;
+    i3.gmres_iterations += info_out.gmres_iterations;
+    if (i3.path != 2) i3.path = 3;
+    if (out) *out = i3;
+    return 0;
+  }
   if (!converged && o.fallback_fp64) {
     // plain FP64 path on a copy of A (BOLA's getrf + laswp + trsm)
     double *acopy = nullptr;

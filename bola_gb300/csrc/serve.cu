@@ -285,7 +285,7 @@ struct Server {
     BOLA_TRY_CUDA(cudaMemcpyAsync(A, r->a, an, cudaMemcpyHostToDevice, s));
     BOLA_TRY_CUDA(cudaMemcpyAsync(B, r->b, bn, cudaMemcpyHostToDevice, s));
     if (o.mode == 0) {
-      bola_mixed_opts mo = {o.factor_kind, 30, 1e-14, 1, 1};
+      bola_mixed_opts mo = {o.factor_kind, 30, 1e-14, 1, 1, 1};
       bola_mixed_info mi{};
       BOLA_TRY(bola_dgesv_mixed_ctx(ctx, n, nr, A, n, B, n, X, n, &mo, &mi, (bola_stream_t)s));
       r->info.path = mi.path;

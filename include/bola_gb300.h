@@ -216,12 +216,15 @@ typedef struct {
   double tolerance;      /* target backward error (default 1e-14) */
   int fallback_fp64;     /* 1: finish with the plain FP64 path when refinement stalls */
   int gmres;             /* 1: switch to GMRES-IR when plain refinement is slow (< 20x per sweep) or stalls */
+  int escalate;          /* 1: when a factor of kind 0-2 cannot reach the tolerance, solve again with
+                            kind 3 before the FP64 fallback */
 } bola_mixed_opts;
 
 typedef struct {
   int iterations;        /* refinement sweeps performed */
   int gmres_iterations;  /* inner GMRES steps (GMRES-IR), 0 when not used */
-  int path;              /* 0 mixed IR, 1 mixed GMRES-IR, 2 plain FP64 fallback */
+  int path;              /* 0 mixed IR, 1 mixed GMRES-IR, 2 plain FP64 fallback,
+                            3 escalated to factor kind 3 and refined there */
   int factor_info;       /* first zero pivot of the low-precision LU (1-based), 0 if none */
   double backward_error; /* of the returned X */
   double condition_estimate; /* max|u_ii| / min|u_ii| of the low-precision factor */

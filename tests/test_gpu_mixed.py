@@ -29,11 +29,11 @@ def make_system(n, nrhs, kappa, seed):
     return A.t().contiguous().reshape(-1), b.t().contiguous().reshape(-1)
 
 
-def solve(A, b, n, nrhs, kind, fallback=1, max_it=30, gmres=1):
+def solve(A, b, n, nrhs, kind, fallback=1, max_it=30, gmres=1, escalate=0):
     from bola_gb300 import _lib
     L = _lib.load()
     x = torch.zeros(n * nrhs, dtype=torch.float64, device="cuda")
-    opts = _lib.MixedOpts(kind, max_it, 1e-14, fallback, gmres)
+    opts = _lib.MixedOpts(kind, max_it, 1e-14, fallback, gmres, escalate)
     info = _lib.MixedInfo()
     st = L.bola_dgesv_mixed(n, nrhs, _p(A), n, _p(b), n, _p(x), n, ctypes.byref(opts), ctypes.byref(info),
                             ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
@@ -135,3 +135,22 @@ def test_fp64_factor_refines_ill_conditioned(kappa, n, nrhs):
     assert info.backward_error <= 1e-14
     assert berr(A, x, b, n, nrhs) <= 1e-14
     assert info.iterations <= 6
+
+
+@pytest.mark.parametrize("kind", [0, 2])
+def test_escalation_to_fp64_accurate_factor(kind):
+    """A factor that cannot refine kappa = 1e10 hands the system to the
+    FP64-accurate factor (path 3) instead of the plain FP64 path."""
+    n, nrhs = 1024, 4
+    A, b = make_system(n, nrhs, 1e10, seed=9)
+    x, info = solve(A, b, n, nrhs, kind, fallback=1, escalate=1)
+    assert info.path == 3
+    assert info.backward_error <= 1e-14 and berr(A, x, b, n, nrhs) <= 1e-14
+
+
+def test_escalation_not_taken_when_refinement_converges():
+    n, nrhs = 1024, 4
+    A, b = make_system(n, nrhs, 1e2, seed=9)
+    x, info = solve(A, b, n, nrhs, 2, fallback=1, escalate=1)
+    assert info.path in (0, 1)
+    assert berr(A, x, b, n, nrhs) <= 1e-14
