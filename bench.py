@@ -420,6 +420,14 @@ def run_serve(args, device):
     return out
 
 
+# DRAM bytes (read + write) per algorithmic byte, from the ncu captures
+# summarised under profiles/ (n=4096 cases): spanel 0.79 MB read for a
+# 2752 x 64 FP32 panel whose algorithmic read + write is 1.41 MB; tc_update
+# 33.2 MB for a 2752^2 step with 60.6 MB algorithmic (writes still in L2);
+# oz_update 71.1 MB for 121 MB.
+TRAFFIC_PER_ALGORITHMIC_BYTE = {"spanel": 0.56, "tc_update": 0.55, "oz_update": 0.59}
+
+
 def roofline_for(name, v, peak_fp64_gflops):
     """The dominant kernel's achieved rate against its bounding peak.
     FP64 kernels: DFMA peak measured in this run.  Tensor-core update: HBM
@@ -436,9 +444,21 @@ def roofline_for(name, v, peak_fp64_gflops):
                 "frac": round(ach / pk, 4), "traffic": None,
                 "peak_source": "FP64 DFMA throughput measured in this run (bola_measure_fp64_peak)"}
     ach = v["bytes"] / secs / 1e9
-    return {"kernel": name, "bound": "hbm", "achieved": round(ach, 2), "peak": hbm, "unit": "GB/s",
-            "frac": round(ach / hbm, 4), "traffic": None,
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s"}
+    out = {"kernel": name, "bound": "hbm", "achieved": round(ach, 2), "peak": hbm, "unit": "GB/s",
+           "frac": round(ach / hbm, 4), "traffic": None,
+           "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s"}
+    per_launch = v["bytes"] / max(v["launches"], 1)
+    ratio = TRAFFIC_PER_ALGORITHMIC_BYTE.get(name)
+    if ratio is not None:
+        # DRAM bytes per launch from one ncu capture (profiles/), scaled by the
+        # algorithmic bytes of this run's average launch
+        out["traffic"] = round(ratio * per_launch)
+        out["algorithmic_bytes_per_launch"] = round(per_launch)
+    if name in ("spanel", "spanel64"):
+        us_col = 1e3 * v["ms"] / max(v["launches"], 1) / 64.0
+        out["note"] = (f"latency-bound: {us_col:.2f} us per panel column (one cluster barrier, a DSMEM push of "
+                       f"the pivot candidate and three CTA barriers per column); the HBM fraction is not its limit")
+    return out
 
 
 # ---------------------------------------------------------------- CPU ----
@@ -489,8 +509,9 @@ def run_reference(args, device):
     del systems
     torch.cuda.empty_cache()
     threads = oracle.get_threads()
-    # warm-up: one solve (bounds the rest of the run to a few minutes)
-    t_warm, _ = cpu_solve_once(*host[0])
+    # warm-up solves (the first one also sizes the run: about 150 s of timed solves at most)
+    warm = max(1, min(args.warmup, 5))
+    t_warm = min(cpu_solve_once(*host[k % len(host)])[0] for k in range(warm))
     steps = max(1, min(args.steps, int(150.0 / max(t_warm, 1e-3))))
     per = []
     for k in range(steps):
@@ -498,11 +519,12 @@ def run_reference(args, device):
         per.append(dt)
     total = sum(per)
     value = steps / total
-    sample = (f"{steps} complete solve(s) n={n} nrhs={nrhs} rotating kappa (getrf + laswp + 2 trsm) after 1 warm-up; "
+    sample = (f"{steps} complete solve(s) n={n} nrhs={nrhs} rotating kappa (getrf + laswp + 2 trsm) after {warm} "
+              f"warm-up solve(s); "
               f"BOLA restated in C on {threads} host threads")
     return {
         "metric": METRIC, "impl": "reference", "value": round(value, 5), "unit": "solves/s", "n_gpus": 1,
-        "steps": steps, "warmup": 1, "ms_per_step": round(1e3 * total / steps, 3), "higher_is_better": True,
+        "steps": steps, "warmup": warm, "ms_per_step": round(1e3 * total / steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic, same systems as --impl ours",
         "config": {"workload": f"dense LU solve n={n} nrhs={nrhs} (BOLA getrf + laswp + 2 trsm), "
                                f"backward error <= {BERR_TARGET:g}",

@@ -432,7 +432,8 @@ int launch_spanel(cudaStream_t s, T *W, int64_t ldw, int64_t mp, int jb, int32_t
   attr1[0].val.clusterDim.z = 1;
   cfg.attrs = attr1;
   cfg.numAttrs = 1;
-  ProfScope prof(s, "spanel", (double)mp * jb * jb, 2.0 * sizeof(T) * (double)mp * jb);
+  ProfScope prof(s, std::is_same<T, double>::value ? "spanel64" : "spanel", (double)mp * jb * jb,
+                 2.0 * sizeof(T) * (double)mp * jb);
   BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, spanel_kernel<T>, W, ldw, mp, jb, ipiv, col0, info, kind, aop, aop_lo, aexp,
                                    cap, R, plan));
   return 0;
