@@ -130,9 +130,10 @@ __device__ __forceinline__ bool stop_flag(const int32_t *info) {
 // BOLA's daxpy(len, alpha, x, 1, y, 1) (src/utilities.rs:107-132 / :140-164):
 // element idx of the vector body (idx < len rounded down to `lanes`) is fused,
 // the scalar tail is not.
+// `lanes` is 2 or 4, so rounding down to it is a mask.
 __device__ __forceinline__ double daxpy_elem(double y, double alpha, double x, int64_t idx,
                                              int64_t len, int lanes) {
-  const int64_t done = (len / lanes) * lanes;
+  const int64_t done = len & ~(int64_t)(lanes - 1);
   return idx < done ? fused(alpha, x, y) : add_prod(y, alpha, x);
 }
 
@@ -142,7 +143,7 @@ __device__ __forceinline__ double daxpy_elem(double y, double alpha, double x, i
 __device__ __forceinline__ double dot_exact(int64_t n, const double *x, int64_t sx, const double *y,
                                             int64_t sy, int lanes) {
   if (n == 0) return 0.0;
-  const int64_t nch = n / lanes;
+  const int64_t nch = lanes == 4 ? (n >> 2) : (n >> 1);  // n / lanes, lanes 2 or 4
   double l0 = 0.0, l1 = 0.0, l2 = 0.0, l3 = 0.0;
   for (int64_t i = 0; i < nch; ++i) {
     const int64_t b = i * lanes;

@@ -27,38 +27,75 @@ __global__ void syrk_beta(bool upper, int64_t n, double beta, double *C, int64_t
   c = beta == 0.0 ? 0.0 : __dmul_rn(c, beta);
 }
 
-// Diagonal 32x32 blocks: blockIdx.y = block, blockIdx.x = column in block,
-// threadIdx.x = row in block.
+// Diagonal 32x32 blocks: blockIdx.y = block, blockIdx.x = column jj in the
+// block, threadIdx.x = row ii.  Each element's chain over k keeps BOLA's
+// order exactly and is FP64-latency-bound, so the 32 columns of a block run
+// on 32 SMs.  A arrives in 32-deep chunks staged in shared memory; the next
+// chunk is prefetched into registers while the current one is consumed.
 __global__ void __launch_bounds__(NB)
 syrk_diag(bool upper, bool trans_t, int64_t n, int64_t k, double alpha, const double *__restrict__ A,
           int64_t lda, double *C, int64_t ldc, int lanes, const int32_t *info) {
+  __shared__ double sA[NB][NB + 1];  // 'N': sA[l][r] = A(j0 + r, p0 + l); 'T': sA[r][l] = A(p0 + l, j0 + r)
+  __shared__ double tl[NB];          // 'N': alpha * A(j0 + jj, p0 + l), the column's multipliers
   if (stop_flag(info)) return;
   const int64_t j0 = (int64_t)blockIdx.y * NB;
   const int jb = (int)imin(NB, n - j0);
   const int jj = blockIdx.x, ii = threadIdx.x;
-  if (jj >= jb || ii >= jb) return;
-  if (upper ? ii > jj : ii < jj) return;
+  if (jj >= jb) return;  // uniform over the CTA
+  const bool active = ii < jb && !(upper ? ii > jj : ii < jj);
+  // BOLA's daxpy for column jj: the element is in the fused vector body or the unfused tail
+  const int64_t len = upper ? jj + 1 : jb - jj;
+  const int64_t idx = upper ? ii : ii - jj;
+  const bool fz = idx < (len & ~(int64_t)(lanes - 1));
+  double pre[NB];
+  auto fetch = [&](int64_t p0) {
+    const int pb = (int)imin(NB, k - p0);
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+      if (trans_t)  // column q of the block, depth row ii
+        pre[q] = (q < jb && ii < pb) ? A[(p0 + ii) + (j0 + q) * lda] : 0.0;
+      else  // depth column q, block row ii
+        pre[q] = (q < pb && ii < jb) ? A[(j0 + ii) + (p0 + q) * lda] : 0.0;
+    }
+  };
   double *cp = C + (j0 + ii) + (j0 + jj) * ldc;
-  double c = *cp;
+  double c = active ? *cp : 0.0;
+  if (k > 0) fetch(0);
   for (int64_t p0 = 0; p0 < k; p0 += NB) {
     const int pb = (int)imin(NB, k - p0);
+    __syncthreads();  // the previous chunk is consumed
+#pragma unroll
+    for (int q = 0; q < NB; ++q) sA[q][ii] = pre[q];  // both layouts: q is l ('N') or r ('T')
+    __syncthreads();
+    // one multiplier per lane, and which are non-zero (BOLA's daxpy skips a
+    // zero scale): the chain below then issues one FP64 instruction per step,
+    // the only one GB300's narrow FP64 pipe must serialise
+    uint32_t nz = 0;
+    if (!trans_t) {
+      const double tv = ii < pb ? __dmul_rn(alpha, sA[ii][jj]) : 0.0;
+      tl[ii] = tv;
+      nz = __ballot_sync(0xffffffffu, tv != 0.0);
+    }
+    __syncthreads();
+    if (p0 + NB < k) fetch(p0 + NB);
+    if (!active) continue;
     if (!trans_t) {
       // syrk_kernel 'N' (src/syrk.rs:201-222): C(:,jj) += (alpha*A(jj,l)) * A(:,l), BOLA's daxpy
-      const double *P = A + j0 + p0 * lda;
-      const int64_t len = upper ? jj + 1 : jb - jj;
-      const int64_t idx = upper ? ii : ii - jj;
-      for (int l = 0; l < pb; ++l) {
-        const double t = __dmul_rn(alpha, P[jj + l * lda]);
-        if (t != 0.0) c = daxpy_elem(c, t, P[ii + l * lda], idx, len, lanes);
+      if (fz) {
+#pragma unroll 4
+        for (int l = 0; l < pb; ++l)
+          if ((nz >> l) & 1u) c = fused(tl[l], sA[l][ii], c);
+      } else {
+        for (int l = 0; l < pb; ++l)
+          if ((nz >> l) & 1u) c = add_prod(c, tl[l], sA[l][ii]);
       }
     } else {
       // syrk_kernel 'T' (src/syrk.rs:223-247): C(ii,jj) += alpha * dot(A(:,ii), A(:,jj))
-      const double *P = A + p0 + j0 * lda;
-      const double t = dot_exact(pb, P + ii * lda, 1, P + jj * lda, 1, lanes);
+      const double t = dot_exact(pb, &sA[ii][0], 1, &sA[jj][0], 1, lanes);
       c = add_prod(c, alpha, t);
     }
   }
-  *cp = c;
+  if (active) *cp = c;
 }
 
 // ---- potrf2 on one <=32 x 32 block in shared memory (src/potrf2.rs:36-80) ----
