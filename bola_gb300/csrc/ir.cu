@@ -540,9 +540,7 @@ int ws_reserve(Workspace &w, int64_t n, int64_t nrhs, int kind, cudaStream_t s) 
   const int64_t n_req = n;  // the factorisation size; buffers may be larger
   if (n > w.n || nrhs > w.nrhs) {
     const int64_t nn = imax(n, w.n), rr = imax(nrhs, w.nrhs);
-    MixedLU keep = w.lu;
-    w.lu = MixedLU();
-    keep.release(s);
+    w.lu.release(s);  // stream-ordered; the LU keeps its streams and events
     ws_free(w);
     n = nn;
     nrhs = rr;
@@ -773,6 +771,7 @@ extern "C" int bola_mixed_ctx_destroy(bola_mixed_ctx ctx) {
   if (!w) return 0;
   cudaDeviceSynchronize();
   ws_free(*w);
+  w->lu.destroy();
   delete w;
   return 0;
 }

@@ -81,26 +81,36 @@ __device__ __forceinline__ void oz_split_pair(double v0, double v1, int lane, in
 // W(m x n, FP64) -= A B^T from the slices of A (rows of capA per slice) and
 // B (capB), exponents eA[m], eB[n]; *err set if a bounded wait expired.
 int oz_update(cudaStream_t s, int64_t m, int64_t n, const CUtensorMap &A, const CUtensorMap &B, int64_t capA,
-              int64_t capB, const int32_t *eA, const int32_t *eB, double *W, int64_t ldw, int32_t *err);
+              int64_t capB, const int32_t *eA, const int32_t *eB, double *W, int64_t ldw, int32_t *err,
+              int64_t boff = 0);
 
 // W(m x n, column-major, ld ldw) -= A * B^T on tcgen05 (kind 0 bf16, 1 tf32,
 // 2 3xTF32 with the lo maps); *err is set non-zero if a bounded wait expired.
+// B's rows start at boff (a column offset into the trailing matrix).
 int tc_update(cudaStream_t s, int kind, int64_t m, int64_t n, const CUtensorMap &A, const CUtensorMap &B,
-              const CUtensorMap &Alo, const CUtensorMap &Blo, float *W, int64_t ldw, int32_t *err);
+              const CUtensorMap &Alo, const CUtensorMap &Blo, float *W, int64_t ldw, int32_t *err, int64_t boff = 0);
 
 // Buffers and tensor maps of the low-precision LU (slu.cu), reusable across
-// factorisations of size <= capacity.
+// factorisations of size <= capacity.  The factorisation looks ahead: the
+// trailing update of step k is split into the next panel's columns (on the
+// high-priority stream sp, with the panels and swaps) and the rest (on the
+// low-priority stream su), so that panel k+1 runs on its cluster while the
+// wide update of step k fills the other SMs.  The A operand is therefore
+// double-buffered by step parity.
 struct MixedLU {
   int64_t n = 0, cap_n = 0;
   int kind = -1;  // 0 bf16, 1 tf32, 2 3xTF32 update operands (FP32 W); 3 exact bf16 slices (FP64 W)
-  void *aop = nullptr, *bop = nullptr;
-  float *aop_lo = nullptr, *bop_lo = nullptr;
-  int32_t *ea = nullptr, *eb = nullptr;  // kind 3: row exponents of the sliced operands
+  void *aop[2] = {nullptr, nullptr}, *bop = nullptr;
+  float *aop_lo[2] = {nullptr, nullptr}, *bop_lo = nullptr;
+  int32_t *ea[2] = {nullptr, nullptr}, *eb = nullptr;  // kind 3: row exponents of the sliced operands
   int32_t *err = nullptr;
   int32_t *plan = nullptr;  // the current panel's composed interchanges: count, rows[128], src[128]
-  CUtensorMap mapA, mapB, mapAlo, mapBlo;
+  CUtensorMap mapA[2], mapB, mapAlo[2], mapBlo;
+  cudaStream_t sp = nullptr, su = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_sw = nullptr, ev_wide = nullptr, ev_done = nullptr;
   int reserve(int64_t n, int kind, cudaStream_t s);
-  void release(cudaStream_t s);
+  void release(cudaStream_t s);  // frees the buffers (stream-ordered on s)
+  void destroy();                // the streams and events too (device idle)
   // LU with partial pivoting of the FP32 matrix W (n x n, ld ldw) in place (kinds 0-2).
   int factor(cudaStream_t s, float *W, int64_t ldw, int32_t *ipiv, int32_t *info);
   // The same for an FP64 W (kind 3).

@@ -91,8 +91,8 @@ constexpr int OZ_THREADS = 256;
 
 __global__ void __launch_bounds__(OZ_THREADS)
 oz_update_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-                 const __grid_constant__ CUtensorMap mapW, int64_t capA, int64_t capB, int64_t m, int64_t n,
-                 const int32_t *__restrict__ eA, const int32_t *__restrict__ eB, int32_t *err) {
+                 const __grid_constant__ CUtensorMap mapW, int64_t capA, int64_t capB, int64_t boff, int64_t m,
+                 int64_t n, const int32_t *__restrict__ eA, const int32_t *__restrict__ eB, int32_t *err) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t bar_load, bar_mma;
   __shared__ uint32_t tmem_slot;
@@ -115,7 +115,7 @@ oz_update_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
     tmem_alloc(&tmem_slot, OZ_TMEM_COLS);
     tmem_relinquish();
   }
-  if (tid < OBN) ebs[tid] = j0 + tid < n ? eB[j0 + tid] : 0;
+  if (tid < OBN) ebs[tid] = j0 + tid < n ? eB[boff + j0 + tid] : 0;
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -127,7 +127,7 @@ oz_update_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
     tma_load_2d(tileW, &mapW, (int32_t)i0, (int32_t)j0, &bar_load);
     for (int t = 0; t < S; ++t) {
       tma_load_2d(tileA + t * A_BOX, &mapA, 0, (int32_t)(t * capA + i0), &bar_load);
-      tma_load_2d(tileB + t * B_BOX, &mapB, 0, (int32_t)(t * capB + j0), &bar_load);
+      tma_load_2d(tileB + t * B_BOX, &mapB, 0, (int32_t)(t * capB + boff + j0), &bar_load);
     }
     if (!bounded_wait(&bar_load, 0)) {
       ok_shared = 0;
@@ -211,7 +211,7 @@ __global__ void oz_split_rows(int64_t rows, const double *__restrict__ X, int64_
 }  // namespace
 
 int oz_update(cudaStream_t s, int64_t m, int64_t n, const CUtensorMap &A, const CUtensorMap &B, int64_t capA,
-              int64_t capB, const int32_t *eA, const int32_t *eB, double *W, int64_t ldw, int32_t *err) {
+              int64_t capB, const int32_t *eA, const int32_t *eB, double *W, int64_t ldw, int32_t *err, int64_t boff) {
   if (m <= 0 || n <= 0) return 0;
   if ((ldw & 1) != 0 || (reinterpret_cast<uintptr_t>(W) & 15) != 0)
     return fail(BOLA_ERR_UNSUPPORTED, "oz_update: W needs an even leading dimension and a 16-byte aligned origin");
@@ -224,7 +224,7 @@ int oz_update(cudaStream_t s, int64_t m, int64_t n, const CUtensorMap &A, const 
   }
   const dim3 grid((unsigned)cdiv(m, OBM), (unsigned)cdiv(n, OBN));
   ProfScope prof(s, "oz_update", 2.0 * (double)m * n * OK * NPAIRS, 16.0 * (double)m * n);
-  oz_update_kernel<<<grid, OZ_THREADS, OZ_SMEM, s>>>(A, B, mapW, capA, capB, m, n, eA, eB, err);
+  oz_update_kernel<<<grid, OZ_THREADS, OZ_SMEM, s>>>(A, B, mapW, capA, capB, boff, m, n, eA, eB, err);
   BOLA_CHECK_LAUNCH();
   return 0;
 }
@@ -250,7 +250,7 @@ extern "C" int bola_dgemm_oz_update(int64_t m, int64_t n, const double *a, const
   CUtensorMap A, B;
   int st = make_kmajor_map(&A, sa, S * m, true, OBM);
   if (st == 0) st = make_kmajor_map(&B, sb, S * n, true, OBN);
-  if (st == 0) st = oz_update(s, m, n, A, B, m, n, ea, eb, w, ldw, err);
+  if (st == 0) st = oz_update(s, m, n, A, B, m, n, ea, eb, w, ldw, err, 0);
   for (void *p : {(void *)sa, (void *)sb, (void *)ea, (void *)eb}) cudaFreeAsync(p, s);
   return st;
 }

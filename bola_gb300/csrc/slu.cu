@@ -442,7 +442,15 @@ int launch_spanel(cudaStream_t s, T *W, int64_t ldw, int64_t mp, int jb, int32_t
 }  // namespace
 
 int MixedLU::reserve(int64_t n_, int kind_, cudaStream_t s) {
-  if (n_ <= cap_n && kind_ == kind && aop) {
+  if (!sp) {
+    int least = 0, greatest = 0;
+    BOLA_TRY_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    BOLA_TRY_CUDA(cudaStreamCreateWithPriority(&sp, cudaStreamNonBlocking, greatest));
+    BOLA_TRY_CUDA(cudaStreamCreateWithPriority(&su, cudaStreamNonBlocking, least));
+    for (cudaEvent_t *e : {&ev_in, &ev_sw, &ev_wide, &ev_done})
+      BOLA_TRY_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  }
+  if (n_ <= cap_n && kind_ == kind && aop[0]) {
     n = n_;
     return 0;
   }
@@ -454,88 +462,134 @@ int MixedLU::reserve(int64_t n_, int kind_, cudaStream_t s) {
   BOLA_TRY_CUDA(cudaMemsetAsync(err, 0, sizeof(int32_t), s));
   if (kind == 3) {
     // exact bf16 slices of L21 and U12^T (OZ_SLICES planes of n rows) and their row exponents
-    BOLA_TRY_CUDA(cudaMallocAsync(&aop, (size_t)OZ_SLICES * n * SNB * 2, s));
+    for (int b = 0; b < 2; ++b) {
+      BOLA_TRY_CUDA(cudaMallocAsync(&aop[b], (size_t)OZ_SLICES * n * SNB * 2, s));
+      BOLA_TRY_CUDA(cudaMallocAsync(&ea[b], sizeof(int32_t) * n, s));
+      BOLA_TRY(make_kmajor_map(&mapA[b], aop[b], OZ_SLICES * n, true, 128));
+    }
     BOLA_TRY_CUDA(cudaMallocAsync(&bop, (size_t)OZ_SLICES * n * SNB * 2, s));
-    BOLA_TRY_CUDA(cudaMallocAsync(&ea, sizeof(int32_t) * n, s));
     BOLA_TRY_CUDA(cudaMallocAsync(&eb, sizeof(int32_t) * n, s));
-    BOLA_TRY(make_kmajor_map(&mapA, aop, OZ_SLICES * n, true, 128));
     BOLA_TRY(make_kmajor_map(&mapB, bop, OZ_SLICES * n, true, 64));
     return 0;
   }
   const size_t esz = kind == 0 ? 2 : 4;
-  BOLA_TRY_CUDA(cudaMallocAsync(&aop, (size_t)n * SNB * esz, s));
-  BOLA_TRY_CUDA(cudaMallocAsync(&bop, (size_t)n * SNB * esz, s));
-  if (kind == 2) {
-    BOLA_TRY_CUDA(cudaMallocAsync(&aop_lo, (size_t)n * SNB * 4, s));
-    BOLA_TRY_CUDA(cudaMallocAsync(&bop_lo, (size_t)n * SNB * 4, s));
-  }
   const bool bf = kind == 0;
-  BOLA_TRY(make_kmajor_map(&mapA, aop, n, bf));
+  for (int b = 0; b < 2; ++b) {
+    BOLA_TRY_CUDA(cudaMallocAsync(&aop[b], (size_t)n * SNB * esz, s));
+    if (kind == 2) BOLA_TRY_CUDA(cudaMallocAsync(&aop_lo[b], (size_t)n * SNB * 4, s));
+    BOLA_TRY(make_kmajor_map(&mapA[b], aop[b], n, bf));
+    BOLA_TRY(make_kmajor_map(&mapAlo[b], kind == 2 ? aop_lo[b] : aop[b], n, bf));
+  }
+  BOLA_TRY_CUDA(cudaMallocAsync(&bop, (size_t)n * SNB * esz, s));
+  if (kind == 2) BOLA_TRY_CUDA(cudaMallocAsync(&bop_lo, (size_t)n * SNB * 4, s));
   BOLA_TRY(make_kmajor_map(&mapB, bop, n, bf));
-  BOLA_TRY(make_kmajor_map(&mapAlo, kind == 2 ? aop_lo : aop, n, bf));
   BOLA_TRY(make_kmajor_map(&mapBlo, kind == 2 ? bop_lo : bop, n, bf));
   return 0;
 }
 
 void MixedLU::release(cudaStream_t s) {
-  for (void **p : {&aop, &bop, reinterpret_cast<void **>(&aop_lo), reinterpret_cast<void **>(&bop_lo),
-                   reinterpret_cast<void **>(&err), reinterpret_cast<void **>(&plan), reinterpret_cast<void **>(&ea),
-                   reinterpret_cast<void **>(&eb)}) {
+  for (void **p : {&aop[0], &aop[1], &bop, reinterpret_cast<void **>(&aop_lo[0]),
+                   reinterpret_cast<void **>(&aop_lo[1]), reinterpret_cast<void **>(&bop_lo),
+                   reinterpret_cast<void **>(&err), reinterpret_cast<void **>(&plan), reinterpret_cast<void **>(&ea[0]),
+                   reinterpret_cast<void **>(&ea[1]), reinterpret_cast<void **>(&eb)}) {
     if (*p) cudaFreeAsync(*p, s);
     *p = nullptr;
   }
   cap_n = 0;
 }
 
-// Right-looking blocked LU of W (n x n FP32), ipiv global 1-based, *info the
-// first zero pivot (the factor is then unusable; the caller falls back).
-int MixedLU::factor(cudaStream_t s, float *W, int64_t ldw, int32_t *ipiv, int32_t *info) {
-  zero_i32<<<1, 1, 0, s>>>(info);
+void MixedLU::destroy() {
+  release(nullptr);
+  for (cudaEvent_t *e : {&ev_in, &ev_sw, &ev_wide, &ev_done}) {
+    if (*e) cudaEventDestroy(*e);
+    *e = nullptr;
+  }
+  for (cudaStream_t *st : {&sp, &su}) {
+    if (*st) cudaStreamDestroy(*st);
+    *st = nullptr;
+  }
+}
+
+namespace {
+
+// Width of the panel starting at j: 64, or 48 for FP64 panels taller than
+// the cluster's shared memory holds at 64 columns (16 x 399 rows).
+int panel_width(bool fp64, int64_t n, int64_t j) {
+  const int64_t mp = n - j;
+  return (int)imin(fp64 && mp > SMAXC * 399 ? 48 : SNB, mp);
+}
+
+}  // namespace
+
+// Right-looking blocked LU of W (n x n), ipiv global 1-based, *info the first
+// zero pivot (the factor is then unusable; the caller falls back).  Kinds 0-2:
+// FP32 W and tc_update; kind 3: FP64 W and the exact-split oz_update.  Per
+// step k: panel, swaps + U12 + B operand, the update of the next panel's
+// columns (all on sp), then the update of the other columns on su, which
+// overlaps panel k+1; the swaps of step k+1 wait for it.
+template <typename T>
+static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int32_t *ipiv, int32_t *info) {
+  constexpr bool fp64 = std::is_same<T, double>::value;
+  const int64_t n = lu.n;
+  BOLA_TRY_CUDA(cudaEventRecord(lu.ev_in, s));
+  BOLA_TRY_CUDA(cudaStreamWaitEvent(lu.sp, lu.ev_in, 0));
+  BOLA_TRY_CUDA(cudaStreamWaitEvent(lu.su, lu.ev_in, 0));
+  zero_i32<<<1, 1, 0, lu.sp>>>(info);
   BOLA_CHECK_LAUNCH();
-  for (int64_t j = 0; j < n; j += SNB) {
-    const int jb = (int)imin(SNB, n - j);
+  int jb = 0;
+  bool wide_pending = false;
+  for (int64_t j = 0, k = 0; j < n; j += jb, ++k) {
+    jb = panel_width(fp64, n, j);
     const int64_t mp = n - j;
     const bool upd = j + jb < n;
-    BOLA_TRY(launch_spanel<float>(s, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, kind,
-                                  upd ? aop : nullptr, aop_lo, nullptr, 0, plan));
+    const int buf = (int)(k & 1);
+    BOLA_TRY(launch_spanel<T>(lu.sp, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, lu.kind,
+                              upd ? lu.aop[buf] : nullptr, fp64 ? nullptr : lu.aop_lo[buf], fp64 ? lu.ea[buf] : nullptr,
+                              lu.cap_n, lu.plan));
+    // the row swaps reach every column: the previous wide update must be done
+    if (wide_pending) BOLA_TRY_CUDA(cudaStreamWaitEvent(lu.sp, lu.ev_wide, 0));
+    wide_pending = false;
     const int64_t others = n - jb;
     if (others > 0) {
-      ProfScope prof(s, "sswap_trsm", (double)jb * jb * (double)(n - j - jb));
-      sswap_trsm<float><<<(unsigned)cdiv(others, 8), 256, 0, s>>>(W, ldw, n, j, jb, plan, kind, upd ? bop : nullptr,
-                                                                   bop_lo, nullptr, 0);
+      ProfScope prof(lu.sp, fp64 ? "sswap_trsm64" : "sswap_trsm", (double)jb * jb * (double)(n - j - jb));
+      sswap_trsm<T><<<(unsigned)cdiv(others, 8), 256, 0, lu.sp>>>(W, ldw, n, j, jb, lu.plan, lu.kind,
+                                                                    upd ? lu.bop : nullptr, fp64 ? nullptr : lu.bop_lo,
+                                                                    fp64 ? lu.eb : nullptr, lu.cap_n);
       BOLA_CHECK_LAUNCH();
     }
-    if (upd) BOLA_TRY(tc_update(s, kind, mp - jb, n - j - jb, mapA, mapB, mapAlo, mapBlo,
-                                W + (j + jb) + (j + jb) * ldw, ldw, err));
+    if (!upd) continue;
+    const int64_t m2 = mp - jb, n2 = n - j - jb;
+    const int64_t nb_next = imin((int64_t)panel_width(fp64, n, j + jb), n2);
+    T *W22 = W + (j + jb) + (j + jb) * ldw;
+    auto update = [&](cudaStream_t st, int64_t cols, int64_t boff) -> int {
+      if constexpr (fp64)
+        return oz_update(st, m2, cols, lu.mapA[buf], lu.mapB, lu.cap_n, lu.cap_n, lu.ea[buf], lu.eb,
+                         W22 + boff * ldw, ldw, lu.err, boff);
+      else
+        return tc_update(st, lu.kind, m2, cols, lu.mapA[buf], lu.mapB, lu.mapAlo[buf], lu.mapBlo,
+                         W22 + boff * ldw, ldw, lu.err, boff);
+    };
+    BOLA_TRY(update(lu.sp, nb_next, 0));  // the next panel's columns
+    if (n2 > nb_next) {
+      BOLA_TRY_CUDA(cudaEventRecord(lu.ev_sw, lu.sp));
+      BOLA_TRY_CUDA(cudaStreamWaitEvent(lu.su, lu.ev_sw, 0));
+      BOLA_TRY(update(lu.su, n2 - nb_next, nb_next));
+      BOLA_TRY_CUDA(cudaEventRecord(lu.ev_wide, lu.su));
+      wide_pending = true;
+    }
   }
+  if (wide_pending) BOLA_TRY_CUDA(cudaStreamWaitEvent(lu.sp, lu.ev_wide, 0));
+  BOLA_TRY_CUDA(cudaEventRecord(lu.ev_done, lu.sp));
+  BOLA_TRY_CUDA(cudaStreamWaitEvent(s, lu.ev_done, 0));
   return 0;
 }
 
-// The same LU of an FP64 W with FP64 panels and swaps and the exact-split
-// tensor-core update (kind 3).  An FP64 panel of 64 columns fits the
-// cluster's shared memory up to 16 x 399 rows; taller panels (n > 6384) take
-// 48 columns (16 x 532 rows), whose update runs with K = 64 zero-padded.
+int MixedLU::factor(cudaStream_t s, float *W, int64_t ldw, int32_t *ipiv, int32_t *info) {
+  return factor_lookahead<float>(*this, s, W, ldw, ipiv, info);
+}
+
 int MixedLU::factor64(cudaStream_t s, double *W, int64_t ldw, int32_t *ipiv, int32_t *info) {
-  zero_i32<<<1, 1, 0, s>>>(info);
-  BOLA_CHECK_LAUNCH();
-  int jb = 0;
-  for (int64_t j = 0; j < n; j += jb) {
-    const int64_t mp = n - j;
-    jb = (int)imin(mp > SMAXC * 399 ? 48 : SNB, mp);
-    const bool upd = j + jb < n;
-    BOLA_TRY(launch_spanel<double>(s, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, 3,
-                                   upd ? aop : nullptr, nullptr, ea, cap_n, plan));
-    const int64_t others = n - jb;
-    if (others > 0) {
-      ProfScope prof(s, "sswap_trsm64", (double)jb * jb * (double)(n - j - jb));
-      sswap_trsm<double><<<(unsigned)cdiv(others, 8), 256, 0, s>>>(W, ldw, n, j, jb, plan, 3, upd ? bop : nullptr,
-                                                                    nullptr, eb, cap_n);
-      BOLA_CHECK_LAUNCH();
-    }
-    if (upd) BOLA_TRY(oz_update(s, mp - jb, n - j - jb, mapA, mapB, cap_n, cap_n, ea, eb,
-                                W + (j + jb) + (j + jb) * ldw, ldw, err));
-  }
-  return 0;
+  return factor_lookahead<double>(*this, s, W, ldw, ipiv, info);
 }
 
 }  // namespace bola

@@ -43,7 +43,7 @@ template <int KIND, int NPASS>
 __global__ void __launch_bounds__(128)
 tc_update_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                  const __grid_constant__ CUtensorMap mapAlo, const __grid_constant__ CUtensorMap mapBlo, int64_t m,
-                 int64_t n, float *__restrict__ W, int64_t ldw, int32_t *err) {
+                 int64_t n, int64_t boff, float *__restrict__ W, int64_t ldw, int32_t *err) {
   using Cfg = TcCfg<KIND, NPASS>;
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t bar_load, bar_mma;
@@ -77,7 +77,8 @@ tc_update_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
       for (int kb = 0; kb < Cfg::KB; ++kb) {
         const int x = kb * (KIND == 0 ? 64 : 32);
         tma_load_2d(tileA + (op * Cfg::KB + kb) * BOX_BYTES, op ? &mapAlo : &mapA, x, (int32_t)i0, &bar_load);
-        tma_load_2d(tileB + (op * Cfg::KB + kb) * BOX_BYTES, op ? &mapBlo : &mapB, x, (int32_t)j0, &bar_load);
+        tma_load_2d(tileB + (op * Cfg::KB + kb) * BOX_BYTES, op ? &mapBlo : &mapB, x, (int32_t)(boff + j0),
+                    &bar_load);
       }
     }
     if (!bounded_wait(&bar_load, 0)) {
@@ -193,7 +194,7 @@ int make_fp64_tile_map(CUtensorMap *map, const double *ptr, int64_t rows, int64_
 }
 
 int tc_update(cudaStream_t s, int kind, int64_t m, int64_t n, const CUtensorMap &A, const CUtensorMap &B,
-              const CUtensorMap &Alo, const CUtensorMap &Blo, float *W, int64_t ldw, int32_t *err) {
+              const CUtensorMap &Alo, const CUtensorMap &Blo, float *W, int64_t ldw, int32_t *err, int64_t boff) {
   if (m <= 0 || n <= 0) return 0;
   const dim3 grid((unsigned)cdiv(m, BM), (unsigned)cdiv(n, BN));
   ProfScope prof(s, "tc_update", 2.0 * (double)m * n * KDIM * (kind == 2 ? 3 : 1), 8.0 * (double)m * n);
@@ -206,7 +207,7 @@ int tc_update(cudaStream_t s, int kind, int64_t m, int64_t n, const CUtensorMap 
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM_LAUNCH)); \
       attr = true;                                                                                        \
     }                                                                                                     \
-    tc_update_kernel<KIND, NPASS><<<grid, 128, Cfg::SMEM_LAUNCH, s>>>(A, B, Alo, Blo, m, n, W, ldw, err); \
+    tc_update_kernel<KIND, NPASS><<<grid, 128, Cfg::SMEM_LAUNCH, s>>>(A, B, Alo, Blo, m, n, boff, W, ldw, err); \
   } while (0)
   if (kind == 0) BOLA_TC(0, 1);
   else if (kind == 1) BOLA_TC(1, 1);
@@ -232,5 +233,5 @@ extern "C" int bola_sgemm_tc_update(int kind, int64_t m, int64_t n, const void *
   BOLA_TRY(make_kmajor_map(&B, b, n, bf16));
   BOLA_TRY(make_kmajor_map(&Alo, kind == 2 ? a_lo : a, m, bf16));
   BOLA_TRY(make_kmajor_map(&Blo, kind == 2 ? b_lo : b, n, bf16));
-  return tc_update((cudaStream_t)stream, kind, m, n, A, B, Alo, Blo, w, ldw, err);
+  return tc_update((cudaStream_t)stream, kind, m, n, A, B, Alo, Blo, w, ldw, err, 0);
 }
