@@ -216,6 +216,20 @@ class Solver:
             raise RuntimeError(f"bola_dgetrs status {st}: {L.bola_last_error().decode()}")
 
 
+def max_over_ranks(values, world, device):
+    """Each timing (ms) as the maximum over the ranks of a replica run (the
+    slowest rank sets the job's time); unchanged for one rank."""
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
+def job_rate(world, steps, total_ms):
+    """Whole-job solves/s: every rank solves `steps` systems in at most total_ms."""
+    return world * steps / (total_ms / 1e3)
+
+
 def time_steps(fn, steps, stream):
     """CUDA-event time of each step on `stream`; synchronised on both sides."""
     torch.cuda.synchronize()
@@ -292,10 +306,7 @@ def run_ours(args, rank, world, device):
         step_e2e(k)
     e2e_total, e2e_per = time_steps(step_e2e, args.steps, stream)
 
-    t = torch.tensor([total_ms, e2e_total, plain_total], dtype=torch.float64, device=device)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    total_ms, e2e_total, plain_total = float(t[0]), float(t[1]), float(t[2])
+    total_ms, e2e_total, plain_total = max_over_ranks([total_ms, e2e_total, plain_total], world, device)
     if rank != 0:
         return None
 
@@ -310,8 +321,8 @@ def run_ours(args, rank, world, device):
                for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])}
     launches = int(sum(v["launches"] for v in prof.values()))
 
-    value = world * args.steps / (total_ms / 1e3)
-    plain_value = world * plain_steps / (plain_total / 1e3)
+    value = job_rate(world, args.steps, total_ms)
+    plain_value = job_rate(world, plain_steps, plain_total)
     out = {
         "metric": METRIC, "value": round(value, 4), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
@@ -333,7 +344,7 @@ def run_ours(args, rank, world, device):
         "backward_error": berr,
         "backward_error_ok": all(v <= BERR_TARGET for v in berr.values()),
         "refinement": paths,
-        "e2e": {"value": round(world * args.steps / (e2e_total / 1e3), 4), "unit": "solves/s",
+        "e2e": {"value": round(job_rate(world, args.steps, e2e_total), 4), "unit": "solves/s",
                 "h2d_bytes_per_step": 8 * (n * n + n * nrhs), "d2h_bytes_per_step": 8 * n * nrhs},
         "roofline": roof,
         "kernels": kernels,

@@ -102,6 +102,28 @@ __device__ __forceinline__ void write_operand_row(int kind, void *op, float *op_
   }
 }
 
+// Row pitch of a panel held in shared memory: at least R + 1 and a multiple
+// of the 16-byte vector (4 floats or 2 doubles), so that a lane can move V
+// consecutive rows of a column in one access.
+template <typename T>
+__host__ __device__ constexpr int panel_pitch(int64_t R) {
+  return (int)(((R + (int64_t)(16 / sizeof(T))) / (int64_t)(16 / sizeof(T))) * (int64_t)(16 / sizeof(T)));
+}
+__device__ __forceinline__ void vload(float (&v)[4], const float *p) {
+  const float4 t = *reinterpret_cast<const float4 *>(p);
+  v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+}
+__device__ __forceinline__ void vload(double (&v)[2], const double *p) {
+  const double2 t = *reinterpret_cast<const double2 *>(p);
+  v[0] = t.x; v[1] = t.y;
+}
+__device__ __forceinline__ void vstore(float *p, const float (&v)[4]) {
+  *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void vstore(double *p, const double (&v)[2]) {
+  *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
+}
+
 // Panel LU of W[0:mp, 0:jb] (W points at the panel's top-left).  ipiv gets
 // global 1-based rows (col0 + local + 1).  CTA cr of the cluster owns panel
 // rows [cr*R, cr*R + R), kept in shared memory column-major with an odd
@@ -139,7 +161,7 @@ spanel_kernel(T *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
   extern __shared__ __align__(16) unsigned char sp_raw[];
   T *sp = reinterpret_cast<T *>(sp_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int RP = (int)R + 1;
+  const int RP = panel_pitch<T>(R);
   const int r0 = (int)(cr * R);
   const int r1 = (int)imin(mp, r0 + R);
   const int nr = r1 > r0 ? r1 - r0 : 0;
@@ -218,21 +240,25 @@ spanel_kernel(T *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
         const int c = j + 1 + warp + 8 * q;
         pr[q] = c < jb ? pprev[c] : T(0);
       }
+      // 16-byte shared-memory accesses: a lane takes V consecutive rows
+      constexpr int V = 16 / (int)sizeof(T);
       const int ib = j > r0 ? j - r0 : 0;
-      for (int il = ib + lane; il < nr; il += 32) {
-        const T l = PE(j - 1, il);
-        T v[8];
+      for (int il0 = (ib & ~(V - 1)) + lane * V; il0 < nr; il0 += 32 * V) {
+        T l[V];
+        vload(l, &sp[(j - 1) * RP + il0]);
+        bool on[V];
+#pragma unroll
+        for (int e = 0; e < V; ++e) on[e] = il0 + e >= ib && il0 + e < nr;
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
           const int c = j + 1 + warp + 8 * q;
-          v[q] = c < jb ? PE(c, il) : T(0);
-        }
+          if (c >= jb) continue;
+          T v[V];
+          vload(v, &sp[c * RP + il0]);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) v[q] = fmaT(-l, pr[q], v[q]);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int c = j + 1 + warp + 8 * q;
-          if (c < jb) PE(c, il) = v[q];
+          for (int e = 0; e < V; ++e)
+            if (on[e]) v[e] = fmaT(-l[e], pr[q], v[e]);
+          vstore(&sp[c * RP + il0], v);
         }
       }
     }
@@ -412,7 +438,7 @@ int launch_spanel(cudaStream_t s, T *W, int64_t ldw, int64_t mp, int jb, int32_t
                   int32_t *info, int kind, void *aop, float *aop_lo, int32_t *aexp, int64_t cap, int32_t *plan) {
   const int C = (int)imin(SMAXC, imax(1, cdiv(mp, SPT)));
   const int64_t R = cdiv(mp, C);
-  const size_t smem = sizeof(T) * (size_t)jb * (size_t)(R + 1);
+  const size_t smem = sizeof(T) * (size_t)jb * (size_t)panel_pitch<T>(R);
   if (smem > 200 * 1024) return fail(BOLA_ERR_UNSUPPORTED, "mixed LU: panel of %lld rows too tall", (long long)mp);
   static bool attr = false;
   if (!attr) {
