@@ -113,18 +113,39 @@ __device__ int group_lu_solve(const SystemDesc &S, int t, int G, int g, double *
     for (int i = k + 1 + t; i < n; i += G) A[i + (int64_t)k * lda] *= inv;
     group_sync(G, g);
     const int m = n - k - 1;
-    for (int e = t; e < m * m; e += G) {
-      const int i = k + 1 + e % m, j = k + 1 + e / m;
-      A[i + (int64_t)j * lda] = fma(-A[i + (int64_t)k * lda], A[k + (int64_t)j * lda], A[i + (int64_t)j * lda]);
+    if (m > 0) {
+      // element e = t, t + G, ... of the m x m trailing block, (i, j) advanced
+      // without a division per element
+      const int dq = G / m, dr = G % m;
+      int i = k + 1 + t % m, j = k + 1 + t / m;
+      for (int e = t; e < m * m; e += G) {
+        A[i + (int64_t)j * lda] = fma(-A[i + (int64_t)k * lda], A[k + (int64_t)j * lda], A[i + (int64_t)j * lda]);
+        i += dr;
+        j += dq;
+        if (i >= n) {
+          i -= m;
+          ++j;
+        }
+      }
     }
     group_sync(G, g);
   }
   if (info) return info;
   // forward: unit lower
   for (int k = 0; k < n; ++k) {
-    for (int e = t; e < (n - k - 1) * nr; e += G) {
-      const int i = k + 1 + e % (n - k - 1), c = e / (n - k - 1);
-      B[i + (int64_t)c * ldb] = fma(-A[i + (int64_t)k * lda], B[k + (int64_t)c * ldb], B[i + (int64_t)c * ldb]);
+    const int m = n - k - 1;
+    if (m > 0) {
+      const int dq = G / m, dr = G % m;
+      int i = k + 1 + t % m, c = t / m;
+      for (int e = t; e < m * nr; e += G) {
+        B[i + (int64_t)c * ldb] = fma(-A[i + (int64_t)k * lda], B[k + (int64_t)c * ldb], B[i + (int64_t)c * ldb]);
+        i += dr;
+        c += dq;
+        if (i >= n) {
+          i -= m;
+          ++c;
+        }
+      }
     }
     group_sync(G, g);
   }
@@ -132,9 +153,18 @@ __device__ int group_lu_solve(const SystemDesc &S, int t, int G, int g, double *
   for (int k = n - 1; k >= 0; --k) {
     for (int c = t; c < nr; c += G) B[k + (int64_t)c * ldb] /= A[k + (int64_t)k * lda];
     group_sync(G, g);
-    for (int e = t; e < k * nr; e += G) {
-      const int i = e % k, c = e / k;
-      B[i + (int64_t)c * ldb] = fma(-A[i + (int64_t)k * lda], B[k + (int64_t)c * ldb], B[i + (int64_t)c * ldb]);
+    if (k > 0) {
+      const int dq = G / k, dr = G % k;
+      int i = t % k, c = t / k;
+      for (int e = t; e < k * nr; e += G) {
+        B[i + (int64_t)c * ldb] = fma(-A[i + (int64_t)k * lda], B[k + (int64_t)c * ldb], B[i + (int64_t)c * ldb]);
+        i += dr;
+        c += dq;
+        if (i >= k) {
+          i -= k;
+          ++c;
+        }
+      }
     }
     group_sync(G, g);
   }
@@ -155,28 +185,56 @@ __device__ int group_chol_solve(const SystemDesc &S, int t, int G, int g) {
     for (int i = k + 1 + t; i < n; i += G) A[i + (int64_t)k * lda] *= inv;
     group_sync(G, g);
     const int m = n - k - 1;
-    for (int e = t; e < m * m; e += G) {
-      const int i = k + 1 + e % m, j = k + 1 + e / m;
-      if (j <= i)
-        A[i + (int64_t)j * lda] = fma(-A[i + (int64_t)k * lda], A[j + (int64_t)k * lda], A[i + (int64_t)j * lda]);
+    if (m > 0) {
+      const int dq = G / m, dr = G % m;
+      int i = k + 1 + t % m, j = k + 1 + t / m;
+      for (int e = t; e < m * m; e += G) {
+        if (j <= i)
+          A[i + (int64_t)j * lda] = fma(-A[i + (int64_t)k * lda], A[j + (int64_t)k * lda], A[i + (int64_t)j * lda]);
+        i += dr;
+        j += dq;
+        if (i >= n) {
+          i -= m;
+          ++j;
+        }
+      }
     }
     group_sync(G, g);
   }
   for (int k = 0; k < n; ++k) {  // L y = b
     for (int c = t; c < nr; c += G) B[k + (int64_t)c * ldb] /= A[k + (int64_t)k * lda];
     group_sync(G, g);
-    for (int e = t; e < (n - k - 1) * nr; e += G) {
-      const int i = k + 1 + e % (n - k - 1), c = e / (n - k - 1);
-      B[i + (int64_t)c * ldb] = fma(-A[i + (int64_t)k * lda], B[k + (int64_t)c * ldb], B[i + (int64_t)c * ldb]);
+    const int m = n - k - 1;
+    if (m > 0) {
+      const int dq = G / m, dr = G % m;
+      int i = k + 1 + t % m, c = t / m;
+      for (int e = t; e < m * nr; e += G) {
+        B[i + (int64_t)c * ldb] = fma(-A[i + (int64_t)k * lda], B[k + (int64_t)c * ldb], B[i + (int64_t)c * ldb]);
+        i += dr;
+        c += dq;
+        if (i >= n) {
+          i -= m;
+          ++c;
+        }
+      }
     }
     group_sync(G, g);
   }
   for (int k = n - 1; k >= 0; --k) {  // L^T x = y
     for (int c = t; c < nr; c += G) B[k + (int64_t)c * ldb] /= A[k + (int64_t)k * lda];
     group_sync(G, g);
-    for (int e = t; e < k * nr; e += G) {
-      const int i = e % k, c = e / k;
-      B[i + (int64_t)c * ldb] = fma(-A[k + (int64_t)i * lda], B[k + (int64_t)c * ldb], B[i + (int64_t)c * ldb]);
+    if (k > 0) {
+      const int dq = G / k, dr = G % k;
+      int i = t % k, c = t / k;
+      for (int e = t; e < k * nr; e += G) {
+        B[i + (int64_t)c * ldb] = fma(-A[k + (int64_t)i * lda], B[k + (int64_t)c * ldb], B[i + (int64_t)c * ldb]);
+        i += dr;
+        c += dq;
+        if (i >= k) {
+          i -= k;
+          ++c;
+        }
+      }
     }
     group_sync(G, g);
   }
