@@ -62,6 +62,40 @@ __device__ __forceinline__ PKey pk_warp_max(const PKey &k) {
   return PKey{a, b, c};
 }
 
+// ---- panel arithmetic ---------------------------------------------------------
+// The panel kernel works on elements of type S in shared memory, loaded from
+// and stored to W of type G, through these operations (the FP32 factor's
+// panel, and the FP64-accurate factor's).
+struct PanelF32 {
+  using S = float;
+  using G = float;
+  static constexpr bool kFP64 = false;
+  __device__ static S zero() { return 0.f; }
+  __device__ static S load(G x) { return x; }
+  __device__ static G store(S x) { return x; }
+  __device__ static S mul(S a, S b) { return a * b; }
+  __device__ static S fnms(S z, S x, S y) { return fmaf(-x, y, z); }
+  __device__ static bool is_zero(S p) { return p == 0.f; }
+  __device__ static S recip(S p) { return p == 0.f ? 0.f : 1.0f / p; }
+  __device__ static PKey key(S v, int g) { return pk_make(v, g); }
+  __device__ static double to_double(S v) { return (double)v; }
+};
+
+struct PanelF64 {
+  using S = double;
+  using G = double;
+  static constexpr bool kFP64 = true;
+  __device__ static S zero() { return 0.0; }
+  __device__ static S load(G x) { return x; }
+  __device__ static G store(S x) { return x; }
+  __device__ static S mul(S a, S b) { return a * b; }
+  __device__ static S fnms(S z, S x, S y) { return fma(-x, y, z); }
+  __device__ static bool is_zero(S p) { return p == 0.0; }
+  __device__ static S recip(S p) { return p == 0.0 ? 0.0 : 1.0 / p; }
+  __device__ static PKey key(S v, int g) { return pk_make(v, g); }
+  __device__ static double to_double(S v) { return v; }
+};
+
 
 __device__ __forceinline__ float tf32_round(float x) {
   uint32_t u = __float_as_uint(x);
@@ -146,13 +180,14 @@ __device__ __forceinline__ void cluster_wait() {
   asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
-template <typename T>
+template <typename P>
 __global__ void __launch_bounds__(SPT)
-spanel_kernel(T *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0, int32_t *info, int kind,
+spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0, int32_t *info, int kind,
               void *aop, float *aop_lo, int32_t *aexp, int64_t cap, int64_t R, int32_t *plan) {
   cg::cluster_group cluster = cg::this_cluster();
   const int C = (int)cluster.num_blocks();
   const int cr = (int)cluster.block_rank();
+  using T = typename P::S;
   __shared__ SSlot<T> slots[2][SMAXC];
   __shared__ T rowj[2][SNB];
   __shared__ T piv[2][SNB];   // pivot rows, up to date (piv[par] = column j's)
@@ -172,12 +207,12 @@ spanel_kernel(T *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
   for (int64_t e = tid; e < (int64_t)ns * jb; e += SPT) {
     const int il = (int)(e % ns);
     const int c = (int)(e / ns);
-    sp[c * RP + il] = W[(r0 + il) + c * ldw];
+    sp[c * RP + il] = P::load(W[(r0 + il) + c * ldw]);
   }
   __syncthreads();
   cluster.sync();  // every CTA of the cluster is running before the first push
 
-  T inv = T(0);  // 1 / pivot of the previous column
+  T inv = P::zero();  // 1 / pivot of the previous column
   for (int j = 0; j < jb; ++j) {
     const int par = j & 1;
     const T *pprev = piv[par ^ 1];
@@ -186,9 +221,9 @@ spanel_kernel(T *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
     PKey best = PKey{0u, 0u, 0u};
     for (int il = tid; il < nr; il += SPT) {
       const int g = r0 + il;
-      if (j > 0 && g >= j) PE(j - 1, il) *= inv;
+      if (j > 0 && g >= j) PE(j - 1, il) = P::mul(PE(j - 1, il), inv);
       if (g < j) continue;
-      const PKey k = pk_make(PE(j, il), g);
+      const PKey k = P::key(PE(j, il), g);
       if (pk_less(best, k)) best = k;
     }
     best = pk_warp_max(best);
@@ -203,14 +238,14 @@ spanel_kernel(T *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
       const int gl = ck.c ? (int)(0xFFFFFFFFu - ck.c) - r0 : -1;  // local row of the candidate
       const bool own_j = j >= r0 && j < r1;
       const int jl = j - r0;
-      T c0 = T(0), c1 = T(0), j0v = T(0), j1v = T(0);
+      T c0 = P::zero(), c1 = P::zero(), j0v = P::zero(), j1v = P::zero();
       if (gl >= 0) {
-        c0 = lane < jb ? PE(lane, gl) : T(0);
-        c1 = lane + 32 < jb ? PE(lane + 32, gl) : T(0);
+        c0 = lane < jb ? PE(lane, gl) : P::zero();
+        c1 = lane + 32 < jb ? PE(lane + 32, gl) : P::zero();
       }
       if (own_j) {
-        j0v = lane < jb ? PE(lane, jl) : T(0);
-        j1v = lane + 32 < jb ? PE(lane + 32, jl) : T(0);
+        j0v = lane < jb ? PE(lane, jl) : P::zero();
+        j1v = lane + 32 < jb ? PE(lane + 32, jl) : P::zero();
       }
       for (int d = warp; d < C; d += SPT / 32) {
         SSlot<T> *rs = cluster.map_shared_rank(&slots[par][cr], d);
@@ -238,7 +273,7 @@ spanel_kernel(T *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
         const int c = j + 1 + warp + 8 * q;
-        pr[q] = c < jb ? pprev[c] : T(0);
+        pr[q] = c < jb ? pprev[c] : P::zero();
       }
       // 16-byte shared-memory accesses: a lane takes V consecutive rows
       constexpr int V = 16 / (int)sizeof(T);
@@ -257,7 +292,7 @@ spanel_kernel(T *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
           vload(v, &sp[c * RP + il0]);
 #pragma unroll
           for (int e = 0; e < V; ++e)
-            if (on[e]) v[e] = fmaT(-l[e], pr[q], v[e]);
+            if (on[e]) v[e] = P::fnms(v[e], l[e], pr[q]);
           vstore(&sp[c * RP + il0], v);
         }
       }
@@ -279,8 +314,8 @@ spanel_kernel(T *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
     if (tid < jb) {
       T pv_ = raw[tid], ov = rowj[par][tid];
       if (j > 0 && tid > j) {
-        pv_ = fmaT(-raw[j - 1], pprev[tid], pv_);
-        ov = fmaT(-rowj[par][j - 1], pprev[tid], ov);
+        pv_ = P::fnms(pv_, raw[j - 1], pprev[tid]);
+        ov = P::fnms(ov, rowj[par][j - 1], pprev[tid]);
       }
       pcur[tid] = pv_;
       oldj[tid] = ov;
@@ -288,9 +323,8 @@ spanel_kernel(T *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
     __syncthreads();
     const T pv = pcur[j];
     if (cr == 0 && tid == 0) ipiv[j] = col0 + jp + 1;
-    inv = T(1) / pv;
-    if (pv == T(0)) {
-      inv = T(0);
+    inv = P::recip(pv);
+    if (P::is_zero(pv)) {
       if (cr == 0 && tid == 0) atomicCAS(info, 0, col0 + j + 1);
     }
     if (jp != j && tid < jb) {
@@ -305,20 +339,20 @@ spanel_kernel(T *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
       for (int il = tid; il < nr; il += SPT) {
         if (r0 + il <= j) continue;
         T &x = PE(j + 1, il);
-        x = fmaT(-(PE(j, il) * inv), pj1, x);
+        x = P::fnms(x, P::mul(PE(j, il), inv), pj1);
       }
     }
   }
   // the last column's multipliers
   for (int il = tid; il < nr; il += SPT)
-    if (r0 + il >= jb) PE(jb - 1, il) *= inv;
+    if (r0 + il >= jb) PE(jb - 1, il) = P::mul(PE(jb - 1, il), inv);
   __syncthreads();
 
   // -- write back the panel and the update's A operand (rows below the panel)
   for (int64_t e = tid; e < (int64_t)ns * jb; e += SPT) {
     const int il = (int)(e % ns);
     const int c = (int)(e / ns);
-    W[(r0 + il) + c * ldw] = sp[c * RP + il];
+    W[(r0 + il) + c * ldw] = P::store(sp[c * RP + il]);
   }
   if (plan != nullptr && cr == 0 && warp == 0) {
     // the panel's interchanges as "row rows[t] takes the old row src[t]",
@@ -337,7 +371,7 @@ spanel_kernel(T *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
     for (int il = tid; il < nr; il += SPT) {
       const int g = r0 + il;
       if (g < jb) continue;
-      if constexpr (std::is_same<T, float>::value) {
+      if constexpr (!P::kFP64) {
         float v[SNB];
 #pragma unroll
         for (int c = 0; c < SNB; ++c) v[c] = c < jb ? PE(c, il) : 0.f;
@@ -346,7 +380,7 @@ spanel_kernel(T *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
         // exact bf16 slices of the row (FP64 factor): exponent, then 8 K values at a time
         uint64_t mb = 0;
         for (int c = 0; c < jb; ++c) {
-          const uint64_t mc = oz_mag((double)PE(c, il));
+          const uint64_t mc = oz_mag(P::to_double(PE(c, il)));
           mb = mc > mb ? mc : mb;
         }
         const int e = oz_exponent(mb);
@@ -357,7 +391,7 @@ spanel_kernel(T *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
 #pragma unroll
           for (int u = 0; u < 8; ++u) {
             __nv_bfloat16 t8[OZ_SLICES];
-            oz_slices(c0 + u < jb ? (double)PE(c0 + u, il) : 0.0, e, t8);
+            oz_slices(c0 + u < jb ? P::to_double(PE(c0 + u, il)) : 0.0, e, t8);
 #pragma unroll
             for (int t = 0; t < OZ_SLICES; ++t) q[t][u] = t8[t];
           }
@@ -433,17 +467,17 @@ sswap_trsm(T *W, int64_t ldw, int64_t n, int64_t j, int jb, const int32_t *plan,
 
 __global__ void zero_i32(int32_t *p) { *p = 0; }
 
-template <typename T>
-int launch_spanel(cudaStream_t s, T *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0,
+template <typename P>
+int launch_spanel(cudaStream_t s, typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0,
                   int32_t *info, int kind, void *aop, float *aop_lo, int32_t *aexp, int64_t cap, int32_t *plan) {
   const int C = (int)imin(SMAXC, imax(1, cdiv(mp, SPT)));
   const int64_t R = cdiv(mp, C);
-  const size_t smem = sizeof(T) * (size_t)jb * (size_t)panel_pitch<T>(R);
+  const size_t smem = sizeof(typename P::S) * (size_t)jb * (size_t)panel_pitch<typename P::S>(R);
   if (smem > 200 * 1024) return fail(BOLA_ERR_UNSUPPORTED, "mixed LU: panel of %lld rows too tall", (long long)mp);
   static bool attr = false;
   if (!attr) {
-    BOLA_TRY_CUDA(cudaFuncSetAttribute(spanel_kernel<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    BOLA_TRY_CUDA(cudaFuncSetAttribute(spanel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    BOLA_TRY_CUDA(cudaFuncSetAttribute(spanel_kernel<P>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    BOLA_TRY_CUDA(cudaFuncSetAttribute(spanel_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     attr = true;
   }
   cudaLaunchConfig_t cfg = {};
@@ -458,9 +492,9 @@ int launch_spanel(cudaStream_t s, T *W, int64_t ldw, int64_t mp, int jb, int32_t
   attr1[0].val.clusterDim.z = 1;
   cfg.attrs = attr1;
   cfg.numAttrs = 1;
-  ProfScope prof(s, std::is_same<T, double>::value ? "spanel64" : "spanel", (double)mp * jb * jb,
-                 2.0 * sizeof(T) * (double)mp * jb);
-  BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, spanel_kernel<T>, W, ldw, mp, jb, ipiv, col0, info, kind, aop, aop_lo, aexp,
+  ProfScope prof(s, P::kFP64 ? "spanel64" : "spanel", (double)mp * jb * jb,
+                 2.0 * sizeof(typename P::G) * (double)mp * jb);
+  BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, spanel_kernel<P>, W, ldw, mp, jb, ipiv, col0, info, kind, aop, aop_lo, aexp,
                                    cap, R, plan));
   return 0;
 }
@@ -569,7 +603,8 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
     const int64_t mp = n - j;
     const bool upd = j + jb < n;
     const int buf = (int)(k & 1);
-    BOLA_TRY(launch_spanel<T>(lu.sp, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, lu.kind,
+    using Pol = typename std::conditional<fp64, PanelF64, PanelF32>::type;
+    BOLA_TRY(launch_spanel<Pol>(lu.sp, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, lu.kind,
                               upd ? lu.aop[buf] : nullptr, fp64 ? nullptr : lu.aop_lo[buf], fp64 ? lu.ea[buf] : nullptr,
                               lu.cap_n, lu.plan));
     // the row swaps reach every column: the previous wide update must be done
