@@ -15,6 +15,9 @@
 // come out bit-identical (for the SIMD width selected).
 #include <cooperative_groups.h>
 
+#include <mutex>
+#include <vector>
+
 #include "common.cuh"
 
 namespace cg = cooperative_groups;
@@ -308,6 +311,7 @@ step_swap_trsm(double *A, int64_t lda, int64_t n, int64_t j, int jb, const int32
 }
 
 __global__ void zero_i32(int32_t *p) { *p = 0; }
+__global__ void copy_i32(const int32_t *src, int32_t *dst) { *dst = *src; }
 
 // Launches panel_lu with the largest cluster (<= 16 CTAs, ~256 rows each)
 // the device can co-schedule.
@@ -382,30 +386,138 @@ int getrf2_rec(cudaStream_t s, int64_t m, int64_t n, double *A, int64_t lda, int
 }
 
 // src/getrf.rs:37-101
-int getrf_blocked(cudaStream_t s, int64_t m, int64_t n, double *A, int64_t lda, int32_t *ipiv, int32_t *info) {
+// Look-ahead resources of one blocked getrf: the high-priority stream for
+// panels, swaps and the next panel's columns, the low-priority stream for the
+// rest of each trailing update, events, and per-step snapshots of *info.
+// Kept in a per-device pool so that concurrent callers each take their own.
+struct GetrfLA {
+  cudaStream_t sp = nullptr, su = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_sw = nullptr, ev_wide = nullptr, ev_done = nullptr;
+  int32_t *snap = nullptr;  // device int32[2]
+};
+std::mutex g_la_mu;
+std::vector<GetrfLA *> g_la_pool[64];
+
+GetrfLA *la_acquire() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
   {
-    ProfScope prof(s, "info_init");
-    zero_i32<<<1, 1, 0, s>>>(info);
+    std::lock_guard<std::mutex> lk(g_la_mu);
+    auto &pool = g_la_pool[dev & 63];
+    if (!pool.empty()) {
+      GetrfLA *la = pool.back();
+      pool.pop_back();
+      return la;
+    }
   }
-  BOLA_CHECK_LAUNCH();
-  if (m == 0 || n == 0) return 0;
+  GetrfLA *la = new GetrfLA();
+  int least = 0, greatest = 0;
+  bool ok = cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess &&
+            cudaStreamCreateWithPriority(&la->sp, cudaStreamNonBlocking, greatest) == cudaSuccess &&
+            cudaStreamCreateWithPriority(&la->su, cudaStreamNonBlocking, least) == cudaSuccess &&
+            cudaMalloc(&la->snap, 2 * sizeof(int32_t)) == cudaSuccess;
+  for (cudaEvent_t *e : {&la->ev_in, &la->ev_sw, &la->ev_wide, &la->ev_done})
+    ok = ok && cudaEventCreateWithFlags(e, cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) return nullptr;  // (leaks the partial set; only on a failing device)
+  return la;
+}
+
+void la_release(GetrfLA *la) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(g_la_mu);
+  g_la_pool[dev & 63].push_back(la);
+}
+
+// BOLA's blocked getrf (src/getrf.rs:37-101) with look-ahead.  Per step k:
+// panel, swaps + trsm, and the update of the next panel's 32 columns on sp;
+// the update of the other columns on su, overlapping panel k+1 (whose swaps
+// wait for it).  Splitting the trailing DGEMM at a column multiple of 4 keeps
+// BOLA's 8x4 edge-tile classification, so every element is computed exactly
+// as in one call.  The wide update stops on its own step's snapshot of
+// *info: a zero pivot found by panel k+1 while it runs must not cut short
+// step k's update, which BOLA completes before factoring panel k+1.
+int getrf_blocked(cudaStream_t s, int64_t m, int64_t n, double *A, int64_t lda, int32_t *ipiv, int32_t *info) {
   const int64_t min_mn = imin(m, n);
-  if (PNB >= min_mn) return getrf2_rec(s, m, n, A, lda, ipiv, info, 0);
-  for (int64_t j = 0; j < min_mn; j += PNB) {
-    const int jb = (int)imin(PNB, min_mn - j);
-    BOLA_TRY(launch_panel(s, A + j + j * lda, lda, m - j, jb, ipiv + j, info, (int32_t)j, (int32_t)j));
-    const int64_t others = n - jb;
-    if (others > 0) {
-      ProfScope prof(s, "getrf_swap_trsm", (double)jb * (jb - 1) * (double)(n - j - jb), 32.0 * jb * (double)others);
-      step_swap_trsm<<<(unsigned)cdiv(others, 8), 256, 0, s>>>(A, lda, n, j, jb, ipiv, info, lanes());
-      BOLA_CHECK_LAUNCH();
+  GetrfLA *la = (m > 0 && n > 0 && PNB < min_mn) ? la_acquire() : nullptr;
+  if (!la) {
+    {
+      ProfScope prof(s, "info_init");
+      zero_i32<<<1, 1, 0, s>>>(info);
     }
-    if (j + jb < n && j + jb < m) {
-      BOLA_TRY(dgemm_exact(s, 'N', 'N', m - j - jb, n - j - jb, jb, -1.0, A + (j + jb) + j * lda, lda,
-                           A + j + (j + jb) * lda, lda, 1.0, A + (j + jb) + (j + jb) * lda, lda, 64, info, 0));
+    BOLA_CHECK_LAUNCH();
+    if (m == 0 || n == 0) return 0;
+    if (PNB >= min_mn) return getrf2_rec(s, m, n, A, lda, ipiv, info, 0);
+    for (int64_t j = 0; j < min_mn; j += PNB) {
+      const int jb = (int)imin(PNB, min_mn - j);
+      BOLA_TRY(launch_panel(s, A + j + j * lda, lda, m - j, jb, ipiv + j, info, (int32_t)j, (int32_t)j));
+      const int64_t others = n - jb;
+      if (others > 0) {
+        ProfScope prof(s, "getrf_swap_trsm", (double)jb * (jb - 1) * (double)(n - j - jb), 32.0 * jb * (double)others);
+        step_swap_trsm<<<(unsigned)cdiv(others, 8), 256, 0, s>>>(A, lda, n, j, jb, ipiv, info, lanes());
+        BOLA_CHECK_LAUNCH();
+      }
+      if (j + jb < n && j + jb < m) {
+        BOLA_TRY(dgemm_exact(s, 'N', 'N', m - j - jb, n - j - jb, jb, -1.0, A + (j + jb) + j * lda, lda,
+                             A + j + (j + jb) * lda, lda, 1.0, A + (j + jb) + (j + jb) * lda, lda, 64, info, 0));
+      }
     }
+    return 0;
   }
-  return 0;
+  int st = 0;
+  auto run = [&]() -> int {
+    BOLA_TRY_CUDA(cudaEventRecord(la->ev_in, s));
+    BOLA_TRY_CUDA(cudaStreamWaitEvent(la->sp, la->ev_in, 0));
+    BOLA_TRY_CUDA(cudaStreamWaitEvent(la->su, la->ev_in, 0));
+    {
+      ProfScope prof(la->sp, "info_init");
+      zero_i32<<<1, 1, 0, la->sp>>>(info);
+    }
+    BOLA_CHECK_LAUNCH();
+    bool wide_pending = false;
+    for (int64_t j = 0, k = 0; j < min_mn; j += PNB, ++k) {
+      const int jb = (int)imin(PNB, min_mn - j);
+      BOLA_TRY(launch_panel(la->sp, A + j + j * lda, lda, m - j, jb, ipiv + j, info, (int32_t)j, (int32_t)j));
+      if (wide_pending) BOLA_TRY_CUDA(cudaStreamWaitEvent(la->sp, la->ev_wide, 0));
+      wide_pending = false;
+      const int64_t others = n - jb;
+      if (others > 0) {
+        ProfScope prof(la->sp, "getrf_swap_trsm", (double)jb * (jb - 1) * (double)(n - j - jb),
+                       32.0 * jb * (double)others);
+        step_swap_trsm<<<(unsigned)cdiv(others, 8), 256, 0, la->sp>>>(A, lda, n, j, jb, ipiv, info, lanes());
+        BOLA_CHECK_LAUNCH();
+      }
+      if (!(j + jb < n && j + jb < m)) continue;
+      const int64_t m2 = m - j - jb, n2 = n - j - jb;
+      const int64_t nb_next = imin((int64_t)PNB, n2);  // a multiple of 4 unless it is all of n2
+      const double *A21 = A + (j + jb) + j * lda, *A12 = A + j + (j + jb) * lda;
+      double *A22 = A + (j + jb) + (j + jb) * lda;
+      BOLA_TRY(dgemm_exact(la->sp, 'N', 'N', m2, nb_next, jb, -1.0, A21, lda, A12, lda, 1.0, A22, lda, 64, info, 0));
+      if (n2 > nb_next) {
+        int32_t *snap = la->snap + (k & 1);
+        copy_i32<<<1, 1, 0, la->sp>>>(info, snap);
+        BOLA_CHECK_LAUNCH();
+        BOLA_TRY_CUDA(cudaEventRecord(la->ev_sw, la->sp));
+        BOLA_TRY_CUDA(cudaStreamWaitEvent(la->su, la->ev_sw, 0));
+        BOLA_TRY(dgemm_exact(la->su, 'N', 'N', m2, n2 - nb_next, jb, -1.0, A21, lda, A12 + nb_next * lda, lda, 1.0,
+                             A22 + nb_next * lda, lda, 64, snap, 0));
+        BOLA_TRY_CUDA(cudaEventRecord(la->ev_wide, la->su));
+        wide_pending = true;
+      }
+    }
+    if (wide_pending) BOLA_TRY_CUDA(cudaStreamWaitEvent(la->sp, la->ev_wide, 0));
+    BOLA_TRY_CUDA(cudaEventRecord(la->ev_done, la->sp));
+    BOLA_TRY_CUDA(cudaStreamWaitEvent(s, la->ev_done, 0));
+    return 0;
+  };
+  st = run();
+  if (st != 0) {
+    // leave nothing of this call running on the look-ahead streams
+    cudaStreamSynchronize(la->sp);
+    cudaStreamSynchronize(la->su);
+  }
+  la_release(la);
+  return st;
 }
 
 }  // namespace bola

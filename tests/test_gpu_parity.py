@@ -143,7 +143,7 @@ def test_getrf_ties_follow_bola_lane_order(both):
     assert same(A1, A2)
 
 
-@pytest.mark.parametrize("col", [0, 5, 40, 95])
+@pytest.mark.parametrize("col", [0, 5, 40, 70, 95])
 def test_getrf_singular_stops_like_bola(both, col):
     g, o = both
     n = 100
