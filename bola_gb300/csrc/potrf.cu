@@ -252,6 +252,37 @@ int potrf2_rec(cudaStream_t s, char uplo, int64_t n, double *A, int64_t lda, int
   return potrf2_rec(s, uplo, n2, a22, lda, info, col0 + (int32_t)n1);
 }
 
+// BOLA's left-looking Cholesky (src/potrf.rs:114-178) computes block column p
+// from all earlier columns at step p: a SYRK chain of length 32p for the
+// diagonal block and a GEMM with K = 32p for the rows below it, both one
+// after the other on the critical path.  Here the same sums are formed
+// right-looking, as soon as their inputs are final:
+//  - every element's SYRK chain runs in column order, so after block p is
+//    final all later diagonal blocks advance their chains by its 32 columns
+//    (one launch for all of them);
+//  - BOLA's GEMM forms one 64-deep chunk at a time (c = fma(alpha, acc, c),
+//    chunks from k = 0), so when a chunk's 64 columns are final it is applied
+//    to every later block column in one block-triangular GEMM; a block whose
+//    K ends in a half chunk gets that 32-deep chunk at its own step.  The
+//    8x4 edge classification depends only on n (block origins are multiples
+//    of 32), so edge elements stay edge elements.
+// The arithmetic per element is BOLA's, in BOLA's order: results are
+// bit-identical.  What differs is the state after a failure: BOLA leaves the
+// columns after the failing block untouched, so the lower (upper) part from
+// the failing block's first sub-diagonal row (column) on is restored from a
+// copy of A taken at entry.
+__global__ void potrf_restore(bool upper, int64_t n, const double *__restrict__ bk, double *A, int64_t lda,
+                              const int32_t *info) {
+  const int32_t f = *info;
+  if (f == 0) return;
+  const int64_t jf = (int64_t)((f - 1) / NB) * NB;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e % n, c = e / n;
+    const int64_t r = upper ? c : i, q = upper ? i : c;  // r: position along the factor's rows, q: its columns
+    if (q >= jf && r >= q && r >= jf + NB) A[i + c * lda] = bk[e];
+  }
+}
+
 int potrf_blocked(cudaStream_t s, char uplo, int64_t n, double *A, int64_t lda, int32_t *info) {
   {
     ProfScope prof(s, "info_init");
@@ -260,28 +291,50 @@ int potrf_blocked(cudaStream_t s, char uplo, int64_t n, double *A, int64_t lda, 
   BOLA_CHECK_LAUNCH();
   if (NB >= n) return potrf2_rec(s, uplo, n, A, lda, info, 0);
   const bool upper = uplo == 'U';
+  Scratch bk;
+  BOLA_TRY(bk.alloc((size_t)n * n * sizeof(double), s));
+  BOLA_TRY_CUDA(cudaMemcpy2DAsync(bk.as<double>(), (size_t)n * sizeof(double), A, (size_t)lda * sizeof(double),
+                                  (size_t)n * sizeof(double), (size_t)n, cudaMemcpyDeviceToDevice, s));
+  const int lan = lanes();
   for (int64_t j = 0; j < n; j += NB) {
-    const int64_t jb = imin(NB, n - j);
+    const int64_t jb = imin(NB, n - j), t = j + jb, n_rem = n - t;
+    const bool odd = (j / NB) & 1;
     double *ajj = A + j + j * lda;
-    const int64_t n_rem = n - j - jb;
+    BOLA_TRY(potrf2_rec(s, uplo, jb, ajj, lda, info, (int32_t)j));
+    if (n_rem == 0) break;
     if (upper) {
-      BOLA_TRY(syrk_exact(s, 'U', 'T', jb, j, -1.0, A + j * lda, lda, 1.0, ajj, lda, info));
-      BOLA_TRY(potrf2_rec(s, 'U', jb, ajj, lda, info, (int32_t)j));
-      if (n_rem > 0) {
-        BOLA_TRY(dgemm_exact(s, 'T', 'N', jb, n_rem, j, -1.0, A + j * lda, lda, A + (j + jb) * lda, lda, 1.0,
-                             A + j + (j + jb) * lda, lda, 64, info, 0));
-        BOLA_TRY(trsm_exact(s, 'L', 'U', 'T', 'N', jb, n_rem, 1.0, ajj, lda, A + j + (j + jb) * lda, lda, info));
-      }
+      if (odd)  // the half chunk [j - 32, j) of this block's GEMM
+        BOLA_TRY(dgemm_exact(s, 'T', 'N', jb, n_rem, NB, -1.0, A + (j - NB) + j * lda, lda, A + (j - NB) + t * lda,
+                             lda, 1.0, A + j + t * lda, lda, 64, info, 0));
+      BOLA_TRY(trsm_exact(s, 'L', 'U', 'T', 'N', jb, n_rem, 1.0, ajj, lda, A + j + t * lda, lda, info));
     } else {
-      BOLA_TRY(syrk_exact(s, 'L', 'N', jb, j, -1.0, A + j, lda, 1.0, ajj, lda, info));
-      BOLA_TRY(potrf2_rec(s, 'L', jb, ajj, lda, info, (int32_t)j));
-      if (n_rem > 0) {
-        BOLA_TRY(dgemm_exact(s, 'N', 'T', n_rem, jb, j, -1.0, A + j + jb, lda, A + j, lda, 1.0,
-                             A + j + jb + j * lda, lda, 64, info, 0));
-        BOLA_TRY(trsm_exact(s, 'R', 'L', 'T', 'N', n_rem, jb, 1.0, ajj, lda, A + j + jb + j * lda, lda, info));
-      }
+      if (odd)
+        BOLA_TRY(dgemm_exact(s, 'N', 'T', n_rem, jb, NB, -1.0, A + t + (j - NB) * lda, lda, A + j + (j - NB) * lda,
+                             lda, 1.0, A + t + j * lda, lda, 64, info, 0));
+      BOLA_TRY(trsm_exact(s, 'R', 'L', 'T', 'N', n_rem, jb, 1.0, ajj, lda, A + t + j * lda, lda, info));
+    }
+    {  // later diagonal blocks: chains advance over columns [j, j + 32)
+      ProfScope prof(s, "syrk_diag", (double)NB * (NB + 1) * (double)NB * (double)cdiv(n_rem, NB));
+      const double *src = upper ? A + j + t * lda : A + t + j * lda;
+      syrk_diag<<<dim3(NB, (unsigned)cdiv(n_rem, NB)), NB, 0, s>>>(upper, upper, n_rem, NB, -1.0, src, lda,
+                                                                  A + t + t * lda, lda, lan, info);
+      BOLA_CHECK_LAUNCH();
+    }
+    if (odd) {  // chunk [j - 32, j + 32) is final: apply it to every later block column
+      const int64_t c0 = j - NB;
+      if (upper)
+        BOLA_TRY(dgemm_exact(s, 'T', 'N', n_rem, n_rem, 2 * NB, -1.0, A + c0 + t * lda, lda, A + c0 + t * lda, lda,
+                             1.0, A + t + t * lda, lda, 64, info, 1));
+      else
+        BOLA_TRY(dgemm_exact(s, 'N', 'T', n_rem, n_rem, 2 * NB, -1.0, A + t + c0 * lda, lda, A + t + c0 * lda, lda,
+                             1.0, A + t + t * lda, lda, 64, info, 2));
     }
   }
+  {
+    ProfScope prof(s, "potrf_restore");
+    potrf_restore<<<2 * (unsigned)num_sms(), 256, 0, s>>>(upper, n, bk.as<double>(), A, lda, info);
+  }
+  BOLA_CHECK_LAUNCH();
   return 0;
 }
 

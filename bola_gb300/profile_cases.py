@@ -5,6 +5,9 @@
     python -m bola_gb300.profile_cases mixed N KIND   # 2 x bola_dgesv_mixed, 16 RHS, A = U[-1,1) + 4 I
     python -m bola_gb300.profile_cases batched COUNT  # 2 x bola_batch_solve, the batched workload (seed 4)
 
+With --scopes, the library's own device timers are on during the last call
+and its per-scope device time is printed after it.
+
 Inputs are made with torch's generator on the device (no torch.linalg, so the
 cases also run under profilers that cannot load its solver libraries).  Each
 run prints its CUDA-event time; exit status 0 means every call succeeded.
@@ -100,11 +103,32 @@ def case_batched(count):
     b.close()
 
 
+def _print_scopes():
+    from . import api
+    prof = api.profile_read()
+    total = sum(v["ms"] for v in prof.values()) or 1.0
+    for name, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"]):
+        print(f"  {name:24s} scopes={v['calls']:6d} launches={v['launches']:6d} {v['ms']:9.3f} ms "
+              f"{100 * v['ms'] / total:5.1f}%")
+
+
 def main(argv):
+    scopes = "--scopes" in argv
+    argv = [a for a in argv if a != "--scopes"]
     if not argv:
         raise SystemExit(__doc__)
     case, args = argv[0], [int(a) for a in argv[1:]]
-    {"getrf": case_getrf, "potrf": case_potrf, "mixed": case_mixed, "batched": case_batched}[case](*args)
+    fn = {"getrf": case_getrf, "potrf": case_potrf, "mixed": case_mixed, "batched": case_batched}[case]
+    if scopes:
+        from . import api
+        fn(*args)  # warm
+        api.profile_reset()
+        api.profile_enable(True)
+        fn(*args)
+        api.profile_enable(False)
+        _print_scopes()
+    else:
+        fn(*args)
 
 
 if __name__ == "__main__":

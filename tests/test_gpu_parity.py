@@ -173,7 +173,7 @@ def test_getrf2_recursive_bitwise(both, n):
 
 
 @pytest.mark.parametrize("uplo", ["L", "U"])
-@pytest.mark.parametrize("n", [1, 3, 32, 33, 64, 100, 257])
+@pytest.mark.parametrize("n", [1, 3, 32, 33, 64, 100, 203, 257, 390])
 def test_potrf_bitwise(both, uplo, n):
     g, o = both
     A = wl.spd_matrix(n, seed=n + 1)
@@ -194,14 +194,15 @@ def test_potrf2_bitwise(both, uplo):
     assert same(A1, A2)
 
 
-@pytest.mark.parametrize("bad", [0, 20, 45, 99])
-def test_potrf_not_spd(gpu, oracle_lib, bad):
-    n = 100
+@pytest.mark.parametrize("uplo", ["L", "U"])
+@pytest.mark.parametrize("n,bad", [(100, 0), (100, 20), (100, 45), (100, 70), (100, 99), (301, 200)])
+def test_potrf_not_spd(gpu, oracle_lib, uplo, n, bad):
+    """BOLA stops at the failing block: later columns keep their input values."""
     A = wl.spd_matrix(n, seed=2)
     A[bad, bad] = -1000.0
     A1, A2 = A.copy(order="F"), A.copy(order="F")
-    info = oracle_lib.potrf("L", n, A1, n)
-    msg = gpu.potrf("L", n, A2, n)
+    info = oracle_lib.potrf(uplo, n, A1, n)
+    msg = gpu.potrf(uplo, n, A2, n)
     assert msg == f"Matrix is not positive-definite. Failure at column {(info - 1) % 32 + 1}."
     assert same(A1, A2)
 
