@@ -96,6 +96,18 @@ int laswp_exact(cudaStream_t s, int64_t n, double *A, int64_t lda, int32_t k1, i
 int getrf2_rec(cudaStream_t s, int64_t m, int64_t n, double *A, int64_t lda, int32_t *ipiv,
                int32_t *info, int32_t col0);
 
+// Look-ahead resources of one blocked factorisation: a high-priority stream
+// for the critical path (panels, the next block's columns), a low-priority
+// stream for the rest of each trailing update, events, and two device ints.
+// Pooled per device, so concurrent callers each take their own set.
+struct LookAhead {
+  cudaStream_t sp = nullptr, su = nullptr;
+  cudaEvent_t ev[8] = {};
+  int32_t *snap = nullptr;  // device int32[2]
+};
+LookAhead *la_acquire();  // nullptr if the resources cannot be created
+void la_release(LookAhead *la);
+
 int potrf2_rec(cudaStream_t s, char uplo, int64_t n, double *A, int64_t lda, int32_t *info,
                int32_t col0);
 
@@ -123,6 +135,10 @@ __device__ __forceinline__ double add_prod(double c, double t, double x) {
 __device__ __forceinline__ double sub_prod(double c, double t, double x) {
   return __dsub_rn(c, __dmul_rn(t, x));
 }
+// x != 0.0 (NaN included) on the integer pipe.  GB300 retires ~2 FP64
+// operations per clock per SM and a comparison takes a slot like an FMA, so
+// the zero tests inside BOLA's update loops are done on the bits.
+__device__ __forceinline__ bool nonzero64(double x) { return (__double_as_longlong(x) << 1) != 0; }
 __device__ __forceinline__ bool stop_flag(const int32_t *info) {
   return info != nullptr && *(volatile const int32_t *)info != 0;
 }
@@ -173,31 +189,33 @@ __device__ __forceinline__ double dot_exact(int64_t n, const double *x, int64_t 
 // position BOLA's four lane-interleaved accumulators give it.  v = -1 marks
 // an element BOLA can never select (NaN; zero in the vector body or tail).
 struct Cand {
-  double v;
+  int64_t v;  // |x|'s bits (ordered like |x|), or -1 (never selectable) / -2 (no candidate)
   int64_t key;  // smaller wins among equal v
   int64_t idx;  // 0-based index in the searched vector
 };
 __device__ __forceinline__ bool cand_better(const Cand &a, const Cand &b) {
-  return a.v > b.v || (a.v == b.v && a.key < b.key);
+  return a.v > b.v || (a.v == b.v && a.key < b.key);  // integer compares: no FP64 slots
 }
 __device__ __forceinline__ Cand make_cand(double x, int64_t idx, int64_t n, int lanes) {
   Cand c;
   c.idx = idx;
-  const double ax = fabs(x);
+  const int64_t ab = __double_as_longlong(x) & INT64_MAX;
+  const bool nan = ab > 0x7ff0000000000000LL;
   const int64_t small = lanes == 4 ? 16 : 8;
-  if (n < small) {  // scalar path, starts from max = -1.0
-    c.v = (ax >= 0.0) ? ax : -1.0;
+  if (n < small) {  // scalar path, starts from max = -1.0: any non-NaN qualifies
+    c.v = nan ? -1 : ab;
     c.key = idx;
     return c;
   }
-  const int64_t chunk = 4 * lanes;
-  const int64_t nch = n / chunk;
-  const int64_t nv = nch * chunk;
-  c.v = (ax > 0.0) ? ax : -1.0;  // vector body and tail start from max = 0.0
+  // vector body and tail start from max = 0.0; chunk = 4 * lanes (8 or 16)
+  const int sl = lanes == 4 ? 2 : 1, sc = sl + 2;
+  const int64_t nch = n >> sc;
+  const int64_t nv = nch << sc;
+  c.v = (nan || ab == 0) ? -1 : ab;
   if (idx < nv) {
-    const int64_t r = idx % chunk;
-    const int64_t lane = r % lanes, acc = r / lanes;
-    c.key = (lane * 4 + acc) * nch + idx / chunk;
+    const int64_t r = idx & ((1 << sc) - 1);
+    const int64_t lane = r & (lanes - 1), acc = r >> sl;
+    c.key = (lane * 4 + acc) * nch + (idx >> sc);
   } else {
     c.key = idx;
   }
@@ -205,7 +223,7 @@ __device__ __forceinline__ Cand make_cand(double x, int64_t idx, int64_t n, int 
 }
 __device__ __forceinline__ Cand cand_none() {
   Cand c;
-  c.v = -2.0;
+  c.v = -2;
   c.key = INT64_MAX;
   c.idx = 0;
   return c;

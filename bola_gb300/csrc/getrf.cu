@@ -31,7 +31,7 @@ constexpr int MAXC = 16;  // largest cluster (non-portable size on sm_103)
 constexpr size_t SMEM_DATA_LIMIT = 200 * 1024;
 
 struct PanelPub {  // what a CTA publishes to the rest of the cluster each column
-  double v;
+  int64_t v;
   int64_t key;
   int64_t g;  // panel row of this CTA's best candidate, -1 if none
   double best_row[PNB];
@@ -39,7 +39,8 @@ struct PanelPub {  // what a CTA publishes to the rest of the cluster each colum
 };
 
 constexpr size_t panel_base_bytes() {
-  return 2 * sizeof(PanelPub) + (PT / 32) * sizeof(Cand) + PNB * sizeof(double) + 4 * sizeof(int64_t);
+  return 2 * sizeof(PanelPub) + (PT / 32) * sizeof(Cand) + PNB * sizeof(double) + 4 * sizeof(int64_t) +
+         2 * sizeof(double);
 }
 
 // Unblocked LU of an mp x nb panel (nb <= 32), iterative_getrf2 of
@@ -57,7 +58,8 @@ panel_lu(double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_t *inf
   Cand *red = reinterpret_cast<Cand *>(pub + 2);
   double *prow = reinterpret_cast<double *>(red + PT / 32);
   int64_t *bc = reinterpret_cast<int64_t *>(prow + PNB);
-  double *data = reinterpret_cast<double *>(bc + 4);
+  double *pinv = reinterpret_cast<double *>(bc + 4);  // 1 / pivot of the current column
+  double *data = pinv + 2;
 
   // Uniform across the cluster: the only writer of *info in this kernel acts
   // after a cluster barrier that every CTA reaches after this read.
@@ -101,7 +103,7 @@ panel_lu(double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_t *inf
         if (cand_better(red[w], b)) b = red[w];
       my->v = b.v;
       my->key = b.key;
-      my->g = (b.v > -2.0) ? j + b.idx : -1;
+      my->g = (b.v > -2) ? j + b.idx : -1;
       bc[0] = my->g;
     }
     __syncthreads();
@@ -121,14 +123,16 @@ panel_lu(double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_t *inf
         c.idx = rp->g;
       }
       c = warp_best(c);
-      if (lane == 0) bc[1] = (c.v < 0.0) ? (int64_t)j : c.idx;  // idamax -> 0 when nothing qualifies
+      if (lane == 0) bc[1] = (c.v < 0) ? (int64_t)j : c.idx;  // idamax -> 0 when nothing qualifies
     }
     __syncthreads();
     const int64_t jp = bc[1];
     const int owner_j = (int)(j / R), owner_p = (int)(jp / R);
     if (tid < nb) {
       const PanelPub *src = cluster.map_shared_rank(my, jp == j ? owner_j : owner_p);
-      prow[tid] = (jp == j) ? src->row_j[tid] : src->best_row[tid];
+      const double v = (jp == j) ? src->row_j[tid] : src->best_row[tid];
+      prow[tid] = v;
+      if (tid == j) pinv[0] = 1.0 / v;  // once per CTA, not once per thread
     }
     __syncthreads();
     const double pv = prow[j];
@@ -149,7 +153,7 @@ panel_lu(double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_t *inf
     __syncthreads();
     // -- reciprocal scale (src/getrf2.rs:152-164) and rank-1 update (ger, src/ger.rs:28-61)
     if (j < mp - 1) {
-      const double inv = 1.0 / pv;
+      const double inv = pinv[0];
       const int64_t mr = mp - j - 1;
       const int64_t rows_vec = (mr / lanes) * lanes;
       const int ncols = nb - j - 1;
@@ -165,7 +169,7 @@ panel_lu(double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_t *inf
         for (int t = 0; t < n_unrolled; t += 2) {
           const int c0 = j + 1 + t;
           const double t0 = -prow[c0], t1 = -prow[c0 + 1];
-          if (t0 == 0.0 && t1 == 0.0) continue;
+          if (!nonzero64(t0) && !nonzero64(t1)) continue;
           double &a0 = el(il, c0);
           double &a1 = el(il, c0 + 1);
           a0 = vec ? fused(x, t0, a0) : add_prod(a0, t0, x);
@@ -174,7 +178,7 @@ panel_lu(double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_t *inf
         if (ncols % 2) {
           const int c = nb - 1;
           const double t = -prow[c];
-          if (t != 0.0) el(il, c) = add_prod(el(il, c), t, x);
+          if (nonzero64(t)) el(il, c) = add_prod(el(il, c), t, x);
         }
       }
     }
@@ -215,7 +219,7 @@ panel_lu_wide(double *A, int64_t lda, int64_t m, int64_t n, int32_t *ipiv, int32
       Cand b = red[0];
       for (int w = 1; w < PT / 32; ++w)
         if (cand_better(red[w], b)) b = red[w];
-      sjp = (b.v < 0.0) ? j : j + b.idx;
+      sjp = (b.v < 0) ? j : j + b.idx;
       ipiv[j] = (int32_t)(sjp + 1);
     }
     __syncthreads();
@@ -249,12 +253,12 @@ panel_lu_wide(double *A, int64_t lda, int64_t m, int64_t n, int32_t *ipiv, int32
         if (ci < n_unrolled) {
           const int64_t p0 = j + 1 + (ci & ~(int64_t)1);
           const double t0 = -A[j + p0 * lda], t1 = -A[j + (p0 + 1) * lda];
-          if (t0 == 0.0 && t1 == 0.0) continue;
+          if (!nonzero64(t0) && !nonzero64(t1)) continue;
           const double t = (c == p0) ? t0 : t1;
           a = ri < rows_vec ? fused(x, t, a) : add_prod(a, t, x);
         } else {
           const double t = -A[j + c * lda];
-          if (t != 0.0) a = add_prod(a, t, x);
+          if (nonzero64(t)) a = add_prod(a, t, x);
         }
       }
     }
@@ -303,7 +307,7 @@ step_swap_trsm(double *A, int64_t lda, int64_t n, int64_t j, int jb, const int32
   double b = lane < jb ? cp[j + lane] : 0.0;
   for (int k = 0; k < jb; ++k) {
     const double bk = __shfl_sync(0xffffffffu, b, k);
-    if (bk == 0.0) continue;
+    if (!nonzero64(bk)) continue;
     if (lane > k && lane < jb)
       b = daxpy_elem(b, -bk, L[lane + k * PNB], lane - k - 1, jb - k - 1, lanes);
   }
@@ -386,43 +390,37 @@ int getrf2_rec(cudaStream_t s, int64_t m, int64_t n, double *A, int64_t lda, int
 }
 
 // src/getrf.rs:37-101
-// Look-ahead resources of one blocked getrf: the high-priority stream for
-// panels, swaps and the next panel's columns, the low-priority stream for the
-// rest of each trailing update, events, and per-step snapshots of *info.
-// Kept in a per-device pool so that concurrent callers each take their own.
-struct GetrfLA {
-  cudaStream_t sp = nullptr, su = nullptr;
-  cudaEvent_t ev_in = nullptr, ev_sw = nullptr, ev_wide = nullptr, ev_done = nullptr;
-  int32_t *snap = nullptr;  // device int32[2]
-};
-std::mutex g_la_mu;
-std::vector<GetrfLA *> g_la_pool[64];
 
-GetrfLA *la_acquire() {
+// ---- look-ahead stream pool (shared by the blocked getrf and potrf) ----------
+namespace {
+std::mutex g_la_mu;
+std::vector<LookAhead *> g_la_pool[64];
+}  // namespace
+
+LookAhead *la_acquire() {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
   {
     std::lock_guard<std::mutex> lk(g_la_mu);
     auto &pool = g_la_pool[dev & 63];
     if (!pool.empty()) {
-      GetrfLA *la = pool.back();
+      LookAhead *la = pool.back();
       pool.pop_back();
       return la;
     }
   }
-  GetrfLA *la = new GetrfLA();
+  LookAhead *la = new LookAhead();
   int least = 0, greatest = 0;
   bool ok = cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess &&
             cudaStreamCreateWithPriority(&la->sp, cudaStreamNonBlocking, greatest) == cudaSuccess &&
             cudaStreamCreateWithPriority(&la->su, cudaStreamNonBlocking, least) == cudaSuccess &&
             cudaMalloc(&la->snap, 2 * sizeof(int32_t)) == cudaSuccess;
-  for (cudaEvent_t *e : {&la->ev_in, &la->ev_sw, &la->ev_wide, &la->ev_done})
-    ok = ok && cudaEventCreateWithFlags(e, cudaEventDisableTiming) == cudaSuccess;
+  for (cudaEvent_t &e : la->ev) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
   if (!ok) return nullptr;  // (leaks the partial set; only on a failing device)
   return la;
 }
 
-void la_release(GetrfLA *la) {
+void la_release(LookAhead *la) {
   int dev = 0;
   cudaGetDevice(&dev);
   std::lock_guard<std::mutex> lk(g_la_mu);
@@ -439,7 +437,7 @@ void la_release(GetrfLA *la) {
 // step k's update, which BOLA completes before factoring panel k+1.
 int getrf_blocked(cudaStream_t s, int64_t m, int64_t n, double *A, int64_t lda, int32_t *ipiv, int32_t *info) {
   const int64_t min_mn = imin(m, n);
-  GetrfLA *la = (m > 0 && n > 0 && PNB < min_mn) ? la_acquire() : nullptr;
+  LookAhead *la = (m > 0 && n > 0 && PNB < min_mn) ? la_acquire() : nullptr;
   if (!la) {
     {
       ProfScope prof(s, "info_init");
@@ -466,9 +464,9 @@ int getrf_blocked(cudaStream_t s, int64_t m, int64_t n, double *A, int64_t lda, 
   }
   int st = 0;
   auto run = [&]() -> int {
-    BOLA_TRY_CUDA(cudaEventRecord(la->ev_in, s));
-    BOLA_TRY_CUDA(cudaStreamWaitEvent(la->sp, la->ev_in, 0));
-    BOLA_TRY_CUDA(cudaStreamWaitEvent(la->su, la->ev_in, 0));
+    BOLA_TRY_CUDA(cudaEventRecord(la->ev[0], s));
+    BOLA_TRY_CUDA(cudaStreamWaitEvent(la->sp, la->ev[0], 0));
+    BOLA_TRY_CUDA(cudaStreamWaitEvent(la->su, la->ev[0], 0));
     {
       ProfScope prof(la->sp, "info_init");
       zero_i32<<<1, 1, 0, la->sp>>>(info);
@@ -478,7 +476,7 @@ int getrf_blocked(cudaStream_t s, int64_t m, int64_t n, double *A, int64_t lda, 
     for (int64_t j = 0, k = 0; j < min_mn; j += PNB, ++k) {
       const int jb = (int)imin(PNB, min_mn - j);
       BOLA_TRY(launch_panel(la->sp, A + j + j * lda, lda, m - j, jb, ipiv + j, info, (int32_t)j, (int32_t)j));
-      if (wide_pending) BOLA_TRY_CUDA(cudaStreamWaitEvent(la->sp, la->ev_wide, 0));
+      if (wide_pending) BOLA_TRY_CUDA(cudaStreamWaitEvent(la->sp, la->ev[2], 0));
       wide_pending = false;
       const int64_t others = n - jb;
       if (others > 0) {
@@ -497,17 +495,17 @@ int getrf_blocked(cudaStream_t s, int64_t m, int64_t n, double *A, int64_t lda, 
         int32_t *snap = la->snap + (k & 1);
         copy_i32<<<1, 1, 0, la->sp>>>(info, snap);
         BOLA_CHECK_LAUNCH();
-        BOLA_TRY_CUDA(cudaEventRecord(la->ev_sw, la->sp));
-        BOLA_TRY_CUDA(cudaStreamWaitEvent(la->su, la->ev_sw, 0));
+        BOLA_TRY_CUDA(cudaEventRecord(la->ev[1], la->sp));
+        BOLA_TRY_CUDA(cudaStreamWaitEvent(la->su, la->ev[1], 0));
         BOLA_TRY(dgemm_exact(la->su, 'N', 'N', m2, n2 - nb_next, jb, -1.0, A21, lda, A12 + nb_next * lda, lda, 1.0,
                              A22 + nb_next * lda, lda, 64, snap, 0));
-        BOLA_TRY_CUDA(cudaEventRecord(la->ev_wide, la->su));
+        BOLA_TRY_CUDA(cudaEventRecord(la->ev[2], la->su));
         wide_pending = true;
       }
     }
-    if (wide_pending) BOLA_TRY_CUDA(cudaStreamWaitEvent(la->sp, la->ev_wide, 0));
-    BOLA_TRY_CUDA(cudaEventRecord(la->ev_done, la->sp));
-    BOLA_TRY_CUDA(cudaStreamWaitEvent(s, la->ev_done, 0));
+    if (wide_pending) BOLA_TRY_CUDA(cudaStreamWaitEvent(la->sp, la->ev[2], 0));
+    BOLA_TRY_CUDA(cudaEventRecord(la->ev[3], la->sp));
+    BOLA_TRY_CUDA(cudaStreamWaitEvent(s, la->ev[3], 0));
     return 0;
   };
   st = run();

@@ -42,7 +42,7 @@ __global__ void idamax_pass2(int64_t nc, const Cand *__restrict__ in, int64_t *r
     best = (l < (int)(blockDim.x >> 5)) ? sh[l] : cand_none();
     best = warp_best(best);
     // BOLA returns index 0 when nothing beats its starting maximum.
-    if (l == 0) *result = best.v < 0.0 ? 0 : best.idx;
+    if (l == 0) *result = best.v < 0 ? 0 : best.idx;
   }
 }
 
@@ -73,12 +73,12 @@ __global__ void ger_kernel(int64_t m, int64_t n, double alpha, const double *__r
     const int64_t j0 = j & ~(int64_t)1;
     const double t0 = __dmul_rn(alpha, y[j0 * ldy]);
     const double t1 = __dmul_rn(alpha, y[(j0 + 1) * ldy]);
-    if (t0 == 0.0 && t1 == 0.0) return;
+    if (!nonzero64(t0) && !nonzero64(t1)) return;
     const double t = (j == j0) ? t0 : t1;
     *ap = (i < rows_vec) ? fused(x[i], t, *ap) : add_prod(*ap, t, x[i]);
   } else {
     const double t = __dmul_rn(alpha, y[j * ldy]);
-    if (t != 0.0) *ap = add_prod(*ap, t, x[i]);
+    if (nonzero64(t)) *ap = add_prod(*ap, t, x[i]);
   }
 }
 

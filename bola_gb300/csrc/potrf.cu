@@ -74,7 +74,7 @@ syrk_diag(bool upper, bool trans_t, int64_t n, int64_t k, double alpha, const do
     if (!trans_t) {
       const double tv = ii < pb ? __dmul_rn(alpha, sA[ii][jj]) : 0.0;
       tl[ii] = tv;
-      nz = __ballot_sync(0xffffffffu, tv != 0.0);
+      nz = __ballot_sync(0xffffffffu, nonzero64(tv));
     }
     __syncthreads();
     if (p0 + NB < k) fetch(p0 + NB);
@@ -105,7 +105,11 @@ constexpr int LDS = NB;
 // trailing half) walked with an explicit stack: device recursion would need
 // more per-thread stack than the default.  Every thread runs the same walk.
 // Returns 0 or the 1-based failing column inside the block.
-__device__ int p2_walk(bool upper, double *a0, int n, int lanes) {
+//
+// 'L': the reciprocal of each diagonal element, which the trsm of every
+// enclosing level multiplies by, is formed once, by the thread that takes
+// the square root, into rdg (indexed by the element's position in the block).
+__device__ int p2_walk(bool upper, double *a0, double *rdg, int n, int lanes) {
   struct Frame {
     int off, n, phase;
   };
@@ -124,7 +128,11 @@ __device__ int p2_walk(bool upper, double *a0, int n, int lanes) {
       const double a11 = a[0];
       __syncthreads();
       if (!(a11 > 0.0)) return f.off + 1;
-      if (tid == 0) a[0] = sqrt(a11);
+      if (tid == 0) {
+        const double d = sqrt(a11);
+        a[0] = d;
+        if (!upper) rdg[f.off] = 1.0 / d;
+      }
       __syncthreads();
       --sp;
       continue;
@@ -167,9 +175,9 @@ __device__ int p2_walk(bool upper, double *a0, int n, int lanes) {
           double b = a21[tid + j * LDS];
           for (int k = 0; k < j; ++k) {
             const double ajk = a[j + k * LDS];
-            if (ajk != 0.0) b = sub_prod(b, ajk, a21[tid + k * LDS]);
+            if (nonzero64(ajk)) b = sub_prod(b, ajk, a21[tid + k * LDS]);
           }
-          b = __dmul_rn(b, 1.0 / a[j + j * LDS]);
+          b = __dmul_rn(b, rdg[f.off + j]);
           a21[tid + j * LDS] = b;
         }
       }
@@ -181,7 +189,7 @@ __device__ int p2_walk(bool upper, double *a0, int n, int lanes) {
         double c = a22[ii + jj * LDS];
         for (int l = 0; l < n1; ++l) {
           const double t = -a21[jj + l * LDS];
-          if (t != 0.0) c = daxpy_elem(c, t, a21[ii + l * LDS], ii - jj, n2 - jj, lanes);
+          if (nonzero64(t)) c = daxpy_elem(c, t, a21[ii + l * LDS], ii - jj, n2 - jj, lanes);
         }
         a22[ii + jj * LDS] = c;
       }
@@ -193,13 +201,17 @@ __device__ int p2_walk(bool upper, double *a0, int n, int lanes) {
   return 0;
 }
 
-__global__ void __launch_bounds__(256)
+// 128 threads: one warp per SMSP, so the SYRK steps' FP64 work never queues
+// two warps on one sub-partition's FP64 pipe.
+constexpr int P2T = 128;
+__global__ void __launch_bounds__(P2T)
 potrf2_block(bool upper, int n, double *A, int64_t lda, int32_t *info, int32_t col0, int lanes) {
   __shared__ double a[LDS * LDS];
+  __shared__ double rdg[LDS];
   if (stop_flag(info)) return;
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) a[(e % n) + (e / n) * LDS] = A[(e % n) + (e / n) * lda];
   __syncthreads();
-  const int r = p2_walk(upper, a, n, lanes);
+  const int r = p2_walk(upper, a, rdg, n, lanes);
   __syncthreads();
   // BOLA stops at the failing column with everything before it written back.
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) A[(e % n) + (e / n) * lda] = a[(e % n) + (e / n) * LDS];
@@ -235,7 +247,7 @@ int potrf2_rec(cudaStream_t s, char uplo, int64_t n, double *A, int64_t lda, int
   if (n == 0) return 0;
   if (n <= NB) {
     ProfScope prof(s, "potrf2_block", (double)n * n * n / 3.0);
-    potrf2_block<<<1, 256, 0, s>>>(upper, (int)n, A, lda, info, col0, lanes());
+    potrf2_block<<<1, P2T, 0, s>>>(upper, (int)n, A, lda, info, col0, lanes());
     BOLA_CHECK_LAUNCH();
     return 0;
   }
@@ -252,14 +264,75 @@ int potrf2_rec(cudaStream_t s, char uplo, int64_t n, double *A, int64_t lda, int
   return potrf2_rec(s, uplo, n2, a22, lda, info, col0 + (int32_t)n1);
 }
 
+namespace {
+
+// One launch of the diagonal-block chain advance: the diagonal blocks of the
+// nt x nt trailing matrix at C advance over the 32 columns (rows for 'U') at
+// src.
+int advance_diag(cudaStream_t s, bool upper, int64_t nt, const double *src, int64_t lda, double *C, int lan,
+                 const int32_t *info) {
+  if (nt <= 0) return 0;
+  ProfScope prof(s, "syrk_diag", (double)NB * (NB + 1) * (double)NB * (double)cdiv(nt, NB));
+  syrk_diag<<<dim3(NB, (unsigned)cdiv(nt, NB)), NB, 0, s>>>(upper, upper, nt, NB, -1.0, src, lda, C, lda, lan, info);
+  BOLA_CHECK_LAUNCH();
+  return 0;
+}
+
+// The 64-deep chunk starting at column (row, for 'U') c0 applied to the block
+// column (row) at t and the rows below it (columns right of it): one block
+// column wide.
+int chunk_narrow(cudaStream_t s, bool upper, int64_t n, int64_t c0, int64_t t, double *A, int64_t lda,
+                 const int32_t *info) {
+  const int64_t below = n - t - NB;
+  if (below <= 0) return 0;
+  if (upper)
+    return dgemm_exact(s, 'T', 'N', NB, below, 2 * NB, -1.0, A + c0 + t * lda, lda, A + c0 + (t + NB) * lda, lda, 1.0,
+                       A + t + (t + NB) * lda, lda, 64, info, 0);
+  return dgemm_exact(s, 'N', 'T', below, NB, 2 * NB, -1.0, A + (t + NB) + c0 * lda, lda, A + t + c0 * lda, lda, 1.0,
+                     A + (t + NB) + t * lda, lda, 64, info, 0);
+}
+
+// The same chunk on every block column (row) from t on: block-triangular.
+int chunk_wide(cudaStream_t s, bool upper, int64_t n, int64_t c0, int64_t t, double *A, int64_t lda,
+               const int32_t *info) {
+  const int64_t nt = n - t;
+  if (nt <= NB) return 0;
+  if (upper)
+    return dgemm_exact(s, 'T', 'N', nt, nt, 2 * NB, -1.0, A + c0 + t * lda, lda, A + c0 + t * lda, lda, 1.0,
+                       A + t + t * lda, lda, 64, info, 1);
+  return dgemm_exact(s, 'N', 'T', nt, nt, 2 * NB, -1.0, A + t + c0 * lda, lda, A + t + c0 * lda, lda, 1.0,
+                     A + t + t * lda, lda, 64, info, 2);
+}
+
+// Block p's own work: potrf2 of its diagonal block, the half chunk [j-32, j)
+// of its GEMM when p is odd, and its triangular solve.
+int block_step(cudaStream_t s, bool upper, int64_t n, int64_t j, double *A, int64_t lda, int32_t *info) {
+  const int64_t jb = imin(NB, n - j), t = j + jb, n_rem = n - t;
+  double *ajj = A + j + j * lda;
+  BOLA_TRY(potrf2_rec(s, upper ? 'U' : 'L', jb, ajj, lda, info, (int32_t)j));
+  if (n_rem == 0) return 0;
+  const bool odd = (j / NB) & 1;
+  if (upper) {
+    if (odd)
+      BOLA_TRY(dgemm_exact(s, 'T', 'N', jb, n_rem, NB, -1.0, A + (j - NB) + j * lda, lda, A + (j - NB) + t * lda, lda,
+                           1.0, A + j + t * lda, lda, 64, info, 0));
+    return trsm_exact(s, 'L', 'U', 'T', 'N', jb, n_rem, 1.0, ajj, lda, A + j + t * lda, lda, info);
+  }
+  if (odd)
+    BOLA_TRY(dgemm_exact(s, 'N', 'T', n_rem, jb, NB, -1.0, A + t + (j - NB) * lda, lda, A + j + (j - NB) * lda, lda,
+                         1.0, A + t + j * lda, lda, 64, info, 0));
+  return trsm_exact(s, 'R', 'L', 'T', 'N', n_rem, jb, 1.0, ajj, lda, A + t + j * lda, lda, info);
+}
+
+}  // namespace
+
 // BOLA's left-looking Cholesky (src/potrf.rs:114-178) computes block column p
 // from all earlier columns at step p: a SYRK chain of length 32p for the
 // diagonal block and a GEMM with K = 32p for the rows below it, both one
 // after the other on the critical path.  Here the same sums are formed
 // right-looking, as soon as their inputs are final:
 //  - every element's SYRK chain runs in column order, so after block p is
-//    final all later diagonal blocks advance their chains by its 32 columns
-//    (one launch for all of them);
+//    final all later diagonal blocks advance their chains by its 32 columns;
 //  - BOLA's GEMM forms one 64-deep chunk at a time (c = fma(alpha, acc, c),
 //    chunks from k = 0), so when a chunk's 64 columns are final it is applied
 //    to every later block column in one block-triangular GEMM; a block whose
@@ -271,6 +344,14 @@ int potrf2_rec(cudaStream_t s, char uplo, int64_t n, double *A, int64_t lda, int
 // columns after the failing block untouched, so the lower (upper) part from
 // the failing block's first sub-diagonal row (column) on is restored from a
 // copy of A taken at entry.
+//
+// Look-ahead: the critical path (potrf2, half chunk, trsm of block p, then
+// the chain advance and chunk for block p+1 only) runs on a high-priority
+// stream; the advance of blocks >= p+2 and the chunk GEMM on block columns
+// >= p+2 run on a low-priority stream behind it.  Ordering: block p+1's
+// advance waits for the previous wide advance (the chains stay in column
+// order), and block p's half chunk / trsm wait for the last wide chunk that
+// covered block column p.
 __global__ void potrf_restore(bool upper, int64_t n, const double *__restrict__ bk, double *A, int64_t lda,
                               const int32_t *info) {
   const int32_t f = *info;
@@ -284,58 +365,89 @@ __global__ void potrf_restore(bool upper, int64_t n, const double *__restrict__ 
 }
 
 int potrf_blocked(cudaStream_t s, char uplo, int64_t n, double *A, int64_t lda, int32_t *info) {
-  {
-    ProfScope prof(s, "info_init");
-    zero_i32<<<1, 1, 0, s>>>(info);
+  if (NB >= n) {
+    {
+      ProfScope prof(s, "info_init");
+      zero_i32<<<1, 1, 0, s>>>(info);
+    }
+    BOLA_CHECK_LAUNCH();
+    return potrf2_rec(s, uplo, n, A, lda, info, 0);
   }
-  BOLA_CHECK_LAUNCH();
-  if (NB >= n) return potrf2_rec(s, uplo, n, A, lda, info, 0);
   const bool upper = uplo == 'U';
+  const int lan = lanes();
   Scratch bk;
   BOLA_TRY(bk.alloc((size_t)n * n * sizeof(double), s));
-  BOLA_TRY_CUDA(cudaMemcpy2DAsync(bk.as<double>(), (size_t)n * sizeof(double), A, (size_t)lda * sizeof(double),
-                                  (size_t)n * sizeof(double), (size_t)n, cudaMemcpyDeviceToDevice, s));
-  const int lan = lanes();
-  for (int64_t j = 0; j < n; j += NB) {
-    const int64_t jb = imin(NB, n - j), t = j + jb, n_rem = n - t;
-    const bool odd = (j / NB) & 1;
-    double *ajj = A + j + j * lda;
-    BOLA_TRY(potrf2_rec(s, uplo, jb, ajj, lda, info, (int32_t)j));
-    if (n_rem == 0) break;
-    if (upper) {
-      if (odd)  // the half chunk [j - 32, j) of this block's GEMM
-        BOLA_TRY(dgemm_exact(s, 'T', 'N', jb, n_rem, NB, -1.0, A + (j - NB) + j * lda, lda, A + (j - NB) + t * lda,
-                             lda, 1.0, A + j + t * lda, lda, 64, info, 0));
-      BOLA_TRY(trsm_exact(s, 'L', 'U', 'T', 'N', jb, n_rem, 1.0, ajj, lda, A + j + t * lda, lda, info));
-    } else {
-      if (odd)
-        BOLA_TRY(dgemm_exact(s, 'N', 'T', n_rem, jb, NB, -1.0, A + t + (j - NB) * lda, lda, A + j + (j - NB) * lda,
-                             lda, 1.0, A + t + j * lda, lda, 64, info, 0));
-      BOLA_TRY(trsm_exact(s, 'R', 'L', 'T', 'N', n_rem, jb, 1.0, ajj, lda, A + t + j * lda, lda, info));
+  LookAhead *la = la_acquire();
+  cudaStream_t sp = la ? la->sp : s, su = la ? la->su : s;
+  auto on = [&](cudaEvent_t e, cudaStream_t from, cudaStream_t to) -> int {
+    if (!la || from == to) return 0;
+    BOLA_TRY_CUDA(cudaEventRecord(e, from));
+    BOLA_TRY_CUDA(cudaStreamWaitEvent(to, e, 0));
+    return 0;
+  };
+  auto run = [&]() -> int {
+    if (la) {
+      BOLA_TRY_CUDA(cudaEventRecord(la->ev[0], s));
+      BOLA_TRY_CUDA(cudaStreamWaitEvent(sp, la->ev[0], 0));
+      BOLA_TRY_CUDA(cudaStreamWaitEvent(su, la->ev[0], 0));
     }
-    {  // later diagonal blocks: chains advance over columns [j, j + 32)
-      ProfScope prof(s, "syrk_diag", (double)NB * (NB + 1) * (double)NB * (double)cdiv(n_rem, NB));
-      const double *src = upper ? A + j + t * lda : A + t + j * lda;
-      syrk_diag<<<dim3(NB, (unsigned)cdiv(n_rem, NB)), NB, 0, s>>>(upper, upper, n_rem, NB, -1.0, src, lda,
-                                                                  A + t + t * lda, lda, lan, info);
-      BOLA_CHECK_LAUNCH();
+    {
+      ProfScope prof(sp, "info_init");
+      zero_i32<<<1, 1, 0, sp>>>(info);
     }
-    if (odd) {  // chunk [j - 32, j + 32) is final: apply it to every later block column
-      const int64_t c0 = j - NB;
-      if (upper)
-        BOLA_TRY(dgemm_exact(s, 'T', 'N', n_rem, n_rem, 2 * NB, -1.0, A + c0 + t * lda, lda, A + c0 + t * lda, lda,
-                             1.0, A + t + t * lda, lda, 64, info, 1));
-      else
-        BOLA_TRY(dgemm_exact(s, 'N', 'T', n_rem, n_rem, 2 * NB, -1.0, A + t + c0 * lda, lda, A + t + c0 * lda, lda,
-                             1.0, A + t + t * lda, lda, 64, info, 2));
+    BOLA_CHECK_LAUNCH();
+    BOLA_TRY_CUDA(cudaMemcpy2DAsync(bk.as<double>(), (size_t)n * sizeof(double), A, (size_t)lda * sizeof(double),
+                                    (size_t)n * sizeof(double), (size_t)n, cudaMemcpyDeviceToDevice, sp));
+    // events: ev[1] critical part of step q done; ev[2 + (q & 1)] wide advance of
+    // step q done; ev[4 + ((q >> 1) & 1)] wide chunk of odd step q done
+    bool syrk_pending = false;
+    int64_t last_wide = -1;  // the last odd step whose wide chunk was issued
+    for (int64_t j = 0, q = 0; j < n; j += NB, ++q) {
+      const int64_t t = j + NB, n_rem = n - t;
+      // block column q last got a wide chunk from odd step q-2 (q odd) or q-3 (q even)
+      const int64_t need = (q & 1) ? q - 2 : q - 3;
+      if (la && need >= 1 && need <= last_wide)
+        BOLA_TRY_CUDA(cudaStreamWaitEvent(sp, la->ev[4 + ((need >> 1) & 1)], 0));
+      BOLA_TRY(block_step(sp, upper, n, j, A, lda, info));
+      if (n_rem <= 0) break;
+      if (la && syrk_pending) BOLA_TRY_CUDA(cudaStreamWaitEvent(sp, la->ev[2 + ((q - 1) & 1)], 0));
+      const double *src_n = upper ? A + j + t * lda : A + t + j * lda;
+      BOLA_TRY(advance_diag(sp, upper, imin(NB, n_rem), src_n, lda, A + t + t * lda, lan, info));
+      const bool odd = q & 1;
+      if (odd) BOLA_TRY(chunk_narrow(sp, upper, n, j - NB, t, A, lda, info));
+      syrk_pending = false;
+      if (n_rem > NB) {
+        BOLA_TRY(on(la ? la->ev[1] : nullptr, sp, su));
+        const int64_t t2 = t + NB;
+        const double *src_w = upper ? A + j + t2 * lda : A + t2 + j * lda;
+        BOLA_TRY(advance_diag(su, upper, n_rem - NB, src_w, lda, A + t2 + t2 * lda, lan, info));
+        if (la) BOLA_TRY_CUDA(cudaEventRecord(la->ev[2 + (q & 1)], su));
+        syrk_pending = true;
+        if (odd) {
+          BOLA_TRY(chunk_wide(su, upper, n, j - NB, t2, A, lda, info));
+          if (la) BOLA_TRY_CUDA(cudaEventRecord(la->ev[4 + ((q >> 1) & 1)], su));
+          last_wide = q;
+        }
+      }
     }
+    BOLA_TRY(on(la ? la->ev[6] : nullptr, su, sp));
+    {
+      ProfScope prof(sp, "potrf_restore");
+      potrf_restore<<<2 * (unsigned)num_sms(), 256, 0, sp>>>(upper, n, bk.as<double>(), A, lda, info);
+    }
+    BOLA_CHECK_LAUNCH();
+    BOLA_TRY(on(la ? la->ev[7] : nullptr, sp, s));
+    return 0;
+  };
+  const int st = run();
+  if (la) {
+    if (st != 0) {  // leave nothing of this call running on the look-ahead streams
+      cudaStreamSynchronize(la->sp);
+      cudaStreamSynchronize(la->su);
+    }
+    la_release(la);
   }
-  {
-    ProfScope prof(s, "potrf_restore");
-    potrf_restore<<<2 * (unsigned)num_sms(), 256, 0, s>>>(upper, n, bk.as<double>(), A, lda, info);
-  }
-  BOLA_CHECK_LAUNCH();
-  return 0;
+  return st;
 }
 
 }  // namespace bola

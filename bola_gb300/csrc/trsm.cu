@@ -50,11 +50,11 @@ left_n_base(int m, int64_t n, bool unit, const double *__restrict__ A, int64_t l
   for (int step = 0; step < m; ++step) {
     const int k = LOWER ? step : m - 1 - step;
     const double bk = __shfl_sync(0xffffffffu, k < 32 ? b0 : b1, k & 31);
-    if (bk == 0.0) continue;  // BOLA skips zero entries (src/trsm.rs:101,141)
+    if (!nonzero64(bk)) continue;  // BOLA skips zero entries (src/trsm.rs:101,141)
     const double u = unit ? bk : bk / sA[k + k * STOP];
     if (k == lane) b0 = u;
     if (k == lane + 32) b1 = u;
-    if (u == 0.0) continue;  // daxpy returns early for a zero scale (src/utilities.rs:108)
+    if (!nonzero64(u)) continue;  // daxpy returns early for a zero scale (src/utilities.rs:108)
     // daxpy over rows k+1..m-1 (lower) or 0..k-1 (upper) with alpha = -u
     const int64_t len = LOWER ? (int64_t)(m - k - 1) : (int64_t)k;
 #pragma unroll
@@ -111,30 +111,54 @@ left_t_base(int m, int64_t n, bool unit, const double *__restrict__ A, int64_t l
 }
 
 // Right side base cases (src/trsm.rs:253-273, 285-305, 317-337, 349-369).
-// V: 0 = rnl, 1 = rnu, 2 = rtl, 3 = rtu.
+// V: 0 = rnl, 1 = rnu, 2 = rtl, 3 = rtu.  A thread per row of B: the CTA's
+// rows of B and the triangle are staged in shared memory (the row chains then
+// never wait on global loads), and the reciprocals of the diagonal, which
+// every row multiplies by, are formed once per CTA.
+constexpr int RB_ROWS = 128;
+
+inline size_t right_base_smem(int n) { return ((size_t)n * n + n + (size_t)RB_ROWS * n) * sizeof(double); }
+
 template <int V>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(RB_ROWS)
 right_base(int64_t m, int n, bool unit, const double *__restrict__ A, int64_t lda, double *B,
            int64_t ldb, const int32_t *info) {
-  __shared__ double sA[STOP * STOP];
+  extern __shared__ double rb_smem[];
+  double *sA = rb_smem;      // n x n, ld n
+  double *rd = sA + n * n;   // 1 / a(j, j)
+  double *sB = rd + n;       // column k of the CTA's rows at sB[k * RB_ROWS]
   if (stop_flag(info)) return;
-  load_tri(sA, A, lda, n);
+  const int64_t i0 = (int64_t)blockIdx.x * RB_ROWS;
+  const int rows = (int)imin(RB_ROWS, m - i0);
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) sA[e] = A[(e % n) + (int64_t)(e / n) * lda];
+  for (int e = threadIdx.x; e < RB_ROWS * n; e += blockDim.x) {
+    const int r = e % RB_ROWS, k = e / RB_ROWS;
+    sB[e] = r < rows ? B[(i0 + r) + (int64_t)k * ldb] : 0.0;
+  }
   __syncthreads();
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m) return;
+  if (!unit && threadIdx.x < n) rd[threadIdx.x] = 1.0 / sA[threadIdx.x * (n + 1)];
+  __syncthreads();
   constexpr bool descending = (V == 0 || V == 3);
-  for (int step = 0; step < n; ++step) {
-    const int j = descending ? n - 1 - step : step;
-    double bj = B[i + j * ldb];
-    const int k0 = descending ? j + 1 : 0;
-    const int k1 = descending ? n : j;
-    for (int k = k0; k < k1; ++k) {
-      // rnl/rnu read a(k, j); rtl/rtu read a(j, k)
-      const double akj = (V <= 1) ? sA[k + j * STOP] : sA[j + k * STOP];
-      if (akj != 0.0) bj = sub_prod(bj, akj, B[i + k * ldb]);
+  if (threadIdx.x < rows) {
+    double *b = sB + threadIdx.x;
+    for (int step = 0; step < n; ++step) {
+      const int j = descending ? n - 1 - step : step;
+      double bj = b[j * RB_ROWS];
+      const int k0 = descending ? j + 1 : 0;
+      const int k1 = descending ? n : j;
+      for (int k = k0; k < k1; ++k) {
+        // rnl/rnu read a(k, j); rtl/rtu read a(j, k)
+        const double akj = (V <= 1) ? sA[k + j * n] : sA[j + k * n];
+        if (nonzero64(akj)) bj = sub_prod(bj, akj, b[k * RB_ROWS]);
+      }
+      if (!unit) bj = __dmul_rn(bj, rd[j]);
+      b[j * RB_ROWS] = bj;
     }
-    if (!unit) bj = __dmul_rn(bj, 1.0 / sA[j + j * STOP]);
-    B[i + j * ldb] = bj;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < RB_ROWS * n; e += blockDim.x) {
+    const int r = e % RB_ROWS, k = e / RB_ROWS;
+    if (r < rows) B[(i0 + r) + (int64_t)k * ldb] = sB[e];
   }
 }
 
@@ -170,18 +194,75 @@ int base_left_t(const Ctx &c, bool lower, int64_t m, int64_t n, const double *A,
   return 0;
 }
 
+// The ascending right base cases (rnu, rtl) for n <= 32, right-looking with
+// the row in registers: once b_k is final it is subtracted from every later
+// column of the row, so each b_j still receives its updates in ascending k and
+// then its scale, exactly as in BOLA's column sweep, but a row's FP64
+// operations no longer form one dependent chain and keep the FP64 pipe full.
+constexpr int RA_ROWS = 64;
+
+template <int V>
+__global__ void __launch_bounds__(RA_ROWS)
+right_base_asc32(int64_t m, int n, bool unit, const double *__restrict__ A, int64_t lda, double *B, int64_t ldb,
+                 const int32_t *info) {
+  static_assert(V == 1 || V == 2, "ascending variants only");
+  __shared__ double sA[32 * 33];  // a(r, c) at sA[r + 33 c]
+  __shared__ double rd[32];
+  if (stop_flag(info)) return;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) sA[(e % n) + (e / n) * 33] = A[(e % n) + (int64_t)(e / n) * lda];
+  __syncthreads();
+  if (!unit && threadIdx.x < n) rd[threadIdx.x] = 1.0 / sA[threadIdx.x * 34];
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * RA_ROWS + threadIdx.x;
+  if (i >= m) return;
+  double b[32];
+#pragma unroll
+  for (int k = 0; k < 32; ++k) b[k] = k < n ? B[i + (int64_t)k * ldb] : 0.0;
+#pragma unroll
+  for (int k = 0; k < 32; ++k) {
+    if (k < n) {
+      if (!unit) b[k] = __dmul_rn(b[k], rd[k]);
+      const double bk = b[k];
+#pragma unroll
+      for (int j = k + 1; j < 32; ++j) {
+        if (j < n) {
+          const double a = (V == 1) ? sA[k + j * 33] : sA[j + k * 33];  // rnu: a(k, j); rtl: a(j, k)
+          const double u = sub_prod(b[j], a, bk);
+          b[j] = nonzero64(a) ? u : b[j];  // BOLA skips a zero a
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 32; ++k)
+    if (k < n) B[i + (int64_t)k * ldb] = b[k];
+}
+
+template <int V>
+int launch_right_base(const Ctx &c, int64_t m, int64_t n, const double *A, int64_t lda, double *B, int64_t ldb) {
+  if constexpr (V == 1 || V == 2) {
+    if (n <= 32) {
+      right_base_asc32<V><<<(unsigned)cdiv(m, RA_ROWS), RA_ROWS, 0, c.s>>>(m, (int)n, c.unit, A, lda, B, ldb, c.info);
+      BOLA_CHECK_LAUNCH();
+      return 0;
+    }
+  }
+  const size_t smem = right_base_smem((int)n);
+  if (smem > 48 * 1024) BOLA_TRY_CUDA(cudaFuncSetAttribute(right_base<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  right_base<V><<<(unsigned)cdiv(m, RB_ROWS), RB_ROWS, smem, c.s>>>(m, (int)n, c.unit, A, lda, B, ldb, c.info);
+  BOLA_CHECK_LAUNCH();
+  return 0;
+}
+
 int base_right(const Ctx &c, int v, int64_t m, int64_t n, const double *A, int64_t lda, double *B,
                int64_t ldb) {
   ProfScope prof(c.s, "trsm_base", (double)m * n * n);
-  const unsigned g = (unsigned)cdiv(m, 128);
   switch (v) {
-    case 0: right_base<0><<<g, 128, 0, c.s>>>(m, (int)n, c.unit, A, lda, B, ldb, c.info); break;
-    case 1: right_base<1><<<g, 128, 0, c.s>>>(m, (int)n, c.unit, A, lda, B, ldb, c.info); break;
-    case 2: right_base<2><<<g, 128, 0, c.s>>>(m, (int)n, c.unit, A, lda, B, ldb, c.info); break;
-    default: right_base<3><<<g, 128, 0, c.s>>>(m, (int)n, c.unit, A, lda, B, ldb, c.info); break;
+    case 0: return launch_right_base<0>(c, m, n, A, lda, B, ldb);
+    case 1: return launch_right_base<1>(c, m, n, A, lda, B, ldb);
+    case 2: return launch_right_base<2>(c, m, n, A, lda, B, ldb);
+    default: return launch_right_base<3>(c, m, n, A, lda, B, ldb);
   }
-  BOLA_CHECK_LAUNCH();
-  return 0;
 }
 
 int gemm_upd(const Ctx &c, char ta, char tb, int64_t m, int64_t n, int64_t k, const double *A, int64_t lda,

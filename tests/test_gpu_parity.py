@@ -225,6 +225,40 @@ def test_laswp_bitwise(gpu, oracle_lib, k1, k2, incx):
     assert np.array_equal(A1, A2)
 
 
+@pytest.mark.parametrize("n", [1, 5, 7, 8, 9, 15, 16, 17, 33, 70, 1000])
+def test_idamax_special_values(both, n):
+    """NaN is never selected, +-inf is, zeros only on the scalar path; ties
+    follow BOLA's lane order."""
+    g, o = both
+    rng = np.random.default_rng(n)
+    cases = [np.zeros(n), np.full(n, np.nan), np.full(n, -0.0), np.full(n, 3.0)]
+    x = rng.integers(-3, 4, size=n).astype(np.float64)
+    x[rng.integers(0, n, size=max(1, n // 5))] = np.nan
+    cases.append(x)
+    y = x.copy()
+    y[rng.integers(0, n)] = -np.inf
+    cases.append(y)
+    z = np.where(np.isnan(x), 0.0, x)
+    cases.append(z)
+    for v in cases:
+        assert g.idamax(v) == o.idamax(v), v
+
+
+def test_getrf_with_nan_and_inf_entries(both):
+    g, o = both
+    n = 70
+    A = wl.uniform_matrix(n, n, seed=5, lo=-1, hi=1)
+    A[10, 3] = np.nan
+    A[50, 40] = np.inf
+    A1, A2 = A.copy(order="F"), A.copy(order="F")
+    p1, p2 = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    r1 = o.getrf(n, n, A1, n, p1)
+    r2 = g.getrf(n, n, A2, n, p2)
+    assert (r1 == 0) == (r2 == 0)
+    assert np.array_equal(p1, p2)
+    assert same(A1, A2)
+
+
 def test_level1_bitwise(both):
     g, o = both
     for n in [1, 7, 8, 15, 16, 17, 100, 1001, 70000]:
