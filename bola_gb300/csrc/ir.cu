@@ -107,6 +107,7 @@ __global__ void compose_perm(int64_t n, const int32_t *ipiv, int32_t *perm) {
   if (threadIdx.x == 0) {
     for (int64_t i = 0; i < n; ++i) {
       const int32_t t = ipiv[i] - 1;
+      if (t < i || t >= n) continue;  // not a pivot LU can produce: never index outside p
       const int32_t v = p[i];
       p[i] = p[t];
       p[t] = v;
@@ -830,10 +831,24 @@ int dgesv_mixed_ws(Workspace &w, int64_t n, int64_t nrhs, const double *a, int64
     col_absmax<<<nr, 256, 0, s>>>(n, b, ldb, nrm + 2 * nr);
   }
   BOLA_CHECK_LAUNCH();
+  // The spread max|u_ii| / min|u_ii| of the low-precision U is a cheap lower
+  // bound on kappa(A).  Above a per-factor-kind limit neither refinement nor
+  // GMRES(24)-IR reaches 1e-14, so the FP64 path is taken at once (if
+  // allowed).  The limits sit at the geometric midpoints between the largest
+  // spread that converged and the smallest that did not, measured on
+  // n = 1024 and 4096 systems with geometric spectra and kappa 1e2/1e6/1e10:
+  // bf16 55 | 560, tf32 93 | 1.3e4, 3xTF32 3.6e3 | 5.5e5.  A wrong call costs
+  // time only: the refinement attempt before the fallback, or an FP64 solve
+  // where the mixed one would have done.  The FP64-accurate factor (kind 3)
+  // refines anything its pivots leave below ~1e13.  The spread only grows as
+  // pivots are added, so the factorisation itself gives up at the first panel
+  // that takes it over the limit, with the decision the whole factor would give.
+  const double limit = o.factor_kind == 0 ? 175.0 : o.factor_kind == 1 ? 1100.0 : o.factor_kind == 2 ? 4.5e4 : 1e13;
+  const double give_up = (o.fallback_fp64 || o.escalate) ? limit : INFINITY;
   if (fp64)
-    BOLA_TRY(w.lu.factor64(s, (double *)w.W, ldW, w.ipiv, w.info));
+    BOLA_TRY(w.lu.factor64(s, (double *)w.W, ldW, w.ipiv, w.info, give_up));
   else
-    BOLA_TRY(w.lu.factor(s, (float *)w.W, n, w.ipiv, w.info));
+    BOLA_TRY(w.lu.factor(s, (float *)w.W, n, w.ipiv, w.info, give_up));
   {
     ProfScope prof(s, "mixed_perm");
     compose_perm<<<1, 1024, sizeof(int32_t) * n, s>>>(n, w.ipiv, w.perm);
@@ -850,6 +865,8 @@ int dgesv_mixed_ws(Workspace &w, int64_t n, int64_t nrhs, const double *a, int64
   double ext[2] = {0.0, 0.0};
   BOLA_TRY_CUDA(cudaMemcpyAsync(ext, w.norms + 5 * MAXRHS, sizeof ext, cudaMemcpyDeviceToHost, s));
   int32_t finfo = 0, ferr = 0;
+  uint64_t trk[3] = {0, 0, 0};
+  BOLA_TRY_CUDA(cudaMemcpyAsync(trk, w.lu.track, sizeof trk, cudaMemcpyDeviceToHost, s));
   BOLA_TRY_CUDA(cudaMemcpyAsync(&finfo, w.info, sizeof finfo, cudaMemcpyDeviceToHost, s));
   BOLA_TRY_CUDA(cudaMemcpyAsync(&ferr, w.lu.err, sizeof ferr, cudaMemcpyDeviceToHost, s));
   BOLA_TRY_CUDA(cudaStreamSynchronize(s));
@@ -859,20 +876,17 @@ int dgesv_mixed_ws(Workspace &w, int64_t n, int64_t nrhs, const double *a, int64
   bool converged = false;
   double berr = INFINITY, prev = INFINITY;
   int path = 0;
-  // The spread max|u_ii| / min|u_ii| of the low-precision U is a cheap lower
-  // bound on kappa(A).  Above a per-factor-kind limit neither refinement nor
-  // GMRES(24)-IR reaches 1e-14, so the FP64 path is taken at once (if
-  // allowed).  The limits sit at the geometric midpoints between the largest
-  // spread that converged and the smallest that did not, measured on
-  // n = 1024 and 4096 systems with geometric spectra and kappa 1e2/1e6/1e10:
-  // bf16 55 | 560, tf32 93 | 1.3e4, 3xTF32 3.6e3 | 5.5e5.  A wrong call costs
-  // time only: the refinement attempt before the fallback, or an FP64 solve
-  // where the mixed one would have done.  The FP64-accurate factor (kind 3)
-  // refines anything its pivots leave below ~1e13.
-  const double limit = o.factor_kind == 0 ? 175.0 : o.factor_kind == 1 ? 1100.0 : o.factor_kind == 2 ? 4.5e4 : 1e13;
+  const bool gave_up = (uint32_t)trk[2] != 0 && !std::isinf(give_up);
+  if (gave_up) {  // the extent over the pivots reached (W beyond them is unfinished)
+    double mx, mn;
+    std::memcpy(&mx, &trk[0], sizeof mx);
+    std::memcpy(&mn, &trk[1], sizeof mn);
+    ext[0] = mx;
+    ext[1] = mn;
+  }
   const double spread = ext[1] > 0.0 ? ext[0] / ext[1] : INFINITY;
   info_out.condition_estimate = spread;
-  const bool hopeless = (o.fallback_fp64 || o.escalate) && !(spread < limit);
+  const bool hopeless = gave_up || ((o.fallback_fp64 || o.escalate) && !(spread < limit));
   if (finfo == 0 && !hopeless) {
     // x0 = correction of b (rscale = ||b||)
     BOLA_TRY(correction(s, w, n, nr, b, ldb, nrm + 2 * nr, x, ldx, true));

@@ -82,13 +82,24 @@ __device__ __forceinline__ void oz_split_pair(double v0, double v1, int lane, in
 // B (capB), exponents eA[m], eB[n]; *err set if a bounded wait expired.
 int oz_update(cudaStream_t s, int64_t m, int64_t n, const CUtensorMap &A, const CUtensorMap &B, int64_t capA,
               int64_t capB, const int32_t *eA, const int32_t *eB, double *W, int64_t ldw, int32_t *err,
-              int64_t boff = 0);
+              int64_t boff = 0, const int32_t *abort = nullptr);
 
 // W(m x n, column-major, ld ldw) -= A * B^T on tcgen05 (kind 0 bf16, 1 tf32,
 // 2 3xTF32 with the lo maps); *err is set non-zero if a bounded wait expired.
 // B's rows start at boff (a column offset into the trailing matrix).
 int tc_update(cudaStream_t s, int kind, int64_t m, int64_t n, const CUtensorMap &A, const CUtensorMap &B,
-              const CUtensorMap &Alo, const CUtensorMap &Blo, float *W, int64_t ldw, int32_t *err, int64_t boff = 0);
+              const CUtensorMap &Alo, const CUtensorMap &Blo, float *W, int64_t ldw, int32_t *err, int64_t boff = 0,
+              const int32_t *abort = nullptr);
+
+// A kernel of an abandoned factorisation returns at once: *abort is read by
+// one thread and the decision shared, so a CTA's barriers stay uniform even
+// while another stream sets the flag.
+__device__ __forceinline__ bool abandoned(const int32_t *abort) {
+  __shared__ int skip;
+  if (threadIdx.x == 0) skip = abort != nullptr && *(volatile const int32_t *)abort != 0;
+  __syncthreads();
+  return skip != 0;
+}
 
 // Buffers and tensor maps of the low-precision LU (slu.cu), reusable across
 // factorisations of size <= capacity.  The factorisation looks ahead: the
@@ -105,6 +116,9 @@ struct MixedLU {
   int32_t *ea[2] = {nullptr, nullptr}, *eb = nullptr;  // kind 3: row exponents of the sliced operands
   int32_t *err = nullptr;
   int32_t *plan = nullptr;  // the current panel's composed interchanges: count, rows[128], src[128]
+  // running extent of |u_ii| over the panels done: [0] max, [1] min (bits of
+  // non-negative doubles, ordered like the values), [2] low word = abandon flag
+  uint64_t *track = nullptr;
   CUtensorMap mapA[2], mapB, mapAlo[2], mapBlo;
   cudaStream_t sp = nullptr, su = nullptr;
   cudaEvent_t ev_in = nullptr, ev_sw = nullptr, ev_wide = nullptr, ev_done = nullptr;
@@ -112,9 +126,12 @@ struct MixedLU {
   void release(cudaStream_t s);  // frees the buffers (stream-ordered on s)
   void destroy();                // the streams and events too (device idle)
   // LU with partial pivoting of the FP32 matrix W (n x n, ld ldw) in place (kinds 0-2).
-  int factor(cudaStream_t s, float *W, int64_t ldw, int32_t *ipiv, int32_t *info);
+  // give_up: the factorisation is abandoned (its kernels return at once) as
+  // soon as max|u_ii| / min|u_ii| over the pivots so far is not below it;
+  // INFINITY never gives up.  abandoned() on the host tells afterwards.
+  int factor(cudaStream_t s, float *W, int64_t ldw, int32_t *ipiv, int32_t *info, double give_up = INFINITY);
   // The same for an FP64 W (kind 3).
-  int factor64(cudaStream_t s, double *W, int64_t ldw, int32_t *ipiv, int32_t *info);
+  int factor64(cudaStream_t s, double *W, int64_t ldw, int32_t *ipiv, int32_t *info, double give_up = INFINITY);
 };
 
 }  // namespace bola

@@ -51,8 +51,9 @@ __device__ __forceinline__ PKey pk_make(float v, int g) {
   return PKey{v == v ? __float_as_uint(v) : 0u, 0u, 0xFFFFFFFFu - (uint32_t)g};
 }
 __device__ __forceinline__ PKey pk_make(double v, int g) {
-  v = fabs(v);
-  const uint64_t u = v == v ? (uint64_t)__double_as_longlong(v) : 0ull;
+  // |v| and the NaN test on the bits: an FP64 comparison would take an FP64 pipe slot
+  uint64_t u = (uint64_t)__double_as_longlong(v) & 0x7fffffffffffffffull;
+  u = u > 0x7ff0000000000000ull ? 0ull : u;
   return PKey{(uint32_t)(u >> 32), (uint32_t)u, 0xFFFFFFFFu - (uint32_t)g};
 }
 __device__ __forceinline__ PKey pk_warp_max(const PKey &k) {
@@ -79,6 +80,12 @@ struct PanelF32 {
   __device__ static S recip(S p) { return p == 0.f ? 0.f : 1.0f / p; }
   __device__ static PKey key(S v, int g) { return pk_make(v, g); }
   __device__ static double to_double(S v) { return (double)v; }
+  // |v| as bits ordered like |v|; NaN above +inf
+  __device__ static uint64_t abs_bits(S v) { return __float_as_uint(v) & 0x7fffffffu; }
+  __device__ static bool is_nan_bits(uint64_t b) { return b > 0x7f800000u; }
+  __device__ static uint64_t bits_to_double_bits(uint64_t b) {
+    return (uint64_t)__double_as_longlong((double)__uint_as_float((uint32_t)b));
+  }
 };
 
 struct PanelF64 {
@@ -90,10 +97,13 @@ struct PanelF64 {
   __device__ static G store(S x) { return x; }
   __device__ static S mul(S a, S b) { return a * b; }
   __device__ static S fnms(S z, S x, S y) { return fma(-x, y, z); }
-  __device__ static bool is_zero(S p) { return p == 0.0; }
-  __device__ static S recip(S p) { return p == 0.0 ? 0.0 : 1.0 / p; }
+  __device__ static bool is_zero(S p) { return !nonzero64(p); }
+  __device__ static S recip(S p) { return nonzero64(p) ? 1.0 / p : 0.0; }
   __device__ static PKey key(S v, int g) { return pk_make(v, g); }
   __device__ static double to_double(S v) { return v; }
+  __device__ static uint64_t abs_bits(S v) { return (uint64_t)__double_as_longlong(v) & 0x7fffffffffffffffull; }
+  __device__ static bool is_nan_bits(uint64_t b) { return b > 0x7ff0000000000000ull; }
+  __device__ static uint64_t bits_to_double_bits(uint64_t b) { return b; }
 };
 
 
@@ -183,8 +193,18 @@ __device__ __forceinline__ void cluster_wait() {
 template <typename P>
 __global__ void __launch_bounds__(SPT)
 spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0, int32_t *info, int kind,
-              void *aop, float *aop_lo, int32_t *aexp, int64_t cap, int64_t R, int32_t *plan) {
+              void *aop, float *aop_lo, int32_t *aexp, int64_t cap, int64_t R, int32_t *plan, uint64_t *track,
+              double give_up) {
   cg::cluster_group cluster = cg::this_cluster();
+  // An abandoned factorisation: the flag was set by an earlier panel on this
+  // stream, so every CTA of the cluster reads the same value.  Identity
+  // pivots keep ipiv valid for the kernels after the factorisation that
+  // compose it (the factor itself is discarded).
+  if (track != nullptr && *(volatile const int32_t *)(track + 2) != 0) {
+    if (cluster.block_rank() == 0)
+      for (int t = threadIdx.x; t < jb; t += blockDim.x) ipiv[t] = col0 + t + 1;
+    return;
+  }
   const int C = (int)cluster.num_blocks();
   const int cr = (int)cluster.block_rank();
   using T = typename P::S;
@@ -193,6 +213,7 @@ spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, 
   __shared__ T piv[2][SNB];   // pivot rows, up to date (piv[par] = column j's)
   __shared__ T oldj[SNB];     // the old row j, up to date (goes to the pivot's place)
   __shared__ PKey wkey[SPT / 32];
+  __shared__ T sinv;          // 1 / pivot of the current column
   extern __shared__ __align__(16) unsigned char sp_raw[];
   T *sp = reinterpret_cast<T *>(sp_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -213,6 +234,9 @@ spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, 
   cluster.sync();  // every CTA of the cluster is running before the first push
 
   T inv = P::zero();  // 1 / pivot of the previous column
+  // |u_jj| of this panel's pivots as ordered integer bits (NaN ignored, as
+  // fmax/fmin ignore it): thread 0 of CTA 0 only, on the integer pipe
+  uint64_t umax = 0, umin = ~0ull;
   for (int j = 0; j < jb; ++j) {
     const int par = j & 1;
     const T *pprev = piv[par ^ 1];
@@ -319,11 +343,19 @@ spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, 
       }
       pcur[tid] = pv_;
       oldj[tid] = ov;
+      if (tid == j) sinv = P::recip(pv_);  // once per CTA, not once per thread
     }
     __syncthreads();
     const T pv = pcur[j];
-    if (cr == 0 && tid == 0) ipiv[j] = col0 + jp + 1;
-    inv = P::recip(pv);
+    if (cr == 0 && tid == 0) {
+      ipiv[j] = col0 + jp + 1;
+      const uint64_t ab = P::abs_bits(pv);
+      if (!P::is_nan_bits(ab)) {
+        umax = ab > umax ? ab : umax;
+        umin = ab < umin ? ab : umin;
+      }
+    }
+    inv = sinv;
     if (P::is_zero(pv)) {
       if (cr == 0 && tid == 0) atomicCAS(info, 0, col0 + j + 1);
     }
@@ -347,6 +379,18 @@ spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, 
   for (int il = tid; il < nr; il += SPT)
     if (r0 + il >= jb) PE(jb - 1, il) = P::mul(PE(jb - 1, il), inv);
   __syncthreads();
+  if (track != nullptr && cr == 0 && tid == 0) {
+    // the running extent of |u_ii| and the give-up test (the spread only grows
+    // as pivots are added, so giving up early decides as the whole factor would)
+    if (umin != ~0ull) {
+      const uint64_t mx = P::bits_to_double_bits(umax), mn = P::bits_to_double_bits(umin);
+      if (mx > track[0]) track[0] = mx;
+      if (mn < track[1]) track[1] = mn;
+    }
+    const double gmx = __longlong_as_double((long long)track[0]), gmn = __longlong_as_double((long long)track[1]);
+    const double spread = gmn > 0.0 ? gmx / gmn : INFINITY;
+    if (!(spread < give_up)) *(volatile int32_t *)(track + 2) = 1;
+  }
 
   // -- write back the panel and the update's A operand (rows below the panel)
   for (int64_t e = tid; e < (int64_t)ns * jb; e += SPT) {
@@ -411,7 +455,8 @@ spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, 
 template <typename T>
 __global__ void __launch_bounds__(256)
 sswap_trsm(T *W, int64_t ldw, int64_t n, int64_t j, int jb, const int32_t *plan, int kind, void *bop,
-           float *bop_lo, int32_t *bexp, int64_t cap) {
+           float *bop_lo, int32_t *bexp, int64_t cap, const int32_t *abort) {
+  if (abort != nullptr && *(volatile const int32_t *)abort != 0) return;  // set before this launch (same stream)
   __shared__ int32_t rows[2 * SNB], src[2 * SNB];
   __shared__ T L[SNB * SNB];
   __shared__ int cnt;
@@ -466,10 +511,16 @@ sswap_trsm(T *W, int64_t ldw, int64_t n, int64_t j, int jb, const int32_t *plan,
 }
 
 __global__ void zero_i32(int32_t *p) { *p = 0; }
+__global__ void track_init(uint64_t *t) {
+  t[0] = 0;                       // max |u_ii| = +0
+  t[1] = 0x7ff0000000000000ull;   // min |u_ii| = +inf
+  t[2] = 0;                       // not abandoned
+}
 
 template <typename P>
 int launch_spanel(cudaStream_t s, typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0,
-                  int32_t *info, int kind, void *aop, float *aop_lo, int32_t *aexp, int64_t cap, int32_t *plan) {
+                  int32_t *info, int kind, void *aop, float *aop_lo, int32_t *aexp, int64_t cap, int32_t *plan,
+                  uint64_t *track, double give_up) {
   const int C = (int)imin(SMAXC, imax(1, cdiv(mp, SPT)));
   const int64_t R = cdiv(mp, C);
   const size_t smem = sizeof(typename P::S) * (size_t)jb * (size_t)panel_pitch<typename P::S>(R);
@@ -495,7 +546,7 @@ int launch_spanel(cudaStream_t s, typename P::G *W, int64_t ldw, int64_t mp, int
   ProfScope prof(s, P::kFP64 ? "spanel64" : "spanel", (double)mp * jb * jb,
                  2.0 * sizeof(typename P::G) * (double)mp * jb);
   BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, spanel_kernel<P>, W, ldw, mp, jb, ipiv, col0, info, kind, aop, aop_lo, aexp,
-                                   cap, R, plan));
+                                   cap, R, plan, track, give_up));
   return 0;
 }
 
@@ -519,6 +570,7 @@ int MixedLU::reserve(int64_t n_, int kind_, cudaStream_t s) {
   kind = kind_;
   BOLA_TRY_CUDA(cudaMallocAsync(&err, sizeof(int32_t), s));
   BOLA_TRY_CUDA(cudaMallocAsync(&plan, sizeof(int32_t) * (1 + 4 * SNB), s));
+  BOLA_TRY_CUDA(cudaMallocAsync(&track, 4 * sizeof(uint64_t), s));
   BOLA_TRY_CUDA(cudaMemsetAsync(err, 0, sizeof(int32_t), s));
   if (kind == 3) {
     // exact bf16 slices of L21 and U12^T (OZ_SLICES planes of n rows) and their row exponents
@@ -550,7 +602,8 @@ int MixedLU::reserve(int64_t n_, int kind_, cudaStream_t s) {
 void MixedLU::release(cudaStream_t s) {
   for (void **p : {&aop[0], &aop[1], &bop, reinterpret_cast<void **>(&aop_lo[0]),
                    reinterpret_cast<void **>(&aop_lo[1]), reinterpret_cast<void **>(&bop_lo),
-                   reinterpret_cast<void **>(&err), reinterpret_cast<void **>(&plan), reinterpret_cast<void **>(&ea[0]),
+                   reinterpret_cast<void **>(&err), reinterpret_cast<void **>(&plan), reinterpret_cast<void **>(&track),
+                   reinterpret_cast<void **>(&ea[0]),
                    reinterpret_cast<void **>(&ea[1]), reinterpret_cast<void **>(&eb)}) {
     if (*p) cudaFreeAsync(*p, s);
     *p = nullptr;
@@ -588,14 +641,21 @@ int panel_width(bool fp64, int64_t n, int64_t j) {
 // columns (all on sp), then the update of the other columns on su, which
 // overlaps panel k+1; the swaps of step k+1 wait for it.
 template <typename T>
-static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int32_t *ipiv, int32_t *info) {
+static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int32_t *ipiv, int32_t *info,
+                            double give_up) {
   constexpr bool fp64 = std::is_same<T, double>::value;
   const int64_t n = lu.n;
   BOLA_TRY_CUDA(cudaEventRecord(lu.ev_in, s));
   BOLA_TRY_CUDA(cudaStreamWaitEvent(lu.sp, lu.ev_in, 0));
   BOLA_TRY_CUDA(cudaStreamWaitEvent(lu.su, lu.ev_in, 0));
   zero_i32<<<1, 1, 0, lu.sp>>>(info);
+  track_init<<<1, 1, 0, lu.sp>>>(lu.track);
   BOLA_CHECK_LAUNCH();
+  // su's first kernels read the flag too: they must see it initialised
+  BOLA_TRY_CUDA(cudaEventRecord(lu.ev_in, lu.sp));
+  BOLA_TRY_CUDA(cudaStreamWaitEvent(lu.su, lu.ev_in, 0));
+  uint64_t *track = std::isinf(give_up) ? nullptr : lu.track;
+  const int32_t *abort = track ? reinterpret_cast<const int32_t *>(track + 2) : nullptr;
   int jb = 0;
   bool wide_pending = false;
   for (int64_t j = 0, k = 0; j < n; j += jb, ++k) {
@@ -606,7 +666,7 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
     using Pol = typename std::conditional<fp64, PanelF64, PanelF32>::type;
     BOLA_TRY(launch_spanel<Pol>(lu.sp, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, lu.kind,
                               upd ? lu.aop[buf] : nullptr, fp64 ? nullptr : lu.aop_lo[buf], fp64 ? lu.ea[buf] : nullptr,
-                              lu.cap_n, lu.plan));
+                              lu.cap_n, lu.plan, track, give_up));
     // the row swaps reach every column: the previous wide update must be done
     if (wide_pending) BOLA_TRY_CUDA(cudaStreamWaitEvent(lu.sp, lu.ev_wide, 0));
     wide_pending = false;
@@ -615,7 +675,7 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
       ProfScope prof(lu.sp, fp64 ? "sswap_trsm64" : "sswap_trsm", (double)jb * jb * (double)(n - j - jb));
       sswap_trsm<T><<<(unsigned)cdiv(others, 8), 256, 0, lu.sp>>>(W, ldw, n, j, jb, lu.plan, lu.kind,
                                                                     upd ? lu.bop : nullptr, fp64 ? nullptr : lu.bop_lo,
-                                                                    fp64 ? lu.eb : nullptr, lu.cap_n);
+                                                                    fp64 ? lu.eb : nullptr, lu.cap_n, abort);
       BOLA_CHECK_LAUNCH();
     }
     if (!upd) continue;
@@ -625,10 +685,10 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
     auto update = [&](cudaStream_t st, int64_t cols, int64_t boff) -> int {
       if constexpr (fp64)
         return oz_update(st, m2, cols, lu.mapA[buf], lu.mapB, lu.cap_n, lu.cap_n, lu.ea[buf], lu.eb,
-                         W22 + boff * ldw, ldw, lu.err, boff);
+                         W22 + boff * ldw, ldw, lu.err, boff, abort);
       else
         return tc_update(st, lu.kind, m2, cols, lu.mapA[buf], lu.mapB, lu.mapAlo[buf], lu.mapBlo,
-                         W22 + boff * ldw, ldw, lu.err, boff);
+                         W22 + boff * ldw, ldw, lu.err, boff, abort);
     };
     BOLA_TRY(update(lu.sp, nb_next, 0));  // the next panel's columns
     if (n2 > nb_next) {
@@ -645,12 +705,12 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
   return 0;
 }
 
-int MixedLU::factor(cudaStream_t s, float *W, int64_t ldw, int32_t *ipiv, int32_t *info) {
-  return factor_lookahead<float>(*this, s, W, ldw, ipiv, info);
+int MixedLU::factor(cudaStream_t s, float *W, int64_t ldw, int32_t *ipiv, int32_t *info, double give_up) {
+  return factor_lookahead<float>(*this, s, W, ldw, ipiv, info, give_up);
 }
 
-int MixedLU::factor64(cudaStream_t s, double *W, int64_t ldw, int32_t *ipiv, int32_t *info) {
-  return factor_lookahead<double>(*this, s, W, ldw, ipiv, info);
+int MixedLU::factor64(cudaStream_t s, double *W, int64_t ldw, int32_t *ipiv, int32_t *info, double give_up) {
+  return factor_lookahead<double>(*this, s, W, ldw, ipiv, info, give_up);
 }
 
 }  // namespace bola

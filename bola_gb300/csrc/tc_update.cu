@@ -43,8 +43,9 @@ template <int KIND, int NPASS>
 __global__ void __launch_bounds__(128)
 tc_update_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                  const __grid_constant__ CUtensorMap mapAlo, const __grid_constant__ CUtensorMap mapBlo, int64_t m,
-                 int64_t n, int64_t boff, float *__restrict__ W, int64_t ldw, int32_t *err) {
+                 int64_t n, int64_t boff, float *__restrict__ W, int64_t ldw, int32_t *err, const int32_t *abort) {
   using Cfg = TcCfg<KIND, NPASS>;
+  if (abandoned(abort)) return;
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t bar_load, bar_mma;
   __shared__ uint32_t tmem_slot;
@@ -194,7 +195,8 @@ int make_fp64_tile_map(CUtensorMap *map, const double *ptr, int64_t rows, int64_
 }
 
 int tc_update(cudaStream_t s, int kind, int64_t m, int64_t n, const CUtensorMap &A, const CUtensorMap &B,
-              const CUtensorMap &Alo, const CUtensorMap &Blo, float *W, int64_t ldw, int32_t *err, int64_t boff) {
+              const CUtensorMap &Alo, const CUtensorMap &Blo, float *W, int64_t ldw, int32_t *err, int64_t boff,
+              const int32_t *abort) {
   if (m <= 0 || n <= 0) return 0;
   const dim3 grid((unsigned)cdiv(m, BM), (unsigned)cdiv(n, BN));
   ProfScope prof(s, "tc_update", 2.0 * (double)m * n * KDIM * (kind == 2 ? 3 : 1), 8.0 * (double)m * n);
@@ -207,7 +209,7 @@ int tc_update(cudaStream_t s, int kind, int64_t m, int64_t n, const CUtensorMap 
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM_LAUNCH)); \
       attr = true;                                                                                        \
     }                                                                                                     \
-    tc_update_kernel<KIND, NPASS><<<grid, 128, Cfg::SMEM_LAUNCH, s>>>(A, B, Alo, Blo, m, n, boff, W, ldw, err); \
+    tc_update_kernel<KIND, NPASS><<<grid, 128, Cfg::SMEM_LAUNCH, s>>>(A, B, Alo, Blo, m, n, boff, W, ldw, err, abort); \
   } while (0)
   if (kind == 0) BOLA_TC(0, 1);
   else if (kind == 1) BOLA_TC(1, 1);

@@ -148,6 +148,29 @@ def test_escalation_to_fp64_accurate_factor(kind):
     assert info.backward_error <= 1e-14 and berr(A, x, b, n, nrhs) <= 1e-14
 
 
+def test_give_up_decides_as_the_whole_factor_would():
+    """The 3xTF32 factor gives up at the first panel whose pivots push the
+    U-diagonal spread over its limit; the spread of the finished factor is at
+    least as large, so the decision is the same, only earlier."""
+    n, nrhs = 2048, 2
+    A, b = make_system(n, nrhs, 1e10, seed=11)
+    _, early = solve(A, b, n, nrhs, 2, fallback=1)            # may give up
+    _, full = solve(A, b, n, nrhs, 2, fallback=0, max_it=0)   # never gives up
+    assert early.path == 2
+    assert 4.5e4 <= early.condition_estimate <= full.condition_estimate
+
+
+def test_escalated_answer_equals_the_fp64_factor_alone():
+    """After giving up on the 3xTF32 factor, the FP64-accurate factor starts
+    from A again: the answer is the one it gives on its own."""
+    n, nrhs = 1024, 3
+    A, b = make_system(n, nrhs, 1e10, seed=12)
+    x2, i2 = solve(A, b, n, nrhs, 2, fallback=1, escalate=1)
+    x3, i3 = solve(A, b, n, nrhs, 3, fallback=1)
+    assert i2.path == 3 and i3.path in (0, 1)
+    assert torch.equal(x2, x3)
+
+
 def test_escalation_not_taken_when_refinement_converges():
     n, nrhs = 1024, 4
     A, b = make_system(n, nrhs, 1e2, seed=9)
