@@ -47,19 +47,22 @@ __device__ __forceinline__ void group_sync(int G, int g) {
   }
 }
 
-// argmax |A[k:n, k]| within a group; ties -> lowest row.  red: 2*MAXG scratch per group.
-__device__ int group_argmax(const double *col, int k, int n, int t, int G, int g, double *redv, int *redi) {
-  double best = -1.0;
+// argmax |A[k:n, k]| within a group; ties -> lowest row; NaN never wins.
+// The comparisons run on the integer pipe: |v|'s bits order like |v| (a
+// double comparison would take a slot of the narrow FP64 pipe per element).
+// red: 2*MAXG scratch per group.
+__device__ int group_argmax(const double *col, int k, int n, int t, int G, int g, long long *redv, int *redi) {
+  long long best = -1;
   int bi = k;
   for (int i = k + t; i < n; i += G) {
-    const double v = fabs(col[i]);
-    if (v > best) {
+    const long long v = __double_as_longlong(col[i]) & 0x7fffffffffffffffll;
+    if (v <= 0x7ff0000000000000ll && v > best) {
       best = v;
       bi = i;
     }
   }
   for (int off = 16; off > 0; off >>= 1) {
-    const double ov = __shfl_down_sync(0xffffffffu, best, off);
+    const long long ov = __shfl_down_sync(0xffffffffu, best, off);
     const int oi = __shfl_down_sync(0xffffffffu, bi, off);
     if (ov > best || (ov == best && oi < bi)) {
       best = ov;
@@ -72,7 +75,7 @@ __device__ int group_argmax(const double *col, int k, int n, int t, int G, int g
     redi[w] = bi;
   }
   group_sync(G, g);
-  double b = redv[0];
+  long long b = redv[0];
   int r = redi[0];
   for (int q = 1; q < nw; ++q)
     if (redv[q] > b || (redv[q] == b && redi[q] < r)) {
@@ -85,17 +88,18 @@ __device__ int group_argmax(const double *col, int k, int n, int t, int G, int g
 
 // LU with partial pivoting of one system by a group; the row interchanges are
 // applied to B as they happen, then L y = P b and U x = y.
-__device__ int group_lu_solve(const SystemDesc &S, int t, int G, int g, double *redv, int *redi) {
+__device__ int group_lu_solve(const SystemDesc &S, int t, int G, int g, long long *redv, int *redi, double *sinv) {
   const int n = S.n, lda = S.lda, ldb = S.ldb, nr = S.nrhs;
   double *A = S.a, *B = S.b;
   int info = 0;
   for (int k = 0; k < n; ++k) {
     const int p = group_argmax(A + (int64_t)k * lda, k, n, t, G, g, redv, redi);
     const double piv = A[p + (int64_t)k * lda];
-    if (piv == 0.0) {
+    if (!nonzero64(piv)) {
       info = k + 1;
       break;
     }
+    if (t == 0) *sinv = 1.0 / piv;  // once per group; published by the barrier below
     if (p != k) {
       for (int j = t; j < n; j += G) {
         const double tmp = A[k + (int64_t)j * lda];
@@ -109,7 +113,7 @@ __device__ int group_lu_solve(const SystemDesc &S, int t, int G, int g, double *
       }
     }
     group_sync(G, g);
-    const double inv = 1.0 / piv;
+    const double inv = *sinv;
     for (int i = k + 1 + t; i < n; i += G) A[i + (int64_t)k * lda] *= inv;
     group_sync(G, g);
     const int m = n - k - 1;
@@ -172,16 +176,23 @@ __device__ int group_lu_solve(const SystemDesc &S, int t, int G, int g, double *
 }
 
 // Cholesky A = L L^T (lower) of one system by a group, then L y = b, L^T x = y.
-__device__ int group_chol_solve(const SystemDesc &S, int t, int G, int g) {
+__device__ int group_chol_solve(const SystemDesc &S, int t, int G, int g, double *sinv) {
   const int n = S.n, lda = S.lda, ldb = S.ldb, nr = S.nrhs;
   double *A = S.a, *B = S.b;
   for (int k = 0; k < n; ++k) {
     const double d = A[k + (int64_t)k * lda];
-    if (!(d > 0.0)) return k + 1;
-    const double r = sqrt(d);
+    // d > 0 (NaN excluded) on the bits
+    const long long db = __double_as_longlong(d);
+    if (!(db > 0 && db <= 0x7ff0000000000000ll)) return k + 1;
+    // the square root and its reciprocal once per group, not once per thread
+    double r = 0.0;
+    if (t == 0) {
+      r = sqrt(d);
+      *sinv = 1.0 / r;
+    }
     group_sync(G, g);
     if (t == 0) A[k + (int64_t)k * lda] = r;
-    const double inv = 1.0 / r;
+    const double inv = *sinv;
     for (int i = k + 1 + t; i < n; i += G) A[i + (int64_t)k * lda] *= inv;
     group_sync(G, g);
     const int m = n - k - 1;
@@ -245,7 +256,8 @@ __global__ void __launch_bounds__(BT)
 batched_solve_kernel(const SystemDesc *__restrict__ sys, const int32_t *__restrict__ items, int32_t nitems,
                      int32_t *counter, int32_t *info) {
   __shared__ int32_t cur[ITEM];
-  __shared__ double redv[MAXG][MAXG];
+  __shared__ long long redv[MAXG][MAXG];
+  __shared__ double sinv[MAXG];
   __shared__ int redi[MAXG][MAXG];
   const int tid = threadIdx.x;
   for (;;) {
@@ -261,7 +273,8 @@ batched_solve_kernel(const SystemDesc *__restrict__ sys, const int32_t *__restri
     if (g < cur[1]) {
       const int id = cur[2 + g];
       const SystemDesc S = sys[id];
-      const int r = S.kind == 1 ? group_chol_solve(S, t, G, g) : group_lu_solve(S, t, G, g, redv[g], redi[g]);
+      const int r =
+          S.kind == 1 ? group_chol_solve(S, t, G, g, &sinv[g]) : group_lu_solve(S, t, G, g, redv[g], redi[g], &sinv[g]);
       if (t == 0) info[id] = r;
     }
     __syncthreads();

@@ -137,7 +137,7 @@ panel_lu(double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_t *inf
     __syncthreads();
     const double pv = prow[j];
     if (cr == 0 && tid == 0) ipiv[j] = (int32_t)(jp + 1);
-    if (!(pv != 0.0)) {  // exact zero pivot: BOLA's "Matrix is singular" (src/getrf2.rs:166-168)
+    if (!nonzero64(pv)) {  // exact zero pivot: BOLA's "Matrix is singular" (src/getrf2.rs:166-168)
       if (cr == 0 && tid == 0) *info = col0 + j + 1;
       failed = true;
       break;
@@ -225,7 +225,7 @@ panel_lu_wide(double *A, int64_t lda, int64_t m, int64_t n, int32_t *ipiv, int32
     __syncthreads();
     const int64_t jp = sjp;
     const double pv = A[jp + j * lda];
-    if (!(pv != 0.0)) {
+    if (!nonzero64(pv)) {
       if (tid == 0) *info = col0 + (int32_t)j + 1;
       return;
     }
