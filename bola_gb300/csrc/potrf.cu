@@ -204,14 +204,114 @@ __device__ int p2_walk(bool upper, double *a0, double *rdg, int n, int lanes) {
 // 128 threads: one warp per SMSP, so the SYRK steps' FP64 work never queues
 // two warps on one sub-partition's FP64 pipe.
 constexpr int P2T = 128;
+constexpr int P2E = (LDS * (LDS + 1) / 2 + P2T - 1) / P2T;  // lower-triangle elements per thread
+
+// Which updates of element (i, j) (i >= j) BOLA's recursion makes fused: bit l
+// set if the update from column l < j is the fused body of a daxpy.  In
+// p2_walk every update of (i, j) comes from a column l < j, in increasing l:
+// first from the SYRK of each frame whose leading half holds l and whose
+// trailing half holds i and j (a daxpy over that half's column jj: element
+// idx = ii - jj of len = n2 - jj, fused below len rounded down to the SIMD
+// width), then, in the frame that separates i from j, from its TRSM (unfused
+// b - a*x for l in [frame start, j)), after which (i, j) is scaled by 1/l_jj.
+__device__ uint32_t fused_updates(int i, int j, int n, int lanes) {
+  uint32_t m = 0;
+  int off = 0, nn = n;
+  while (nn > 1) {
+    const int n1 = nn / 2, n2 = nn - n1, split = off + n1;
+    if (j >= split) {  // (i, j) in the trailing half: SYRK from l in [off, split)
+      const int jj = j - split, idx = i - j, len = n2 - jj;
+      if (idx < (len & ~(lanes - 1))) m |= ((1u << n1) - 1u) << off;
+      off = split;
+      nn = n2;
+    } else if (i >= split) {  // below the leading half: the TRSM, unfused
+      break;
+    } else {
+      nn = n1;
+    }
+  }
+  return m;
+}
+
+// potrf2 'L' of the block in shared memory, right-looking: column l is
+// finished (square root, 1/l_ll, the column scaled), then every element
+// (i, j > l) takes its update from column l, fused or not as BOLA's recursion
+// does it.  Every element sees BOLA's operations in BOLA's order, so the factor
+// is bit-identical; the dependent chain per column is one square root and
+// one reciprocal instead of the recursion's chains of solves.  Returns 0 or
+// the 1-based failing column; the block is then not in BOLA's state (the
+// caller redoes it with p2_walk).
+__device__ int p2_right_looking(double *a, double *rdg, int n, int lanes) {
+  __shared__ int fail;
+  const int tid = threadIdx.x;
+  int ei[P2E], ej[P2E];
+  uint32_t em[P2E];
+#pragma unroll
+  for (int s = 0; s < P2E; ++s) {  // element e = tid + s * P2T of the packed lower triangle, column by column
+    int e = tid + s * P2T, j = 0;
+    while (j < n && e >= n - j) {
+      e -= n - j;
+      ++j;
+    }
+    ei[s] = j < n ? j + e : -1;
+    ej[s] = j;
+    em[s] = j < n ? fused_updates(j + e, j, n, lanes) : 0u;
+  }
+  if (tid == 0) fail = 0;
+  __syncthreads();
+  for (int l = 0; l < n; ++l) {
+    if (tid == 0) {
+      const double d = a[l + l * LDS];
+      const long long db = __double_as_longlong(d);
+      if (db > 0 && db <= 0x7ff0000000000000ll) {  // d > 0, not NaN
+        const double r = sqrt(d);
+        a[l + l * LDS] = r;
+        rdg[l] = 1.0 / r;
+      } else {
+        fail = l + 1;
+      }
+    }
+    __syncthreads();
+    if (fail) return fail;
+    const double rl = rdg[l];
+#pragma unroll
+    for (int s = 0; s < P2E; ++s)
+      if (ej[s] == l && ei[s] > l) a[ei[s] + l * LDS] = __dmul_rn(a[ei[s] + l * LDS], rl);
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < P2E; ++s) {
+      const int i = ei[s], j = ej[s];
+      if (i < 0 || j <= l) continue;
+      const double ljl = a[j + l * LDS];
+      if (!nonzero64(ljl)) continue;  // BOLA skips a zero multiplier
+      const double lil = a[i + l * LDS];
+      double &c = a[i + j * LDS];
+      c = ((em[s] >> l) & 1u) ? fused(-ljl, lil, c) : __dsub_rn(c, __dmul_rn(ljl, lil));
+    }
+    __syncthreads();
+  }
+  return 0;
+}
+
 __global__ void __launch_bounds__(P2T)
 potrf2_block(bool upper, int n, double *A, int64_t lda, int32_t *info, int32_t col0, int lanes) {
   __shared__ double a[LDS * LDS];
+  __shared__ double a0[LDS * LDS];  // the input, for a failing 'L' block
   __shared__ double rdg[LDS];
   if (stop_flag(info)) return;
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) a[(e % n) + (e / n) * LDS] = A[(e % n) + (e / n) * lda];
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const double v = A[(e % n) + (e / n) * lda];
+    a[(e % n) + (e / n) * LDS] = v;
+    a0[(e % n) + (e / n) * LDS] = v;
+  }
   __syncthreads();
-  const int r = p2_walk(upper, a, rdg, n, lanes);
+  int r = upper ? p2_walk(true, a, rdg, n, lanes) : p2_right_looking(a, rdg, n, lanes);
+  if (!upper && r) {  // BOLA's state at a failure is its recursion's: redo the block that way
+    __syncthreads();
+    for (int e = threadIdx.x; e < LDS * LDS; e += blockDim.x) a[e] = a0[e];
+    __syncthreads();
+    r = p2_walk(false, a, rdg, n, lanes);
+  }
   __syncthreads();
   // BOLA stops at the failing column with everything before it written back.
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) A[(e % n) + (e / n) * lda] = a[(e % n) + (e / n) * LDS];

@@ -194,15 +194,21 @@ int base_left_t(const Ctx &c, bool lower, int64_t m, int64_t n, const double *A,
   return 0;
 }
 
-// The ascending right base cases (rnu, rtl) for n <= 32, right-looking with
-// the row in registers: once b_k is final it is subtracted from every later
-// column of the row, so each b_j still receives its updates in ascending k and
-// then its scale, exactly as in BOLA's column sweep, but a row's FP64
-// operations no longer form one dependent chain and keep the FP64 pipe full.
-constexpr int RA_ROWS = 64;
+// The ascending right base cases (rnu, rtl) for n <= 32, right-looking: once
+// b_k is final it is subtracted from every later column of the row, so each
+// b_j still receives its updates in ascending k and then its scale, exactly as
+// in BOLA's column sweep.  A row is spread over RL = 4 lanes, lane q holding
+// columns q, q+4, ..., q+28 in registers: b_k is finished by its lane and
+// broadcast by a shuffle, and each lane updates its own later columns.  The
+// FP64 pipe retires a warp instruction in the same time whether 1 or 32 lanes
+// work, and a row's work is one dependent sweep; spreading a row over 4 lanes
+// cuts the instructions on a warp's path about 3.5-fold.
+constexpr int RL = 4;             // lanes per row
+constexpr int RA_THREADS = 64;    // 16 rows per CTA
+constexpr int RA_ROWS = RA_THREADS / RL;
 
 template <int V>
-__global__ void __launch_bounds__(RA_ROWS)
+__global__ void __launch_bounds__(RA_THREADS)
 right_base_asc32(int64_t m, int n, bool unit, const double *__restrict__ A, int64_t lda, double *B, int64_t ldb,
                  const int32_t *info) {
   static_assert(V == 1 || V == 2, "ascending variants only");
@@ -213,36 +219,45 @@ right_base_asc32(int64_t m, int n, bool unit, const double *__restrict__ A, int6
   __syncthreads();
   if (!unit && threadIdx.x < n) rd[threadIdx.x] = 1.0 / sA[threadIdx.x * 34];
   __syncthreads();
-  const int64_t i = (int64_t)blockIdx.x * RA_ROWS + threadIdx.x;
-  if (i >= m) return;
-  double b[32];
+  const int lane = threadIdx.x & 31, q = lane & (RL - 1), base = lane & ~(RL - 1);
+  const int64_t i = (int64_t)blockIdx.x * RA_ROWS + threadIdx.x / RL;
+  const bool row = i < m;  // lanes of a missing row still take part in the shuffles
+  double b[32 / RL];
 #pragma unroll
-  for (int k = 0; k < 32; ++k) b[k] = k < n ? B[i + (int64_t)k * ldb] : 0.0;
+  for (int c = 0; c < 32 / RL; ++c) {
+    const int j = q + RL * c;
+    b[c] = (row && j < n) ? B[i + (int64_t)j * ldb] : 0.0;
+  }
 #pragma unroll
   for (int k = 0; k < 32; ++k) {
     if (k < n) {
-      if (!unit) b[k] = __dmul_rn(b[k], rd[k]);
-      const double bk = b[k];
+      if (!unit && q == (k & (RL - 1))) b[k / RL] = __dmul_rn(b[k / RL], rd[k]);
+      const double bk = __shfl_sync(0xffffffffu, b[k / RL], base + (k & (RL - 1)));
 #pragma unroll
-      for (int j = k + 1; j < 32; ++j) {
-        if (j < n) {
+      for (int c = 0; c < 32 / RL; ++c) {
+        const int j = q + RL * c;
+        if (j > k && j < n) {
           const double a = (V == 1) ? sA[k + j * 33] : sA[j + k * 33];  // rnu: a(k, j); rtl: a(j, k)
-          const double u = sub_prod(b[j], a, bk);
-          b[j] = nonzero64(a) ? u : b[j];  // BOLA skips a zero a
+          const double u = sub_prod(b[c], a, bk);
+          b[c] = nonzero64(a) ? u : b[c];  // BOLA skips a zero a
         }
       }
     }
   }
+  if (!row) return;
 #pragma unroll
-  for (int k = 0; k < 32; ++k)
-    if (k < n) B[i + (int64_t)k * ldb] = b[k];
+  for (int c = 0; c < 32 / RL; ++c) {
+    const int j = q + RL * c;
+    if (j < n) B[i + (int64_t)j * ldb] = b[c];
+  }
 }
 
 template <int V>
 int launch_right_base(const Ctx &c, int64_t m, int64_t n, const double *A, int64_t lda, double *B, int64_t ldb) {
   if constexpr (V == 1 || V == 2) {
     if (n <= 32) {
-      right_base_asc32<V><<<(unsigned)cdiv(m, RA_ROWS), RA_ROWS, 0, c.s>>>(m, (int)n, c.unit, A, lda, B, ldb, c.info);
+      right_base_asc32<V><<<(unsigned)cdiv(m, RA_ROWS), RA_THREADS, 0, c.s>>>(m, (int)n, c.unit, A, lda, B, ldb,
+                                                                             c.info);
       BOLA_CHECK_LAUNCH();
       return 0;
     }
