@@ -437,7 +437,9 @@ void la_release(LookAhead *la) {
 // step k's update, which BOLA completes before factoring panel k+1.
 int getrf_blocked(cudaStream_t s, int64_t m, int64_t n, double *A, int64_t lda, int32_t *ipiv, int32_t *info) {
   const int64_t min_mn = imin(m, n);
-  LookAhead *la = (m > 0 && n > 0 && PNB < min_mn) ? la_acquire() : nullptr;
+  // look-ahead pays from a few hundred columns on; below that its events and
+  // the extra launches cost more than the overlap saves
+  LookAhead *la = (m > 0 && n > 0 && min_mn >= 512) ? la_acquire() : nullptr;
   if (!la) {
     {
       ProfScope prof(s, "info_init");

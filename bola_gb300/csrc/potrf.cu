@@ -464,16 +464,47 @@ __global__ void potrf_restore(bool upper, int64_t n, const double *__restrict__ 
   }
 }
 
+// BOLA's blocking literally (left-looking), for small orders: below ~512 the
+// look-ahead streams, the input copy and the extra launches of the
+// right-looking form cost more than its shorter critical path saves.
+int potrf_left_looking(cudaStream_t s, bool upper, int64_t n, double *A, int64_t lda, int32_t *info) {
+  for (int64_t j = 0; j < n; j += NB) {
+    const int64_t jb = imin(NB, n - j), n_rem = n - j - jb;
+    double *ajj = A + j + j * lda;
+    if (upper) {
+      BOLA_TRY(syrk_exact(s, 'U', 'T', jb, j, -1.0, A + j * lda, lda, 1.0, ajj, lda, info));
+      BOLA_TRY(potrf2_rec(s, 'U', jb, ajj, lda, info, (int32_t)j));
+      if (n_rem > 0) {
+        BOLA_TRY(dgemm_exact(s, 'T', 'N', jb, n_rem, j, -1.0, A + j * lda, lda, A + (j + jb) * lda, lda, 1.0,
+                             A + j + (j + jb) * lda, lda, 64, info, 0));
+        BOLA_TRY(trsm_exact(s, 'L', 'U', 'T', 'N', jb, n_rem, 1.0, ajj, lda, A + j + (j + jb) * lda, lda, info));
+      }
+    } else {
+      BOLA_TRY(syrk_exact(s, 'L', 'N', jb, j, -1.0, A + j, lda, 1.0, ajj, lda, info));
+      BOLA_TRY(potrf2_rec(s, 'L', jb, ajj, lda, info, (int32_t)j));
+      if (n_rem > 0) {
+        BOLA_TRY(dgemm_exact(s, 'N', 'T', n_rem, jb, j, -1.0, A + j + jb, lda, A + j, lda, 1.0,
+                             A + j + jb + j * lda, lda, 64, info, 0));
+        BOLA_TRY(trsm_exact(s, 'R', 'L', 'T', 'N', n_rem, jb, 1.0, ajj, lda, A + j + jb + j * lda, lda, info));
+      }
+    }
+  }
+  return 0;
+}
+
+constexpr int64_t RIGHT_LOOKING_MIN_N = 512;
+
 int potrf_blocked(cudaStream_t s, char uplo, int64_t n, double *A, int64_t lda, int32_t *info) {
-  if (NB >= n) {
+  const bool upper = uplo == 'U';
+  if (n < RIGHT_LOOKING_MIN_N) {
     {
       ProfScope prof(s, "info_init");
       zero_i32<<<1, 1, 0, s>>>(info);
     }
     BOLA_CHECK_LAUNCH();
-    return potrf2_rec(s, uplo, n, A, lda, info, 0);
+    if (NB >= n) return potrf2_rec(s, uplo, n, A, lda, info, 0);
+    return potrf_left_looking(s, upper, n, A, lda, info);
   }
-  const bool upper = uplo == 'U';
   const int lan = lanes();
   Scratch bk;
   BOLA_TRY(bk.alloc((size_t)n * n * sizeof(double), s));

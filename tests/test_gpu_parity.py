@@ -143,10 +143,10 @@ def test_getrf_ties_follow_bola_lane_order(both):
     assert same(A1, A2)
 
 
-@pytest.mark.parametrize("col", [0, 5, 40, 70, 95])
-def test_getrf_singular_stops_like_bola(both, col):
+@pytest.mark.parametrize("n,col", [(100, 0), (100, 5), (100, 40), (100, 70), (100, 95), (600, 3), (600, 333),
+                                   (700, 690)])
+def test_getrf_singular_stops_like_bola(both, n, col):
     g, o = both
-    n = 100
     A = wl.uniform_matrix(n, n, seed=17, lo=-1, hi=1)
     A[:, col] = 0.0
     A1, A2 = A.copy(order="F"), A.copy(order="F")
@@ -173,7 +173,7 @@ def test_getrf2_recursive_bitwise(both, n):
 
 
 @pytest.mark.parametrize("uplo", ["L", "U"])
-@pytest.mark.parametrize("n", [1, 3, 32, 33, 64, 100, 203, 257, 390])
+@pytest.mark.parametrize("n", [1, 3, 32, 33, 64, 100, 203, 257, 390, 545, 777])
 def test_potrf_bitwise(both, uplo, n):
     g, o = both
     A = wl.spd_matrix(n, seed=n + 1)
@@ -195,7 +195,8 @@ def test_potrf2_bitwise(both, uplo):
 
 
 @pytest.mark.parametrize("uplo", ["L", "U"])
-@pytest.mark.parametrize("n,bad", [(100, 0), (100, 20), (100, 45), (100, 70), (100, 99), (301, 200)])
+@pytest.mark.parametrize("n,bad", [(100, 0), (100, 20), (100, 45), (100, 70), (100, 99), (301, 200),
+                                   (600, 5), (600, 70), (600, 450), (700, 699)])
 def test_potrf_not_spd(gpu, oracle_lib, uplo, n, bad):
     """BOLA stops at the failing block: later columns keep their input values."""
     A = wl.spd_matrix(n, seed=2)
