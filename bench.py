@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-systems", type=int, default=20000)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-plain-configs", action="store_true")
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[25.0, 50.0, 100.0, 200.0])
     ap.add_argument("--serve-requests", type=int, default=300)
     ap.add_argument("--serve-pool", type=int, default=48)
@@ -336,7 +337,9 @@ def run_ours(args, rank, world, device):
                    "replicas": "one independent solve stream per GPU (no collective)",
                    "l2": "inputs larger than L2 (512 MiB matrix per step)"},
         "latency_ms": {"p50": round(statistics.median(per), 3),
-                       "p99": round(float(np.percentile(per, 99)), 3)},
+                       "p99": round(float(np.percentile(per, 99)), 3),
+                       "median_by_kappa": {f"{systems[q]['kappa']:.0e}": round(statistics.median(per[q::len(systems)]), 3)
+                                           for q in range(min(len(systems), len(per)))}},
         "plain_fp64": {"value": round(plain_value, 4), "unit": "solves/s", "steps": plain_steps,
                        "ms_per_step": round(plain_total / plain_steps, 3),
                        "path": "BOLA-exact bola_dgetrf + bola_dgetrs (FP64, NB=32)"},
@@ -353,6 +356,9 @@ def run_ours(args, rank, world, device):
     clocks = clk.summary()
     if clocks is not None:
         out["clocks"] = clocks
+    if not args.no_plain_configs:
+        out["factor_kinds"] = run_factor_kinds(systems, n, nrhs, device)
+        out["plain_configs"] = run_plain_configs(device, peak_fp64)
     if not args.no_batched:
         out["batched"] = run_batched(args, device, peak_fp64)
     if not args.no_serve:
@@ -405,6 +411,127 @@ def run_batched(args, device, peak_fp64):
             "group_sizes": table,
             "autotune_ms": {str(k): {str(g): round(t, 3) for g, t in v.items()} for k, v in trials.items()},
             "info_all_zero": ok_info, "max_backward_error_sample": worst}
+
+
+def run_plain_configs(device, peak_fp64):
+    """The BOLA-exact FP64 drop-ins at their published sizes: DGEMM NN 1024
+    (alpha = beta = 1, A, B, C U[0,1)), DGETRF 4096 (U[-1,1)), DPOTRF 'L' 4096
+    (B B^T / n + I), DTRSM L,L,N,U 4096 x 1024 with the unit-lower factor of
+    that getrf.  Median of 5 calls after 2 warm-up calls, each timed alone with
+    CUDA events; a 256 MiB buffer is rewritten between calls (L2 flushed)."""
+    from bola_gb300 import _lib
+    L = _lib.load()
+    st = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(st.cuda_stream)
+
+    def P(t):
+        return ctypes.c_void_p(t.data_ptr())
+
+    def ok(status, what):
+        if status != 0:
+            raise RuntimeError(f"{what}: status {status}: {L.bola_last_error().decode()}")
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
+
+    def timed(fn, prep):
+        ts = []
+        for r in range(7):
+            prep()
+            flush.fill_(r)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            fn()
+            e1.record(st)
+            torch.cuda.synchronize()
+            if r >= 2:
+                ts.append(e0.elapsed_time(e1))
+        return statistics.median(ts)
+
+    def entry(ms, flops):
+        gf = flops / (ms / 1e3) / 1e9
+        return {"ms": round(ms, 3), "gflops": round(gf, 1),
+                "fp64_peak_frac": round(gf / peak_fp64, 4) if peak_fp64 else None}
+
+    g = torch.Generator(device=device)
+    out = {"peak_fp64_gflops": round(peak_fp64, 1) if peak_fp64 else None}
+    n = 1024
+    g.manual_seed(0)
+    A = torch.rand(n * n, dtype=torch.float64, device=device, generator=g)
+    B = torch.rand(n * n, dtype=torch.float64, device=device, generator=g)
+    C0 = torch.rand(n * n, dtype=torch.float64, device=device, generator=g)
+    C = torch.empty_like(C0)
+    ms = timed(lambda: ok(L.bola_dgemm(b"N", b"N", n, n, n, 1.0, P(A), n, P(B), n, 1.0, P(C), n, sp), "dgemm"),
+               lambda: C.copy_(C0))
+    out["dgemm_nn_1024"] = entry(ms, 2.0 * n ** 3)
+    n = 4096
+    A = torch.rand(n * n, dtype=torch.float64, device=device, generator=g)
+    B = torch.rand(n * n, dtype=torch.float64, device=device, generator=g)
+    C0 = torch.rand(n * n, dtype=torch.float64, device=device, generator=g)
+    C = torch.empty_like(C0)
+    ms = timed(lambda: ok(L.bola_dgemm(b"N", b"N", n, n, n, 1.0, P(A), n, P(B), n, 1.0, P(C), n, sp), "dgemm"),
+               lambda: C.copy_(C0))
+    out["dgemm_nn_4096"] = entry(ms, 2.0 * n ** 3)
+    del B, C0, C
+    g.manual_seed(1)
+    A0 = torch.rand(n * n, dtype=torch.float64, device=device, generator=g) * 2 - 1
+    ipiv = torch.empty(n, dtype=torch.int32, device=device)
+    info = torch.zeros(1, dtype=torch.int32, device=device)
+    ms = timed(lambda: ok(L.bola_dgetrf(n, n, P(A), n, P(ipiv), P(info), sp), "dgetrf"), lambda: A.copy_(A0))
+    out["dgetrf_4096"] = entry(ms, 2.0 * n ** 3 / 3 - n ** 2 / 2 + 5.0 * n / 6)
+    out["dgetrf_4096"]["info"] = int(info)
+    LU = A.clone()
+    g.manual_seed(11)
+    X0 = torch.rand(n * 1024, dtype=torch.float64, device=device, generator=g) * 2 - 1
+    X = torch.empty_like(X0)
+    ms = timed(lambda: ok(L.bola_dtrsm(b"L", b"L", b"N", b"U", n, 1024, 1.0, P(LU), n, P(X), n, sp), "dtrsm"),
+               lambda: X.copy_(X0))
+    out["dtrsm_llnu_4096x1024"] = entry(ms, float(n) * n * 1024 - n * 1024)
+    del LU, X0, X
+    g.manual_seed(2)
+    Bm = torch.rand(n, n, dtype=torch.float64, device=device, generator=g) * 2 - 1
+    S0 = (Bm @ Bm.t() / n + torch.eye(n, dtype=torch.float64, device=device)).reshape(-1)
+    del Bm
+    ms = timed(lambda: ok(L.bola_dpotrf(b"L", n, P(A), n, P(info), sp), "dpotrf"), lambda: A.copy_(S0))
+    out["dpotrf_l_4096"] = entry(ms, n ** 3 / 3 + n ** 2 / 2 + n / 6)
+    out["dpotrf_l_4096"]["info"] = int(info)
+    return out
+
+
+def run_factor_kinds(systems, n, nrhs, device):
+    """Config 3 per factor precision: each kind (0 bf16, 1 tf32, 2 3xTF32 with
+    FP32 storage, 3 FP64-accurate) on each kappa, escalation and fallback on,
+    median of 2 timed solves after one warm-up."""
+    from bola_gb300 import _lib
+    L = _lib.load()
+    st = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(st.cuda_stream)
+    x = torch.zeros(n * nrhs, dtype=torch.float64, device=device)
+    out = {}
+    names = {0: "bf16", 1: "tf32", 2: "3xtf32", 3: "fp64-accurate"}
+    for kind in (0, 1, 2, 3):
+        row = {}
+        for sysd in systems:
+            opts, info = _lib.MixedOpts(kind, 30, BERR_TARGET, 1, 1, 1), _lib.MixedInfo()
+            ts = []
+            for r in range(3):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                status = L.bola_dgesv_mixed(n, nrhs, ctypes.c_void_p(sysd["A"].data_ptr()), n,
+                                            ctypes.c_void_p(sysd["b"].data_ptr()), n, ctypes.c_void_p(x.data_ptr()),
+                                            n, ctypes.byref(opts), ctypes.byref(info), sp)
+                e1.record(st)
+                torch.cuda.synchronize()
+                if status != 0:
+                    raise RuntimeError(f"bola_dgesv_mixed: {L.bola_last_error().decode()}")
+                if r >= 1:
+                    ts.append(e0.elapsed_time(e1))
+            row[f"{sysd['kappa']:.0e}"] = {
+                "ms": round(statistics.median(ts), 3),
+                "path": ["IR", "GMRES-IR", "fp64-fallback", "escalated-to-fp64-accurate"][info.path],
+                "iterations": info.iterations, "gmres_iterations": info.gmres_iterations,
+                "backward_error": info.backward_error, "condition_estimate": info.condition_estimate}
+        out[names[kind]] = row
+    return out
 
 
 def run_serve(args, device):

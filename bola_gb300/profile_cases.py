@@ -3,6 +3,8 @@
     python -m bola_gb300.profile_cases getrf N        # 2 x bola_dgetrf, A uniform[-1,1), seed 1
     python -m bola_gb300.profile_cases potrf N        # 2 x bola_dpotrf('L'), A = B B^T / n + I, seed 2
     python -m bola_gb300.profile_cases mixed N KIND   # 2 x bola_dgesv_mixed, 16 RHS, A = U[-1,1) + 4 I
+    python -m bola_gb300.profile_cases mixed N KIND E # the same on A = Q1 diag(s) Q2, kappa = 10^E, escalation on
+                                                      # (Q from torch's QR of seeded Gaussians: needs torch.linalg)
     python -m bola_gb300.profile_cases batched COUNT  # 2 x bola_batch_solve, the batched workload (seed 4)
 
 With --scopes, the library's own device timers are on during the last call
@@ -68,17 +70,23 @@ def case_potrf(n):
         print(f"potrf n={n} {ms:.2f} ms info={int(info)}")
 
 
-def case_mixed(n, kind):
+def case_mixed(n, kind, kappa_exp=None):
     L = _lib.load()
     nrhs = 16
     g = torch.Generator(device="cuda")
     g.manual_seed(5)
-    A = torch.rand(n, n, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
-    A += 4 * torch.eye(n, dtype=torch.float64, device="cuda")
+    if kappa_exp is None:
+        A = torch.rand(n, n, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+        A += 4 * torch.eye(n, dtype=torch.float64, device="cuda")
+    else:
+        q1, _ = torch.linalg.qr(torch.randn(n, n, dtype=torch.float64, device="cuda", generator=g))
+        q2, _ = torch.linalg.qr(torch.randn(n, n, dtype=torch.float64, device="cuda", generator=g))
+        sigma = torch.logspace(0.0, -float(kappa_exp), n, dtype=torch.float64, device="cuda")
+        A = (q1 * sigma) @ q2
     A = A.t().contiguous().reshape(-1)
     b = torch.rand(n * nrhs, dtype=torch.float64, device="cuda", generator=g)
     x = torch.zeros(n * nrhs, dtype=torch.float64, device="cuda")
-    opts, info = _lib.MixedOpts(kind, 30, 1e-14, 1, 1), _lib.MixedInfo()
+    opts, info = _lib.MixedOpts(kind, 30, 1e-14, 1, 1, 0 if kappa_exp is None else 1), _lib.MixedInfo()
     s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     for _ in range(2):
         ms = _timed(lambda: _check(L, L.bola_dgesv_mixed(n, nrhs, _p(A), n, _p(b), n, _p(x), n, ctypes.byref(opts),
