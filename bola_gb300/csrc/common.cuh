@@ -135,6 +135,15 @@ __device__ __forceinline__ double add_prod(double c, double t, double x) {
 __device__ __forceinline__ double sub_prod(double c, double t, double x) {
   return __dsub_rn(c, __dmul_rn(t, x));
 }
+// Split cluster barrier: ARRIVE (release) and WAIT (acquire), so that work
+// between them overlaps the other CTAs' arrival.
+__device__ __forceinline__ void cluster_arrive() {
+  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() {
+  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 // x != 0.0 (NaN included) on the integer pipe.  GB300 retires ~2 FP64
 // operations per clock per SM and a comparison takes a slot like an FMA, so
 // the zero tests inside BOLA's update loops are done on the bits.

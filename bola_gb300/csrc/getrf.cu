@@ -196,6 +196,218 @@ panel_lu(double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_t *inf
   cluster.sync();  // no CTA may leave while another can still read its shared memory
 }
 
+// BOLA's rank-1 step (src/getrf2.rs:152-164 with src/ger.rs:28-61) on one
+// element: row g (panel row), column c, by pivot p.  x is the row's scaled
+// multiplier, prow the pivot row.  ger walks columns p+1.. in pairs, skipping
+// a pair whose two pivot-row entries are both zero, with the fused vector
+// body for rows below mr rounded down to the SIMD width and the unfused tail
+// after; an odd last column is always unfused (and skipped when zero).
+struct GerStep {
+  int p, nun;       // pivot column, columns of the paired part (ncols rounded down to even)
+  int64_t vec_end;  // rows g with g - p - 1 < vec_end take the fused body
+};
+__device__ __forceinline__ GerStep ger_step(int p, int nb, int64_t mp, int lanes) {
+  GerStep s;
+  s.p = p;
+  s.nun = (nb - p - 1) & ~1;
+  s.vec_end = (mp - p - 1) & ~(int64_t)(lanes - 1);
+  return s;
+}
+// -1: the column is skipped, 0: unfused, 1: fused body (rows permitting)
+__device__ __forceinline__ int ger_mode(const GerStep &s, const double *prow, int c) {
+  const int o = c - s.p - 1;
+  if (o < s.nun) {
+    const bool any = nonzero64(prow[c]) || nonzero64(prow[s.p + 1 + (o ^ 1)]);
+    return any ? 1 : -1;
+  }
+  return nonzero64(prow[c]) ? 0 : -1;
+}
+__device__ __forceinline__ double ger_apply(const GerStep &s, int mode, double a, double x, double pc, int64_t g) {
+  if (mode < 0) return a;
+  const double t = -pc;
+  return (mode == 1 && g - s.p - 1 < s.vec_end) ? fused(x, t, a) : add_prod(a, t, x);
+}
+
+// What a CTA pushes into every CTA of the cluster for one column: its pivot
+// candidate and that row (left before pivot j-1's update of columns > j).
+struct XSlot {
+  long long v, key, g, pad;  // Cand (g: panel row, -1 if the CTA has none)
+  double row[PNB];
+};
+
+// The same unblocked LU as panel_lu (BOLA's iterative_getrf2), rows in shared
+// memory, with one split cluster barrier per column instead of a full one and
+// three rounds of remote reads.  Per column j:
+//   (a) this CTA's candidate in column j is found (BOLA's lane-ordered idamax
+//       keys), one CTA barrier;
+//   (b) every warp pushes the CTA's candidate row (and row j, if owned) into
+//       its share of the cluster's CTAs, one CTA barrier, cluster ARRIVE;
+//   (c) the rank-1 update of pivot j-1 on columns j+1.. (deferred), while the
+//       other CTAs arrive; cluster WAIT;
+//   (d) every CTA picks the same winner from its own slots and brings the
+//       pushed rows up to date (the owner's same operation for pivot j-1 on
+//       columns > j), one CTA barrier; zero pivot -> stop as BOLA does;
+//   (e) the swap, one CTA barrier, the multipliers of column j scaled and the
+//       update of column j+1 only (the next column searched).
+// Every element sees BOLA's operations in BOLA's order: A, ipiv and info are
+// bit-identical to panel_lu's.
+__global__ void __launch_bounds__(PT)
+panel_lu_split(double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_t *info, int32_t add_on_success,
+               int32_t col0, int lanes, int64_t R) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = (int)cluster.num_blocks();
+  const int cr = (int)cluster.block_rank();
+  __shared__ XSlot slots[2][MAXC];
+  __shared__ double rowj[2][PNB];
+  __shared__ double piv[2][PNB];  // pivot rows, up to date (piv[j & 1] = column j's)
+  __shared__ double oldj[PNB];    // the old row j, up to date (goes to the pivot's place)
+  __shared__ Cand wc[PT / 32];
+  __shared__ double sinv;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double *data = reinterpret_cast<double *>(smem_raw);
+
+  // Uniform across the cluster: the only writer of *info here acts after
+  // the cluster barriers that every CTA passes after this read.
+  if (stop_flag(info)) return;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t r0 = (int64_t)cr * R;
+  const int64_t r1 = imin(mp, r0 + R);
+  const int64_t nr = r1 > r0 ? r1 - r0 : 0;
+  auto el = [&](int c, int64_t il) -> double & { return data[(int64_t)c * R + il]; };
+  for (int64_t e = tid; e < nr * nb; e += PT) {
+    const int64_t il = e % nr;
+    const int c = (int)(e / nr);
+    el(c, il) = A[(r0 + il) + (int64_t)c * lda];
+  }
+  __syncthreads();
+  cluster.sync();  // every CTA runs before the first push
+
+  const int steps = (int)imin(mp, nb);
+  bool failed = false;
+  double inv = 0.0;
+  for (int j = 0; j < steps; ++j) {
+    const int par = j & 1;
+    const double *pprev = piv[par ^ 1];
+    // (a)
+    Cand best = cand_none();
+    for (int64_t il = tid; il < nr; il += PT) {
+      const int64_t g = r0 + il;
+      if (g < j) continue;
+      const Cand c = make_cand(el(j, il), g - j, mp - j, lanes);
+      if (cand_better(c, best)) best = c;
+    }
+    best = warp_best(best);
+    if (lane == 0) wc[warp] = best;
+    __syncthreads();
+    // (b)
+    {
+      Cand cb = wc[0];
+#pragma unroll
+      for (int w = 1; w < PT / 32; ++w)
+        if (cand_better(wc[w], cb)) cb = wc[w];
+      const int64_t gl = cb.v > -2 ? j + cb.idx - r0 : -1;  // local row of the candidate
+      const bool own_j = j >= r0 && j < r1;
+      const double cv = (gl >= 0 && lane < nb) ? el(lane, gl) : 0.0;
+      const double jv = (own_j && lane < nb) ? el(lane, j - r0) : 0.0;
+      for (int d = warp; d < C; d += PT / 32) {
+        XSlot *rs = cluster.map_shared_rank(&slots[par][cr], d);
+        if (lane == 0) {
+          rs->v = cb.v;
+          rs->key = cb.key;
+          rs->g = gl >= 0 ? j + cb.idx : -1;
+        }
+        rs->row[lane] = cv;
+        if (own_j) cluster.map_shared_rank(&rowj[par][0], d)[lane] = jv;
+      }
+    }
+    __syncthreads();  // the rows are read before the deferred update changes them
+    cluster_arrive();
+    // (c) pivot j-1 on columns j+1.., rows >= j
+    if (j > 0 && j + 1 < nb && j - 1 < steps - 1) {
+      const GerStep gs = ger_step(j - 1, nb, mp, lanes);
+      for (int64_t il = tid; il < nr; il += PT) {
+        const int64_t g = r0 + il;
+        if (g < j) continue;
+        const double x = el(j - 1, il);
+        for (int c = j + 1; c < nb; ++c) {
+          const int mode = ger_mode(gs, pprev, c);
+          el(c, il) = ger_apply(gs, mode, el(c, il), x, pprev[c], g);
+        }
+      }
+    }
+    cluster_wait();
+    // (d) the winner, identical in every CTA
+    Cand wk = cand_none();
+    int ws = 0;
+    {
+      Cand k = cand_none();
+      if (lane < C) {
+        k.v = slots[par][lane].v;
+        k.key = slots[par][lane].key;
+        k.idx = slots[par][lane].g;
+      }
+      wk = warp_best(k);
+      wk.v = __shfl_sync(0xffffffffu, wk.v, 0);
+      wk.key = __shfl_sync(0xffffffffu, wk.key, 0);
+      wk.idx = __shfl_sync(0xffffffffu, wk.idx, 0);
+      const unsigned m = __ballot_sync(0xffffffffu, lane < C && k.v == wk.v && k.key == wk.key && k.idx == wk.idx);
+      ws = m ? __ffs(m) - 1 : 0;
+    }
+    const int64_t jp = wk.v < 0 ? (int64_t)j : wk.idx;  // idamax -> 0 when nothing qualifies
+    const double *raw = jp == j ? rowj[par] : slots[par][ws].row;
+    double *pcur = piv[par];
+    if (tid < nb) {
+      double pv_ = raw[tid], ov = rowj[par][tid];
+      if (j > 0 && tid > j && j - 1 < steps - 1) {
+        const GerStep gs = ger_step(j - 1, nb, mp, lanes);
+        const int mode = ger_mode(gs, pprev, tid);
+        pv_ = ger_apply(gs, mode, pv_, raw[j - 1], pprev[tid], jp);
+        ov = ger_apply(gs, mode, ov, rowj[par][j - 1], pprev[tid], j);
+      }
+      pcur[tid] = pv_;
+      oldj[tid] = ov;
+      if (tid == j) sinv = 1.0 / pv_;  // once per CTA
+    }
+    __syncthreads();
+    const double pv = pcur[j];
+    if (cr == 0 && tid == 0) ipiv[j] = (int32_t)(jp + 1);
+    if (!nonzero64(pv)) {  // exact zero pivot: BOLA's "Matrix is singular" (src/getrf2.rs:166-168)
+      if (cr == 0 && tid == 0) *info = col0 + j + 1;
+      failed = true;
+      break;
+    }
+    inv = sinv;
+    // (e)
+    if (jp != j && tid < nb) {
+      if (j >= r0 && j < r1) el(tid, j - r0) = pcur[tid];
+      if (jp >= r0 && jp < r1) el(tid, jp - r0) = oldj[tid];
+    }
+    __syncthreads();
+    if (j < mp - 1) {
+      const bool next = j + 1 < nb && j < steps - 1;
+      const GerStep gs = ger_step(j, nb, mp, lanes);
+      const int mode = next ? ger_mode(gs, pcur, j + 1) : -1;
+      for (int64_t il = tid; il < nr; il += PT) {
+        const int64_t g = r0 + il;
+        if (g <= j) continue;
+        const double x = __dmul_rn(el(j, il), inv);
+        el(j, il) = x;
+        if (next) el(j + 1, il) = ger_apply(gs, mode, el(j + 1, il), x, pcur[j + 1], g);
+      }
+    }
+  }
+  if (!failed && cr == 0 && add_on_success != 0)
+    for (int t = tid; t < steps; t += PT) ipiv[t] += add_on_success;
+  __syncthreads();
+  for (int64_t e = tid; e < nr * nb; e += PT) {
+    const int64_t il = e % nr;
+    const int c = (int)(e / nr);
+    A[(r0 + il) + (int64_t)c * lda] = el(c, il);
+  }
+  cluster.sync();  // no CTA may leave while another can still read its shared memory
+}
+
 // iterative_getrf2 for a short, wide matrix (m <= 32 rows, any n): one CTA,
 // data in global memory.
 __global__ void __launch_bounds__(PT)
@@ -328,11 +540,13 @@ int launch_panel(cudaStream_t s, double *A, int64_t lda, int64_t mp, int nb, int
   for (;; C = C > 1 ? (C + 1) / 2 : 0) {
     if (C == 0) return fail(BOLA_ERR_CUDA, "panel_lu: no cluster size could be scheduled");
     const int64_t R = cdiv(mp, C);
-    size_t smem = panel_base_bytes() + (size_t)R * nb * sizeof(double);
-    const bool use_smem = smem <= SMEM_DATA_LIMIT;
-    if (!use_smem) smem = panel_base_bytes();
+    // rows in shared memory: the split-barrier kernel; taller panels keep
+    // their rows in global memory (panel_lu)
+    const size_t rows_bytes = (size_t)R * nb * sizeof(double);
+    const bool use_smem = rows_bytes <= SMEM_DATA_LIMIT;
+    const size_t smem = use_smem ? rows_bytes : panel_base_bytes();
     void (*kern)(double *, int64_t, int64_t, int, int32_t *, int32_t *, int32_t, int32_t, int, int64_t) =
-        use_smem ? panel_lu<true> : panel_lu<false>;
+        use_smem ? panel_lu_split : panel_lu<false>;
     BOLA_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_DATA_LIMIT + 4096));
     BOLA_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     cudaLaunchConfig_t cfg = {};

@@ -183,12 +183,6 @@ __device__ __forceinline__ void vstore(double *p, const double (&v)[2]) {
 // deferred update reached their columns > j: the same fmaf the owner does);
 // swap; one CTA barrier; the update of column j+1 only (the next pivot
 // column).  Multipliers of column j are scaled when column j+1 is searched.
-__device__ __forceinline__ void cluster_arrive() {
-  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void cluster_wait() {
-  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
 
 template <typename P>
 __global__ void __launch_bounds__(SPT)
