@@ -2,15 +2,18 @@
 // (src/getrf.rs:37-101, src/getrf2.rs:39-185).
 //
 // Blocked right-looking LU with BOLA's NB = 32.  Per block column:
-//   1. panel_lu: one thread-block CLUSTER (up to 16 CTAs, the panel's rows
-//      spread over them and held in shared memory) factors the (m-j) x 32
-//      panel column by column: warp-shuffle idamax under BOLA's lane order,
-//      pivot-row exchange through distributed shared memory, reciprocal scale
-//      and BOLA's pairwise rank-1 update — one cluster barrier per column.
+//   1. panel_lu_split: one thread-block CLUSTER (up to 16 CTAs, the panel's
+//      rows spread over them and held in shared memory) factors the
+//      (m-j) x 32 panel column by column: warp-shuffle idamax under BOLA's
+//      lane order, candidate rows pushed through distributed shared memory,
+//      reciprocal scale and BOLA's pairwise rank-1 update — one split cluster
+//      barrier per column (panel_lu, rows in global memory, for taller panels).
 //   2. step_swap_trsm: the 32 row interchanges applied to every other column
 //      (BOLA's two laswp calls) fused with BOLA's 32-row unit-lower trsm on
 //      the right block row.
-//   3. the exact DGEMM for the rank-32 trailing update.
+//   3. the exact DGEMM for the rank-32 trailing update (from n = 512 on split:
+//      the next panel's columns on a high-priority stream, the rest overlapping
+//      the next panel on a low-priority one).
 // Every element sees the same operation sequence as in BOLA, so A and ipiv
 // come out bit-identical (for the SIMD width selected).
 #include <cooperative_groups.h>
@@ -44,9 +47,9 @@ constexpr size_t panel_base_bytes() {
 }
 
 // Unblocked LU of an mp x nb panel (nb <= 32), iterative_getrf2 of
-// src/getrf2.rs:131-185.  SMEM: the CTA's rows live in shared memory
-// (column-major, ld R) while it works; otherwise they stay in global memory.
-template <bool SMEM>
+// src/getrf2.rs:131-185, for panels too tall for the cluster's shared memory:
+// the rows stay in global memory (L2), one full cluster barrier per column.
+// Panels whose rows fit in shared memory take panel_lu_split below.
 __global__ void __launch_bounds__(PT)
 panel_lu(double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_t *info, int32_t add_on_success,
          int32_t col0, int lanes, int64_t R) {
@@ -59,7 +62,6 @@ panel_lu(double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_t *inf
   double *prow = reinterpret_cast<double *>(red + PT / 32);
   int64_t *bc = reinterpret_cast<int64_t *>(prow + PNB);
   double *pinv = reinterpret_cast<double *>(bc + 4);  // 1 / pivot of the current column
-  double *data = pinv + 2;
 
   // Uniform across the cluster: the only writer of *info in this kernel acts
   // after a cluster barrier that every CTA reaches after this read.
@@ -69,16 +71,7 @@ panel_lu(double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_t *inf
   const int64_t r0 = (int64_t)cr * R;
   const int64_t r1 = imin(mp, r0 + R);
   const int64_t nr = r1 > r0 ? r1 - r0 : 0;
-  auto el = [&](int64_t il, int c) -> double & {
-    return SMEM ? data[(int64_t)c * R + il] : A[(r0 + il) + (int64_t)c * lda];
-  };
-  if (SMEM) {
-    for (int64_t e = tid; e < nr * nb; e += PT) {
-      const int64_t il = e % nr;
-      const int c = (int)(e / nr);
-      data[(int64_t)c * R + il] = A[(r0 + il) + (int64_t)c * lda];
-    }
-  }
+  auto el = [&](int64_t il, int c) -> double & { return A[(r0 + il) + (int64_t)c * lda]; };
   __syncthreads();
 
   const int steps = (int)imin(mp, nb);
@@ -186,13 +179,6 @@ panel_lu(double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_t *inf
   }
   if (!failed && cr == 0 && add_on_success != 0)
     for (int t = tid; t < steps; t += PT) ipiv[t] += add_on_success;
-  if (SMEM) {
-    for (int64_t e = tid; e < nr * nb; e += PT) {
-      const int64_t il = e % nr;
-      const int c = (int)(e / nr);
-      A[(r0 + il) + (int64_t)c * lda] = data[(int64_t)c * R + il];
-    }
-  }
   cluster.sync();  // no CTA may leave while another can still read its shared memory
 }
 
@@ -546,7 +532,7 @@ int launch_panel(cudaStream_t s, double *A, int64_t lda, int64_t mp, int nb, int
     const bool use_smem = rows_bytes <= SMEM_DATA_LIMIT;
     const size_t smem = use_smem ? rows_bytes : panel_base_bytes();
     void (*kern)(double *, int64_t, int64_t, int, int32_t *, int32_t *, int32_t, int32_t, int, int64_t) =
-        use_smem ? panel_lu_split : panel_lu<false>;
+        use_smem ? panel_lu_split : panel_lu;
     BOLA_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_DATA_LIMIT + 4096));
     BOLA_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     cudaLaunchConfig_t cfg = {};

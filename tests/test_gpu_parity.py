@@ -115,7 +115,7 @@ def test_syrk_blas_definition_where_bola_misaddresses(gpu, uplo, trans):
 
 
 @pytest.mark.parametrize("m,n", [(3, 3), (31, 31), (32, 32), (33, 33), (100, 100), (257, 257), (300, 200),
-                                 (200, 300), (1000, 1000), (20, 90), (90, 20)])
+                                 (200, 300), (1000, 1000), (20, 90), (90, 20), (13000, 40)])
 def test_getrf_bitwise(both, m, n):
     g, o = both
     A = wl.uniform_matrix(m, n, seed=m * 7 + n, lo=-1, hi=1)
