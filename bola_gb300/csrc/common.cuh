@@ -148,6 +148,17 @@ __device__ __forceinline__ void cluster_wait() {
 // operations per clock per SM and a comparison takes a slot like an FMA, so
 // the zero tests inside BOLA's update loops are done on the bits.
 __device__ __forceinline__ bool nonzero64(double x) { return (__double_as_longlong(x) << 1) != 0; }
+// f ? fma(alpha, x, y) : y + alpha*x (fused body or unfused tail of one of
+// BOLA's SIMD loops), with the choice made per warp when the warp agrees: a
+// per-lane select would issue the FMA, the multiply and the add for every
+// lane (four times the FP64 slots of the FMA alone, measured), while a warp
+// whose lanes all take the same form issues only that form.
+__device__ __forceinline__ double fused_or_unfused(bool f, double alpha, double x, double y) {
+  const unsigned m = __activemask();
+  if (__all_sync(m, f)) return __fma_rn(alpha, x, y);
+  if (!__any_sync(m, f)) return __dadd_rn(y, __dmul_rn(alpha, x));
+  return f ? __fma_rn(alpha, x, y) : __dadd_rn(y, __dmul_rn(alpha, x));
+}
 __device__ __forceinline__ bool stop_flag(const int32_t *info) {
   return info != nullptr && *(volatile const int32_t *)info != 0;
 }
@@ -159,7 +170,7 @@ __device__ __forceinline__ bool stop_flag(const int32_t *info) {
 __device__ __forceinline__ double daxpy_elem(double y, double alpha, double x, int64_t idx,
                                              int64_t len, int lanes) {
   const int64_t done = len & ~(int64_t)(lanes - 1);
-  return idx < done ? fused(alpha, x, y) : add_prod(y, alpha, x);
+  return fused_or_unfused(idx < done, alpha, x, y);
 }
 
 // BOLA's dot_product(n, x, 1, y, 1) (src/utilities.rs:22-54 / :62-92) with

@@ -165,8 +165,8 @@ panel_lu(double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_t *inf
           if (!nonzero64(t0) && !nonzero64(t1)) continue;
           double &a0 = el(il, c0);
           double &a1 = el(il, c0 + 1);
-          a0 = vec ? fused(x, t0, a0) : add_prod(a0, t0, x);
-          a1 = vec ? fused(x, t1, a1) : add_prod(a1, t1, x);
+          a0 = fused_or_unfused(vec, x, t0, a0);
+          a1 = fused_or_unfused(vec, x, t1, a1);
         }
         if (ncols % 2) {
           const int c = nb - 1;
@@ -211,7 +211,7 @@ __device__ __forceinline__ int ger_mode(const GerStep &s, const double *prow, in
 __device__ __forceinline__ double ger_apply(const GerStep &s, int mode, double a, double x, double pc, int64_t g) {
   if (mode < 0) return a;
   const double t = -pc;
-  return (mode == 1 && g - s.p - 1 < s.vec_end) ? fused(x, t, a) : add_prod(a, t, x);
+  return fused_or_unfused(mode == 1 && g - s.p - 1 < s.vec_end, x, t, a);
 }
 
 // What a CTA pushes into every CTA of the cluster for one column: its pivot
@@ -453,7 +453,7 @@ panel_lu_wide(double *A, int64_t lda, int64_t m, int64_t n, int32_t *ipiv, int32
           const double t0 = -A[j + p0 * lda], t1 = -A[j + (p0 + 1) * lda];
           if (!nonzero64(t0) && !nonzero64(t1)) continue;
           const double t = (c == p0) ? t0 : t1;
-          a = ri < rows_vec ? fused(x, t, a) : add_prod(a, t, x);
+          a = fused_or_unfused(ri < rows_vec, x, t, a);
         } else {
           const double t = -A[j + c * lda];
           if (nonzero64(t)) a = add_prod(a, t, x);

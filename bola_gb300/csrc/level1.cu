@@ -75,7 +75,7 @@ __global__ void ger_kernel(int64_t m, int64_t n, double alpha, const double *__r
     const double t1 = __dmul_rn(alpha, y[(j0 + 1) * ldy]);
     if (!nonzero64(t0) && !nonzero64(t1)) return;
     const double t = (j == j0) ? t0 : t1;
-    *ap = (i < rows_vec) ? fused(x[i], t, *ap) : add_prod(*ap, t, x[i]);
+    *ap = fused_or_unfused(i < rows_vec, x[i], t, *ap);
   } else {
     const double t = __dmul_rn(alpha, y[j * ldy]);
     if (nonzero64(t)) *ap = add_prod(*ap, t, x[i]);

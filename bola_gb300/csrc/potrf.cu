@@ -286,7 +286,7 @@ __device__ int p2_right_looking(double *a, double *rdg, int n, int lanes) {
       if (!nonzero64(ljl)) continue;  // BOLA skips a zero multiplier
       const double lil = a[i + l * LDS];
       double &c = a[i + j * LDS];
-      c = ((em[s] >> l) & 1u) ? fused(-ljl, lil, c) : __dsub_rn(c, __dmul_rn(ljl, lil));
+      c = fused_or_unfused((em[s] >> l) & 1u, -ljl, lil, c);  // unfused: c + (-l_jl) l_il = c - l_jl l_il
     }
     __syncthreads();
   }

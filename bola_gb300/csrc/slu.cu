@@ -481,9 +481,16 @@ sswap_trsm(T *W, int64_t ldw, int64_t n, int64_t j, int jb, const int32_t *plan,
   if (col < j + jb) return;
   T b0 = lane < jb ? cp[j + lane] : T(0);
   T b1 = lane + 32 < jb ? cp[j + lane + 32] : T(0);
-  for (int k = 0; k < jb; ++k) {
-    const T bk = __shfl_sync(0xffffffffu, k < 32 ? b0 : b1, k & 31);
+  // rows 0..31 take updates from k < 32 only: two loops, so that no warp
+  // instruction runs with every lane idle (an FP64 one costs its full slot)
+  const int k0 = jb < 32 ? jb : 32;
+  for (int k = 0; k < k0; ++k) {
+    const T bk = __shfl_sync(0xffffffffu, b0, k);
     if (lane > k) b0 = fmaT(-L[lane + k * SNB], bk, b0);
+    if (lane + 32 < jb) b1 = fmaT(-L[lane + 32 + k * SNB], bk, b1);
+  }
+  for (int k = 32; k < jb; ++k) {
+    const T bk = __shfl_sync(0xffffffffu, b1, k - 32);
     if (lane + 32 > k && lane + 32 < jb) b1 = fmaT(-L[lane + 32 + k * SNB], bk, b1);
   }
   if (lane < jb) cp[j + lane] = b0;
