@@ -128,6 +128,37 @@ def test_getrf_bitwise(both, m, n):
     assert same(A1, A2), np.abs(A1 - A2).max()
 
 
+@pytest.mark.parametrize("m,n,pad", [(900, 600, 5), (600, 900, 3), (700, 700, 64)])
+def test_getrf_lookahead_rectangular_padded(both, m, n, pad):
+    """The look-ahead path (min(m, n) >= 512) on rectangular matrices whose
+    leading dimension exceeds m; the padding rows must stay untouched."""
+    g, o = both
+    lda = m + pad
+    A = np.asfortranarray(wl.uniform_matrix(lda, n, seed=m + 3 * n + pad, lo=-1, hi=1))
+    A1, A2 = A.copy(order="F"), A.copy(order="F")
+    p1 = np.zeros(min(m, n), np.int32)
+    p2 = np.zeros(min(m, n), np.int32)
+    assert o.getrf(m, n, A1, lda, p1) == 0
+    assert g.getrf(m, n, A2, lda, p2) == 0
+    assert np.array_equal(p1, p2)
+    assert same(A1, A2)
+    assert np.array_equal(A2[m:, :], A[m:, :])
+
+
+@pytest.mark.parametrize("uplo", ["L", "U"])
+def test_potrf_right_looking_padded(both, uplo):
+    g, o = both
+    n, lda = 600, 611
+    S = wl.spd_matrix(n, seed=21)
+    A = np.asfortranarray(wl.uniform_matrix(lda, n, seed=22, lo=-1, hi=1))
+    A[:n, :] = S
+    A1, A2 = A.copy(order="F"), A.copy(order="F")
+    assert o.potrf(uplo, n, A1, lda) == 0
+    assert g.potrf(uplo, n, A2, lda) == 0
+    assert same(A1, A2)
+    assert np.array_equal(A2[n:, :], A[n:, :])
+
+
 def test_getrf_ties_follow_bola_lane_order(both):
     """Integer matrices make exact pivot ties common."""
     g, o = both
