@@ -197,16 +197,21 @@ __device__ int group_chol_solve(const SystemDesc &S, int t, int G, int g, double
     group_sync(G, g);
     const int m = n - k - 1;
     if (m > 0) {
-      const int dq = G / m, dr = G % m;
-      int i = k + 1 + t % m, j = k + 1 + t / m;
-      for (int e = t; e < m * m; e += G) {
-        if (j <= i)
-          A[i + (int64_t)j * lda] = fma(-A[i + (int64_t)k * lda], A[j + (int64_t)k * lda], A[i + (int64_t)j * lda]);
-        i += dr;
-        j += dq;
-        if (i >= n) {
-          i -= m;
-          ++j;
+      // the lower triangle of the m x m trailing block only, packed column by
+      // column (column jj holds rows jj..m-1): walking the full square would
+      // issue the FP64 update for the upper half too, predicated off
+      int ii = t, jj = 0;
+      while (ii >= m && jj < m) {
+        ii -= m - jj - 1;
+        ++jj;
+      }
+      for (int e = t; e < m * (m + 1) / 2; e += G) {
+        const int i = k + 1 + ii, j = k + 1 + jj;
+        A[i + (int64_t)j * lda] = fma(-A[i + (int64_t)k * lda], A[j + (int64_t)k * lda], A[i + (int64_t)j * lda]);
+        ii += G;
+        while (ii >= m && jj < m) {
+          ii -= m - jj - 1;
+          ++jj;
         }
       }
     }
