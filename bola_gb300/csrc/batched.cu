@@ -86,6 +86,105 @@ __device__ int group_argmax(const double *col, int k, int n, int t, int G, int g
   return r;
 }
 
+// ---- blocked factorisation pieces -------------------------------------------
+// The factorisations below run in panels of PB columns: pivots inside the
+// panel update only the panel's columns; the rest of the matrix then gets the
+// whole panel at once (U12 by a small forward substitution, A22 by register
+// tiles of TR x TC elements per thread), so each trailing element is loaded
+// and stored once per panel instead of once per pivot.  Every element still
+// receives fma(-l_ik, u_kj, a_ij) for k in increasing order, with the values
+// the unblocked order gives it (row interchanges move whole rows, deferred
+// updates included), so results are those of the unblocked algorithm, bit for
+// bit.
+constexpr int PB = 8;
+constexpr int TR = 4, TC = 4;
+
+// A[c0:n, c0:n] -= A[c0:n, k0:k0+kb] * A[k0:k0+kb, c0:n] (lower = false), or
+// its lower triangle -= A[c0:n, k0:k0+kb] * A[c0:n, k0:k0+kb]^T (lower = true),
+// with c0 = k0 + kb.
+__device__ void group_trailing(double *A, int lda, int n, int k0, int kb, bool lower, int t, int G) {
+  const int c0 = k0 + kb, m2 = n - c0;
+  if (m2 <= 0) return;
+  const int tr = (m2 + TR - 1) / TR, tc = (m2 + TC - 1) / TC;
+  // tile (ti, tj): the full tr x tc grid, or its lower triangle (ti >= tj) packed by columns
+  int ti = t, tj = 0, dq = 0, dr = 0;
+  if (lower) {
+    while (ti >= tr && tj < tr) {
+      ti -= tr - tj - 1;
+      ++tj;
+    }
+  } else {
+    dq = G / tr;
+    dr = G % tr;
+    ti = t % tr;
+    tj = t / tr;
+  }
+  const int ntiles = lower ? tr * (tr + 1) / 2 : tr * tc;
+  for (int e = t; e < ntiles; e += G) {
+    const int i0 = c0 + ti * TR, j0 = c0 + tj * TC;
+    double acc[TR][TC];
+#pragma unroll
+    for (int r = 0; r < TR; ++r)
+#pragma unroll
+      for (int c = 0; c < TC; ++c) {
+        const int i = i0 + r, j = j0 + c;
+        acc[r][c] = (i < n && j < n) ? A[i + (int64_t)j * lda] : 0.0;
+      }
+    for (int q = 0; q < kb; ++q) {
+      const int64_t kq = (int64_t)(k0 + q) * lda;
+      double l[TR], u[TC];
+#pragma unroll
+      for (int r = 0; r < TR; ++r) l[r] = i0 + r < n ? A[i0 + r + kq] : 0.0;
+#pragma unroll
+      for (int c = 0; c < TC; ++c)
+        u[c] = j0 + c < n ? (lower ? A[j0 + c + kq] : A[(k0 + q) + (int64_t)(j0 + c) * lda]) : 0.0;
+#pragma unroll
+      for (int r = 0; r < TR; ++r)
+#pragma unroll
+        for (int c = 0; c < TC; ++c) acc[r][c] = fma(-l[r], u[c], acc[r][c]);
+    }
+#pragma unroll
+    for (int r = 0; r < TR; ++r)
+#pragma unroll
+      for (int c = 0; c < TC; ++c) {
+        const int i = i0 + r, j = j0 + c;
+        if (i < n && j < n && (!lower || i >= j)) A[i + (int64_t)j * lda] = acc[r][c];
+      }
+    if (lower) {
+      ti += G;
+      while (ti >= tr && tj < tr) {
+        ti -= tr - tj - 1;
+        ++tj;
+      }
+    } else {
+      ti += dr;
+      tj += dq;
+      if (ti >= tr) {
+        ti -= tr;
+        ++tj;
+      }
+    }
+  }
+}
+
+// U12 = L11^-1 A12 for the panel rows k0..k0+kb-1 (unit lower L11), a column
+// per thread: row r takes fma(-l_rq, u_q, u_r) for q < r in increasing q.
+__device__ void group_u12(double *A, int lda, int n, int k0, int kb, int t, int G) {
+  for (int j = k0 + kb + t; j < n; j += G) {
+    double u[PB];
+#pragma unroll
+    for (int r = 0; r < PB; ++r) u[r] = r < kb ? A[(k0 + r) + (int64_t)j * lda] : 0.0;
+#pragma unroll
+    for (int q = 0; q < PB - 1; ++q)
+#pragma unroll
+      for (int r = q + 1; r < PB; ++r)
+        if (r < kb) u[r] = fma(-A[(k0 + r) + (int64_t)(k0 + q) * lda], u[q], u[r]);
+#pragma unroll
+    for (int r = 1; r < PB; ++r)
+      if (r < kb) A[(k0 + r) + (int64_t)j * lda] = u[r];
+  }
+}
+
 // LU with partial pivoting of one system by a group; the row interchanges are
 // applied to B as they happen, then L y = P b and U x = y.
 __device__ int group_lu_solve(const SystemDesc &S, int t, int G, int g, long long *redv, int *redi, double *sinv) {
@@ -116,13 +215,16 @@ __device__ int group_lu_solve(const SystemDesc &S, int t, int G, int g, long lon
     const double inv = *sinv;
     for (int i = k + 1 + t; i < n; i += G) A[i + (int64_t)k * lda] *= inv;
     group_sync(G, g);
-    const int m = n - k - 1;
-    if (m > 0) {
-      // element e = t, t + G, ... of the m x m trailing block, (i, j) advanced
-      // without a division per element
+    // the rank-1 update on the rest of this panel's columns; the columns after
+    // the panel get the whole panel at once below
+    const int k0 = k - k % PB, kend = k0 + PB < n ? k0 + PB : n;
+    const int m = n - k - 1, w = kend - k - 1;
+    if (m > 0 && w > 0) {
+      // element e = t, t + G, ... of the m x w block, (i, j) advanced without a
+      // division per element
       const int dq = G / m, dr = G % m;
       int i = k + 1 + t % m, j = k + 1 + t / m;
-      for (int e = t; e < m * m; e += G) {
+      for (int e = t; e < m * w; e += G) {
         A[i + (int64_t)j * lda] = fma(-A[i + (int64_t)k * lda], A[k + (int64_t)j * lda], A[i + (int64_t)j * lda]);
         i += dr;
         j += dq;
@@ -133,6 +235,12 @@ __device__ int group_lu_solve(const SystemDesc &S, int t, int G, int g, long lon
       }
     }
     group_sync(G, g);
+    if (k + 1 == kend && kend < n) {  // the panel is done: U12, then A22
+      group_u12(A, lda, n, k0, kend - k0, t, G);
+      group_sync(G, g);
+      group_trailing(A, lda, n, k0, kend - k0, false, t, G);
+      group_sync(G, g);
+    }
   }
   if (info) return info;
   // forward: unit lower
@@ -195,27 +303,34 @@ __device__ int group_chol_solve(const SystemDesc &S, int t, int G, int g, double
     const double inv = *sinv;
     for (int i = k + 1 + t; i < n; i += G) A[i + (int64_t)k * lda] *= inv;
     group_sync(G, g);
-    const int m = n - k - 1;
-    if (m > 0) {
-      // the lower triangle of the m x m trailing block only, packed column by
-      // column (column jj holds rows jj..m-1): walking the full square would
-      // issue the FP64 update for the upper half too, predicated off
+    // the rank-1 update on the rest of this panel's columns, lower part only,
+    // packed column by column (column jj, global k+1+jj, holds rows jj..m-1):
+    // walking the full square would issue the FP64 update for the upper half
+    // too, predicated off
+    const int k0 = k - k % PB, kend = k0 + PB < n ? k0 + PB : n;
+    const int m = n - k - 1, w = kend - k - 1;
+    if (m > 0 && w > 0) {
       int ii = t, jj = 0;
-      while (ii >= m && jj < m) {
+      while (ii >= m && jj < w) {
         ii -= m - jj - 1;
         ++jj;
       }
-      for (int e = t; e < m * (m + 1) / 2; e += G) {
+      const int total = w * m - w * (w - 1) / 2;
+      for (int e = t; e < total; e += G) {
         const int i = k + 1 + ii, j = k + 1 + jj;
         A[i + (int64_t)j * lda] = fma(-A[i + (int64_t)k * lda], A[j + (int64_t)k * lda], A[i + (int64_t)j * lda]);
         ii += G;
-        while (ii >= m && jj < m) {
+        while (ii >= m && jj < w) {
           ii -= m - jj - 1;
           ++jj;
         }
       }
     }
     group_sync(G, g);
+    if (k + 1 == kend && kend < n) {  // the panel is done: the trailing lower triangle
+      group_trailing(A, lda, n, k0, kend - k0, true, t, G);
+      group_sync(G, g);
+    }
   }
   for (int k = 0; k < n; ++k) {  // L y = b
     for (int c = t; c < nr; c += G) B[k + (int64_t)c * ldb] /= A[k + (int64_t)k * lda];
