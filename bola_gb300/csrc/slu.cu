@@ -21,6 +21,7 @@
 
 #include "common.cuh"
 #include "mixed.cuh"
+#include "sm100.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -32,10 +33,36 @@ constexpr int SPT = 256;  // threads per panel CTA
 constexpr int SMAXC = 16;
 
 template <typename T>
-struct SSlot {
+struct alignas(16) SSlot {
   uint32_t k0, k1, k2, pad;  // pivot key (see PKey)
   T v[SNB];                  // the candidate row
 };
+
+// Asynchronous stores into another CTA's shared memory that complete by
+// adding their byte count to that CTA's mbarrier (st.async): the receiver
+// waits on its own mbarrier instead of a cluster-wide barrier.
+__device__ __forceinline__ uint32_t cluster_addr(const void *local, int rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(sm100::smem_u32(local)), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void st_async(uint32_t addr, float v, uint32_t bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(addr),
+               "r"(__float_as_uint(v)), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void st_async(uint32_t addr, double v, uint32_t bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];" ::"r"(addr),
+               "l"(__double_as_longlong(v)), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void st_async4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d,
+                                          uint32_t bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(
+                   addr),
+               "r"(a), "r"(b), "r"(c), "r"(d), "r"(bar)
+               : "memory");
+}
 
 // Pivot key, compared lexicographically: the bits of |v| (high word, low
 // word; the low word is 0 for FP32) and ~row, so the largest magnitude wins
@@ -176,19 +203,24 @@ __device__ __forceinline__ void vstore(double *p, const double (&v)[2]) {
 //
 // Per column j: pivot search in column j, one CTA barrier, every warp pushes
 // the CTA's candidate row (and row j if the CTA owns it) into its share of
-// the CTAs, cluster-barrier ARRIVE; then, while the other CTAs catch up, the
-// rank-1 update of pivot j-1 on columns j+1.. (deferred from the previous
-// column); cluster-barrier WAIT; every CTA picks the same winner from its own
-// slots and brings the pushed rows up to date (they left before pivot j-1's
-// deferred update reached their columns > j: the same fmaf the owner does);
-// swap; one CTA barrier; the update of column j+1 only (the next pivot
-// column).  Multipliers of column j are scaled when column j+1 is searched.
+// the CTAs with asynchronous remote stores that count their bytes on the
+// receiver's mbarrier (st.async), one CTA barrier; then, while the other
+// CTAs' pushes arrive, the rank-1 update of pivot j-1 on columns j+1..
+// (deferred from the previous column); a wait on this CTA's own mbarrier for
+// every CTA's push (no cluster-wide barrier: a CTA pushes column j+1 only
+// after it has read column j's slots, which is what makes the double-buffered
+// slots safe); every CTA picks the same winner from its own slots and brings
+// the pushed rows up to date (they left before pivot j-1's deferred update
+// reached their columns > j: the same fmaf the owner does); swap; one CTA
+// barrier; the update of column j+1 only (the next pivot column).
+// Multipliers of column j are scaled when column j+1 is searched.  Waits are
+// bounded: a push that never lands sets *err and ends the panel.
 
 template <typename P>
 __global__ void __launch_bounds__(SPT)
 spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0, int32_t *info, int kind,
               void *aop, float *aop_lo, int32_t *aexp, int64_t cap, int64_t R, int32_t *plan, uint64_t *track,
-              double give_up) {
+              double give_up, int32_t *err) {
   cg::cluster_group cluster = cg::this_cluster();
   // An abandoned factorisation: the flag was set by an earlier panel on this
   // stream, so every CTA of the cluster reads the same value.  Identity
@@ -208,6 +240,8 @@ spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, 
   __shared__ T oldj[SNB];     // the old row j, up to date (goes to the pivot's place)
   __shared__ PKey wkey[SPT / 32];
   __shared__ T sinv;          // 1 / pivot of the current column
+  __shared__ uint64_t xbar[2];  // completes when every CTA's push for a column has landed here
+  __shared__ int sfail;
   extern __shared__ __align__(16) unsigned char sp_raw[];
   T *sp = reinterpret_cast<T *>(sp_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -224,8 +258,18 @@ spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, 
     const int c = (int)(e / ns);
     sp[c * RP + il] = P::load(W[(r0 + il) + c * ldw]);
   }
+  if (tid == 0) {
+    sm100::mbar_init(&xbar[0], 1);
+    sm100::mbar_init(&xbar[1], 1);
+    sm100::fence_mbar_init();
+    sfail = 0;
+  }
   __syncthreads();
-  cluster.sync();  // every CTA of the cluster is running before the first push
+  cluster.sync();  // every CTA runs, its mbarriers initialised, before the first push
+  // bytes that land in this CTA per column: a slot from every CTA, row j from its owner
+  constexpr uint32_t SLOT_BYTES = 16 + SNB * sizeof(T), ROW_BYTES = SNB * sizeof(T);
+  const uint32_t xbytes = (uint32_t)C * SLOT_BYTES + ROW_BYTES;
+  bool failed = false;
 
   T inv = P::zero();  // 1 / pivot of the previous column
   // |u_jj| of this panel's pivots as ordered integer bits (NaN ignored, as
@@ -234,6 +278,9 @@ spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, 
   for (int j = 0; j < jb; ++j) {
     const int par = j & 1;
     const T *pprev = piv[par ^ 1];
+    // this column's phase of xbar[par] (its previous phase, column j-2, was
+    // waited for by every thread): expect the pushes
+    if (tid == 0) sm100::mbar_arrive_expect_tx(&xbar[par], xbytes);
     // -- the multipliers of column j-1, then this CTA's pivot candidate in
     // column j: key = (|v| bits, ~row), max wins, ties -> lowest row
     PKey best = PKey{0u, 0u, 0u};
@@ -266,23 +313,19 @@ spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, 
         j1v = lane + 32 < jb ? PE(lane + 32, jl) : P::zero();
       }
       for (int d = warp; d < C; d += SPT / 32) {
-        SSlot<T> *rs = cluster.map_shared_rank(&slots[par][cr], d);
-        if (lane == 0) {
-          rs->k0 = ck.a;
-          rs->k1 = ck.b;
-          rs->k2 = ck.c;
-        }
-        rs->v[lane] = c0;
-        rs->v[lane + 32] = c1;
+        const uint32_t rbar = cluster_addr(&xbar[par], d);
+        const uint32_t rs = cluster_addr(&slots[par][cr], d);
+        if (lane == 0) st_async4(rs, ck.a, ck.b, ck.c, 0u, rbar);
+        st_async(rs + 16 + lane * (uint32_t)sizeof(T), c0, rbar);
+        st_async(rs + 16 + (lane + 32) * (uint32_t)sizeof(T), c1, rbar);
         if (own_j) {
-          T *rj = cluster.map_shared_rank(&rowj[par][0], d);
-          rj[lane] = j0v;
-          rj[lane + 32] = j1v;
+          const uint32_t rj = cluster_addr(&rowj[par][0], d);
+          st_async(rj + lane * (uint32_t)sizeof(T), j0v, rbar);
+          st_async(rj + (lane + 32) * (uint32_t)sizeof(T), j1v, rbar);
         }
       }
     }
     __syncthreads();  // the rows are read before the deferred update changes them
-    cluster_arrive();
     // -- the deferred rank-1 update of pivot j-1 on columns j+1..jb-1, rows >= j:
     // lanes walk rows, warps take every 8th column; the pivot-row values sit
     // in registers, so a thread's 8 loads are all in flight together
@@ -315,7 +358,18 @@ spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, 
         }
       }
     }
-    cluster_wait();
+    // every CTA's push for this column has landed (bounded: a missing push
+    // sets the error flag and ends the panel, never a hang)
+    {
+      const bool ok = sm100::bounded_wait(&xbar[par], (uint32_t)(j >> 1) & 1u);
+      if (!ok) sfail = 1;
+      __syncthreads();
+      if (sfail) {
+        if (tid == 0) atomicExch(err, 5);
+        failed = true;
+        break;
+      }
+    }
     // -- the winner, identical in every CTA: lane s reads slot s, warp max
     PKey wk;
     int ws = 0;
@@ -369,6 +423,7 @@ spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, 
       }
     }
   }
+  if (!failed) {  // (after a failed exchange the error flag fails the whole call)
   // the last column's multipliers
   for (int il = tid; il < nr; il += SPT)
     if (r0 + il >= jb) PE(jb - 1, il) = P::mul(PE(jb - 1, il), inv);
@@ -441,7 +496,8 @@ spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, 
       }
     }
   }
-  cluster.sync();
+  }
+  cluster.sync();  // no CTA leaves while another may still push into it
 }
 
 // The panel's interchanges on all other columns, U12 = L11^-1 A12 on the
@@ -521,7 +577,7 @@ __global__ void track_init(uint64_t *t) {
 template <typename P>
 int launch_spanel(cudaStream_t s, typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0,
                   int32_t *info, int kind, void *aop, float *aop_lo, int32_t *aexp, int64_t cap, int32_t *plan,
-                  uint64_t *track, double give_up) {
+                  uint64_t *track, double give_up, int32_t *err) {
   const int C = (int)imin(SMAXC, imax(1, cdiv(mp, SPT)));
   const int64_t R = cdiv(mp, C);
   const size_t smem = sizeof(typename P::S) * (size_t)jb * (size_t)panel_pitch<typename P::S>(R);
@@ -547,7 +603,7 @@ int launch_spanel(cudaStream_t s, typename P::G *W, int64_t ldw, int64_t mp, int
   ProfScope prof(s, P::kFP64 ? "spanel64" : "spanel", (double)mp * jb * jb,
                  2.0 * sizeof(typename P::G) * (double)mp * jb);
   BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, spanel_kernel<P>, W, ldw, mp, jb, ipiv, col0, info, kind, aop, aop_lo, aexp,
-                                   cap, R, plan, track, give_up));
+                                   cap, R, plan, track, give_up, err));
   return 0;
 }
 
@@ -667,7 +723,7 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
     using Pol = typename std::conditional<fp64, PanelF64, PanelF32>::type;
     BOLA_TRY(launch_spanel<Pol>(lu.sp, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, lu.kind,
                               upd ? lu.aop[buf] : nullptr, fp64 ? nullptr : lu.aop_lo[buf], fp64 ? lu.ea[buf] : nullptr,
-                              lu.cap_n, lu.plan, track, give_up));
+                              lu.cap_n, lu.plan, track, give_up, lu.err));
     // the row swaps reach every column: the previous wide update must be done
     if (wide_pending) BOLA_TRY_CUDA(cudaStreamWaitEvent(lu.sp, lu.ev_wide, 0));
     wide_pending = false;
