@@ -594,8 +594,9 @@ def roofline_for(name, v, peak_fp64_gflops):
         out["algorithmic_bytes_per_launch"] = round(per_launch)
     if name in ("spanel", "spanel64"):
         us_col = 1e3 * v["ms"] / max(v["launches"], 1) / 64.0
-        out["note"] = (f"latency-bound: {us_col:.2f} us per panel column (one cluster barrier, a DSMEM push of "
-                       f"the pivot candidate and three CTA barriers per column); the HBM fraction is not its limit")
+        out["note"] = (f"latency-bound: {us_col:.2f} us per panel column (an all-to-all exchange of the CTAs' "
+                       f"pivot candidates by st.async onto mbarriers and four CTA barriers per column); the HBM "
+                       f"fraction is not its limit")
     return out
 
 
