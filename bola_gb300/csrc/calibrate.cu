@@ -1,7 +1,8 @@
 // calibrate.cu — FP64 throughput probe of the device the library runs on.
 //
-// GB300 has no published FP64 figure that this build trusts, so roofline
-// fractions of the FP64 kernels are stated against this measurement: eight
+// The FP64 rate of a GB300 is far below its tensor rates and not a number to
+// take from a datasheet, so roofline fractions of the FP64 kernels are stated
+// against this measurement: eight
 // independent register-resident DFMA chains per thread, four 256-thread
 // blocks per SM, ~20 ms, timed with CUDA events.
 #include "common.cuh"
