@@ -871,7 +871,9 @@ int dgesv_mixed_ws(Workspace &w, int64_t n, int64_t nrhs, const double *a, int64
   BOLA_TRY_CUDA(cudaMemcpyAsync(&ferr, w.lu.err, sizeof ferr, cudaMemcpyDeviceToHost, s));
   BOLA_TRY_CUDA(cudaStreamSynchronize(s));
   info_out.factor_info = finfo;
-  if (ferr != 0) return fail(BOLA_ERR_CUDA, "mixed LU: tensor-core update timed out (%d)", ferr);
+  // a bounded wait gave up: 5 the panel's candidate exchange, others a
+  // tensor-core update's pipeline (the factor is then unusable)
+  if (ferr != 0) return fail(BOLA_ERR_CUDA, "mixed LU: a bounded wait expired (code %d)", ferr);
 
   bool converged = false;
   double berr = INFINITY, prev = INFINITY;
