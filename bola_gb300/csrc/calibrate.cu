@@ -6,6 +6,7 @@
 // independent register-resident DFMA chains per thread, four 256-thread
 // blocks per SM, ~20 ms, timed with CUDA events.
 #include "common.cuh"
+#include "sm100.cuh"
 
 namespace bola {
 namespace {
@@ -57,5 +58,46 @@ extern "C" int bola_measure_fp64_peak(double *gflops) {
   cudaFree(sink);
   const double flops = 2.0 * 8.0 * iters * (double)grid.x * block.x;
   *gflops = flops / (best * 1e6);
+  return 0;
+}
+
+// ---- bounded-wait self-test --------------------------------------------------
+namespace bola {
+namespace {
+
+// Waits that can only end by giving up: an mbarrier with one expected arrival
+// that never comes, and a flag that nothing sets.
+__global__ void bounded_wait_selftest(int32_t *flag_err, uint32_t polls) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    sm100::mbar_init(&bar, 1);
+    sm100::fence_mbar_init();
+  }
+  __syncthreads();
+  const bool done = sm100::bounded_wait(&bar, 0u, polls);
+  if (!done && threadIdx.x == 0) atomicOr(flag_err, 1);
+  if (threadIdx.x == 0) {
+    uint32_t p = 0;
+    for (;;) {
+      int v;
+      asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(flag_err + 1) : "memory");
+      if (v != 0) break;
+      if (++p > polls) {
+        atomicOr(flag_err, 2);
+        break;
+      }
+      __nanosleep(64);
+    }
+  }
+}
+
+}  // namespace
+}  // namespace bola
+
+extern "C" int bola_selftest_bounded_waits(int32_t *flag_err, uint32_t polls, bola_stream_t stream) {
+  using namespace bola;
+  if (flag_err == nullptr) return -1;
+  bounded_wait_selftest<<<1, 64, 0, (cudaStream_t)stream>>>(flag_err, polls);
+  BOLA_CHECK_LAUNCH();
   return 0;
 }

@@ -65,6 +65,15 @@ int bola_profile_read(int index, char *name, int name_len, int64_t *calls, int64
  * same device and clocks.  Synchronises the device. */
 int bola_measure_fp64_peak(double *gflops);
 
+/* Self-test of the library's bounded waits (no BOLA counterpart): one kernel
+ * waits on an mbarrier that nothing completes and on a device flag that
+ * nothing sets (flag_err[1], which must be 0), each for at most `polls`
+ * polls, and ORs 1 (mbarrier) and 2 (flag) into flag_err[0] when it gives
+ * up — the path every panel, tensor-core pipeline and dataflow solve takes
+ * when a wait expires.  The kernel returns normally; the context stays
+ * usable.  Asynchronous on the stream. */
+int bola_selftest_bounded_waits(int32_t *flag_err, uint32_t polls, bola_stream_t stream);
+
 /* ---- Level 1 ---------------------------------------------------------- */
 
 /* Replaces idamax(n, x) -> usize, src/idamax.rs:23 (x86_64) / :141 (aarch64).
