@@ -7,9 +7,13 @@
 // diagonal blocks use BOLA's syrk_kernel: per element a chain of daxpy
 // updates ('N') or of 32-deep dot products ('T') — one thread per element.
 //
-// POTRF is BOLA's left-looking blocked Cholesky (NB = 32): diagonal SYRK,
-// the 32x32 recursive potrf2 inside one CTA's shared memory, the panel GEMM
-// (split-K when the panel is skinny) and the right/left triangular solve.
+// POTRF is BOLA's blocked Cholesky (NB = 32): diagonal SYRK, the 32x32
+// potrf2 inside one CTA's shared memory, the panel GEMM and the triangular
+// solve.  Below n = 512 the steps run in BOLA's left-looking order; from 512
+// on the same per-element sums are formed right-looking with look-ahead on
+// two streams (potrf_blocked below says why the results are identical).  The
+// 'L' potrf2 block runs column by column with BOLA's fused/unfused pattern
+// per element; 'U' and failing blocks use BOLA's recursion.
 #include "common.cuh"
 
 namespace bola {
