@@ -9,7 +9,8 @@
 // of persistent 256-thread CTAs pulls items from an atomic counter; the CTA
 // splits into 256/G groups, each factoring one system in place in global
 // memory (L2-resident: at most 512 KB per system) with partial pivoting (LU)
-// or Cholesky, and then solving its right-hand sides.  A group synchronises
+// or Cholesky in panels of 8 columns (register-tiled trailing updates), and
+// then solving its right-hand sides.  A group synchronises
 // with its own named barrier, so a system's arithmetic never depends on which
 // systems share its CTA: every result is the same alone and in any mix.
 // FP64 throughout; all waits are barriers (no spin loops).

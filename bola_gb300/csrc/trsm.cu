@@ -7,7 +7,9 @@
 //   left, no transpose  — column forward/back substitution with BOLA's daxpy
 //                         (a warp per right-hand side, rows across lanes);
 //   left, transpose     — dot-style substitution, one thread per column;
-//   right               — column sweeps, one thread per row of B.
+//   right               — column sweeps, one thread per row of B; the
+//                         ascending ones (rnu, rtl) for n <= 32
+//                         right-looking, a row over 4 lanes in registers.
 #include "common.cuh"
 
 namespace bola {
