@@ -9,7 +9,7 @@
 //
 // POTRF is BOLA's blocked Cholesky (NB = 32): diagonal SYRK, the 32x32
 // potrf2 inside one CTA's shared memory, the panel GEMM and the triangular
-// solve.  Below n = 512 the steps run in BOLA's left-looking order; from 512
+// solve.  Below n = 320 the steps run in BOLA's left-looking order; from 320
 // on the same per-element sums are formed right-looking with look-ahead on
 // two streams (potrf_blocked below says why the results are identical).  The
 // 'L' potrf2 block runs column by column with BOLA's fused/unfused pattern
@@ -468,7 +468,7 @@ __global__ void potrf_restore(bool upper, int64_t n, const double *__restrict__ 
   }
 }
 
-// BOLA's blocking literally (left-looking), for small orders: below ~512 the
+// BOLA's blocking literally (left-looking), for small orders: below ~320 the
 // look-ahead streams, the input copy and the extra launches of the
 // right-looking form cost more than its shorter critical path saves.
 int potrf_left_looking(cudaStream_t s, bool upper, int64_t n, double *A, int64_t lda, int32_t *info) {
@@ -496,7 +496,7 @@ int potrf_left_looking(cudaStream_t s, bool upper, int64_t n, double *A, int64_t
   return 0;
 }
 
-constexpr int64_t RIGHT_LOOKING_MIN_N = 512;
+constexpr int64_t RIGHT_LOOKING_MIN_N = 320;
 
 int potrf_blocked(cudaStream_t s, char uplo, int64_t n, double *A, int64_t lda, int32_t *info) {
   const bool upper = uplo == 'U';
