@@ -348,7 +348,11 @@ def run_ours(args, rank, world, device):
         "backward_error_ok": all(v <= BERR_TARGET for v in berr.values()),
         "refinement": paths,
         "e2e": {"value": round(job_rate(world, args.steps, e2e_total), 4), "unit": "solves/s",
-                "h2d_bytes_per_step": 8 * (n * n + n * nrhs), "d2h_bytes_per_step": 8 * n * nrhs},
+                "h2d_bytes_per_step": 8 * (n * n + n * nrhs), "d2h_bytes_per_step": 8 * n * nrhs,
+                "ms_per_step": round(e2e_total / args.steps, 3),
+                "latency_ms": {"p50": round(statistics.median(e2e_per), 3),
+                               "p99": round(float(np.percentile(e2e_per, 99)), 3)},
+                "per_step_ms": [round(x, 2) for x in e2e_per]},
         "roofline": roof,
         "kernels": kernels,
         "gpu_launches": launches,
