@@ -13,6 +13,8 @@
 //     c = fma(alpha, acc, c)
 // and in BOLA's partial edge tiles (rows >= m rounded down to 8, or columns
 // >= n rounded down to 4): c = c + (alpha * op(B)[k,j]) * op(A)[i,k], unfused.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "common.cuh"
@@ -281,9 +283,15 @@ Tile choose_tile(int64_t m8, int64_t n4, int sms) {
 
 }  // namespace
 
-int dgemm_exact(cudaStream_t s, char ta, char tb, int64_t m, int64_t n, int64_t k, double alpha,
-                const double *A, int64_t lda, const double *B, int64_t ldb, double beta, double *C,
-                int64_t ldc, int kc, const int32_t *info, int tri) {
+namespace {
+
+// The exact DGEMM.  Split-K partial sums go to stream-ordered temporary
+// memory, or, when `fixed` is given, to that caller-provided device buffer of
+// `fixed_bytes` (a shape whose partial sums do not fit is rejected before
+// anything is launched).
+int dgemm_body(cudaStream_t s, char ta, char tb, int64_t m, int64_t n, int64_t k, double alpha,
+               const double *A, int64_t lda, const double *B, int64_t ldb, double beta, double *C,
+               int64_t ldc, int kc, const int32_t *info, int tri, double *fixed, size_t fixed_bytes) {
   if (m <= 0 || n <= 0) return 0;
   const bool TA = upc(ta) != 'N', TB = upc(tb) != 'N';
   const int64_t K = (alpha == 0.0 || k < 0) ? 0 : k;  // alpha == 0: only the beta pass
@@ -301,16 +309,24 @@ int dgemm_exact(cudaStream_t s, char ta, char tb, int64_t m, int64_t n, int64_t 
       nsplit = cdiv(nchunks, cps);
       const double bytes = 8.0 * (double)nchunks * (double)m8 * (double)n4;
       partial = nsplit >= 2 && bytes <= (1u << 30);
+      if (partial && fixed != nullptr && bytes > (double)fixed_bytes)
+        return fail(BOLA_ERR_UNSUPPORTED,
+                    "bola_dgemm_noalloc: this shape needs %.0f bytes of split-K scratch, the static scratch "
+                    "holds %zu bytes (%lld chunks x %lld x %lld doubles); use bola_dgemm",
+                    bytes, fixed_bytes, (long long)nchunks, (long long)m8, (long long)n4);
     }
     ProfScope prof(s, "dgemm", 2.0 * (double)m8 * (double)n4 * (double)K,
                    8.0 * ((double)m8 * K + (double)K * n4 + 2.0 * (double)m8 * n4), partial ? 2 : 1);
     if (partial) {
-      Scratch P;
-      BOLA_TRY(P.alloc((size_t)(8 * nchunks * m8 * n4), s));
+      // Every partial sum the fold reads is written by this call's partial
+      // pass, so a reused buffer (the fixed one) needs no clearing.
+      Scratch Ps;
+      if (fixed == nullptr) BOLA_TRY(Ps.alloc((size_t)(8 * nchunks * m8 * n4), s));
+      double *P = fixed != nullptr ? fixed : Ps.as<double>();
       dim3 grid((unsigned)cdiv(m8, t.bm), (unsigned)cdiv(n4, t.bn), (unsigned)nsplit);
 #define BOLA_LT(a, b)                                                                            \
   launch_tile<a, b>(t, true, s, grid, m8, n4, K, alpha, A, lda, B, ldb, beta, C, ldc, kc, info, tri, \
-                    cps, P.as<double>())
+                    cps, P)
       if (!TA && !TB) BOLA_LT(false, false);
       else if (!TA && TB) BOLA_LT(false, true);
       else if (TA && !TB) BOLA_LT(true, false);
@@ -318,8 +334,7 @@ int dgemm_exact(cudaStream_t s, char ta, char tb, int64_t m, int64_t n, int64_t 
 #undef BOLA_LT
       BOLA_CHECK_LAUNCH();
       const int64_t tot = m8 * n4;
-      gemm_fold<<<(unsigned)cdiv(tot, 256), 256, 0, s>>>(m8, n4, nchunks, alpha, beta, P.as<double>(), C,
-                                                        ldc, info, tri);
+      gemm_fold<<<(unsigned)cdiv(tot, 256), 256, 0, s>>>(m8, n4, nchunks, alpha, beta, P, C, ldc, info, tri);
       BOLA_CHECK_LAUNCH();
     } else {
       dim3 grid((unsigned)cdiv(m8, t.bm), (unsigned)cdiv(n4, t.bn), 1);
@@ -349,6 +364,14 @@ int dgemm_exact(cudaStream_t s, char ta, char tb, int64_t m, int64_t n, int64_t 
   return 0;
 }
 
+}  // namespace
+
+int dgemm_exact(cudaStream_t s, char ta, char tb, int64_t m, int64_t n, int64_t k, double alpha,
+                const double *A, int64_t lda, const double *B, int64_t ldb, double beta, double *C,
+                int64_t ldc, int kc, const int32_t *info, int tri) {
+  return dgemm_body(s, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, kc, info, tri, nullptr, 0);
+}
+
 }  // namespace bola
 
 extern "C" int bola_dgemm(char transa, char transb, int64_t m, int64_t n, int64_t k, double alpha,
@@ -373,8 +396,10 @@ extern "C" int bola_dgemm(char transa, char transb, int64_t m, int64_t n, int64_
 // For callers that may not allocate device memory (see bola_dgemm_noalloc in
 // include/bola_gb300.h).  When the output is too small to keep every SM busy,
 // bola_dgemm splits K and parks one partial accumulator per K chunk in
-// stream-ordered temporary memory; this variant parks them in a fixed array
-// that lives in the library's own device image instead.
+// stream-ordered temporary memory; this variant runs the same body (the same
+// tile, split and launches, so its results are bola_dgemm's bit for bit) with
+// the partial sums parked in a fixed array that lives in the library's own
+// device image instead.
 
 namespace bola {
 namespace {
@@ -386,23 +411,35 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchBytes / sizeof(double)];
 
 std::mutex g_noalloc_mu;
-double *g_noalloc_ptr[kMaxDevices] = {};
+struct NoAllocSlot {
+  unsigned long long ctx_id = 0;  // the context the address belongs to (0: none yet)
+  double *ptr = nullptr;
+};
+NoAllocSlot g_noalloc_slot[kMaxDevices];
 
-// Device address of the scratch array on the current device.  The host-side
-// symbol is only a stand-in, so the address is looked up once per device with
-// that device current and cached.
+// Device address of the scratch array in the current context.  The host-side
+// symbol is only a stand-in, so the address is looked up with the device
+// current and cached per device together with the context's unique id: a
+// device reset destroys the context and unloads the module, and the next
+// context may place the array elsewhere, so a new id means a new lookup.
 int noalloc_scratch(double **out) {
   int dev = 0;
   BOLA_TRY_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return fail(BOLA_ERR_UNSUPPORTED, "bola_dgemm_noalloc: device %d out of range", dev);
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (g_noalloc_ptr[dev] == nullptr) {
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (cuCtxGetCurrent(&ctx) != CUDA_SUCCESS || ctx == nullptr || cuCtxGetId(ctx, &id) != CUDA_SUCCESS) id = 0;
+  NoAllocSlot &slot = g_noalloc_slot[dev];
+  if (slot.ptr == nullptr || id == 0 || slot.ctx_id != id) {
     void *p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-    g_noalloc_ptr[dev] = static_cast<double *>(p);
+    if (id == 0 && cuCtxGetCurrent(&ctx) == CUDA_SUCCESS && ctx != nullptr) cuCtxGetId(ctx, &id);
+    slot.ptr = static_cast<double *>(p);
+    slot.ctx_id = id;
   }
-  *out = g_noalloc_ptr[dev];
+  *out = slot.ptr;
   return 0;
 }
 
@@ -413,78 +450,16 @@ extern "C" int bola_dgemm_noalloc(char transa, char transb, int64_t m, int64_t n
                                   const double *a, int64_t lda, const double *b, int64_t ldb, double beta,
                                   double *c, int64_t ldc, bola_stream_t stream) {
   using namespace bola;
-  cudaStream_t s = (cudaStream_t)stream;
   if (m < 0) return -3;
   if (n < 0) return -4;
   if (k < 0) return -5;
   if (m == 0 || n == 0) return 0;
-  const bool TA = upc(transa) != 'N', TB = upc(transb) != 'N';
-  if (k > 0 && alpha != 0.0 && lda < imax(1, TA ? k : m)) return -8;
-  if (k > 0 && alpha != 0.0 && ldb < imax(1, TB ? n : k)) return -10;
+  const bool ta = upc(transa) != 'N', tb = upc(transb) != 'N';
+  if (k > 0 && alpha != 0.0 && lda < imax(1, ta ? k : m)) return -8;
+  if (k > 0 && alpha != 0.0 && ldb < imax(1, tb ? n : k)) return -10;
   if (ldc < imax(1, m)) return -13;
-  const int kc = 64;
-  const int64_t K = (alpha == 0.0) ? 0 : k;
-  const int64_t m8 = (m / 8) * 8, n4 = (n / 4) * 4;
-  const int sms = num_sms();
-  if (m8 > 0 && n4 > 0) {
-    // the same shape decisions as bola_dgemm, so results are bit-identical
-    Tile t = choose_tile(m8, n4, sms);
-    const int64_t nchunks = (K + kc - 1) / kc;
-    const int64_t tiles = cdiv(m8, t.bm) * cdiv(n4, t.bn);
-    bool partial = false;
-    int64_t cps = 0, nsplit = 1;
-    if (tiles < sms && nchunks >= 2) {
-      const int64_t t32 = cdiv(m8, 32) * cdiv(n4, 32);
-      nsplit = imin(nchunks, cdiv(2 * (int64_t)sms, t32));
-      cps = cdiv(nchunks, nsplit);
-      nsplit = cdiv(nchunks, cps);
-      const double bytes = 8.0 * (double)nchunks * (double)m8 * (double)n4;
-      partial = nsplit >= 2 && bytes <= (1u << 30);
-      if (partial && bytes > (double)kNoAllocScratchBytes)
-        return fail(BOLA_ERR_UNSUPPORTED,
-                    "bola_dgemm_noalloc: this shape needs %.0f bytes of split-K scratch, the static scratch "
-                    "holds %zu bytes (%lld chunks x %lld x %lld doubles); use bola_dgemm",
-                    bytes, kNoAllocScratchBytes, (long long)nchunks, (long long)m8, (long long)n4);
-    }
-    if (partial) {
-      double *P = nullptr;
-      BOLA_TRY(noalloc_scratch(&P));
-      // Every scratch element the fold reads is written by the partial pass of
-      // the same call, so nothing has to be cleared between calls.
-      dim3 grid((unsigned)cdiv(m8, 32), (unsigned)cdiv(n4, 32), (unsigned)nsplit);
-      Tile t32{32, 32};
-#define BOLA_LT(x, y) \
-  launch_tile<x, y>(t32, true, s, grid, m8, n4, K, alpha, a, lda, b, ldb, beta, c, ldc, kc, nullptr, 0, cps, P)
-      if (!TA && !TB) BOLA_LT(false, false);
-      else if (!TA && TB) BOLA_LT(false, true);
-      else if (TA && !TB) BOLA_LT(true, false);
-      else BOLA_LT(true, true);
-#undef BOLA_LT
-      BOLA_CHECK_LAUNCH();
-      gemm_fold<<<(unsigned)cdiv(m8 * n4, 256), 256, 0, s>>>(m8, n4, nchunks, alpha, beta, P, c, ldc, nullptr, 0);
-      BOLA_CHECK_LAUNCH();
-    } else {
-      dim3 grid((unsigned)cdiv(m8, t.bm), (unsigned)cdiv(n4, t.bn), 1);
-#define BOLA_LT(x, y) \
-  launch_tile<x, y>(t, false, s, grid, m8, n4, K, alpha, a, lda, b, ldb, beta, c, ldc, kc, nullptr, 0, 0, nullptr)
-      if (!TA && !TB) BOLA_LT(false, false);
-      else if (!TA && TB) BOLA_LT(false, true);
-      else if (TA && !TB) BOLA_LT(true, false);
-      else BOLA_LT(true, true);
-#undef BOLA_LT
-      BOLA_CHECK_LAUNCH();
-    }
-  }
-  const int64_t ne = (m - m8) * n + m8 * (n - n4);
-  if (ne > 0) {
-    const unsigned g = (unsigned)cdiv(ne, 128);
-#define BOLA_LE(x, y) gemm_edge<x, y><<<g, 128, 0, s>>>(m, n, m8, n4, K, alpha, a, lda, b, ldb, beta, c, ldc, nullptr, 0)
-    if (!TA && !TB) BOLA_LE(false, false);
-    else if (!TA && TB) BOLA_LE(false, true);
-    else if (TA && !TB) BOLA_LE(true, false);
-    else BOLA_LE(true, true);
-#undef BOLA_LE
-    BOLA_CHECK_LAUNCH();
-  }
-  return 0;
+  double *P = nullptr;
+  BOLA_TRY(noalloc_scratch(&P));
+  return dgemm_body((cudaStream_t)stream, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, 64, nullptr,
+                    0, P, kNoAllocScratchBytes);
 }

@@ -139,7 +139,10 @@ int bola_dsyrk(char uplo, char trans, int64_t n, int64_t k, double alpha, const 
  *     BOLA_ERR_UNSUPPORTED and a message in bola_last_error().
  *   - The first call on each device looks up the array's device address
  *     (cudaGetSymbolAddress) with that device current; make that first call
- *     before any stream capture.
+ *     before any stream capture.  The address is cached with the id of the
+ *     device's context: after a device reset the first call in the new
+ *     context looks it up again, and that call too belongs before any
+ *     capture.
  *   - All calls on a device share the one array: calls whose kernels can
  *     overlap on the GPU (different streams, no ordering) race on it.  Calls
  *     on one stream are safe; each call writes every scratch value it later

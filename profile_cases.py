@@ -1,11 +1,11 @@
 """Small fixed workloads for profiling the library's kernels (ncu, timers).
 
-    python -m bola_gb300.profile_cases getrf N        # 2 x bola_dgetrf, A uniform[-1,1), seed 1
-    python -m bola_gb300.profile_cases potrf N        # 2 x bola_dpotrf('L'), A = B B^T / n + I, seed 2
-    python -m bola_gb300.profile_cases mixed N KIND   # 2 x bola_dgesv_mixed, 16 RHS, A = U[-1,1) + 4 I
-    python -m bola_gb300.profile_cases mixed N KIND E # the same on A = Q1 diag(s) Q2, kappa = 10^E, escalation on
-                                                      # (Q from torch's QR of seeded Gaussians: needs torch.linalg)
-    python -m bola_gb300.profile_cases batched COUNT  # 2 x bola_batch_solve, the batched workload (seed 4)
+    python profile_cases.py getrf N        # 2 x bola_dgetrf, A uniform[-1,1), seed 1
+    python profile_cases.py potrf N        # 2 x bola_dpotrf('L'), A = B B^T / n + I, seed 2
+    python profile_cases.py mixed N KIND   # 2 x bola_dgesv_mixed, 16 RHS, A = U[-1,1) + 4 I
+    python profile_cases.py mixed N KIND E # the same on A = Q1 diag(s) Q2, kappa = 10^E, escalation on
+                                    # (Q from torch's QR of seeded Gaussians: needs torch.linalg)
+    python profile_cases.py batched COUNT  # 2 x bola_batch_solve, the batched workload (seed 4)
 
 With --scopes, the library's own device timers are on during the last call
 and its per-scope device time is printed after it.
@@ -19,7 +19,7 @@ import sys
 
 import torch
 
-from . import _lib
+from bola_gb300 import _lib
 
 
 def _p(t):

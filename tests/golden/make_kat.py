@@ -1,19 +1,21 @@
 """Extract BOLA's own known-answer tests into tests/golden/bola_kat.json.
 
-Reads the Rust test sources of the BOLA crate (path given as argv[1],
-default /root/reference) as TEXT: each listed test function's `let` literals
+Reads the Rust test sources of the BOLA crate (the crate's root directory,
+a required argument) as TEXT: each listed test function's `let` literals
 (arrays and scalars) are parsed out, and the call it makes is recorded with
 the file:line of the test.  The JSON it writes is the fixture the test-suite
 uses; the suite itself never reads the BOLA sources.
 
-    python tests/golden/make_kat.py /root/reference
+    python tests/golden/make_kat.py <path-to-bola-crate>
 """
 import json
 import os
 import re
 import sys
 
-ROOT = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: make_kat.py <path-to-bola-crate>")
+ROOT = sys.argv[1]
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "bola_kat.json")
 
 # (file, test fn, routine, call arguments in BOLA's order; names refer to the

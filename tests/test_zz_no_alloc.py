@@ -40,8 +40,8 @@ def _operands(ta, tb, m, n, k, seed):
     A = torch.rand((m * k,), dtype=torch.float64, device="cuda", generator=g) * 2 - 1
     B = torch.rand((k * n,), dtype=torch.float64, device="cuda", generator=g) * 2 - 1
     C = torch.rand((m * n,), dtype=torch.float64, device="cuda", generator=g) * 2 - 1
-    lda = m if ta == "N" else k
-    ldb = k if tb == "N" else n
+    lda = max(1, m if ta == "N" else k)
+    ldb = max(1, k if tb == "N" else n)
     return A, lda, B, ldb, C
 
 
@@ -58,6 +58,11 @@ SHAPES = [
     ("T", "N", 1001, 24, 3000, 0.5, -2.0),   # split-K plus partial 8x4 edge tiles
     ("N", "N", 300, 200, 129, 1.0, 0.0),     # split-K, beta = 0
     ("N", "N", 2048, 2048, 64, 1.0, 1.0),    # enough tiles: no scratch used
+    # fewer 64x64 tiles than SMs but more than twice as many 32x32 tiles: a
+    # split count taken from 32x32 tiles would not split at all here
+    ("N", "N", 1024, 512, 256, 1.0, 1.0),
+    ("N", "T", 512, 64, 640, 0.0, 0.5),      # alpha = 0: only the beta pass
+    ("T", "T", 256, 96, 0, 2.0, -1.0),       # k = 0: only the beta pass
 ]
 
 
