@@ -417,6 +417,34 @@ struct NoAllocSlot {
 };
 NoAllocSlot g_noalloc_slot[kMaxDevices];
 
+// Unique id of the calling thread's current context (0 if none or unknown).
+// The driver functions are reached through the runtime's entry-point query,
+// so the library does not link the driver library directly.
+unsigned long long current_context_id() {
+  using GetCurrentFn = CUresult (*)(CUcontext *);
+  using GetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+  static GetCurrentFn get_current = nullptr;
+  static GetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrentFn>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetIdFn>(p);
+  });
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current == nullptr || get_id == nullptr || get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr ||
+      get_id(ctx, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
+
 // Device address of the scratch array in the current context.  The host-side
 // symbol is only a stand-in, so the address is looked up with the device
 // current and cached per device together with the context's unique id: a
@@ -427,15 +455,13 @@ int noalloc_scratch(double **out) {
   BOLA_TRY_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return fail(BOLA_ERR_UNSUPPORTED, "bola_dgemm_noalloc: device %d out of range", dev);
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  CUcontext ctx = nullptr;
-  unsigned long long id = 0;
-  if (cuCtxGetCurrent(&ctx) != CUDA_SUCCESS || ctx == nullptr || cuCtxGetId(ctx, &id) != CUDA_SUCCESS) id = 0;
   NoAllocSlot &slot = g_noalloc_slot[dev];
+  unsigned long long id = current_context_id();
   if (slot.ptr == nullptr || id == 0 || slot.ctx_id != id) {
     void *p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-    if (id == 0 && cuCtxGetCurrent(&ctx) == CUDA_SUCCESS && ctx != nullptr) cuCtxGetId(ctx, &id);
+    if (id == 0) id = current_context_id();  // the lookup initialised the context
     slot.ptr = static_cast<double *>(p);
     slot.ctx_id = id;
   }
