@@ -38,6 +38,9 @@ SIGNATURES = {
     "bola_dgemm_noalloc": (_int, [_c, _c, _i64, _i64, _i64, _d, _p, _i64, _p, _i64, _d, _p, _i64, _p]),
     "bola_sgemm_tc_update": (_int, [_int, _i64, _i64, _p, _p, _p, _p, _p, _i64, _p, _p]),
     "bola_dgemm_oz_update": (_int, [_i64, _i64, _p, _p, _p, _i64, _p, _p]),
+    "bola_sgetrf_mixed": (_int, [_int, _i64, _p, _i64, _p, _p, _p]),
+    "bola_spotrf_mixed": (_int, [_int, _i64, _p, _i64, _p, _p]),
+    "bola_dgemv_oz": (_int, [_i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p]),
     "bola_dtrsm": (_int, [_c, _c, _c, _c, _i64, _i64, _d, _p, _i64, _p, _i64, _p]),
     "bola_dsyrk": (_int, [_c, _c, _i64, _i64, _d, _p, _i64, _d, _p, _i64, _p]),
     "bola_dgetrf": (_int, [_i64, _i64, _p, _i64, _p, _p, _p]),
@@ -58,11 +61,12 @@ class MixedOpts(ctypes.Structure):
 class MixedInfo(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("gmres_iterations", ctypes.c_int), ("path", ctypes.c_int),
                 ("factor_info", ctypes.c_int), ("backward_error", ctypes.c_double),
-                ("condition_estimate", ctypes.c_double)]
+                ("condition_estimate", ctypes.c_double), ("factorization", ctypes.c_int), ("reserved", ctypes.c_int)]
 
 
 SIGNATURES["bola_dgesv_mixed"] = (_int, [_i64, _i64, _p, _i64, _p, _i64, _p, _i64, ctypes.POINTER(MixedOpts),
                                          ctypes.POINTER(MixedInfo), _p])
+SIGNATURES["bola_dposv_mixed"] = SIGNATURES["bola_dgesv_mixed"]
 
 
 
@@ -77,6 +81,8 @@ SIGNATURES.update({
     "bola_mixed_ctx_destroy": (_int, [_p]),
     "bola_mixed_ctx_bytes": (_i64, [_p]),
     "bola_dgesv_mixed_ctx": (_int, [_p, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, ctypes.POINTER(MixedOpts),
+                                    ctypes.POINTER(MixedInfo), _p]),
+    "bola_dposv_mixed_ctx": (_int, [_p, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, ctypes.POINTER(MixedOpts),
                                     ctypes.POINTER(MixedInfo), _p]),
     "bola_batch_plan_create": (_int, [_i32, _p, _p, _p, _p]),
     "bola_batch_solve": (_int, [_p, _p, _p, _p]),
@@ -98,7 +104,8 @@ class RequestInfo(ctypes.Structure):
     """bola_request_info (include/bola_gb300.h)."""
     _fields_ = [("status", ctypes.c_int32), ("path", ctypes.c_int32), ("iterations", ctypes.c_int32),
                 ("info", ctypes.c_int32), ("backward_error", ctypes.c_double), ("t_submit", ctypes.c_double),
-                ("t_admit", ctypes.c_double), ("t_done", ctypes.c_double)]
+                ("t_admit", ctypes.c_double), ("t_done", ctypes.c_double), ("factorization", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 SIGNATURES.update({

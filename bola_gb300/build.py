@@ -22,7 +22,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
 # units whose kernels may let the compiler contract a*b+c
-FMAD_OK = {"mixed.cu", "tc_update.cu", "slu.cu", "ir.cu", "batched.cu", "serve.cu", "oz_update.cu"}
+FMAD_OK = {"mixed.cu", "tc_update.cu", "slu.cu", "ir.cu", "batched.cu", "serve.cu", "oz_update.cu", "oz_residual.cu"}
 
 
 def _sources():

@@ -60,15 +60,6 @@ __global__ void convert_scaled(int64_t n, const double *__restrict__ A, int64_t 
   W[i + j * ldw] = (T)(A[i + j * lda] * scale[j / TB]);
 }
 
-// ||A||_inf: one thread per row, columns walked in order (coalesced across threads).
-__global__ void row_abs_sums(int64_t n, const double *__restrict__ A, int64_t lda, double *rows) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  double s = 0.0;
-  for (int64_t j = 0; j < n; ++j) s += fabs(A[i + j * lda]);
-  rows[i] = s;
-}
-
 // max|u_ii| and min|u_ii| of the low-precision U (one CTA): a cheap lower
 // bound on the conditioning the refinement will face.
 template <typename T>
@@ -151,25 +142,30 @@ __global__ void max_of(int64_t n, const double *v, double *out) {
   }
 }
 
-// y[i, c] = fl32(r[perm[i], c] / rscale[c])
+// y[i, c] = fl32(pre[p] r[p, c] / rscale[c]), p = perm[i] (pre: the row
+// scale of a Cholesky's D A D, or none)
 template <typename T>
 __global__ void permute_scale_down(int64_t n, int nrhs, const double *__restrict__ r, int64_t ldr,
-                                   const int32_t *perm, const double *rscale, T *__restrict__ y) {
+                                   const int32_t *perm, const double *rscale, T *__restrict__ y, const double *pre) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n * nrhs) return;
   const int64_t i = e % n, c = e / n;
   const double s = rscale[c];
-  y[i + c * n] = s > 0.0 ? (T)(r[perm[i] + c * ldr] / s) : T(0);
+  const int64_t p = perm[i];
+  const double v = pre != nullptr ? r[p + c * ldr] * pre[p] : r[p + c * ldr];
+  y[i + c * n] = s > 0.0 ? (T)(v / s) : T(0);
 }
 
-// x[i, c] += S_i * rscale[c] * y[i, c]   (or x = ... when assign)
+// x[i, c] += S_i * rscale[c] * y[i, c]   (or x = ... when assign); S_i is
+// the column scale of the LU's 64-column block, or the row scale postrow[i]
+// of a Cholesky
 template <typename T>
 __global__ void update_x(int64_t n, int nrhs, const T *__restrict__ y, const double *scale, const double *rscale,
-                         double *__restrict__ x, int64_t ldx, int assign) {
+                         double *__restrict__ x, int64_t ldx, int assign, const double *postrow) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n * nrhs) return;
   const int64_t i = e % n, c = e / n;
-  const double d = (double)y[i + c * n] * scale[i / TB] * rscale[c];
+  const double d = (double)y[i + c * n] * (postrow != nullptr ? postrow[i] : scale[i / TB]) * rscale[c];
   double *p = x + i + c * ldx;
   *p = assign ? d : *p + d;
 }
@@ -180,6 +176,38 @@ __global__ void copy_cols(int64_t n, int nrhs, const double *__restrict__ src, i
   if (e >= n * nrhs) return;
   const int64_t i = e % n, c = e / n;
   dst[i + c * ldd] = src[i + c * lds];
+}
+
+// Symmetric scaling of an SPD matrix: d_i = 2^-k with a_ii 2^-2k in
+// [0.5, 2), exact, so D A D has an O(1) diagonal.  A diagonal entry that is
+// not positive and finite gets d_i = 1 (the Cholesky then stops at it).
+__global__ void sym_scale(int64_t n, const double *__restrict__ A, int64_t lda, double *d) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double a = A[i + i * lda];
+  if (!(a > 0.0) || !isfinite(a)) {
+    d[i] = 1.0;
+    return;
+  }
+  int e = 0;
+  frexp(a, &e);
+  d[i] = ldexp(1.0, -(e >> 1));
+}
+
+// W = fl(D A D), lower triangle only (the Cholesky reads no other part).
+template <typename T>
+__global__ void convert_sym_lower(int64_t n, const double *__restrict__ A, int64_t lda, const double *d,
+                                  T *__restrict__ W, int64_t ldw) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n * n) return;
+  const int64_t i = e % n, j = e / n;
+  if (i < j) return;
+  W[i + j * ldw] = (T)(A[i + j * lda] * d[i] * d[j]);
+}
+
+__global__ void iota_perm(int64_t n, int32_t *perm) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) perm[i] = (int32_t)i;
 }
 
 // Inverses of the 64x64 diagonal blocks of L (unit lower) and U, once per
@@ -223,18 +251,6 @@ diag_block_inverses(int64_t n, const T *__restrict__ W, int64_t ldw, T *Dl, T *D
   for (int i = 0; i < TB; ++i) U[i + j * TB] = x[i];
 }
 
-// Blocked triangular solve with nrhs <= 32 right-hand sides (n x nrhs, ld n)
-// in ONE launch, as a dataflow over the 64-row blocks.  LOWER: unit-lower L,
-// blocks solved top to bottom; else U, bottom to top.  Each CTA takes the
-// next block in solve order from an atomic ticket, so it only ever waits for
-// blocks held by CTAs that started before it (no co-residency assumption).
-// It folds in the blocks solved before its own, in solve order, each as soon
-// as that block's flag carries this launch's epoch:
-//   acc -= L[blk, k] x_k      (the tile of W is loaded before the wait)
-// then solves its own block with the precomputed inverse of the diagonal
-// block, x_blk = Dinv acc, writes it to `out` and publishes its flag.  Waits
-// are bounded: on expiry *err is set (the host fails the solve) and the CTA
-// goes on, so that every later wait still ends.
 __device__ __forceinline__ int ld_acquire(const int32_t *p) {
   int v;
   asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -245,31 +261,126 @@ __device__ __forceinline__ void st_release(int32_t *p, int v) {
   asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// Blocked triangular solve with nrhs <= 32 right-hand sides (n x nrhs, ld n)
+// in ONE launch, as a dataflow over the 64-row blocks.  LOWER: unit-lower L,
+// blocks solved top to bottom; else U, bottom to top.  Each CTA takes the
+// next block in solve order from an atomic ticket, so it only ever waits for
+// blocks held by CTAs that started before it (no co-residency assumption).
+// A solved block is published as 64-bit words (value bits, launch epoch):
+// a reader spins on the words themselves, so one round trip to L2 both
+// signals and delivers a block, and a writer needs no release fence (each
+// word is written atomically and carries its own epoch).  The CTA folds in
+// the blocks solved before its predecessor as they appear,
+//   acc -= T[blk, k] x_k              (the tile of W is loaded before the wait)
+// applies the inverse of its diagonal block, c = Dinv acc, and then needs
+// only one 64 x 64 product once its predecessor p is published:
+//   x_blk = c - M x_p,   M = Dinv T[blk, p]   (precomputed per factorisation).
+// Waits are bounded: on expiry *err is set (the host fails the solve) and the
+// CTA goes on, so that every later wait still ends.
+__device__ __forceinline__ unsigned long long ld_word(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_word(unsigned long long *p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// M[b] = Dinv_b T_b (column-major 64 x 64), T_b the block coupling block b
+// to its predecessor in solve order: L[b, b-1] (lower), U[b, b+1] (upper).
 template <bool LOWER>
 __global__ void __launch_bounds__(256)
-trsv_dataflow(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, const float *__restrict__ Dinv,
-              const float *__restrict__ y, float *out, int32_t *flags, int32_t *ticket, int32_t epoch, int32_t *err) {
-  __shared__ float Ls[TB][TB + 1];  // Ls[k][r] = tile(r, k)
-  __shared__ float xs[MAXRHS][TB];
+couple_blocks(int64_t n, const float *__restrict__ W, int64_t ldw, const float *__restrict__ Dinv, float *M) {
+  __shared__ float D[TB][TB + 1], T[TB][TB + 1];
+  const int nb = (int)cdiv(n, TB);
+  const int b = blockIdx.x;
+  const int k = LOWER ? b - 1 : b + 1;
+  if (k < 0 || k >= nb) return;
+  const int64_t i0 = (int64_t)b * TB, k0 = (int64_t)k * TB;
+  const int kb = (int)imin(TB, n - i0), kbk = (int)imin(TB, n - k0);
+  for (int e = threadIdx.x; e < TB * TB; e += 256) {
+    const int r = e % TB, c = e / TB;
+    D[r][c] = Dinv[(int64_t)b * TB * TB + e];
+    T[r][c] = (r < kb && c < kbk) ? W[(i0 + r) + (k0 + c) * ldw] : 0.f;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < TB * TB; e += 256) {
+    const int r = e % TB, c = e / TB;
+    float v = 0.f;
+#pragma unroll 16
+    for (int q = 0; q < TB; ++q) v = fmaf(D[r][q], T[q][c], v);
+    M[(int64_t)b * TB * TB + e] = v;
+  }
+}
+
+// acc[c] (c < RH) -= sum_kk A[kk][r] X[kk][g RH + c]
+template <int RH>
+__device__ __forceinline__ void block_product(float (&acc)[RH], const float (*A)[TB + 4], const float (*X)[4 * RH],
+                                              int r, int g) {
+#pragma unroll 8
+  for (int kk = 0; kk < TB; ++kk) {
+    const float a = A[kk][r];
+#pragma unroll
+    for (int c = 0; c < RH; c += 4) {
+      const float4 x = *reinterpret_cast<const float4 *>(&X[kk][g * RH + c]);
+      acc[c] = fmaf(-a, x.x, acc[c]);
+      acc[c + 1] = fmaf(-a, x.y, acc[c + 1]);
+      acc[c + 2] = fmaf(-a, x.z, acc[c + 2]);
+      acc[c + 3] = fmaf(-a, x.w, acc[c + 3]);
+    }
+  }
+}
+
+// Spins until block k's words carry this launch's epoch, into X[kk][c].
+template <int RH>
+__device__ __forceinline__ void take_block(const unsigned long long *xw, int64_t n, int nrhs, int64_t k0, int kbk,
+                                           uint32_t epoch, float (*X)[4 * RH], int32_t *err) {
+  for (int e = threadIdx.x; e < TB * 4 * RH; e += 256) {
+    const int kk = e % TB, c = e / TB;
+    float v = 0.f;
+    if (kk < kbk && c < nrhs) {
+      const unsigned long long *p = xw + (k0 + kk) + (int64_t)c * n;
+      unsigned long long w = ld_word(p);
+      int polls = 0;
+      while ((uint32_t)(w >> 32) != epoch) {
+        if (++polls > (1 << 22)) {
+          atomicExch(err, 3);
+          break;
+        }
+        w = ld_word(p);
+      }
+      v = __uint_as_float((uint32_t)w);
+    }
+    X[kk][c] = v;
+  }
+}
+
+template <bool LOWER, int RH>
+__global__ void __launch_bounds__(256)
+trsv_words(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, const float *__restrict__ Dinv,
+           const float *__restrict__ M, const float *__restrict__ y, float *out, unsigned long long *xw,
+           int32_t *ticket, uint32_t epoch, int32_t *err) {
+  __shared__ __align__(16) float A[TB][TB + 4];   // a 64 x 64 operand, A[kk][r] = operand(r, kk)
+  __shared__ __align__(16) float X[TB][4 * RH];   // X[kk][c]
   __shared__ int sb;
   const int tid = threadIdx.x;
-  const int nb = (int)((n + TB - 1) / TB);
+  const int nb = (int)cdiv(n, TB);
   if (tid == 0) sb = atomicAdd(ticket, 1);
   __syncthreads();
   const int t = sb;
   const int b = LOWER ? t : nb - 1 - t;
   const int64_t i0 = (int64_t)b * TB;
   const int kb = (int)imin(TB, n - i0);
-  const int r = tid & (TB - 1), cg = tid >> 6;  // row of the block, right-hand-side group (4 groups)
-  constexpr int NQ = MAXRHS / 4;
-  float acc[NQ];
+  const int r = tid & (TB - 1), g = tid >> 6;  // row of the block, right-hand-side group (4 groups of RH)
+  float acc[RH];
 #pragma unroll
-  for (int q = 0; q < NQ; ++q) {
-    const int c = cg + 4 * q;
-    acc[q] = (c < nrhs && r < kb) ? y[i0 + r + (int64_t)c * n] : 0.f;
+  for (int c = 0; c < RH; ++c) {
+    const int cc = g * RH + c;
+    acc[c] = (cc < nrhs && r < kb) ? y[i0 + r + (int64_t)cc * n] : 0.f;
   }
   constexpr int PER = TB * TB / 256;
-  for (int sidx = 0; sidx < t; ++sidx) {
+  // the blocks solved before the predecessor
+  for (int sidx = 0; sidx + 1 < t; ++sidx) {
     const int k = LOWER ? sidx : nb - 1 - sidx;
     const int64_t k0 = (int64_t)k * TB;
     const int kbk = (int)imin(TB, n - k0);
@@ -280,59 +391,61 @@ trsv_dataflow(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, con
       const int rr = e % TB, kk = e / TB;
       lv[q] = (rr < kb && kk < kbk) ? W[(i0 + rr) + (k0 + kk) * ldw] : 0.f;
     }
-    if (tid == 0) {
-      int polls = 0;
-      while (ld_acquire(flags + k) != epoch) {
-        if (++polls > (1 << 21)) {
-          atomicExch(err, 3);
-          break;
-        }
-        __nanosleep(64);
-      }
-    }
-    __syncthreads();
+    take_block<RH>(xw, n, nrhs, k0, kbk, epoch, X, err);
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
       const int e = tid + 256 * q;
-      Ls[e / TB][e % TB] = lv[q];
-    }
-    for (int e = tid; e < TB * nrhs; e += 256) {
-      const int kk = e % TB, c = e / TB;
-      xs[c][kk] = kk < kbk ? __ldcg(out + k0 + kk + (int64_t)c * n) : 0.f;
+      A[e / TB][e % TB] = lv[q];
     }
     __syncthreads();
-#pragma unroll 8
-    for (int kk = 0; kk < TB; ++kk) {
-      const float a = Ls[kk][r];
-#pragma unroll
-      for (int q = 0; q < NQ; ++q)
-        if (cg + 4 * q < nrhs) acc[q] = fmaf(-a, xs[cg + 4 * q][kk], acc[q]);
-    }
+    block_product<RH>(acc, A, X, r, g);
     __syncthreads();
   }
-  // the diagonal block: x = Dinv acc
+  // c = Dinv acc: acc into X as a 64 x (4 RH) operand, Dinv into A
+#pragma unroll
+  for (int c = 0; c < RH; ++c) X[r][g * RH + c] = acc[c];
   const float *D = Dinv + (int64_t)b * TB * TB;
 #pragma unroll
   for (int q = 0; q < PER; ++q) {
     const int e = tid + 256 * q;
-    Ls[e / TB][e % TB] = D[e];
+    A[e / TB][e % TB] = D[e];
   }
-#pragma unroll
-  for (int q = 0; q < NQ; ++q)
-    if (cg + 4 * q < nrhs) xs[cg + 4 * q][r] = acc[q];
   __syncthreads();
+  float cv[RH];
 #pragma unroll
-  for (int q = 0; q < NQ; ++q) {
-    const int c = cg + 4 * q;
-    if (c >= nrhs) continue;
-    float v = 0.f;
-#pragma unroll 8
-    for (int kk = 0; kk < TB; ++kk) v = fmaf(Ls[kk][r], xs[c][kk], v);
-    if (r < kb) out[i0 + r + (int64_t)c * n] = v;
+  for (int c = 0; c < RH; ++c) cv[c] = 0.f;
+  block_product<RH>(cv, A, X, r, g);  // cv = -Dinv acc
+  __syncthreads();
+  if (t > 0) {
+    // the predecessor: x = c - M x_p
+    const int p = LOWER ? b - 1 : b + 1;
+    const int64_t p0 = (int64_t)p * TB;
+    const int kbp = (int)imin(TB, n - p0);
+    const float *Mb = M + (int64_t)b * TB * TB;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int e = tid + 256 * q;
+      A[e / TB][e % TB] = Mb[e];
+    }
+    take_block<RH>(xw, n, nrhs, p0, kbp, epoch, X, err);
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < RH; ++c) cv[c] = -cv[c];
+    block_product<RH>(cv, A, X, r, g);
+  } else {
+#pragma unroll
+    for (int c = 0; c < RH; ++c) cv[c] = -cv[c];
   }
-  __threadfence();
-  __syncthreads();
-  if (tid == 0) st_release(flags + b, epoch);
+  if (r < kb) {
+#pragma unroll
+    for (int c = 0; c < RH; ++c) {
+      const int cc = g * RH + c;
+      if (cc >= nrhs) continue;
+      const int64_t idx = i0 + r + (int64_t)cc * n;
+      out[idx] = cv[c];
+      st_word(xw + idx, ((unsigned long long)epoch << 32) | __float_as_uint(cv[c]));
+    }
+  }
 }
 
 // The FP64 form of the same dataflow, for the FP64-storage factor.  GB300's
@@ -402,6 +515,8 @@ trsv_dataflow64(int64_t n, int nrhs, const double *__restrict__ W, int64_t ldw, 
 struct TrsvSync {
   int32_t *flags = nullptr, *ticket = nullptr, *err = nullptr;
   int32_t epoch = 0;
+  unsigned long long *xw = nullptr;  // published blocks of the FP32 solves (value, epoch)
+  const float *Ml = nullptr, *Mu = nullptr;  // Dinv times the coupling block, per 64-row block
 };
 
 // y (right-hand sides) -> out (solution); y is not modified.
@@ -424,12 +539,30 @@ int trsv(cudaStream_t s, bool lower, int64_t n, int nrhs, const float *W, int64_
          const float *y, float *out, TrsvSync &sync) {
   ProfScope prof(s, lower ? "trsv_lower" : "trsv_upper", (double)n * n * nrhs, 4.0 * (double)n * n / 2, 1);
   const unsigned nb = (unsigned)cdiv(n, TB);
-  const int32_t epoch = ++sync.epoch;
+  const uint32_t epoch = (uint32_t)++sync.epoch;
   BOLA_TRY_CUDA(cudaMemsetAsync(sync.ticket, 0, sizeof(int32_t), s));
-  if (lower)
-    trsv_dataflow<true><<<nb, 256, 0, s>>>(n, nrhs, W, ldw, Dinv, y, out, sync.flags, sync.ticket, epoch, sync.err);
-  else
-    trsv_dataflow<false><<<nb, 256, 0, s>>>(n, nrhs, W, ldw, Dinv, y, out, sync.flags, sync.ticket, epoch, sync.err);
+  const float *M = lower ? sync.Ml : sync.Mu;
+#define BOLA_TRSV(LW, RH) \
+  trsv_words<LW, RH><<<nb, 256, 0, s>>>(n, nrhs, W, ldw, Dinv, M, y, out, sync.xw, sync.ticket, epoch, sync.err)
+  if (nrhs <= 16) {
+    if (lower) BOLA_TRSV(true, 4);
+    else BOLA_TRSV(false, 4);
+  } else {
+    if (lower) BOLA_TRSV(true, 8);
+    else BOLA_TRSV(false, 8);
+  }
+#undef BOLA_TRSV
+  BOLA_CHECK_LAUNCH();
+  return 0;
+}
+
+// Dinv times the coupling blocks of the FP32 factor's L and U (once per factorisation).
+int couple(cudaStream_t s, int64_t n, const float *W, int64_t ldw, const float *Dl, const float *Du, float *Ml,
+           float *Mu) {
+  ProfScope prof(s, "trsv_couple", 4.0 * (double)cdiv(n, TB) * TB * TB * TB, 0.0, 2);
+  const unsigned nb = (unsigned)cdiv(n, TB);
+  couple_blocks<true><<<nb, 256, 0, s>>>(n, W, ldw, Dl, Ml);
+  couple_blocks<false><<<nb, 256, 0, s>>>(n, W, ldw, Du, Mu);
   BOLA_CHECK_LAUNCH();
   return 0;
 }
@@ -519,21 +652,33 @@ struct Workspace {
   double *V = nullptr, *Z = nullptr, *H = nullptr;  // GMRES basis, preconditioned basis, Hessenberg column
   double *hn = nullptr;                              // per-column 2-norms (GMRES)
   int32_t *ipiv = nullptr, *perm = nullptr, *info = nullptr;
+  bool chol = false;           // the current factor is a Cholesky (in LU form)
+  double *dscale = nullptr;    // its row scale D (W = D A D)
+  void *dg = nullptr;          // scratch: the diagonal of L (8-byte elements)
+  float *Mc = nullptr;         // FP32 factors: Dinv times the coupling blocks, lower then upper
   TrsvSync ts;  // dataflow triangular solves
   MixedLU lu;
+  OzMatrix oz;  // A's digit planes: the FP64-accurate products of the refinement
 };
 
 void ws_free(Workspace &w) {
   for (void *p : {(void *)w.W, (void *)w.y, (void *)w.z, (void *)w.Dl, (void *)w.Du, (void *)w.scale, (void *)w.r,
                   (void *)w.d, (void *)w.norms, (void *)w.rowsum, (void *)w.ipiv, (void *)w.perm, (void *)w.info,
-                  (void *)w.V, (void *)w.Z, (void *)w.H, (void *)w.hn, (void *)w.ts.flags, (void *)w.ts.ticket})
+                  (void *)w.V, (void *)w.Z, (void *)w.H, (void *)w.hn, (void *)w.ts.flags, (void *)w.ts.ticket,
+                  (void *)w.dscale, w.dg, (void *)w.Mc, (void *)w.ts.xw})
     if (p) cudaFree(p);
   w.ts.flags = w.ts.ticket = w.ts.err = nullptr;
   w.lu.release(nullptr);
+  w.oz.release();
   w.W = w.y = w.z = w.Dl = w.Du = nullptr;
   w.wbytes = 0;
   w.scale = w.r = w.d = w.norms = w.rowsum = w.V = w.Z = w.H = w.hn = nullptr;
   w.ipiv = w.perm = w.info = nullptr;
+  w.dscale = nullptr;
+  w.dg = nullptr;
+  w.Mc = nullptr;
+  w.ts.xw = nullptr;
+  w.ts.Ml = w.ts.Mu = nullptr;
   w.n = w.nrhs = w.bytes = 0;
 }
 
@@ -561,6 +706,8 @@ int ws_reserve(Workspace &w, int64_t n, int64_t nrhs, int kind, cudaStream_t s) 
     BOLA_TRY(alloc(&w.d, sizeof(double) * n * nrhs));
     BOLA_TRY(alloc(&w.norms, sizeof(double) * 6 * MAXRHS));
     BOLA_TRY(alloc(&w.rowsum, sizeof(double) * n));
+    BOLA_TRY(alloc(&w.dscale, sizeof(double) * n));
+    BOLA_TRY(alloc(&w.dg, sizeof(double) * n));
     BOLA_TRY(alloc(&w.ipiv, sizeof(int32_t) * n));
     BOLA_TRY(alloc(&w.perm, sizeof(int32_t) * n));
     BOLA_TRY(alloc(&w.info, sizeof(int32_t)));
@@ -570,6 +717,12 @@ int ws_reserve(Workspace &w, int64_t n, int64_t nrhs, int kind, cudaStream_t s) 
     BOLA_TRY(alloc(&w.hn, sizeof(double) * MAXRHS));
     BOLA_TRY(alloc(&w.ts.flags, sizeof(int32_t) * cdiv(n, TB) * MAXRHS));
     BOLA_TRY(alloc(&w.ts.ticket, sizeof(int32_t) * 2));
+    BOLA_TRY(alloc(&w.Mc, sizeof(float) * 2 * cdiv(n, TB) * TB * TB));
+    BOLA_TRY(alloc(&w.ts.xw, sizeof(unsigned long long) * n * MAXRHS));
+    // the published words start from epoch 0, which no launch uses
+    BOLA_TRY_CUDA(cudaMemset(w.ts.xw, 0, sizeof(unsigned long long) * n * MAXRHS));
+    w.ts.Ml = w.Mc;
+    w.ts.Mu = w.Mc + cdiv(n, TB) * TB * TB;
     w.ts.err = w.ts.ticket + 1;
     BOLA_TRY_CUDA(cudaMemset(w.ts.flags, 0, sizeof(int32_t) * cdiv(n, TB) * MAXRHS));
     BOLA_TRY_CUDA(cudaMemset(w.ts.ticket, 0, sizeof(int32_t) * 2));
@@ -589,6 +742,9 @@ int ws_reserve(Workspace &w, int64_t n, int64_t nrhs, int kind, cudaStream_t s) 
     w.wbytes = wneed;
     w.bytes += (int64_t)wneed;
   }
+  const int64_t oz_before = w.oz.bytes;
+  BOLA_TRY(w.oz.reserve(n_req));
+  w.bytes += w.oz.bytes - oz_before;
   return w.lu.reserve(n_req, kind, s);
 }
 
@@ -602,19 +758,19 @@ int correction(cudaStream_t s, Workspace &w, int64_t n, int nrhs, const double *
   if (w.fkind == 3) {
     double *y = static_cast<double *>(w.y), *z = static_cast<double *>(w.z);
     const double *W = static_cast<const double *>(w.W);
-    permute_scale_down<double><<<g, 256, 0, s>>>(n, nrhs, r, ldr, w.perm, rs, y);
+    permute_scale_down<double><<<g, 256, 0, s>>>(n, nrhs, r, ldr, w.perm, rs, y, w.chol ? w.dscale : nullptr);
     BOLA_CHECK_LAUNCH();
     BOLA_TRY(trsv(s, true, n, nrhs, W, w.ldW, static_cast<const double *>(w.Dl), y, z, w.ts));
     BOLA_TRY(trsv(s, false, n, nrhs, W, w.ldW, static_cast<const double *>(w.Du), z, y, w.ts));
-    update_x<double><<<g, 256, 0, s>>>(n, nrhs, y, w.scale, rs, x, ldx, assign ? 1 : 0);
+    update_x<double><<<g, 256, 0, s>>>(n, nrhs, y, w.scale, rs, x, ldx, assign ? 1 : 0, w.chol ? w.dscale : nullptr);
   } else {
     float *y = static_cast<float *>(w.y), *z = static_cast<float *>(w.z);
     const float *W = static_cast<const float *>(w.W);
-    permute_scale_down<float><<<g, 256, 0, s>>>(n, nrhs, r, ldr, w.perm, rs, y);
+    permute_scale_down<float><<<g, 256, 0, s>>>(n, nrhs, r, ldr, w.perm, rs, y, w.chol ? w.dscale : nullptr);
     BOLA_CHECK_LAUNCH();
     BOLA_TRY(trsv(s, true, n, nrhs, W, n, static_cast<const float *>(w.Dl), y, z, w.ts));
     BOLA_TRY(trsv(s, false, n, nrhs, W, n, static_cast<const float *>(w.Du), z, y, w.ts));
-    update_x<float><<<g, 256, 0, s>>>(n, nrhs, y, w.scale, rs, x, ldx, assign ? 1 : 0);
+    update_x<float><<<g, 256, 0, s>>>(n, nrhs, y, w.scale, rs, x, ldx, assign ? 1 : 0, w.chol ? w.dscale : nullptr);
   }
   BOLA_CHECK_LAUNCH();
   return 0;
@@ -625,10 +781,8 @@ int residual_berr(cudaStream_t s, Workspace &w, int64_t n, int nr, const double 
                   int64_t ldb, const double *x, int64_t ldx, double *berr) {
   double *nrm = w.norms;
   {
-    ProfScope prof(s, "mixed_residual", 2.0 * (double)n * n * nr, 8.0 * (double)n * n, 4);
-    copy_cols<<<(unsigned)cdiv(n * nr, 256), 256, 0, s>>>(n, nr, b, ldb, w.r, n);
-    BOLA_CHECK_LAUNCH();
-    BOLA_TRY(dgemm_exact(s, 'N', 'N', n, nr, n, -1.0, a, lda, x, ldx, 1.0, w.r, n, 64, nullptr, 0));
+    ProfScope prof(s, "mixed_residual", 2.0 * (double)n * n * nr, 2.0 * OZ_SA * (double)n * n, 4 * (int)cdiv(nr, 16) + 2);
+    BOLA_TRY(w.oz.product(s, nr, x, ldx, b, ldb, w.r, n, w.ts.err));
     col_absmax<<<nr, 256, 0, s>>>(n, w.r, n, nrm);
     col_absmax<<<nr, 256, 0, s>>>(n, x, ldx, nrm + nr);
   }
@@ -640,7 +794,7 @@ int residual_berr(cudaStream_t s, Workspace &w, int64_t n, int nr, const double 
   BOLA_TRY_CUDA(cudaStreamSynchronize(s));
   if (terr != 0) {
     cudaMemsetAsync(w.ts.err, 0, sizeof(int32_t), s);
-    return fail(BOLA_ERR_CUDA, "mixed: a triangular-solve wait expired (%d)", terr);
+    return fail(BOLA_ERR_CUDA, "mixed: a bounded wait expired in the refinement (code %d)", terr);
   }
   double e = 0.0;
   for (int c = 0; c < nr; ++c) {
@@ -680,8 +834,8 @@ int gmres_step(cudaStream_t s, Workspace &w, int64_t n, int nr, const double *a,
     BOLA_CHECK_LAUNCH();
     BOLA_TRY(correction(s, w, n, nr, Vk, n, beta_d, Zk, n, true));
     {
-      ProfScope prof(s, "gmres_matvec", 2.0 * (double)n * n * nr, 8.0 * (double)n * n);
-      BOLA_TRY(dgemm_exact(s, 'N', 'N', n, nr, n, 1.0, a, lda, Zk, n, 0.0, w.d, n, 64, nullptr, 0));
+      ProfScope prof(s, "gmres_matvec", 2.0 * (double)n * n * nr, 2.0 * OZ_SA * (double)n * n, 4 * (int)cdiv(nr, 16));
+      BOLA_TRY(w.oz.product(s, nr, Zk, n, nullptr, 0, w.d, n, w.ts.err));
     }
     {
       ProfScope prof(s, "gmres_orth", 8.0 * (double)n * nr * (k + 1), 0.0, 6);
@@ -746,8 +900,9 @@ using namespace bola;
 namespace bola {
 namespace {
 
-int dgesv_mixed_ws(Workspace &w, int64_t n, int64_t nrhs, const double *a, int64_t lda, const double *b, int64_t ldb,
-                   double *x, int64_t ldx, const bola_mixed_opts *opts, bola_mixed_info *out, cudaStream_t s);
+int dgesv_mixed_ws(Workspace &w, bool chol, int64_t n, int64_t nrhs, const double *a, int64_t lda, const double *b,
+                   int64_t ldb, double *x, int64_t ldx, const bola_mixed_opts *opts, bola_mixed_info *out,
+                   cudaStream_t s);
 
 }  // namespace
 }  // namespace bola
@@ -758,7 +913,24 @@ extern "C" int bola_dgesv_mixed(int64_t n, int64_t nrhs, const double *a, int64_
   int dev = 0;
   BOLA_TRY_CUDA(cudaGetDevice(&dev));
   std::lock_guard<std::mutex> lk(g_ws_mu);
-  return dgesv_mixed_ws(g_ws[dev & 63], n, nrhs, a, lda, b, ldb, x, ldx, opts, out, (cudaStream_t)stream);
+  return dgesv_mixed_ws(g_ws[dev & 63], false, n, nrhs, a, lda, b, ldb, x, ldx, opts, out, (cudaStream_t)stream);
+}
+
+extern "C" int bola_dposv_mixed(int64_t n, int64_t nrhs, const double *a, int64_t lda, const double *b, int64_t ldb,
+                                double *x, int64_t ldx, const bola_mixed_opts *opts, bola_mixed_info *out,
+                                bola_stream_t stream) {
+  int dev = 0;
+  BOLA_TRY_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_ws_mu);
+  return dgesv_mixed_ws(g_ws[dev & 63], true, n, nrhs, a, lda, b, ldb, x, ldx, opts, out, (cudaStream_t)stream);
+}
+
+extern "C" int bola_dposv_mixed_ctx(bola_mixed_ctx ctx, int64_t n, int64_t nrhs, const double *a, int64_t lda,
+                                    const double *b, int64_t ldb, double *x, int64_t ldx,
+                                    const bola_mixed_opts *opts, bola_mixed_info *out, bola_stream_t stream) {
+  Workspace *w = reinterpret_cast<Workspace *>(ctx);
+  if (!w) return -1;
+  return dgesv_mixed_ws(*w, true, n, nrhs, a, lda, b, ldb, x, ldx, opts, out, (cudaStream_t)stream);
 }
 
 extern "C" int bola_mixed_ctx_create(bola_mixed_ctx *ctx) {
@@ -787,14 +959,15 @@ extern "C" int bola_dgesv_mixed_ctx(bola_mixed_ctx ctx, int64_t n, int64_t nrhs,
                                     const bola_mixed_opts *opts, bola_mixed_info *out, bola_stream_t stream) {
   Workspace *w = reinterpret_cast<Workspace *>(ctx);
   if (!w) return -1;
-  return dgesv_mixed_ws(*w, n, nrhs, a, lda, b, ldb, x, ldx, opts, out, (cudaStream_t)stream);
+  return dgesv_mixed_ws(*w, false, n, nrhs, a, lda, b, ldb, x, ldx, opts, out, (cudaStream_t)stream);
 }
 
 namespace bola {
 namespace {
 
-int dgesv_mixed_ws(Workspace &w, int64_t n, int64_t nrhs, const double *a, int64_t lda, const double *b, int64_t ldb,
-                   double *x, int64_t ldx, const bola_mixed_opts *opts, bola_mixed_info *out, cudaStream_t s) {
+int dgesv_mixed_ws(Workspace &w, bool chol, int64_t n, int64_t nrhs, const double *a, int64_t lda, const double *b,
+                   int64_t ldb, double *x, int64_t ldx, const bola_mixed_opts *opts, bola_mixed_info *out,
+                   cudaStream_t s) {
   if (n < 0) return -1;
   if (nrhs < 0 || nrhs > MAXRHS) return -2;
   if (lda < imax(1, n)) return -4;
@@ -812,6 +985,7 @@ int dgesv_mixed_ws(Workspace &w, int64_t n, int64_t nrhs, const double *a, int64
   if (n > 8192) return fail(BOLA_ERR_UNSUPPORTED, "bola_dgesv_mixed: n = %lld > 8192", (long long)n);
   BOLA_TRY(ws_reserve(w, n, nrhs, o.factor_kind, s));
   w.fkind = o.factor_kind;
+  w.chol = chol;
   const bool fp64 = o.factor_kind == 3;
   const int64_t ldW = fp64 ? cdiv(n, 32) * 32 : n;
   w.ldW = ldW;
@@ -819,14 +993,26 @@ int dgesv_mixed_ws(Workspace &w, int64_t n, int64_t nrhs, const double *a, int64
   double *nrm = w.norms;  // [0..nr): ||r||, [nr..2nr): ||x||, [2nr..3nr): ||b||, [3nr]: ||A||
 
   // scale, convert, factor
-  {
-    ProfScope prof(s, "mixed_convert", 0.0, 12.0 * (double)n * n);
+  if (chol) {
+    // W = D A D (lower triangle), D a power of two per row making the diagonal O(1)
+    ProfScope prof(s, "mixed_convert", 0.0, 6.0 * (double)n * n, 2);
+    sym_scale<<<(unsigned)cdiv(n, 256), 256, 0, s>>>(n, a, lda, w.dscale);
+    if (fp64)
+      convert_sym_lower<double><<<(unsigned)cdiv(n * n, 256), 256, 0, s>>>(n, a, lda, w.dscale, (double *)w.W, ldW);
+    else
+      convert_sym_lower<float><<<(unsigned)cdiv(n * n, 256), 256, 0, s>>>(n, a, lda, w.dscale, (float *)w.W, n);
+  } else {
+    ProfScope prof(s, "mixed_convert", 0.0, 12.0 * (double)n * n, 2);
     colblock_scale<<<(unsigned)cdiv(n, TB), 512, 0, s>>>(n, a, lda, w.scale);
     if (fp64)
       convert_scaled<double><<<(unsigned)cdiv(n * n, 256), 256, 0, s>>>(n, a, lda, w.scale, (double *)w.W, ldW);
     else
       convert_scaled<float><<<(unsigned)cdiv(n * n, 256), 256, 0, s>>>(n, a, lda, w.scale, (float *)w.W, n);
-    row_abs_sums<<<(unsigned)cdiv(n, 128), 128, 0, s>>>(n, a, lda, w.rowsum);
+  }
+  BOLA_CHECK_LAUNCH();
+  BOLA_TRY(w.oz.split(s, a, lda, w.rowsum));  // A's digit planes and its row sums
+  {
+    ProfScope prof(s, "mixed_norms", 0.0, 8.0 * (double)n * nr, 2);
     max_of<<<1, 1024, 0, s>>>(n, w.rowsum, nrm + 3 * nr);
     col_absmax<<<nr, 256, 0, s>>>(n, b, ldb, nrm + 2 * nr);
   }
@@ -845,19 +1031,34 @@ int dgesv_mixed_ws(Workspace &w, int64_t n, int64_t nrhs, const double *a, int64
   // that takes it over the limit, with the decision the whole factor would give.
   const double limit = o.factor_kind == 0 ? 175.0 : o.factor_kind == 1 ? 1100.0 : o.factor_kind == 2 ? 4.5e4 : 1e13;
   const double give_up = (o.fallback_fp64 || o.escalate) ? limit : INFINITY;
-  if (fp64)
+  if (chol) {
+    // Cholesky (no pivoting), then its LU form L D^-1, D L^T for the solves
+    if (fp64) {
+      BOLA_TRY(w.lu.factor_chol64(s, (double *)w.W, ldW, w.info, give_up));
+      BOLA_TRY(chol_lu_form<double>(s, n, (double *)w.W, ldW, (double *)w.dg));
+    } else {
+      BOLA_TRY(w.lu.factor_chol(s, (float *)w.W, n, w.info, give_up));
+      BOLA_TRY(chol_lu_form<float>(s, n, (float *)w.W, n, (float *)w.dg));
+    }
+  } else if (fp64) {
     BOLA_TRY(w.lu.factor64(s, (double *)w.W, ldW, w.ipiv, w.info, give_up));
-  else
+  } else {
     BOLA_TRY(w.lu.factor(s, (float *)w.W, n, w.ipiv, w.info, give_up));
+  }
   {
     ProfScope prof(s, "mixed_perm");
-    compose_perm<<<1, 1024, sizeof(int32_t) * n, s>>>(n, w.ipiv, w.perm);
+    if (chol)
+      iota_perm<<<(unsigned)cdiv(n, 256), 256, 0, s>>>(n, w.perm);
+    else
+      compose_perm<<<1, 1024, sizeof(int32_t) * n, s>>>(n, w.ipiv, w.perm);
     const unsigned nb = (unsigned)cdiv(n, TB);
     if (fp64) {
       diag_block_inverses<double><<<nb, TB, 0, s>>>(n, (const double *)w.W, ldW, (double *)w.Dl, (double *)w.Du);
       diag_extent<double><<<1, 1024, 0, s>>>(n, (const double *)w.W, ldW, w.norms + 5 * MAXRHS);
     } else {
       diag_block_inverses<float><<<nb, TB, 0, s>>>(n, (const float *)w.W, n, (float *)w.Dl, (float *)w.Du);
+      BOLA_TRY(couple(s, n, (const float *)w.W, n, (const float *)w.Dl, (const float *)w.Du, w.Mc,
+                      w.Mc + cdiv(n, TB) * TB * TB));
       diag_extent<float><<<1, 1024, 0, s>>>(n, (const float *)w.W, n, w.norms + 5 * MAXRHS);
     }
   }
@@ -871,9 +1072,18 @@ int dgesv_mixed_ws(Workspace &w, int64_t n, int64_t nrhs, const double *a, int64
   BOLA_TRY_CUDA(cudaMemcpyAsync(&ferr, w.lu.err, sizeof ferr, cudaMemcpyDeviceToHost, s));
   BOLA_TRY_CUDA(cudaStreamSynchronize(s));
   info_out.factor_info = finfo;
+  info_out.factorization = chol ? 1 : 0;
   // a bounded wait gave up: 5 the panel's candidate exchange, others a
   // tensor-core update's pipeline (the factor is then unusable)
   if (ferr != 0) return fail(BOLA_ERR_CUDA, "mixed LU: a bounded wait expired (code %d)", ferr);
+  if (chol && finfo != 0 && !(o.escalate && o.factor_kind < 3)) {
+    // a pivot that is not positive: A is not SPD at this precision (or at
+    // all) and no FP64-accurate Cholesky is left to try; the mixed LU takes
+    // over with the same options
+    BOLA_TRY(dgesv_mixed_ws(w, false, n, nrhs, a, lda, b, ldb, x, ldx, &o, out, s));
+    if (out) out->factor_info = finfo;
+    return 0;
+  }
 
   bool converged = false;
   double berr = INFINITY, prev = INFINITY;
@@ -940,7 +1150,7 @@ int dgesv_mixed_ws(Workspace &w, int64_t n, int64_t nrhs, const double *a, int64
     o3.factor_kind = 3;
     o3.escalate = 0;
     bola_mixed_info i3;
-    BOLA_TRY(dgesv_mixed_ws(w, n, nrhs, a, lda, b, ldb, x, ldx, &o3, &i3, s));
+    BOLA_TRY(dgesv_mixed_ws(w, chol, n, nrhs, a, lda, b, ldb, x, ldx, &o3, &i3, s));
     i3.iterations += info_out.iterations;
     i3.gmres_iterations += info_out.gmres_iterations;
     if (i3.path != 2) i3.path = 3;
@@ -962,6 +1172,7 @@ int dgesv_mixed_ws(Workspace &w, int64_t n, int64_t nrhs, const double *a, int64
     cudaFreeAsync(acopy, s);
     if (st != 0) return st;
     info_out.path = 2;
+    info_out.factorization = 0;
     // backward error of the FP64 answer
     BOLA_TRY(residual_berr(s, w, n, nr, a, lda, b, ldb, x, ldx, &berr));
     info_out.backward_error = berr;

@@ -78,18 +78,117 @@ __device__ __forceinline__ void oz_split_pair(double v0, double v1, int lane, in
   }
 }
 
+// ---- FP64-accurate products A X on the tensor cores (oz_residual.cu) ----
+// A is split once into OZ_SA digit planes (8-bit signed digits under a scale
+// per row), X per product into OZ_SX planes (a scale per column); the planes
+// pairs (t, u) with t + u <= OZ_D are accumulated exactly.
+constexpr int OZ_SA = 7, OZ_SX = 8, OZ_D = 7;
+
+// Tensor map for a row-major bf16 array with kdim K values per row (row pitch
+// kp elements, a multiple of 64), `rows` rows, boxes of 64 K x box_rows rows,
+// 128-byte swizzle; K beyond kdim reads as zero.
+int make_kmajor_map2(CUtensorMap *map, const void *ptr, int64_t kdim, int64_t rows, int64_t kp, int box_rows);
+
+struct OzMatrix {
+  int64_t n = 0, cap = 0, mrows = 0, kp = 0, bytes = 0;
+  bool ready = false;
+  __nv_bfloat16 *planes = nullptr, *xplanes = nullptr;
+  int32_t *e = nullptr, *f = nullptr;  // exponents of A's rows and of X's columns
+  unsigned long long *rmax = nullptr, *acc = nullptr;
+  double *psum = nullptr;
+  CUtensorMap mapA, mapX;
+  int reserve(int64_t n);
+  void release();
+  // A's digit planes; rowsum (optional, n doubles) gets sum_j |a_ij|
+  int split(cudaStream_t s, const double *A, int64_t lda, double *rowsum);
+  // out = b - A x (b != nullptr) or A x for nr columns; *err set if a bounded wait expired
+  int product(cudaStream_t s, int nr, const double *x, int64_t ldx, const double *b, int64_t ldb, double *out,
+              int64_t ldo, int32_t *err);
+};
+
+// Round to the nearest tf32 value (10 mantissa bits), ties away from zero.
+__device__ __forceinline__ float tf32_round(float x) {
+  uint32_t u = __float_as_uint(x);
+  u = (u + 0x1000u) & ~0x1FFFu;
+  return __uint_as_float(u);
+}
+
+// Writes one 64-wide row of an update operand (K-major, row `r`).
+__device__ __forceinline__ void write_operand_row(int kind, void *op, float *op_lo, int64_t r, const float *v) {
+  if (kind == 0) {
+    __nv_bfloat16 *d = static_cast<__nv_bfloat16 *>(op) + r * 64;
+#pragma unroll
+    for (int c = 0; c < 64; c += 8) {
+      __align__(16) __nv_bfloat16 t[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) t[u] = __float2bfloat16_rn(v[c + u]);
+      *reinterpret_cast<uint4 *>(d + c) = *reinterpret_cast<const uint4 *>(t);
+    }
+  } else {
+    float *d = static_cast<float *>(op) + r * 64;
+    float *dl = op_lo + r * 64;
+#pragma unroll
+    for (int c = 0; c < 64; c += 4) {
+      float4 h, l;
+      h.x = tf32_round(v[c]);
+      h.y = tf32_round(v[c + 1]);
+      h.z = tf32_round(v[c + 2]);
+      h.w = tf32_round(v[c + 3]);
+      *reinterpret_cast<float4 *>(d + c) = h;
+      if (kind == 2) {
+        l.x = tf32_round(v[c] - h.x);
+        l.y = tf32_round(v[c + 1] - h.y);
+        l.z = tf32_round(v[c + 2] - h.z);
+        l.w = tf32_round(v[c + 3] - h.w);
+        *reinterpret_cast<float4 *>(dl + c) = l;
+      }
+    }
+  }
+}
+
+// Writes the exact bf16 slices of one 64-wide FP64 row (K-major row r of a
+// kind-3 operand with cap rows per slice plane) and its exponent.
+__device__ __forceinline__ void write_slices_row(const double (&v)[64], int64_t r, int64_t cap, __nv_bfloat16 *out,
+                                                 int32_t *ex) {
+  uint64_t mb = 0;
+#pragma unroll
+  for (int c = 0; c < 64; ++c) {
+    const uint64_t mc = oz_mag(v[c]);
+    mb = mc > mb ? mc : mb;
+  }
+  const int e = oz_exponent(mb);
+  ex[r] = e;
+#pragma unroll
+  for (int c0 = 0; c0 < 64; c0 += 8) {
+    __align__(16) __nv_bfloat16 q[OZ_SLICES][8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      __nv_bfloat16 t8[OZ_SLICES];
+      oz_slices(v[c0 + u], e, t8);
+#pragma unroll
+      for (int t = 0; t < OZ_SLICES; ++t) q[t][u] = t8[t];
+    }
+#pragma unroll
+    for (int t = 0; t < OZ_SLICES; ++t)
+      *reinterpret_cast<uint4 *>(out + ((int64_t)t * cap + r) * 64 + c0) = *reinterpret_cast<const uint4 *>(q[t]);
+  }
+}
+
 // W(m x n, FP64) -= A B^T from the slices of A (rows of capA per slice) and
 // B (capB), exponents eA[m], eB[n]; *err set if a bounded wait expired.
+// lower: only tiles that reach the diagonal or below it (row >= boff + column
+// somewhere in the tile) are updated: the trailing update of a Cholesky.
 int oz_update(cudaStream_t s, int64_t m, int64_t n, const CUtensorMap &A, const CUtensorMap &B, int64_t capA,
               int64_t capB, const int32_t *eA, const int32_t *eB, double *W, int64_t ldw, int32_t *err,
-              int64_t boff = 0, const int32_t *abort = nullptr);
+              int64_t boff = 0, const int32_t *abort = nullptr, bool lower = false);
 
 // W(m x n, column-major, ld ldw) -= A * B^T on tcgen05 (kind 0 bf16, 1 tf32,
 // 2 3xTF32 with the lo maps); *err is set non-zero if a bounded wait expired.
 // B's rows start at boff (a column offset into the trailing matrix).
+// lower: only tiles reaching the diagonal or below it (as oz_update).
 int tc_update(cudaStream_t s, int kind, int64_t m, int64_t n, const CUtensorMap &A, const CUtensorMap &B,
               const CUtensorMap &Alo, const CUtensorMap &Blo, float *W, int64_t ldw, int32_t *err, int64_t boff = 0,
-              const int32_t *abort = nullptr);
+              const int32_t *abort = nullptr, bool lower = false);
 
 // A kernel of an abandoned factorisation returns at once: *abort is read by
 // one thread and the decision shared, so a CTA's barriers stay uniform even
@@ -108,6 +207,11 @@ __device__ __forceinline__ bool abandoned(const int32_t *abort) {
 // low-priority stream su), so that panel k+1 runs on its cluster while the
 // wide update of step k fills the other SMs.  The A operand is therefore
 // double-buffered by step parity.
+// The LU form of a finished Cholesky factor (chol.cu): unit-lower L D^-1
+// below the diagonal, D L^T on and above it (D = diag(L)); dg: n scratch.
+template <typename T>
+int chol_lu_form(cudaStream_t s, int64_t n, T *W, int64_t ldw, T *dg);
+
 struct MixedLU {
   int64_t n = 0, cap_n = 0;
   int kind = -1;  // 0 bf16, 1 tf32, 2 3xTF32 update operands (FP32 W); 3 exact bf16 slices (FP64 W)
@@ -120,6 +224,7 @@ struct MixedLU {
   // non-negative doubles, ordered like the values), [2] low word = abandon flag
   uint64_t *track = nullptr;
   CUtensorMap mapA[2], mapB, mapAlo[2], mapBlo;
+  CUtensorMap mapA64[2];  // kind 3: the A operand in 64-row boxes (the B side of a Cholesky update)
   cudaStream_t sp = nullptr, su = nullptr;
   cudaEvent_t ev_in = nullptr, ev_sw = nullptr, ev_wide = nullptr, ev_done = nullptr;
   int reserve(int64_t n, int kind, cudaStream_t s);
@@ -132,6 +237,10 @@ struct MixedLU {
   int factor(cudaStream_t s, float *W, int64_t ldw, int32_t *ipiv, int32_t *info, double give_up = INFINITY);
   // The same for an FP64 W (kind 3).
   int factor64(cudaStream_t s, double *W, int64_t ldw, int32_t *ipiv, int32_t *info, double give_up = INFINITY);
+  // Cholesky W = L L^T of the lower triangle of an SPD W (chol.cu): L in the
+  // lower triangle; *info = the first column whose pivot is not positive.
+  int factor_chol(cudaStream_t s, float *W, int64_t ldw, int32_t *info, double give_up = INFINITY);
+  int factor_chol64(cudaStream_t s, double *W, int64_t ldw, int32_t *info, double give_up = INFINITY);
 };
 
 }  // namespace bola

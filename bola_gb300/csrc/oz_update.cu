@@ -93,7 +93,9 @@ __global__ void __launch_bounds__(OZ_THREADS)
 oz_update_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                  const __grid_constant__ CUtensorMap mapW, int64_t capA, int64_t capB, int64_t boff, int64_t m,
                  int64_t n, const int32_t *__restrict__ eA, const int32_t *__restrict__ eB, int32_t *err,
-                 const int32_t *abort) {
+                 const int32_t *abort, int lower) {
+  // a Cholesky update leaves the tiles strictly above the diagonal alone
+  if (lower && boff + (int64_t)blockIdx.y * OBN >= (int64_t)blockIdx.x * OBM + OBM) return;
   if (abandoned(abort)) return;
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t bar_load, bar_mma;
@@ -214,7 +216,7 @@ __global__ void oz_split_rows(int64_t rows, const double *__restrict__ X, int64_
 
 int oz_update(cudaStream_t s, int64_t m, int64_t n, const CUtensorMap &A, const CUtensorMap &B, int64_t capA,
               int64_t capB, const int32_t *eA, const int32_t *eB, double *W, int64_t ldw, int32_t *err, int64_t boff,
-              const int32_t *abort) {
+              const int32_t *abort, bool lower) {
   if (m <= 0 || n <= 0) return 0;
   if ((ldw & 1) != 0 || (reinterpret_cast<uintptr_t>(W) & 15) != 0)
     return fail(BOLA_ERR_UNSUPPORTED, "oz_update: W needs an even leading dimension and a 16-byte aligned origin");
@@ -227,7 +229,8 @@ int oz_update(cudaStream_t s, int64_t m, int64_t n, const CUtensorMap &A, const 
   }
   const dim3 grid((unsigned)cdiv(m, OBM), (unsigned)cdiv(n, OBN));
   ProfScope prof(s, "oz_update", 2.0 * (double)m * n * OK * NPAIRS, 16.0 * (double)m * n);
-  oz_update_kernel<<<grid, OZ_THREADS, OZ_SMEM, s>>>(A, B, mapW, capA, capB, boff, m, n, eA, eB, err, abort);
+  oz_update_kernel<<<grid, OZ_THREADS, OZ_SMEM, s>>>(A, B, mapW, capA, capB, boff, m, n, eA, eB, err, abort,
+                                                     lower ? 1 : 0);
   BOLA_CHECK_LAUNCH();
   return 0;
 }

@@ -285,10 +285,15 @@ struct Server {
     BOLA_TRY_CUDA(cudaMemcpyAsync(A, r->a, an, cudaMemcpyHostToDevice, s));
     BOLA_TRY_CUDA(cudaMemcpyAsync(B, r->b, bn, cudaMemcpyHostToDevice, s));
     if (o.mode == 0) {
+      // SPD requests (kind 1) take the mixed Cholesky, the others the mixed LU
       bola_mixed_opts mo = {o.factor_kind, 30, 1e-14, 1, 1, 1};
       bola_mixed_info mi{};
-      BOLA_TRY(bola_dgesv_mixed_ctx(ctx, n, nr, A, n, B, n, X, n, &mo, &mi, (bola_stream_t)s));
-      r->info.path = mi.path;
+      if (r->kind == 1)
+        BOLA_TRY(bola_dposv_mixed_ctx(ctx, n, nr, A, n, B, n, X, n, &mo, &mi, (bola_stream_t)s));
+      else
+        BOLA_TRY(bola_dgesv_mixed_ctx(ctx, n, nr, A, n, B, n, X, n, &mo, &mi, (bola_stream_t)s));
+      r->info.factorization = mi.factorization;
+      r->info.path = mi.path == 3 ? 4 : mi.path;  // (3 is the batched path here)
       r->info.iterations = mi.iterations;
       r->info.info = mi.factor_info;
       r->info.backward_error = mi.backward_error;
@@ -318,6 +323,7 @@ struct Server {
     BOLA_TRY_CUDA(cudaStreamSynchronize(s));
     r->info.info = hinfo;
     r->info.path = 2;
+    r->info.factorization = r->kind == 1 ? 1 : 0;
     return 0;
   }
 
@@ -418,6 +424,7 @@ struct Server {
       r->info.backward_error = hb[i];
       r->info.info = hi[i];
       r->info.path = 3;
+      r->info.factorization = r->kind;
     }
     return 0;
   }

@@ -134,45 +134,6 @@ struct PanelF64 {
 };
 
 
-__device__ __forceinline__ float tf32_round(float x) {
-  uint32_t u = __float_as_uint(x);
-  u = (u + 0x1000u) & ~0x1FFFu;
-  return __uint_as_float(u);
-}
-
-// Writes one 64-wide row of an update operand (K-major, row `r`).
-__device__ __forceinline__ void write_operand_row(int kind, void *op, float *op_lo, int64_t r, const float *v) {
-  if (kind == 0) {
-    __nv_bfloat16 *d = static_cast<__nv_bfloat16 *>(op) + r * SNB;
-#pragma unroll
-    for (int c = 0; c < SNB; c += 8) {
-      __align__(16) __nv_bfloat16 t[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) t[u] = __float2bfloat16_rn(v[c + u]);
-      *reinterpret_cast<uint4 *>(d + c) = *reinterpret_cast<const uint4 *>(t);
-    }
-  } else {
-    float *d = static_cast<float *>(op) + r * SNB;
-    float *dl = op_lo + r * SNB;
-#pragma unroll
-    for (int c = 0; c < SNB; c += 4) {
-      float4 h, l;
-      h.x = tf32_round(v[c]);
-      h.y = tf32_round(v[c + 1]);
-      h.z = tf32_round(v[c + 2]);
-      h.w = tf32_round(v[c + 3]);
-      *reinterpret_cast<float4 *>(d + c) = h;
-      if (kind == 2) {
-        l.x = tf32_round(v[c] - h.x);
-        l.y = tf32_round(v[c + 1] - h.y);
-        l.z = tf32_round(v[c + 2] - h.z);
-        l.w = tf32_round(v[c + 3] - h.w);
-        *reinterpret_cast<float4 *>(dl + c) = l;
-      }
-    }
-  }
-}
-
 // Row pitch of a panel held in shared memory: at least R + 1 and a multiple
 // of the 16-byte vector (4 floats or 2 doubles), so that a lane can move V
 // consecutive rows of a column in one access.
@@ -253,10 +214,23 @@ spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, 
   auto PE = [&](int c, int il) -> T & { return sp[c * RP + il]; };
   const int ns = nr;
 
-  for (int64_t e = tid; e < (int64_t)ns * jb; e += SPT) {
-    const int il = (int)(e % ns);
-    const int c = (int)(e / ns);
-    sp[c * RP + il] = P::load(W[(r0 + il) + c * ldw]);
+  // a thread's rows, 16 columns at a time, all of those loads in flight together
+  for (int il0 = tid; il0 < ns; il0 += 2 * SPT) {
+    const int il1 = il0 + SPT;
+    for (int c0 = 0; c0 < jb; c0 += 16) {
+      typename P::G t0[16], t1[16];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        t0[c] = c0 + c < jb ? W[(r0 + il0) + (int64_t)(c0 + c) * ldw] : typename P::G(0);
+        t1[c] = (il1 < ns && c0 + c < jb) ? W[(r0 + il1) + (int64_t)(c0 + c) * ldw] : typename P::G(0);
+      }
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        if (c0 + c >= jb) break;
+        sp[(c0 + c) * RP + il0] = P::load(t0[c]);
+        if (il1 < ns) sp[(c0 + c) * RP + il1] = P::load(t1[c]);
+      }
+    }
   }
   if (tid == 0) {
     sm100::mbar_init(&xbar[0], 1);
@@ -442,10 +416,10 @@ spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, 
   }
 
   // -- write back the panel and the update's A operand (rows below the panel)
-  for (int64_t e = tid; e < (int64_t)ns * jb; e += SPT) {
-    const int il = (int)(e % ns);
-    const int c = (int)(e / ns);
-    W[(r0 + il) + c * ldw] = P::store(sp[c * RP + il]);
+  for (int il = tid; il < ns; il += SPT) {
+    typename P::G *wr = W + (r0 + il);
+#pragma unroll 8
+    for (int c = 0; c < jb; ++c) wr[(int64_t)c * ldw] = P::store(sp[c * RP + il]);
   }
   if (plan != nullptr && cr == 0 && warp == 0) {
     // the panel's interchanges as "row rows[t] takes the old row src[t]",
@@ -500,6 +474,525 @@ spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, 
   cluster.sync();  // no CTA leaves while another may still push into it
 }
 
+// ---- tournament panel (the FP32 factors) ----------------------------------------
+// Partial pivoting exchanges the pivot candidates of every CTA once per
+// column, so a cluster panel pays 64 cluster round trips.  The FP32 factors
+// (kinds 0-2) select their pivots by tournament instead (TSLU, the panel
+// step of communication-avoiding LU): per group of TG = 8 columns,
+//   1. every warp runs partial pivoting on its own rows over the group's
+//      columns (in registers, on scratch copies) and nominates TG rows;
+//   2. warp 0 runs it again on the CTA's 8 x TG nominees (their current
+//      values, not the warps' eliminated copies) and keeps TG;
+//   3. each CTA pushes its TG nominees into every CTA's shared memory
+//      (st.async onto the receiver's mbarrier: one exchange per group instead
+//      of one per column);
+//   4. while the pushes fly, each CTA applies the previous group's update to
+//      its rows' columns right of the current group (look-ahead: the previous
+//      group only updated the current group's columns before the search);
+//   5. every CTA runs partial pivoting on the same C x TG stacked nominees and
+//      so picks the same TG pivot rows, with their multipliers; the pivots' U
+//      rows right of the group come from the pushed rows, brought up to date
+//      with the previous group's update first (the pushed multipliers of that
+//      group travel with them);
+//   6. every CTA gives its rows the group's multipliers (forward substitution
+//      through the TG x TG block of U) and updates the next group's columns.
+// Rows never move during the panel (a per-row state records which column a
+// row is the pivot of); the interchanges (LAPACK ipiv) are derived at the end
+// and every row is written back once, to its final position.  The pivots are
+// not those of column-by-column partial pivoting; their growth is that of
+// tournament pivoting (CALU), and only the FP64 refinement decides accuracy.
+constexpr int TG = 8;     // columns per tournament group
+constexpr int TPT = 256;  // threads per panel CTA (8 warps)
+constexpr int TRPL = 2;   // panel rows per thread: R <= TPT * TRPL = 512
+
+struct alignas(16) TSlot {
+  uint32_t row, pad0, pad1, pad2;  // panel row of the nominee, or 0xFFFFFFFF (none)
+  float v[SNB];                    // its values from column pb on: v[k] = column pb + k
+};
+
+// Partial pivoting over gw <= TG columns of the candidates a warp holds
+// (candidate l + 32 r sits in row r of lane l).  The pivot key is |v| with
+// its 8 lowest bits replaced by 255 - candidate, so that one warp reduction
+// finds the pivot (the lowest mantissa bits do not matter for the pivot's
+// quality; ties go to the lowest candidate; a NaN never wins).  Writes the
+// selected candidates in order to sel[] (on every lane) and returns their
+// count.  RECORD: the multipliers each selected row had before its selection
+// go to Lrec[t][s] (s < t), and the pivot rows' eliminated values in group
+// column k >= t to Urec[k * uk + t].
+template <int RPL, bool RECORD>
+__device__ __forceinline__ int warp_gepp(float (&v)[RPL][TG], bool (&live)[RPL], int gw, int (&sel)[TG],
+                                         float (*Lrec)[TG], float *Urec, int uk) {
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  float lm[RPL][TG];
+  int cnt = 0;
+#pragma unroll
+  for (int t = 0; t < TG; ++t) {
+    if (t >= gw) break;
+    uint32_t key = 0u;
+#pragma unroll
+    for (int r = 0; r < RPL; ++r) {
+      if (!live[r]) continue;
+      const float x = fabsf(v[r][t]);
+      const uint32_t a = x == x ? __float_as_uint(x) : 0u;
+      const uint32_t k = (a & ~0xFFu) | (uint32_t)(255 - (lane + 32 * r));
+      key = k > key ? k : key;
+    }
+    const uint32_t mk = __reduce_max_sync(FULL, key);
+    if (mk == 0u) break;  // no live candidate left (a live one has a key >= 128)
+    const int slot = 255 - (int)(mk & 0xFFu);
+    const int wl = slot & 31, wr = slot >> 5;
+    float pv[TG];
+#pragma unroll
+    for (int k = 0; k < TG; ++k) {
+      float x = v[0][k];
+#pragma unroll
+      for (int r = 1; r < RPL; ++r)
+        if (wr == r) x = v[r][k];
+      pv[k] = __shfl_sync(FULL, x, wl);
+    }
+    sel[t] = slot;
+    if (lane == wl) {
+#pragma unroll
+      for (int r = 0; r < RPL; ++r)
+        if (r == wr) {
+          live[r] = false;
+          if (RECORD) {
+#pragma unroll
+            for (int s = 0; s < t; ++s) Lrec[t][s] = lm[r][s];
+          }
+        }
+    }
+    if (RECORD && lane == 0) {
+#pragma unroll
+      for (int k = t; k < TG; ++k) Urec[k * uk + t] = pv[k];
+    }
+    const float inv = pv[t] != 0.f ? __frcp_rn(pv[t]) : 0.f;
+#pragma unroll
+    for (int r = 0; r < RPL; ++r) {
+      if (!live[r]) continue;
+      const float l = v[r][t] * inv;
+      if (RECORD) lm[r][t] = l;
+#pragma unroll
+      for (int k = t + 1; k < TG; ++k) v[r][k] = fmaf(-l, pv[k], v[r][k]);
+    }
+    ++cnt;
+  }
+  return cnt;
+}
+
+// Dynamic shared memory of the tournament panel: the rows (column-major,
+// pitch RP, 64 columns, zero beyond jb), the double-buffered nominee slots
+// (C x TG per buffer) and the row states.
+__host__ __device__ constexpr size_t tpanel_smem(int64_t R, int C) {
+  return sizeof(float) * (size_t)SNB * (size_t)panel_pitch<float>(R) + 2 * (size_t)C * TG * sizeof(TSlot) +
+         sizeof(int16_t) * (size_t)(R + 8);
+}
+
+// a -= sum_s l[s] u[s] (s = 0..7, in order)
+__device__ __forceinline__ float rank8(float a, const float (&l)[TG], const float4 &u0, const float4 &u1) {
+  a = fmaf(-l[0], u0.x, a);
+  a = fmaf(-l[1], u0.y, a);
+  a = fmaf(-l[2], u0.z, a);
+  a = fmaf(-l[3], u0.w, a);
+  a = fmaf(-l[4], u1.x, a);
+  a = fmaf(-l[5], u1.y, a);
+  a = fmaf(-l[6], u1.z, a);
+  a = fmaf(-l[7], u1.w, a);
+  return a;
+}
+
+__global__ void __launch_bounds__(TPT, 1)
+tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0, int32_t *info, int kind,
+              void *aop, float *aop_lo, int64_t R, int32_t *plan, uint64_t *track, double give_up, int32_t *err) {
+  cg::cluster_group cluster = cg::this_cluster();
+  // an abandoned factorisation (flag set by an earlier panel on this stream,
+  // so every CTA reads the same value): identity pivots keep ipiv valid
+  if (track != nullptr && *(volatile const int32_t *)(track + 2) != 0) {
+    if (cluster.block_rank() == 0)
+      for (int t = threadIdx.x; t < jb; t += blockDim.x) ipiv[t] = col0 + t + 1;
+    return;
+  }
+  const int C = (int)cluster.num_blocks();
+  const int cr = (int)cluster.block_rank();
+  __shared__ uint64_t xbar[2];             // completes when every CTA's nominees of a group have landed
+  __shared__ int32_t cand1[TPT / 32][TG];  // each warp's nominees (local rows, -1: none)
+  __shared__ int32_t cand2[TG];            // the CTA's nominees
+  __shared__ int32_t win[SNB];             // panel row of the pivot of each column
+  __shared__ int32_t wslot[TG];            // the group's pivots as slot indices
+  __shared__ float Lg[TG][TG];             // the group pivots' multipliers within the group
+  __shared__ __align__(16) float UgT[2][SNB][TG];  // U rows of a group's pivots, transposed (two groups)
+  __shared__ float invp[TG];
+  __shared__ int32_t posin[SNB], at_[SNB], ipg[SNB];  // interchange bookkeeping (CTA 0)
+  __shared__ int sfail;
+  extern __shared__ __align__(16) unsigned char tp_raw[];
+  const int RP = panel_pitch<float>(R);
+  float *sp = reinterpret_cast<float *>(tp_raw);
+  TSlot *slots = reinterpret_cast<TSlot *>(tp_raw + sizeof(float) * (size_t)SNB * RP);
+  int16_t *rstate = reinterpret_cast<int16_t *>(tp_raw + sizeof(float) * (size_t)SNB * RP +
+                                                2 * (size_t)C * TG * sizeof(TSlot));
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int r0 = (int)(cr * R);
+  const int r1 = (int)imin(mp, r0 + R);
+  const int nr = r1 > r0 ? r1 - r0 : 0;
+
+  // the panel into shared memory: a thread's rows, 32 columns at a time, with
+  // all of those loads in flight together (the copy is latency-bound otherwise)
+#pragma unroll
+  for (int c0 = 0; c0 < SNB; c0 += 32) {
+    float t[TRPL][32];
+#pragma unroll
+    for (int r = 0; r < TRPL; ++r) {
+      const int il = tid + TPT * r;
+#pragma unroll
+      for (int c = 0; c < 32; ++c)
+        t[r][c] = (il < nr && c0 + c < jb) ? W[(r0 + il) + (int64_t)(c0 + c) * ldw] : 0.f;
+    }
+#pragma unroll
+    for (int r = 0; r < TRPL; ++r) {
+      const int il = tid + TPT * r;
+      if (il < nr)
+#pragma unroll
+        for (int c = 0; c < 32; ++c) sp[(c0 + c) * RP + il] = t[r][c];
+    }
+  }
+  for (int il = tid; il < nr; il += TPT) rstate[il] = -1;  // -1: not a pivot yet; j: the pivot of column j
+  if (tid == 0) {
+    sm100::mbar_init(&xbar[0], 1);
+    sm100::mbar_init(&xbar[1], 1);
+    sm100::fence_mbar_init();
+    sfail = 0;
+  }
+  __syncthreads();
+  cluster.sync();  // every CTA runs, its mbarriers initialised, before the first push
+
+  bool failed = false;
+  uint64_t umax = 0, umin = ~0ull;  // |u_jj| bits (CTA 0, thread 0)
+  const int ngroups = (int)cdiv(jb, TG);
+  for (int g = 0; g < ngroups; ++g) {
+    const int c0 = g * TG, gw = (int)imin(TG, jb - c0), par = g & 1, ub = g & 1;
+    const int pb = c0 >= TG ? c0 - TG : 0;  // first pushed column: the previous group's multipliers on
+    const int nv = SNB - pb;                // values pushed per nominee (a multiple of 8)
+    const int nq = 1 + nv / 4;
+    if (tid == 0) sm100::mbar_arrive_expect_tx(&xbar[par], (uint32_t)(C * gw * (16 + 4 * nv)));
+    // -- 1. each warp's nominees from its own rows (the group's columns are current)
+    {
+      float v[TRPL][TG];
+      bool live[TRPL];
+#pragma unroll
+      for (int r = 0; r < TRPL; ++r) {
+        const int il = warp * 32 + lane + TPT * r;
+        live[r] = il < nr && rstate[il] < 0;
+#pragma unroll
+        for (int k = 0; k < TG; ++k) v[r][k] = live[r] ? sp[(c0 + k) * RP + il] : 0.f;
+      }
+      int sel[TG];
+      const int cnt = warp_gepp<TRPL, false>(v, live, gw, sel, nullptr, nullptr, 0);
+      if (lane < TG) {
+        int il = -1;
+#pragma unroll
+        for (int t = 0; t < TG; ++t)
+          if (t == lane && t < cnt) il = warp * 32 + (sel[t] & 31) + TPT * (sel[t] >> 5);
+        cand1[warp][lane] = il;
+      }
+    }
+    __syncthreads();
+    // -- 2. the CTA's nominees from the warps' (warp 0)
+    if (warp == 0) {
+      constexpr int NC1 = (TPT / 32) * TG;  // 64 candidates: 2 per lane
+      float v[NC1 / 32][TG];
+      bool live[NC1 / 32];
+      int cil[NC1 / 32];
+#pragma unroll
+      for (int r = 0; r < NC1 / 32; ++r) {
+        const int ci = lane + 32 * r;
+        cil[r] = cand1[ci / TG][ci % TG];
+        live[r] = cil[r] >= 0;
+#pragma unroll
+        for (int k = 0; k < TG; ++k) v[r][k] = live[r] ? sp[(c0 + k) * RP + cil[r]] : 0.f;
+      }
+      int sel[TG];
+      const int cnt = warp_gepp<NC1 / 32, false>(v, live, gw, sel, nullptr, nullptr, 0);
+#pragma unroll
+      for (int t = 0; t < TG; ++t) {
+        int il = -1;
+        if (t < cnt) {
+          const int sl = sel[t];
+          int x = cil[0];
+#pragma unroll
+          for (int r = 1; r < NC1 / 32; ++r)
+            if ((sl >> 5) == r) x = cil[r];
+          il = __shfl_sync(0xffffffffu, x, sl & 31);
+        }
+        if (lane == 0) cand2[t] = il;
+      }
+    }
+    __syncthreads();
+    // -- 3. push the nominees (columns pb..63) into every CTA: slot cr * gw + s of buffer par
+    for (int e = tid; e < C * gw * nq; e += TPT) {
+      const int q = e % nq, s = (e / nq) % gw, d = e / (nq * gw);
+      const int il = cand2[s];
+      const uint32_t rbar = cluster_addr(&xbar[par], d);
+      const uint32_t rs = cluster_addr(&slots[(size_t)par * C * TG + cr * gw + s], d);
+      if (q == 0) {
+        st_async4(rs, il >= 0 ? (uint32_t)(r0 + il) : 0xFFFFFFFFu, 0u, 0u, 0u, rbar);
+      } else {
+        const int k = (q - 1) * 4;
+        uint32_t w4[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) w4[u] = il >= 0 ? __float_as_uint(sp[(pb + k + u) * RP + il]) : 0u;
+        st_async4(rs + 16 + 4 * k, w4[0], w4[1], w4[2], w4[3], rbar);
+      }
+    }
+    __syncthreads();  // the pushes have read the nominees' rows before they change
+    // -- 4. the previous group's update on the columns right of this group
+    if (g > 0) {
+      const float(*U)[TG] = UgT[ub ^ 1];
+#pragma unroll
+      for (int r = 0; r < TRPL; ++r) {
+        const int il = tid + TPT * r;
+        if (il >= nr || rstate[il] >= 0) continue;
+        float l[TG];
+#pragma unroll
+        for (int s2 = 0; s2 < TG; ++s2) l[s2] = sp[(pb + s2) * RP + il];
+        for (int k = c0 + TG; k < SNB; ++k) {
+          const float4 u0 = *reinterpret_cast<const float4 *>(&U[k][0]);
+          const float4 u1 = *reinterpret_cast<const float4 *>(&U[k][4]);
+          sp[k * RP + il] = rank8(sp[k * RP + il], l, u0, u1);
+        }
+      }
+    }
+    // every CTA's nominees have landed (bounded: a missing push sets the
+    // error flag and ends the panel, never a hang)
+    if (!sm100::bounded_wait(&xbar[par], (uint32_t)(g >> 1) & 1u)) sfail = 1;
+    __syncthreads();
+    if (sfail) {
+      if (tid == 0) atomicExch(err, 5);
+      failed = true;
+      break;
+    }
+    const TSlot *sl = slots + (size_t)par * C * TG;
+    // -- 5. the group's pivots from all nominees: the same in every CTA
+    if (warp == 0) {
+      constexpr int NC3 = SMAXC * TG / 32;  // up to 128 candidates: 4 per lane
+      float v[NC3][TG];
+      bool live[NC3];
+#pragma unroll
+      for (int r = 0; r < NC3; ++r) {
+        const int ci = lane + 32 * r;
+        live[r] = ci < C * gw && sl[ci].row != 0xFFFFFFFFu;
+#pragma unroll
+        for (int k = 0; k < TG; ++k) v[r][k] = live[r] ? sl[ci].v[c0 - pb + k] : 0.f;
+      }
+      int sel[TG];
+      const int cnt = warp_gepp<NC3, true>(v, live, gw, sel, Lg, &UgT[ub][c0][0], TG);
+      // the panel always has at least gw rows that are not pivots yet, so
+      // cnt == gw; a shortfall would mean a corrupted exchange
+      if (cnt < gw && lane == 0) atomicExch(err, 6);
+      if (lane < TG) {
+        int s2 = 0;
+#pragma unroll
+        for (int t = 0; t < TG; ++t)
+          if (t == lane) s2 = sel[t];
+        if (lane < cnt) {
+          wslot[lane] = s2;
+          win[c0 + lane] = (int32_t)sl[s2].row;
+        } else if (lane < gw) {
+          wslot[lane] = -1;
+          win[c0 + lane] = -1;
+        }
+      }
+    }
+    __syncthreads();
+    if (win[c0 + gw - 1] < 0) {  // (err is set) leave the group loop uniformly
+      failed = true;
+      break;
+    }
+    // the pivots' U rows right of the group: the pushed rows brought up to
+    // date with the previous group's update, then eliminated within the group
+    for (int k = c0 + gw + tid; k < SNB; k += TPT) {
+      float u[TG];
+#pragma unroll
+      for (int t = 0; t < TG; ++t) {
+        u[t] = 0.f;
+        if (t >= gw) continue;
+        const TSlot &w = sl[wslot[t]];
+        float a = w.v[k - pb];
+        if (g > 0) {
+          float l[TG];
+#pragma unroll
+          for (int s2 = 0; s2 < TG; ++s2) l[s2] = w.v[s2];
+          a = rank8(a, l, *reinterpret_cast<const float4 *>(&UgT[ub ^ 1][k][0]),
+                    *reinterpret_cast<const float4 *>(&UgT[ub ^ 1][k][4]));
+        }
+#pragma unroll
+        for (int q = 0; q < t; ++q) a = fmaf(-Lg[t][q], u[q], a);
+        u[t] = a;
+      }
+      *reinterpret_cast<float4 *>(&UgT[ub][k][0]) = make_float4(u[0], u[1], u[2], u[3]);
+      *reinterpret_cast<float4 *>(&UgT[ub][k][4]) = make_float4(u[4], u[5], u[6], u[7]);
+    }
+    if (tid < gw) {
+      const float pv = UgT[ub][c0 + tid][tid];
+      invp[tid] = pv != 0.f ? __frcp_rn(pv) : 0.f;
+      const int row = win[c0 + tid];
+      if (row >= r0 && row < r1) rstate[row - r0] = (int16_t)(c0 + tid);
+    }
+    if (cr == 0 && tid == 0) {
+      for (int t = 0; t < gw; ++t) {
+        const float pv = UgT[ub][c0 + t][t];
+        if (pv == 0.f) atomicCAS(info, 0, col0 + c0 + t + 1);
+        const uint64_t ab = __float_as_uint(pv) & 0x7fffffffu;
+        if (ab <= 0x7f800000u) {
+          umax = ab > umax ? ab : umax;
+          umin = ab < umin ? ab : umin;
+        }
+      }
+    }
+    __syncthreads();
+    // -- 6. this CTA's rows: pivot rows take their final values; the others
+    // their multipliers and the update of the next group's columns
+#pragma unroll
+    for (int r = 0; r < TRPL; ++r) {
+      const int il = tid + TPT * r;
+      if (il >= nr) continue;
+      const int st = rstate[il];
+      if (st >= 0 && st < c0) continue;  // the pivot of an earlier group: final
+      if (st >= c0) {
+        const int t = st - c0;
+        for (int s2 = 0; s2 < t; ++s2) sp[(c0 + s2) * RP + il] = Lg[t][s2];
+        for (int k = c0 + t; k < SNB; ++k) sp[k * RP + il] = UgT[ub][k][t];
+        continue;
+      }
+      float l[TG];
+#pragma unroll
+      for (int s2 = 0; s2 < TG; ++s2) {
+        l[s2] = 0.f;
+        if (s2 >= gw) continue;
+        float a = sp[(c0 + s2) * RP + il];
+#pragma unroll
+        for (int q = 0; q < s2; ++q) a = fmaf(-l[q], UgT[ub][c0 + s2][q], a);
+        l[s2] = a * invp[s2];
+        sp[(c0 + s2) * RP + il] = l[s2];
+      }
+      const int k1 = (int)imin(SNB, c0 + 2 * TG);
+      for (int k = c0 + TG; k < k1; ++k) {
+        const float4 u0 = *reinterpret_cast<const float4 *>(&UgT[ub][k][0]);
+        const float4 u1 = *reinterpret_cast<const float4 *>(&UgT[ub][k][4]);
+        sp[k * RP + il] = rank8(sp[k * RP + il], l, u0, u1);
+      }
+    }
+    __syncthreads();
+  }
+  if (!failed) {
+    // -- the interchanges (CTA 0): LAPACK's sequence of row swaps that puts
+    // the pivot of column j in row j, from the pivot list.  Rows below the
+    // panel's first jb never move until they become a pivot; rows among the
+    // first jb are tracked: at_[q] = the row now in position q < jb,
+    // posin[x] = the position of original row x < jb.
+    if (cr == 0 && tid == 0) {
+      for (int x = 0; x < jb; ++x) posin[x] = at_[x] = x;
+      for (int j = 0; j < jb; ++j) {
+        const int x = win[j];
+        const int q = x < jb ? posin[x] : x;
+        ipg[j] = col0 + q + 1;
+        const int r = at_[j];
+        if (r != x) {
+          if (q < jb) at_[q] = r;
+          posin[r] = q;
+        }
+        at_[j] = x;
+        if (x < jb) posin[x] = j;
+      }
+      for (int j = 0; j < jb; ++j) ipiv[j] = ipg[j];
+    }
+    __syncthreads();
+    if (track != nullptr && cr == 0 && tid == 0) {
+      if (umin != ~0ull) {
+        const uint64_t mx = (uint64_t)__double_as_longlong((double)__uint_as_float((uint32_t)umax));
+        const uint64_t mn = (uint64_t)__double_as_longlong((double)__uint_as_float((uint32_t)umin));
+        if (mx > track[0]) track[0] = mx;
+        if (mn < track[1]) track[1] = mn;
+      }
+      const double gmx = __longlong_as_double((long long)track[0]), gmn = __longlong_as_double((long long)track[1]);
+      const double spread = gmn > 0.0 ? gmx / gmn : INFINITY;
+      if (!(spread < give_up)) *(volatile int32_t *)(track + 2) = 1;
+    }
+    // final position of each of this CTA's rows
+    auto dest = [&](int il) -> int {
+      const int st = rstate[il];
+      if (st >= 0) return st;
+      if (cr == 0 && il < jb) return posin[il];
+      return r0 + il;
+    };
+    // -- write back the panel, each row to its final position
+#pragma unroll
+    for (int r = 0; r < TRPL; ++r) {
+      const int il = tid + TPT * r;
+      if (il >= nr) continue;
+      float *wr = W + dest(il);
+#pragma unroll 8
+      for (int c = 0; c < jb; ++c) wr[(int64_t)c * ldw] = sp[c * RP + il];
+    }
+    if (plan != nullptr && cr == 0 && warp == 0) {
+      // the interchanges as "row rows[t] takes the old row src[t]" for the swap kernel
+      SwapPlan p;
+      p.ix0 = 0;
+      p.i1 = col0 + 1;
+      p.i2 = col0 + jb;
+      p.i_inc = 1;
+      p.incx = 1;
+      const int cnt = compose_swaps_warp<4, int32_t>(p, ipg, plan + 1, plan + 1 + 2 * SNB);
+      if (lane == 0) plan[0] = cnt;
+    }
+    if (aop != nullptr) {  // rows below the panel's top: the update's K-major A operand
+      for (int il = tid; il < nr; il += TPT) {
+        const int dst = dest(il);
+        if (dst < jb) continue;
+        float v[SNB];
+#pragma unroll
+        for (int c = 0; c < SNB; ++c) v[c] = c < jb ? sp[c * RP + il] : 0.f;
+        write_operand_row(kind, aop, aop_lo, dst - jb, v);
+      }
+    }
+  }
+  cluster.sync();  // no CTA leaves while another may still push into it
+}
+
+int launch_tpanel(cudaStream_t s, float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0,
+                  int32_t *info, int kind, void *aop, float *aop_lo, int32_t *plan, uint64_t *track, double give_up,
+                  int32_t *err) {
+  const int C = (int)imin(SMAXC, imax(1, cdiv(mp, TPT)));
+  const int64_t R = cdiv(mp, C);
+  // CTA 0 must hold the panel's first jb rows (the interchange bookkeeping)
+  if (R > (int64_t)TPT * TRPL || R < jb)
+    return fail(BOLA_ERR_UNSUPPORTED, "mixed LU: panel of %lld x %d not supported", (long long)mp, jb);
+  const size_t smem = tpanel_smem(R, C);
+  static bool attr = false;
+  if (!attr) {
+    BOLA_TRY_CUDA(cudaFuncSetAttribute(tpanel_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    BOLA_TRY_CUDA(cudaFuncSetAttribute(tpanel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)tpanel_smem(TPT * TRPL, SMAXC)));
+    attr = true;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)C, 1, 1);
+  cfg.blockDim = dim3(TPT, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)C;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  ProfScope prof(s, "tpanel", (double)mp * jb * jb, 8.0 * (double)mp * jb);
+  BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, tpanel_kernel, W, ldw, mp, jb, ipiv, col0, info, kind, aop, aop_lo, R, plan,
+                                   track, give_up, err));
+  return 0;
+}
+
 // The panel's interchanges on all other columns, U12 = L11^-1 A12 on the
 // right ones and their K-major B operand.  A warp per column.
 template <typename T>
@@ -516,9 +1009,18 @@ sswap_trsm(T *W, int64_t ldw, int64_t n, int64_t j, int jb, const int32_t *plan,
     rows[t] = plan[1 + t];
     src[t] = plan[1 + 2 * SNB + t];
   }
-  for (int e = threadIdx.x; e < jb * jb; e += blockDim.x) {
-    const int r = e % jb, c = e / jb;
-    L[r + c * SNB] = W[(j + r) + (j + c) * ldw];
+  // the 64 x 64 diagonal block (L11 below its diagonal), all of a thread's loads in flight together
+  {
+    constexpr int PER = SNB * SNB / 256;
+    T t[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int e = threadIdx.x + 256 * q;
+      const int r = e % SNB, c = e / SNB;
+      t[q] = (r < jb && c < jb) ? W[(j + r) + (j + c) * ldw] : T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < PER; ++q) L[threadIdx.x + 256 * q] = t[q];
   }
   __syncthreads();
   const int lane = threadIdx.x & 31;
@@ -635,6 +1137,7 @@ int MixedLU::reserve(int64_t n_, int kind_, cudaStream_t s) {
       BOLA_TRY_CUDA(cudaMallocAsync(&aop[b], (size_t)OZ_SLICES * n * SNB * 2, s));
       BOLA_TRY_CUDA(cudaMallocAsync(&ea[b], sizeof(int32_t) * n, s));
       BOLA_TRY(make_kmajor_map(&mapA[b], aop[b], OZ_SLICES * n, true, 128));
+      BOLA_TRY(make_kmajor_map(&mapA64[b], aop[b], OZ_SLICES * n, true, 64));
     }
     BOLA_TRY_CUDA(cudaMallocAsync(&bop, (size_t)OZ_SLICES * n * SNB * 2, s));
     BOLA_TRY_CUDA(cudaMallocAsync(&eb, sizeof(int32_t) * n, s));
@@ -720,10 +1223,13 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
     const int64_t mp = n - j;
     const bool upd = j + jb < n;
     const int buf = (int)(k & 1);
-    using Pol = typename std::conditional<fp64, PanelF64, PanelF32>::type;
-    BOLA_TRY(launch_spanel<Pol>(lu.sp, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, lu.kind,
-                              upd ? lu.aop[buf] : nullptr, fp64 ? nullptr : lu.aop_lo[buf], fp64 ? lu.ea[buf] : nullptr,
-                              lu.cap_n, lu.plan, track, give_up, lu.err));
+    if constexpr (fp64)
+      BOLA_TRY(launch_spanel<PanelF64>(lu.sp, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, lu.kind,
+                                       upd ? lu.aop[buf] : nullptr, nullptr, lu.ea[buf], lu.cap_n, lu.plan, track,
+                                       give_up, lu.err));
+    else
+      BOLA_TRY(launch_tpanel(lu.sp, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, lu.kind,
+                             upd ? lu.aop[buf] : nullptr, lu.aop_lo[buf], lu.plan, track, give_up, lu.err));
     // the row swaps reach every column: the previous wide update must be done
     if (wide_pending) BOLA_TRY_CUDA(cudaStreamWaitEvent(lu.sp, lu.ev_wide, 0));
     wide_pending = false;
@@ -771,3 +1277,26 @@ int MixedLU::factor64(cudaStream_t s, double *W, int64_t ldw, int32_t *ipiv, int
 }
 
 }  // namespace bola
+
+// The low-precision LU alone, for tests and profiling: W (n x n FP32,
+// column-major, ld ldw) is replaced by its factors (unit-lower L below the
+// diagonal, U on and above), ipiv (device, 1-based, LAPACK order) and *info
+// (device: the first exact-zero pivot, 1-based, or 0).  Synchronous.
+extern "C" int bola_sgetrf_mixed(int kind, int64_t n, float *w, int64_t ldw, int32_t *ipiv, int32_t *info,
+                                 bola_stream_t stream) {
+  using namespace bola;
+  if (kind < 0 || kind > 2) return -1;
+  if (n < 0 || n > 8192) return -2;
+  if (ldw < imax(1, n)) return -4;
+  if (n == 0) return 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  MixedLU lu;
+  int st = lu.reserve(n, kind, s);
+  if (st == 0) st = lu.factor(s, w, ldw, ipiv, info);
+  int32_t err = 0;
+  if (st == 0 && lu.err) st = cudaMemcpyAsync(&err, lu.err, sizeof err, cudaMemcpyDeviceToHost, s) == cudaSuccess ? 0 : BOLA_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess && st == 0) st = fail(BOLA_ERR_CUDA, "bola_sgetrf_mixed: %s", cudaGetErrorString(cudaGetLastError()));
+  lu.destroy();
+  if (st == 0 && err != 0) st = fail(BOLA_ERR_CUDA, "mixed LU: a bounded wait expired (code %d)", err);
+  return st;
+}

@@ -43,8 +43,11 @@ template <int KIND, int NPASS>
 __global__ void __launch_bounds__(128)
 tc_update_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                  const __grid_constant__ CUtensorMap mapAlo, const __grid_constant__ CUtensorMap mapBlo, int64_t m,
-                 int64_t n, int64_t boff, float *__restrict__ W, int64_t ldw, int32_t *err, const int32_t *abort) {
+                 int64_t n, int64_t boff, float *__restrict__ W, int64_t ldw, int32_t *err, const int32_t *abort,
+                 int lower) {
   using Cfg = TcCfg<KIND, NPASS>;
+  // a Cholesky update leaves the tiles strictly above the diagonal alone
+  if (lower && boff + (int64_t)blockIdx.y * BN >= (int64_t)blockIdx.x * BM + BM) return;
   if (abandoned(abort)) return;
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t bar_load, bar_mma;
@@ -177,6 +180,20 @@ int make_kmajor_map(CUtensorMap *map, const void *ptr, int64_t rows, bool bf16, 
   return 0;
 }
 
+int make_kmajor_map2(CUtensorMap *map, const void *ptr, int64_t kdim, int64_t rows, int64_t kp, int box_rows) {
+  EncodeFn enc = encode_fn();
+  if (!enc) return fail(BOLA_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  const cuuint64_t dims[2] = {(cuuint64_t)kdim, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)kp * 2};
+  const cuuint32_t box[2] = {64u, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(BOLA_ERR_CUDA, "cuTensorMapEncodeTiled (digit planes) failed (%d)", (int)r);
+  return 0;
+}
+
 // FP64 column-major matrix (rows x cols, ld), boxes of box_rows x box_cols,
 // no swizzle (ld * 8 and the origin must be multiples of 16 bytes).
 int make_fp64_tile_map(CUtensorMap *map, const double *ptr, int64_t rows, int64_t cols, int64_t ld, int box_rows,
@@ -196,7 +213,7 @@ int make_fp64_tile_map(CUtensorMap *map, const double *ptr, int64_t rows, int64_
 
 int tc_update(cudaStream_t s, int kind, int64_t m, int64_t n, const CUtensorMap &A, const CUtensorMap &B,
               const CUtensorMap &Alo, const CUtensorMap &Blo, float *W, int64_t ldw, int32_t *err, int64_t boff,
-              const int32_t *abort) {
+              const int32_t *abort, bool lower) {
   if (m <= 0 || n <= 0) return 0;
   const dim3 grid((unsigned)cdiv(m, BM), (unsigned)cdiv(n, BN));
   ProfScope prof(s, "tc_update", 2.0 * (double)m * n * KDIM * (kind == 2 ? 3 : 1), 8.0 * (double)m * n);
@@ -209,7 +226,7 @@ int tc_update(cudaStream_t s, int kind, int64_t m, int64_t n, const CUtensorMap 
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM_LAUNCH)); \
       attr = true;                                                                                        \
     }                                                                                                     \
-    tc_update_kernel<KIND, NPASS><<<grid, 128, Cfg::SMEM_LAUNCH, s>>>(A, B, Alo, Blo, m, n, boff, W, ldw, err, abort); \
+    tc_update_kernel<KIND, NPASS><<<grid, 128, Cfg::SMEM_LAUNCH, s>>>(A, B, Alo, Blo, m, n, boff, W, ldw, err, abort, lower ? 1 : 0); \
   } while (0)
   if (kind == 0) BOLA_TC(0, 1);
   else if (kind == 1) BOLA_TC(1, 1);

@@ -21,7 +21,7 @@ import torch
 from . import _lib
 
 MODES = {"mixed": 0, "fp64": 1}
-PATHS = {0: "mixed-ir", 1: "gmres-ir", 2: "fp64", 3: "batched-fp64"}
+PATHS = {0: "mixed-ir", 1: "gmres-ir", 2: "fp64", 3: "batched-fp64", 4: "fp64-accurate-factor"}
 KAPPAS = (1e2, 1e6, 1e10)
 
 
@@ -95,6 +95,7 @@ class Server:
         del self._keep[rid]
         rec = {"id": rid, "n": n, "nrhs": nrhs, "status": st, "path": PATHS.get(info.path, str(info.path)),
                "iterations": info.iterations, "info": info.info, "backward_error": info.backward_error,
+               "factorization": "cholesky" if info.factorization == 1 else "lu",
                "t_submit": info.t_submit, "t_admit": info.t_admit, "t_done": info.t_done,
                "latency": info.t_done - info.t_submit}
         if st != 0:

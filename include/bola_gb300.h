@@ -161,6 +161,38 @@ int bola_dgemm_noalloc(char transa, char transb, int64_t m, int64_t n, int64_t k
 int bola_sgemm_tc_update(int kind, int64_t m, int64_t n, const void *a, const void *b, const void *a_lo,
                          const void *b_lo, float *w, int64_t ldw, int32_t *err, bola_stream_t stream);
 
+/* The low-precision LU of bola_dgesv_mixed alone (no BOLA counterpart;
+ * exposed for testing and profiling): W (n x n FP32, column-major, ld ldw,
+ * n <= 8192) is replaced by P W = L U (unit-lower L below the diagonal, U on
+ * and above), blocked right-looking with 64-column panels whose pivots are
+ * chosen by tournament (8-column groups) and tcgen05 trailing updates of the
+ * given kind (0 bf16, 1 tf32, 2 3xTF32).  ipiv (device, n entries) gets
+ * LAPACK-style 1-based interchanges, *info (device) the first exact-zero
+ * pivot (1-based) or 0.  Synchronous. */
+int bola_sgetrf_mixed(int kind, int64_t n, float *w, int64_t ldw, int32_t *ipiv, int32_t *info,
+                      bola_stream_t stream);
+
+/* The low-precision Cholesky of bola_dposv_mixed alone (no BOLA counterpart;
+ * exposed for testing and profiling): the lower triangle of W (n x n FP32 SPD,
+ * ld ldw, n <= 8192) is replaced by L, W = L L^T, with tcgen05 trailing
+ * updates of the given kind (0 bf16, 1 tf32, 2 3xTF32).  *info (device) =
+ * the first column whose pivot is not positive (1-based), or 0.  Synchronous. */
+int bola_spotrf_mixed(int kind, int64_t n, float *w, int64_t ldw, int32_t *info, bola_stream_t stream);
+
+/* FP64-accurate matrix product on the bf16 tensor cores (no BOLA
+ * counterpart; the residuals and GMRES products of bola_dgesv_mixed, exposed
+ * for testing and profiling): out = b - A x, or out = A x when b is NULL,
+ * with A n x n and x, b, out n x nrhs (FP64, column-major).  A is split
+ * exactly into 7 planes of 8-bit digits under a power-of-two scale per row,
+ * x into 8 planes under a scale per column; every plane pair of weight
+ * 2^-56 or more is accumulated exactly (integer partial sums in FP32 on
+ * tcgen05, combined in 64-bit fixed point).  Error per element at most about
+ * 2^-54 n max_j|a_ij| max|x_c| + 2^-52 |(A x)_ic| (the roundings of the
+ * digits and of the final FP64 sum); a row of A or a column of x holding an
+ * Inf or NaN gives NaN.  Allocates its digit planes per call; synchronous. */
+int bola_dgemv_oz(int64_t n, int64_t nrhs, const double *a, int64_t lda, const double *x, int64_t ldx,
+                  const double *b, int64_t ldb, double *out, int64_t ldo, bola_stream_t stream);
+
 /* FP64-accurate update on the bf16 tensor cores (no BOLA counterpart; the
  * trailing update of factor_kind 3 of bola_dgesv_mixed, exposed for
  * testing):  W (m x n, FP64, column-major, ld ldw) -= A B^T with A (m x 64)
@@ -240,9 +272,28 @@ typedef struct {
   int factor_info;       /* first zero pivot of the low-precision LU (1-based), 0 if none */
   double backward_error; /* of the returned X */
   double condition_estimate; /* max|u_ii| / min|u_ii| of the low-precision factor */
+  int factorization;     /* the factor the answer was refined with: 0 LU, 1 Cholesky */
+  int reserved;
 } bola_mixed_info;
 
 int bola_dgesv_mixed(int64_t n, int64_t nrhs, const double *a, int64_t lda, const double *b, int64_t ldb,
+                     double *x, int64_t ldx, const bola_mixed_opts *opts, bola_mixed_info *info,
+                     bola_stream_t stream);
+
+/* Mixed-precision solve of a symmetric positive definite system (no BOLA
+ * counterpart; the FP64 answer it must reach is BOLA's potrf('L') + potrs
+ * solve, src/potrf.rs:101-181).  A is n x n SPD, stored in full (the
+ * factorisation reads its lower triangle, the FP64 residuals all of it).
+ * W = fl(D A D) with D a power of two per row (unit-order diagonal) is
+ * factored W = L L^T on the tensor cores (64-column panels: the diagonal
+ * block in one CTA, L21 as a parallel triangular solve, no pivoting; the
+ * trailing update W22 -= L21 L21^T only on tiles reaching the diagonal),
+ * then refined in FP64 exactly as bola_dgesv_mixed refines (IR, GMRES-IR,
+ * escalation to the FP64-accurate factor kind 3, here a Cholesky too).  A
+ * pivot that is not positive means A is not SPD at the factor's precision:
+ * the call then solves with the mixed LU (info->factorization = 0).  Same
+ * options, limits and return codes as bola_dgesv_mixed. */
+int bola_dposv_mixed(int64_t n, int64_t nrhs, const double *a, int64_t lda, const double *b, int64_t ldb,
                      double *x, int64_t ldx, const bola_mixed_opts *opts, bola_mixed_info *info,
                      bola_stream_t stream);
 
@@ -255,6 +306,9 @@ int bola_mixed_ctx_create(bola_mixed_ctx *ctx);
 int bola_mixed_ctx_destroy(bola_mixed_ctx ctx);
 int64_t bola_mixed_ctx_bytes(bola_mixed_ctx ctx);
 int bola_dgesv_mixed_ctx(bola_mixed_ctx ctx, int64_t n, int64_t nrhs, const double *a, int64_t lda, const double *b,
+                         int64_t ldb, double *x, int64_t ldx, const bola_mixed_opts *opts, bola_mixed_info *info,
+                         bola_stream_t stream);
+int bola_dposv_mixed_ctx(bola_mixed_ctx ctx, int64_t n, int64_t nrhs, const double *a, int64_t lda, const double *b,
                          int64_t ldb, double *x, int64_t ldx, const bola_mixed_opts *opts, bola_mixed_info *info,
                          bola_stream_t stream);
 
@@ -298,7 +352,8 @@ int bola_batch_plan_destroy(bola_batch_plan plan);
  * hbm_budget_bytes.  Requests with n > small_n run on `slots` workers, each
  * with its own stream and mixed-solver context (several run at once); in
  * mode 0 they take bola_dgesv_mixed_ctx (tensor-core LU, FP64 refinement,
- * FP64 fallback; SPD systems are solved by the same LU), in mode 1 the plain
+ * FP64 fallback), or bola_dposv_mixed_ctx for SPD requests (kind 1: the
+ * tensor-core Cholesky, the same refinement), in mode 1 the plain
  * FP64 path (bola_dgetrf/bola_dgetrs, or bola_dpotrf/bola_dpotrs for SPD).
  * Requests with n <= small_n (at most 256) are gathered continuously: every
  * admitted small request waiting when the previous batch ends goes into the
@@ -320,11 +375,14 @@ typedef struct {
 
 typedef struct {
   int32_t status;        /* 0 queued, 1 running, 2 done; < 0 error code */
-  int32_t path;          /* 0 mixed IR, 1 GMRES-IR, 2 FP64, 3 batched FP64 */
+  int32_t path;          /* 0 mixed IR, 1 GMRES-IR, 2 FP64, 3 batched FP64,
+                            4 escalated to the FP64-accurate factor and refined there */
   int32_t iterations;    /* refinement sweeps (mixed paths) */
   int32_t info;          /* factorisation info (0 = success) */
   double backward_error; /* max over right-hand sides */
   double t_submit, t_admit, t_done; /* seconds since the server was created */
+  int32_t factorization; /* 0 LU, 1 Cholesky (the factor the answer came from) */
+  int32_t reserved;
 } bola_request_info;
 
 typedef struct bola_server_st *bola_server;
