@@ -343,7 +343,7 @@ __device__ __forceinline__ void take_block(const unsigned long long *xw, int64_t
       unsigned long long w = ld_word(p);
       int polls = 0;
       while ((uint32_t)(w >> 32) != epoch) {
-        if (++polls > (1 << 22)) {
+        if (++polls > (1 << 20)) {
           atomicExch(err, 3);
           break;
         }
@@ -1057,8 +1057,8 @@ int dgesv_mixed_ws(Workspace &w, bool chol, int64_t n, int64_t nrhs, const doubl
       diag_extent<double><<<1, 1024, 0, s>>>(n, (const double *)w.W, ldW, w.norms + 5 * MAXRHS);
     } else {
       diag_block_inverses<float><<<nb, TB, 0, s>>>(n, (const float *)w.W, n, (float *)w.Dl, (float *)w.Du);
-      BOLA_TRY(couple(s, n, (const float *)w.W, n, (const float *)w.Dl, (const float *)w.Du, w.Mc,
-                      w.Mc + cdiv(n, TB) * TB * TB));
+      BOLA_TRY(couple(s, n, (const float *)w.W, n, (const float *)w.Dl, (const float *)w.Du,
+                      const_cast<float *>(w.ts.Ml), const_cast<float *>(w.ts.Mu)));
       diag_extent<float><<<1, 1024, 0, s>>>(n, (const float *)w.W, n, w.norms + 5 * MAXRHS);
     }
   }
