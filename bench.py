@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=300)
     ap.add_argument("--serve-pool", type=int, default=48)
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-forward-error", action="store_true")
     return ap.parse_args()
 
 
@@ -262,13 +263,22 @@ def run_ours(args, rank, world, device):
     for k in range(args.warmup):
         step(k)
     torch.cuda.synchronize()
-    # every system once, outside the timed region: the answer must meet the target
-    berr, paths = {}, {}
+    # every system once, outside the timed region: the answer must meet the
+    # target, and its forward error against the oracle's FP64 solve (BOLA's
+    # getrf + laswp + two trsm, on the host cores) is reported
+    berr, paths, fwd = {}, {}, {}
     for s in systems:
         info = solver.solve_mixed(s["A"], s["b"])
         torch.cuda.synchronize()
         key = f"{s['kappa']:.0e}"
         berr[key] = backward_error(s["A"], solver.x, s["b"], n, nrhs)
+        if not args.no_forward_error:
+            _, x_or = cpu_solve_once(*host_system(s, n, nrhs))
+            x = solver.x.cpu().numpy().reshape(nrhs, n).T
+            x_true = s["x_true"].cpu().numpy()
+            fwd[key] = {"vs_oracle": float(np.abs(x - x_or).max() / np.abs(x_or).max()),
+                        "oracle_vs_x_true": float(np.abs(x_or - x_true).max() / np.abs(x_true).max()),
+                        "kappa_u": s["kappa"] * 2.0 ** -53}
         paths[key] = {"path": ["mixed-IR", "mixed-GMRES-IR", "fp64-fallback", "fp64-accurate-factor-IR"][info.path],
                       "iterations": info.iterations, "gmres_iterations": info.gmres_iterations,
                       "reported_backward_error": info.backward_error}
@@ -346,6 +356,7 @@ def run_ours(args, rank, world, device):
         "speedup_vs_plain_fp64": round(value / plain_value, 3),
         "backward_error": berr,
         "backward_error_ok": all(v <= BERR_TARGET for v in berr.values()),
+        "forward_error": fwd,
         "refinement": paths,
         "e2e": {"value": round(job_rate(world, args.steps, e2e_total), 4), "unit": "solves/s",
                 "h2d_bytes_per_step": 8 * (n * n + n * nrhs), "d2h_bytes_per_step": 8 * n * nrhs,
@@ -376,15 +387,16 @@ def run_batched(args, device, peak_fp64):
     """20,000 independent systems (n uniform in [8, 256], half LU on
     diagonally dominant, half Cholesky on SPD matrices, nrhs uniform in
     [1, 8], seed 4) solved in one persistent launch replayed from a CUDA
-    graph; group sizes autotuned per size bucket in this run."""
+    graph; group size and panel width autotuned per size bucket, and the
+    register tile per plan, in this run."""
     from bola_gb300.batch import Batch, autotune, config4_batch, time_solve
     count = args.batch_systems
     ns, nrhs, kinds, fill = config4_batch(count, seed=4, device=device)
     b = Batch(ns, nrhs, kinds, device=device)
     fill(b)
     A0, B0 = b.A.clone(), b.B.clone()
-    table, trials = autotune(b)
-    b.replan(table)
+    tuning, trials = autotune(b)
+    b.replan(tuning)
     b.solve(graph=True)
     torch.cuda.synchronize()
     ok_info = int((b.info != 0).sum()) == 0
@@ -412,7 +424,7 @@ def run_batched(args, device, peak_fp64):
             "ms_min": round(min(times), 3), "steps": steps, "launches_per_batch": 1, "graph": True,
             "gflops": round(flops / (ms / 1e3) / 1e9, 1),
             "fp64_peak_frac": round(flops / (ms / 1e3) / 1e9 / peak_fp64, 4) if peak_fp64 else None,
-            "group_sizes": table,
+            "tuning": tuning.as_dict(),
             "autotune_ms": {str(k): {str(g): round(t, 3) for g, t in v.items()} for k, v in trials.items()},
             "info_all_zero": ok_info, "max_backward_error_sample": worst}
 

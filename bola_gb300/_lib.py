@@ -70,6 +70,12 @@ SIGNATURES["bola_dposv_mixed"] = SIGNATURES["bola_dgesv_mixed"]
 
 
 
+class BatchTuning(ctypes.Structure):
+    """bola_batch_tuning (include/bola_gb300.h)."""
+    _fields_ = [("group_size", ctypes.c_int32 * 8), ("panel_width", ctypes.c_int32 * 8),
+                ("tile_rows", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
 class System(ctypes.Structure):
     """bola_system (include/bola_gb300.h)."""
     _fields_ = [("n", ctypes.c_int32), ("nrhs", ctypes.c_int32), ("kind", ctypes.c_int32), ("lda", ctypes.c_int32),
@@ -85,6 +91,9 @@ SIGNATURES.update({
     "bola_dposv_mixed_ctx": (_int, [_p, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, ctypes.POINTER(MixedOpts),
                                     ctypes.POINTER(MixedInfo), _p]),
     "bola_batch_plan_create": (_int, [_i32, _p, _p, _p, _p]),
+    "bola_batch_plan_create_tuned": (_int, [_i32, _p, _p, ctypes.POINTER(BatchTuning), _p]),
+    "bola_batch_tuning_save": (_int, [ctypes.c_char_p, ctypes.POINTER(BatchTuning)]),
+    "bola_batch_tuning_load": (_int, [ctypes.c_char_p, ctypes.POINTER(BatchTuning), _p]),
     "bola_batch_solve": (_int, [_p, _p, _p, _p]),
     "bola_batch_solve_graph": (_int, [_p, _p, _p, _p]),
     "bola_batch_plan_info": (_int, [_p, _p, _p, _p]),
@@ -97,7 +106,9 @@ class ServerOpts(ctypes.Structure):
     """bola_server_opts (include/bola_gb300.h)."""
     _fields_ = [("slots", ctypes.c_int32), ("small_n", ctypes.c_int32), ("max_batch", ctypes.c_int32),
                 ("mode", ctypes.c_int32), ("factor_kind", ctypes.c_int32), ("group_size", ctypes.c_int32 * 8),
-                ("reserved", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_int64)]
+                ("reserved", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_int64),
+                ("panel_width", ctypes.c_int32 * 8), ("tile_rows", ctypes.c_int32), ("reserved2", ctypes.c_int32)]
+
 
 
 class RequestInfo(ctypes.Structure):

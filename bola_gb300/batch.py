@@ -16,11 +16,11 @@ class Batch:
     """A batch of systems A_i X_i = B_i on one device.
 
     ns, nrhs, kinds: per-system order, right-hand-side count and kind (0 LU,
-    1 Cholesky).  group_size: optional 8-entry table of threads per system for
-    the size buckets (the autotuner's output); None = library defaults.
+    1 Cholesky).  tuning: a Tuning (the autotuner's output, or one loaded from
+    its JSON file), or an 8-entry group-size table; None = library defaults.
     """
 
-    def __init__(self, ns, nrhs, kinds, device="cuda", group_size=None):
+    def __init__(self, ns, nrhs, kinds, device="cuda", tuning=None):
         self.L = _lib.load()
         self.ns = np.asarray(ns, dtype=np.int32)
         self.nrhs = np.asarray(nrhs, dtype=np.int32)
@@ -42,19 +42,18 @@ class Batch:
         raw = np.frombuffer(desc, dtype=np.uint8)
         self.desc = torch.from_numpy(raw.copy()).to(device)
         self.plan = ctypes.c_void_p()
-        self.replan(group_size)
+        self.replan(tuning)
 
-    def replan(self, group_size=None):
-        """(Re)build the plan with an 8-entry group-size table (None = defaults)."""
+    def replan(self, tuning=None):
+        """(Re)build the plan with a Tuning, an 8-entry group-size table, or the defaults (None)."""
         self.close()
-        gs = None
-        if group_size is not None:
-            gs = (ctypes.c_int32 * 8)(*[int(v) for v in group_size])
-        self.group_size = None if group_size is None else [int(v) for v in group_size]
-        st = self.L.bola_batch_plan_create(self.count, self.ns.ctypes.data_as(ctypes.c_void_p),
-                                           self.kinds.ctypes.data_as(ctypes.c_void_p),
-                                           ctypes.cast(gs, ctypes.c_void_p) if gs is not None else None,
-                                           ctypes.byref(self.plan))
+        if tuning is not None and not isinstance(tuning, Tuning):
+            tuning = Tuning(group_size=tuning)
+        self.tuning = tuning
+        st = self.L.bola_batch_plan_create_tuned(self.count, self.ns.ctypes.data_as(ctypes.c_void_p),
+                                                 self.kinds.ctypes.data_as(ctypes.c_void_p),
+                                                 ctypes.byref(tuning.c()) if tuning is not None else None,
+                                                 ctypes.byref(self.plan))
         if st != 0:
             raise RuntimeError(f"bola_batch_plan_create: {st} {self.L.bola_last_error().decode()}")
 
@@ -118,6 +117,40 @@ def config4_batch(count, seed=4, device="cuda", nmin=8, nmax=256, rmax=8):
 BUCKET_N = (16, 32, 48, 64, 96, 128, 192, 256)
 DEFAULT_GROUPS = (32, 32, 64, 64, 128, 128, 256, 256)
 GROUP_CHOICES = (32, 64, 128, 256)
+PANEL_CHOICES = (8, 12, 16)
+TILE_CHOICES = (4, 2)
+
+
+class Tuning:
+    """The batched solver's tuning table (bola_batch_tuning): per size bucket
+    the group size and the panel width, and one register-tile height."""
+
+    def __init__(self, group_size=None, panel_width=None, tile_rows=4):
+        self.group_size = [int(v) for v in (group_size or DEFAULT_GROUPS)]
+        self.panel_width = [int(v) for v in (panel_width or (8,) * 8)]
+        self.tile_rows = int(tile_rows)
+
+    def c(self):
+        return _lib.BatchTuning((ctypes.c_int32 * 8)(*self.group_size), (ctypes.c_int32 * 8)(*self.panel_width),
+                                self.tile_rows, 0)
+
+    def as_dict(self):
+        return {"group_size": self.group_size, "panel_width": self.panel_width, "tile_rows": self.tile_rows}
+
+    def save(self, path):
+        """Writes the table as JSON through the library (bola_batch_tuning_save)."""
+        st = _lib.load().bola_batch_tuning_save(str(path).encode(), ctypes.byref(self.c()))
+        if st != 0:
+            raise RuntimeError(f"bola_batch_tuning_save: {st} {_lib.load().bola_last_error().decode()}")
+
+    @classmethod
+    def load(cls, path):
+        """Reads a table written by save (bola_batch_tuning_load); returns (Tuning, SM count it was measured on)."""
+        t, sms = _lib.BatchTuning(), ctypes.c_int32()
+        st = _lib.load().bola_batch_tuning_load(str(path).encode(), ctypes.byref(t), ctypes.byref(sms))
+        if st != 0:
+            raise ValueError(f"bola_batch_tuning_load: {st} {_lib.load().bola_last_error().decode()}")
+        return cls(list(t.group_size), list(t.panel_width), t.tile_rows or 4), sms.value
 
 
 def bucket_of(n):
@@ -144,12 +177,17 @@ def time_solve(batch, A0, B0, reps, graph=True):
     return best
 
 
-def autotune(batch, reps=3):
-    """Per size bucket, the group size (threads per system) with the shortest
-    solve of that bucket's systems of `batch` (measured on a sub-batch holding
-    copies of them).  Returns (table of 8 group sizes, {bucket: {G: ms}})."""
+def autotune(batch, reps=3, path=None):
+    """Per size bucket, the (group size, panel width) pair with the shortest
+    solve of that bucket's systems of `batch` (a sub-batch holding copies of
+    them), then the register tile with the shortest solve of the whole batch
+    under that table.  Every choice leaves each system's operation order
+    unchanged (results are bit-identical), so only time decides.  Writes the
+    table to `path` as JSON if given.  Returns (Tuning, trials), trials =
+    {bucket: {"G/PB": ms}, "tile": {rows: ms}}."""
     buckets = np.array([bucket_of(int(n)) for n in batch.ns])
-    table, trials = list(DEFAULT_GROUPS), {}
+    best = Tuning()
+    trials = {}
     for b in range(len(BUCKET_N)):
         idx = np.nonzero(buckets == b)[0]
         if len(idx) == 0:
@@ -161,11 +199,26 @@ def autotune(batch, reps=3):
         A0, B0 = sub.A.clone(), sub.B.clone()
         trials[b] = {}
         for g in GROUP_CHOICES:
-            t = list(DEFAULT_GROUPS)
-            t[b] = g
-            sub.replan(t)
-            sub.solve(graph=False)  # warm-up
-            trials[b][g] = time_solve(sub, A0, B0, reps, graph=False)
-        table[b] = min(trials[b], key=trials[b].get)
+            for pw in PANEL_CHOICES:
+                t = Tuning(best.group_size, best.panel_width, best.tile_rows)
+                t.group_size[b], t.panel_width[b] = g, pw
+                sub.replan(t)
+                sub.solve(graph=False)  # warm-up
+                trials[b][f"{g}/{pw}"] = time_solve(sub, A0, B0, reps, graph=False)
+        g, pw = min(trials[b], key=trials[b].get).split("/")
+        best.group_size[b], best.panel_width[b] = int(g), int(pw)
         sub.close()
-    return table, trials
+    A0, B0 = batch.A.clone(), batch.B.clone()
+    trials["tile"] = {}
+    for tr in TILE_CHOICES:
+        t = Tuning(best.group_size, best.panel_width, tr)
+        batch.replan(t)
+        batch.solve(graph=False)
+        trials["tile"][tr] = time_solve(batch, A0, B0, reps, graph=False)
+    best.tile_rows = min(trials["tile"], key=trials["tile"].get)
+    batch.A.copy_(A0)
+    batch.B.copy_(B0)
+    batch.replan(best)
+    if path is not None:
+        best.save(path)
+    return best, trials

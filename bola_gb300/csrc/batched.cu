@@ -16,8 +16,11 @@
 // FP64 throughout; all waits are barriers (no spin loops).
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "common.cuh"
@@ -27,7 +30,7 @@ namespace {
 
 constexpr int BT = 256;         // threads per CTA
 constexpr int MAXG = BT / 32;   // groups per CTA at most
-constexpr int ITEM = 2 + MAXG;  // ints per work item: G, count, system ids
+constexpr int ITEM = 3 + MAXG;  // ints per work item: G, count, panel width, system ids
 constexpr int NBUCKET = 8;
 // upper n of each bucket (inclusive)
 constexpr int BUCKET_N[NBUCKET] = {16, 32, 48, 64, 96, 128, 192, 1 << 30};
@@ -97,12 +100,16 @@ __device__ int group_argmax(const double *col, int k, int n, int t, int G, int g
 // the unblocked order gives it (row interchanges move whole rows, deferred
 // updates included), so results are those of the unblocked algorithm, bit for
 // bit.
-constexpr int PB = 8;
-constexpr int TR = 4, TC = 4;
+// The panel width PB (8, 12 or 16 columns) is chosen per size bucket and
+// travels with each work item; the register tile TR x TC (TC = 4, TR = 4 or
+// 2) is chosen per plan, since it sets the kernel's register count.  Neither
+// changes any element's sequence of operations.
+constexpr int TC = 4;
 
 // A[c0:n, c0:n] -= A[c0:n, k0:k0+kb] * A[k0:k0+kb, c0:n] (lower = false), or
 // its lower triangle -= A[c0:n, k0:k0+kb] * A[c0:n, k0:k0+kb]^T (lower = true),
 // with c0 = k0 + kb.
+template <int TR>
 __device__ void group_trailing(double *A, int lda, int n, int k0, int kb, bool lower, int t, int G) {
   const int c0 = k0 + kb, m2 = n - c0;
   if (m2 <= 0) return;
@@ -170,6 +177,7 @@ __device__ void group_trailing(double *A, int lda, int n, int k0, int kb, bool l
 
 // U12 = L11^-1 A12 for the panel rows k0..k0+kb-1 (unit lower L11), a column
 // per thread: row r takes fma(-l_rq, u_q, u_r) for q < r in increasing q.
+template <int PB>
 __device__ void group_u12(double *A, int lda, int n, int k0, int kb, int t, int G) {
   for (int j = k0 + kb + t; j < n; j += G) {
     double u[PB];
@@ -188,6 +196,7 @@ __device__ void group_u12(double *A, int lda, int n, int k0, int kb, int t, int 
 
 // LU with partial pivoting of one system by a group; the row interchanges are
 // applied to B as they happen, then L y = P b and U x = y.
+template <int PB, int TR>
 __device__ int group_lu_solve(const SystemDesc &S, int t, int G, int g, long long *redv, int *redi, double *sinv) {
   const int n = S.n, lda = S.lda, ldb = S.ldb, nr = S.nrhs;
   double *A = S.a, *B = S.b;
@@ -237,9 +246,9 @@ __device__ int group_lu_solve(const SystemDesc &S, int t, int G, int g, long lon
     }
     group_sync(G, g);
     if (k + 1 == kend && kend < n) {  // the panel is done: U12, then A22
-      group_u12(A, lda, n, k0, kend - k0, t, G);
+      group_u12<PB>(A, lda, n, k0, kend - k0, t, G);
       group_sync(G, g);
-      group_trailing(A, lda, n, k0, kend - k0, false, t, G);
+      group_trailing<TR>(A, lda, n, k0, kend - k0, false, t, G);
       group_sync(G, g);
     }
   }
@@ -285,6 +294,7 @@ __device__ int group_lu_solve(const SystemDesc &S, int t, int G, int g, long lon
 }
 
 // Cholesky A = L L^T (lower) of one system by a group, then L y = b, L^T x = y.
+template <int PB, int TR>
 __device__ int group_chol_solve(const SystemDesc &S, int t, int G, int g, double *sinv) {
   const int n = S.n, lda = S.lda, ldb = S.ldb, nr = S.nrhs;
   double *A = S.a, *B = S.b;
@@ -329,7 +339,7 @@ __device__ int group_chol_solve(const SystemDesc &S, int t, int G, int g, double
     }
     group_sync(G, g);
     if (k + 1 == kend && kend < n) {  // the panel is done: the trailing lower triangle
-      group_trailing(A, lda, n, k0, kend - k0, true, t, G);
+      group_trailing<TR>(A, lda, n, k0, kend - k0, true, t, G);
       group_sync(G, g);
     }
   }
@@ -373,6 +383,12 @@ __device__ int group_chol_solve(const SystemDesc &S, int t, int G, int g, double
   return 0;
 }
 
+template <int PB, int TR>
+__device__ int group_solve(const SystemDesc &S, int t, int G, int g, long long *redv, int *redi, double *sinv) {
+  return S.kind == 1 ? group_chol_solve<PB, TR>(S, t, G, g, sinv) : group_lu_solve<PB, TR>(S, t, G, g, redv, redi, sinv);
+}
+
+template <int TR>
 __global__ void __launch_bounds__(BT)
 batched_solve_kernel(const SystemDesc *__restrict__ sys, const int32_t *__restrict__ items, int32_t nitems,
                      int32_t *counter, int32_t *info) {
@@ -392,10 +408,12 @@ batched_solve_kernel(const SystemDesc *__restrict__ sys, const int32_t *__restri
     if (G == 0) break;
     const int g = tid / G, t = tid % G;
     if (g < cur[1]) {
-      const int id = cur[2 + g];
+      const int id = cur[3 + g];
       const SystemDesc S = sys[id];
-      const int r =
-          S.kind == 1 ? group_chol_solve(S, t, G, g, &sinv[g]) : group_lu_solve(S, t, G, g, redv[g], redi[g], &sinv[g]);
+      const int pb = cur[2];
+      const int r = pb == 16   ? group_solve<16, TR>(S, t, G, g, redv[g], redi[g], &sinv[g])
+                    : pb == 12 ? group_solve<12, TR>(S, t, G, g, redv[g], redi[g], &sinv[g])
+                               : group_solve<8, TR>(S, t, G, g, redv[g], redi[g], &sinv[g]);
       if (t == 0) info[id] = r;
     }
     __syncthreads();
@@ -409,6 +427,7 @@ struct Plan {
   int grid = 0;
   double flops = 0.0;
   int group[NBUCKET];
+  int tile = 4;  // register tile rows of the kernel (4 or 2)
   cudaGraphExec_t exec = nullptr;
   const void *g_sys = nullptr;
   const void *g_info = nullptr;
@@ -425,12 +444,15 @@ int bucket_of(int n) {
 // Work items of a batch: per size bucket, systems by decreasing n, BT/G
 // systems per item; items by decreasing cost.  flat holds ITEM int32 per item.
 int batch_items(int32_t count, const int32_t *n, const int32_t *kind, const int32_t *group_size,
-                std::vector<int32_t> &flat, int32_t *nitems, int *group, double *flops) {
+                std::vector<int32_t> &flat, int32_t *nitems, int *group, double *flops, const int32_t *panel_width) {
   static const int kDefault[NBUCKET] = {32, 32, 64, 64, 128, 128, 256, 256};
+  int pbw[NBUCKET];
   for (int b = 0; b < NBUCKET; ++b) {
     int gsz = group_size ? group_size[b] : kDefault[b];
     if (gsz != 32 && gsz != 64 && gsz != 128 && gsz != 256) gsz = kDefault[b];
     group[b] = gsz;
+    const int pw = panel_width ? panel_width[b] : 8;
+    pbw[b] = (pw == 12 || pw == 16) ? pw : 8;
   }
   double fl = 0.0;
   std::vector<std::vector<int>> byb(NBUCKET);
@@ -454,10 +476,11 @@ int batch_items(int32_t count, const int32_t *n, const int32_t *kind, const int3
       It it;
       it.v.assign(ITEM, 0);
       it.v[0] = G;
+      it.v[2] = pbw[b];
       int c = 0;
       double cost = 0.0;
       for (size_t q = s; q < ids.size() && c < per; ++q, ++c) {
-        it.v[2 + c] = ids[q];
+        it.v[3 + c] = ids[q];
         cost = std::max(cost, (double)n[ids[q]] * n[ids[q]] * n[ids[q]] / G);
       }
       it.v[1] = c;
@@ -473,20 +496,31 @@ int batch_items(int32_t count, const int32_t *n, const int32_t *kind, const int3
   return 0;
 }
 
-int batch_grid(int32_t nitems) {
+int batch_grid(int32_t nitems, int tile) {
   int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batched_solve_kernel, BT, 0);
+  if (tile == 2)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batched_solve_kernel<2>, BT, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batched_solve_kernel<4>, BT, 0);
   return std::max(1, std::min((int)nitems, num_sms() * std::max(occ, 1)));
+}
+
+void launch_kernel(cudaStream_t s, int tile, int grid, const bola_system *systems, const int32_t *items,
+                   int32_t nitems, int32_t *counter, int32_t *info) {
+  const SystemDesc *sd = reinterpret_cast<const SystemDesc *>(systems);
+  if (tile == 2)
+    batched_solve_kernel<2><<<grid, BT, 0, s>>>(sd, items, nitems, counter, info);
+  else
+    batched_solve_kernel<4><<<grid, BT, 0, s>>>(sd, items, nitems, counter, info);
 }
 
 // One persistent launch over nitems work items (device array); *counter is
 // the work queue's head and is reset here.
 int batch_launch(cudaStream_t s, const bola_system *systems, const int32_t *items, int32_t nitems, int32_t *counter,
-                 int32_t *info) {
+                 int32_t *info, int tile) {
   if (nitems == 0) return 0;
   BOLA_TRY_CUDA(cudaMemsetAsync(counter, 0, sizeof(int32_t), s));
-  batched_solve_kernel<<<batch_grid(nitems), BT, 0, s>>>(reinterpret_cast<const SystemDesc *>(systems), items,
-                                                         nitems, counter, info);
+  launch_kernel(s, tile, batch_grid(nitems, tile), systems, items, nitems, counter, info);
   BOLA_CHECK_LAUNCH();
   return 0;
 }
@@ -500,14 +534,17 @@ using namespace bola;
 
 extern "C" {
 
-int bola_batch_plan_create(int32_t count, const int32_t *n, const int32_t *kind, const int32_t *group_size,
-                           bola_batch_plan *plan_out) {
+int bola_batch_plan_create_tuned(int32_t count, const int32_t *n, const int32_t *kind,
+                                 const bola_batch_tuning *tuning, bola_batch_plan *plan_out) {
   if (count < 0) return -1;
   if (!plan_out) return -5;
+  if (tuning && tuning->tile_rows != 0 && tuning->tile_rows != 2 && tuning->tile_rows != 4) return -4;
   Plan *P = new Plan();
   P->count = count;
+  P->tile = (tuning && tuning->tile_rows == 2) ? 2 : 4;
   std::vector<int32_t> flat;
-  const int st = batch_items(count, n, kind, group_size, flat, &P->nitems, P->group, &P->flops);
+  const int st = batch_items(count, n, kind, tuning ? tuning->group_size : nullptr, flat, &P->nitems, P->group,
+                             &P->flops, tuning ? tuning->panel_width : nullptr);
   if (st != 0) {
     delete P;
     return st;
@@ -518,9 +555,17 @@ int bola_batch_plan_create(int32_t count, const int32_t *n, const int32_t *kind,
     return fail(BOLA_ERR_CUDA, "bola_batch_plan_create: device allocation failed");
   }
   if (!flat.empty()) cudaMemcpy(P->items, flat.data(), sizeof(int32_t) * flat.size(), cudaMemcpyHostToDevice);
-  P->grid = batch_grid(P->nitems);
+  P->grid = batch_grid(P->nitems, P->tile);
   *plan_out = reinterpret_cast<bola_batch_plan>(P);
   return 0;
+}
+
+int bola_batch_plan_create(int32_t count, const int32_t *n, const int32_t *kind, const int32_t *group_size,
+                           bola_batch_plan *plan_out) {
+  bola_batch_tuning t;
+  std::memset(&t, 0, sizeof t);
+  if (group_size) std::memcpy(t.group_size, group_size, sizeof t.group_size);
+  return bola_batch_plan_create_tuned(count, n, kind, &t, plan_out);
 }
 
 int bola_batch_solve(bola_batch_plan plan, const bola_system *systems, int32_t *info, bola_stream_t stream) {
@@ -530,8 +575,7 @@ int bola_batch_solve(bola_batch_plan plan, const bola_system *systems, int32_t *
   if (P->nitems == 0) return 0;
   ProfScope prof(s, "batched_solve", P->flops, 0.0, 2);
   BOLA_TRY_CUDA(cudaMemsetAsync(P->counter, 0, sizeof(int32_t), s));
-  batched_solve_kernel<<<P->grid, BT, 0, s>>>(reinterpret_cast<const SystemDesc *>(systems), P->items, P->nitems,
-                                              P->counter, info);
+  launch_kernel(s, P->tile, P->grid, systems, P->items, P->nitems, P->counter, info);
   BOLA_CHECK_LAUNCH();
   return 0;
 }
@@ -551,8 +595,7 @@ int bola_batch_solve_graph(bola_batch_plan plan, const bola_system *systems, int
     cudaGraph_t g;
     BOLA_TRY_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
     cudaMemsetAsync(P->counter, 0, sizeof(int32_t), cap);
-    batched_solve_kernel<<<P->grid, BT, 0, cap>>>(reinterpret_cast<const SystemDesc *>(systems), P->items,
-                                                  P->nitems, P->counter, info);
+    launch_kernel(cap, P->tile, P->grid, systems, P->items, P->nitems, P->counter, info);
     BOLA_TRY_CUDA(cudaStreamEndCapture(cap, &g));
     BOLA_TRY_CUDA(cudaGraphInstantiate(&P->exec, g, 0));
     cudaGraphDestroy(g);
@@ -585,3 +628,88 @@ int bola_batch_plan_destroy(bola_batch_plan plan) {
 }
 
 }  // extern "C"
+
+// ---- the tuning table on disk --------------------------------------------------
+namespace {
+
+// The integers of the JSON array that follows "key": in text (at most cap).
+int json_ints(const std::string &text, const char *key, int32_t *out, int cap) {
+  const std::string k = std::string("\"") + key + "\"";
+  size_t p = text.find(k);
+  if (p == std::string::npos) return -1;
+  p = text.find_first_not_of(" \t\r\n:", p + k.size());
+  if (p == std::string::npos) return -1;
+  if (text[p] != '[') {  // a scalar
+    char *end = nullptr;
+    const long v = std::strtol(text.c_str() + p, &end, 10);
+    if (end == text.c_str() + p) return -1;
+    out[0] = (int32_t)v;
+    return 1;
+  }
+  int cnt = 0;
+  ++p;
+  while (cnt < cap) {
+    p = text.find_first_not_of(" \t\r\n,", p);
+    if (p == std::string::npos) return -1;
+    if (text[p] == ']') break;
+    char *end = nullptr;
+    const long v = std::strtol(text.c_str() + p, &end, 10);
+    if (end == text.c_str() + p) return -1;
+    out[cnt++] = (int32_t)v;
+    p = (size_t)(end - text.c_str());
+  }
+  return cnt;
+}
+
+}  // namespace
+
+extern "C" int bola_batch_tuning_save(const char *path, const bola_batch_tuning *t) {
+  if (!path || !t) return -1;
+  FILE *f = std::fopen(path, "w");
+  if (!f) return fail(-2, "bola_batch_tuning_save: cannot write %s", path);
+  int dev = 0;
+  cudaDeviceProp prop;
+  std::memset(&prop, 0, sizeof prop);
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaGetDeviceProperties(&prop, dev);
+  std::fprintf(f, "{\n  \"format\": \"bola_gb300 batched tuning 1\",\n  \"device\": \"%s\",\n  \"sms\": %d,\n",
+               prop.name, prop.multiProcessorCount);
+  const int32_t *arrs[2] = {t->group_size, t->panel_width};
+  const char *names[2] = {"group_size", "panel_width"};
+  for (int a = 0; a < 2; ++a) {
+    std::fprintf(f, "  \"%s\": [", names[a]);
+    for (int b = 0; b < NBUCKET; ++b) std::fprintf(f, "%d%s", arrs[a][b], b + 1 < NBUCKET ? ", " : "");
+    std::fprintf(f, "],\n");
+  }
+  std::fprintf(f, "  \"tile_rows\": %d\n}\n", t->tile_rows);
+  std::fclose(f);
+  return 0;
+}
+
+extern "C" int bola_batch_tuning_load(const char *path, bola_batch_tuning *t, int32_t *sms_recorded) {
+  if (!path || !t) return -1;
+  FILE *f = std::fopen(path, "r");
+  if (!f) return fail(-2, "bola_batch_tuning_load: cannot read %s", path);
+  std::string text;
+  char buf[4096];
+  size_t got;
+  while ((got = std::fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, got);
+  std::fclose(f);
+  bola_batch_tuning r;
+  std::memset(&r, 0, sizeof r);
+  int32_t sms = 0;
+  if (json_ints(text, "group_size", r.group_size, NBUCKET) != NBUCKET ||
+      json_ints(text, "panel_width", r.panel_width, NBUCKET) != NBUCKET ||
+      json_ints(text, "tile_rows", &r.tile_rows, 1) != 1)
+    return fail(-2, "bola_batch_tuning_load: %s is not a tuning table", path);
+  json_ints(text, "sms", &sms, 1);
+  for (int b = 0; b < NBUCKET; ++b) {
+    const int g = r.group_size[b], w = r.panel_width[b];
+    if ((g != 0 && g != 32 && g != 64 && g != 128 && g != 256) || (w != 0 && w != 8 && w != 12 && w != 16))
+      return fail(-3, "bola_batch_tuning_load: bucket %d has group %d / panel width %d", b, g, w);
+  }
+  if (r.tile_rows != 0 && r.tile_rows != 2 && r.tile_rows != 4)
+    return fail(-3, "bola_batch_tuning_load: tile_rows %d", r.tile_rows);
+  *t = r;
+  if (sms_recorded) *sms_recorded = sms;
+  return 0;
+}

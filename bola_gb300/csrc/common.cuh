@@ -122,9 +122,10 @@ __device__ __forceinline__ double fmaT(double a, double b, double c) { return fm
 // (flat int32 records, *nitems of them; group = the 8 per-bucket group sizes
 // used) and one persistent launch over items already on the device.
 int batch_items(int32_t count, const int32_t *n, const int32_t *kind, const int32_t *group_size,
-                std::vector<int32_t> &flat, int32_t *nitems, int *group, double *flops);
+                std::vector<int32_t> &flat, int32_t *nitems, int *group, double *flops,
+                const int32_t *panel_width = nullptr);
 int batch_launch(cudaStream_t s, const bola_system *systems, const int32_t *items, int32_t nitems, int32_t *counter,
-                 int32_t *info);
+                 int32_t *info, int tile = 4);
 
 // ---- device side -------------------------------------------------------------
 __device__ __forceinline__ double fused(double a, double b, double c) { return __fma_rn(a, b, c); }

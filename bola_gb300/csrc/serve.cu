@@ -378,7 +378,7 @@ struct Server {
     int32_t nitems = 0;
     int group[8];
     BOLA_TRY(batch_items(cnt, ns.data(), kinds.data(), o.group_size[0] ? o.group_size : nullptr, flat, &nitems, group,
-                         nullptr));
+                         nullptr, o.panel_width[0] ? o.panel_width : nullptr));
     BOLA_TRY(data.ensure(sizeof(double) * (2 * na + 2 * nb), s));
     BOLA_TRY(desc.ensure(sizeof(bola_system) * cnt, s));
     BOLA_TRY(items.ensure(sizeof(int32_t) * flat.size(), s));
@@ -409,7 +409,7 @@ struct Server {
     BOLA_TRY_CUDA(cudaMemcpyAsync(A, A0, sizeof(double) * na, cudaMemcpyDeviceToDevice, s));
     BOLA_TRY_CUDA(cudaMemcpyAsync(X, B0, sizeof(double) * nb, cudaMemcpyDeviceToDevice, s));
     BOLA_TRY(batch_launch(s, (const bola_system *)desc.p, (const int32_t *)items.p, nitems, (int32_t *)counter.p,
-                          (int32_t *)info.p));
+                          (int32_t *)info.p, o.tile_rows == 2 ? 2 : 4));
     BOLA_TRY(launch_berr(s, bs, dsys, djobs, dacc, (double *)berr.p));  // synchronises s
     // results back through the same staging buffer
     std::vector<double> hb(cnt);

@@ -39,11 +39,16 @@ class Server:
     """
 
     def __init__(self, slots=4, small_n=256, max_batch=256, mode="mixed", factor_kind=2,
-                 hbm_budget_bytes=120 * 10**9, group_size=None):
+                 hbm_budget_bytes=120 * 10**9, group_size=None, tuning=None):
         self.L = _lib.load()
         o = _lib.ServerOpts()
         o.slots, o.small_n, o.max_batch = int(slots), int(small_n), int(max_batch)
         o.mode, o.factor_kind = MODES[mode], int(factor_kind)
+        if tuning is not None:  # a batch.Tuning: group sizes, panel widths, register tile
+            group_size = tuning.group_size
+            for i, v in enumerate(tuning.panel_width):
+                o.panel_width[i] = int(v)
+            o.tile_rows = int(tuning.tile_rows)
         if group_size is not None:
             for i, v in enumerate(group_size):
                 o.group_size[i] = int(v)

@@ -335,6 +335,32 @@ typedef struct bola_batch_plan_st *bola_batch_plan;
  * NULL = built-in defaults.  Returns -2 for an n outside 1..256. */
 int bola_batch_plan_create(int32_t count, const int32_t *n, const int32_t *kind, const int32_t *group_size,
                            bola_batch_plan *plan);
+
+/* The tuning table of the batched solver, per size bucket (n <= 16, 32, 48,
+ * 64, 96, 128, 192, 256): group_size = threads per system (32/64/128/256),
+ * panel_width = columns per factorisation panel (8/12/16); and tile_rows =
+ * rows of the per-thread register tile of the trailing updates (4 or 2,
+ * with 4 columns), one value per plan because it sets the kernel's register
+ * count.  Zero entries take the built-in defaults (group sizes 32..256 by
+ * bucket, panel width 8, tile 4).  None of the three changes any system's
+ * operation order: a tuned plan gives bit-identical results. */
+typedef struct {
+  int32_t group_size[8];
+  int32_t panel_width[8];
+  int32_t tile_rows;
+  int32_t reserved;
+} bola_batch_tuning;
+/* bola_batch_plan_create with a full tuning table (NULL = defaults); -4 for a
+ * tile_rows other than 0, 2 or 4. */
+int bola_batch_plan_create_tuned(int32_t count, const int32_t *n, const int32_t *kind,
+                                 const bola_batch_tuning *tuning, bola_batch_plan *plan);
+/* Writes / reads a tuning table as JSON ({"group_size": [...], "panel_width":
+ * [...], "tile_rows": r, "device": name, "sms": count}).  The loader checks
+ * every value and returns -2 for a file it cannot read or parse, -3 for a
+ * table whose values are out of range; *sms_recorded (may be NULL) gets the
+ * SM count of the device the table was measured on. */
+int bola_batch_tuning_save(const char *path, const bola_batch_tuning *tuning);
+int bola_batch_tuning_load(const char *path, bola_batch_tuning *tuning, int32_t *sms_recorded);
 /* systems: device array of `count` descriptors; info: device int32[count]. */
 int bola_batch_solve(bola_batch_plan plan, const bola_system *systems, int32_t *info, bola_stream_t stream);
 /* Same solve through a CUDA graph captured on first use for these pointers
@@ -371,6 +397,9 @@ typedef struct {
   int32_t group_size[8];/* batched group sizes per bucket; all 0 = defaults */
   int32_t reserved;
   int64_t hbm_budget_bytes; /* admission budget for requests' device buffers */
+  int32_t panel_width[8];   /* batched panel widths per bucket (bola_batch_tuning); all 0 = default 8 */
+  int32_t tile_rows;        /* batched register tile rows (2 or 4); 0 = 4 */
+  int32_t reserved2;
 } bola_server_opts;
 
 typedef struct {

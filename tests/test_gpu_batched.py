@@ -87,3 +87,49 @@ def test_failures_stay_in_their_system():
     assert (info[others] == 0).all()
     for i in others:
         assert torch.equal(b.b_view(i), X_ok[int(b.b_off[i]):int(b.b_off[i + 1])].view(int(b.nrhs[i]), -1).t())
+
+
+def test_every_tuning_choice_is_bit_identical():
+    """Group size, panel width and register tile change the schedule, never
+    an element's operation order: every choice gives the same bits."""
+    from bola_gb300.batch import Tuning
+    b = _batch(160, seed=21, nmin=1, nmax=256)
+    A0, B0 = _snapshot(b)
+    b.solve()
+    torch.cuda.synchronize()
+    ref_A, ref_B = b.A.clone(), b.B.clone()
+    for g, pw, tr in [(32, 12, 4), (64, 16, 2), (128, 8, 2), (256, 12, 4), (32, 16, 2)]:
+        b.A.copy_(A0)
+        b.B.copy_(B0)
+        b.replan(Tuning([g] * 8, [pw] * 8, tr))
+        b.solve()
+        torch.cuda.synchronize()
+        assert torch.equal(b.A, ref_A) and torch.equal(b.B, ref_B), (g, pw, tr)
+
+
+def test_autotuned_plan_is_persisted_bit_identical_and_no_slower(tmp_path):
+    from bola_gb300.batch import Batch, Tuning, autotune, time_solve
+    b = _batch(2000, seed=4)
+    A0, B0 = _snapshot(b)
+    b.solve()
+    torch.cuda.synchronize()
+    ref_B = b.B.clone()
+    b.A.copy_(A0)
+    b.B.copy_(B0)
+    path = tmp_path / "batched_tuning.json"
+    tuned, trials = autotune(b, reps=2, path=path)
+    loaded, _ = Tuning.load(path)  # what a later process loads at plan creation
+    assert loaded.as_dict() == tuned.as_dict()
+    fresh = Batch(b.ns, b.nrhs, b.kinds, tuning=loaded)
+    fresh.A.copy_(A0)
+    fresh.B.copy_(B0)
+    fresh.solve()
+    torch.cuda.synchronize()
+    assert torch.equal(fresh.B, ref_B)
+    b.replan(None)  # the built-in defaults
+    t_default = time_solve(b, A0, B0, 5, graph=False)  # (minimum over the repetitions)
+    t_tuned = time_solve(fresh, A0, B0, 5, graph=False)
+    # the tuned table is the measured best of a set that contains the defaults
+    assert t_tuned <= 1.10 * t_default, (t_tuned, t_default, tuned.as_dict())
+    fresh.close()
+    b.close()
