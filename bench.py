@@ -57,9 +57,9 @@ def parse():
     ap.add_argument("--batch-systems", type=int, default=20000)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-plain-configs", action="store_true")
-    ap.add_argument("--serve-rates", type=float, nargs="+", default=[25.0, 50.0, 100.0, 200.0])
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[25.0, 50.0, 100.0, 200.0, 400.0, 800.0, 1600.0])
     ap.add_argument("--serve-requests", type=int, default=300)
-    ap.add_argument("--serve-pool", type=int, default=48)
+    ap.add_argument("--serve-pool", type=int, default=128)
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-forward-error", action="store_true")
     return ap.parse_args()
@@ -553,10 +553,11 @@ def run_factor_kinds(systems, n, nrhs, device):
 def run_serve(args, device):
     """The serving loop: Poisson arrivals (seed 5) at swept rates of requests
     with n log-uniform in [16, 4096], nrhs U[1, 32], 70 % LU / 30 % SPD,
-    kappa in {1e2, 1e6, 1e10}; mixed server (tensor-core LU + FP64
-    refinement, small requests batched) against the plain FP64 per-request
-    server; inputs from pinned host memory, results copied back."""
-    from bola_gb300.serve import Server, poisson_trace, request_pool, run_trace, summarize
+    kappa in {1e2, 1e6, 1e10}; mixed server (tensor-core LU, or Cholesky for
+    the SPD requests, + FP64 refinement, small requests batched) against the
+    plain FP64 per-request server; inputs from pinned host memory, results
+    copied back.  The sweep runs until each server saturates (its knee)."""
+    from bola_gb300.serve import Server, knee, poisson_trace, request_pool, run_trace, summarize
     pool = request_pool(args.serve_pool, seed=5, device=device)
     out = {"workload": f"{args.serve_requests} requests per rate from a pool of {args.serve_pool} seeded systems "
                        f"(mean n {np.mean([p['n'] for p in pool]):.0f}), 4 slots, admission budget 120 GB",
@@ -571,6 +572,7 @@ def run_serve(args, device):
                 tr = poisson_trace(rate, args.serve_requests, len(pool), seed=5)
                 recs, _ = run_trace(srv, pool, tr)
                 out[mode][str(rate)] = summarize(recs)
+        out[mode + "_knee"] = knee(out[mode])
     return out
 
 

@@ -64,6 +64,16 @@ __device__ __forceinline__ void st_async4(uint32_t addr, uint32_t a, uint32_t b,
                : "memory");
 }
 
+// Bulk copy of `bytes` (a multiple of 16) from this CTA's shared memory into
+// another CTA's (cluster addresses dst and bar), completing on the
+// receiver's mbarrier; the issuing thread commits it as a bulk group.
+__device__ __forceinline__ void bulk_push(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "r"(sm100::smem_u32(src)), "r"(bytes), "r"(bar)
+      : "memory");
+}
+
 // Pivot key, compared lexicographically: the bits of |v| (high word, low
 // word; the low word is 0 for FP32) and ~row, so the largest magnitude wins
 // and ties go to the lowest row; a NaN never wins.
@@ -625,6 +635,7 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
   __shared__ float invp[TG];
   __shared__ int32_t posin[SNB], at_[SNB], ipg[SNB];  // interchange bookkeeping (CTA 0)
   __shared__ int sfail;
+  __shared__ TSlot stage[TG];              // this CTA's nominees, as they are pushed
   extern __shared__ __align__(16) unsigned char tp_raw[];
   const int RP = panel_pitch<float>(R);
   float *sp = reinterpret_cast<float *>(tp_raw);
@@ -674,7 +685,7 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
     const int pb = c0 >= TG ? c0 - TG : 0;  // first pushed column: the previous group's multipliers on
     const int nv = SNB - pb;                // values pushed per nominee (a multiple of 8)
     const int nq = 1 + nv / 4;
-    if (tid == 0) sm100::mbar_arrive_expect_tx(&xbar[par], (uint32_t)(C * gw * (16 + 4 * nv)));
+    if (tid == 0) sm100::mbar_arrive_expect_tx(&xbar[par], (uint32_t)(C * gw * sizeof(TSlot)));
     // -- 1. each warp's nominees from its own rows (the group's columns are current)
     {
       float v[TRPL][TG];
@@ -726,25 +737,35 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
         }
         if (lane == 0) cand2[t] = il;
       }
+      // the previous group's bulk pushes have read the staging slots
+      if (lane == 0) sm100::bulk_wait_read0();
     }
     __syncthreads();
-    // -- 3. push the nominees (columns pb..63) into every CTA: slot cr * gw + s of buffer par
-    for (int e = tid; e < C * gw * nq; e += TPT) {
-      const int q = e % nq, s = (e / nq) % gw, d = e / (nq * gw);
-      const int il = cand2[s];
-      const uint32_t rbar = cluster_addr(&xbar[par], d);
-      const uint32_t rs = cluster_addr(&slots[(size_t)par * C * TG + cr * gw + s], d);
+    // -- 3. push the nominees (columns pb..63): staged as gw slots, then one
+    // bulk copy into every CTA (slots cr * gw .. of its buffer par)
+    for (int e = tid; e < gw * nq; e += TPT) {
+      const int q = e % nq, s2 = e / nq;
+      const int il = cand2[s2];
       if (q == 0) {
-        st_async4(rs, il >= 0 ? (uint32_t)(r0 + il) : 0xFFFFFFFFu, 0u, 0u, 0u, rbar);
+        stage[s2].row = il >= 0 ? (uint32_t)(r0 + il) : 0xFFFFFFFFu;
       } else {
         const int k = (q - 1) * 4;
-        uint32_t w4[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) w4[u] = il >= 0 ? __float_as_uint(sp[(pb + k + u) * RP + il]) : 0u;
-        st_async4(rs + 16 + 4 * k, w4[0], w4[1], w4[2], w4[3], rbar);
+        float4 w4;
+        w4.x = il >= 0 ? sp[(pb + k) * RP + il] : 0.f;
+        w4.y = il >= 0 ? sp[(pb + k + 1) * RP + il] : 0.f;
+        w4.z = il >= 0 ? sp[(pb + k + 2) * RP + il] : 0.f;
+        w4.w = il >= 0 ? sp[(pb + k + 3) * RP + il] : 0.f;
+        *reinterpret_cast<float4 *>(&stage[s2].v[k]) = w4;
       }
     }
-    __syncthreads();  // the pushes have read the nominees' rows before they change
+    sm100::fence_proxy_async_smem();  // the staged slots, visible to the bulk copies
+    __syncthreads();
+    if (tid == 0) {
+      for (int d = 0; d < C; ++d)
+        bulk_push(cluster_addr(&slots[(size_t)par * C * TG + cr * gw], d), stage, (uint32_t)(gw * sizeof(TSlot)),
+                  cluster_addr(&xbar[par], d));
+      sm100::bulk_commit();
+    }
     // -- 4. the previous group's update on the columns right of this group
     if (g > 0) {
       const float(*U)[TG] = UgT[ub ^ 1];
@@ -956,6 +977,7 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
       }
     }
   }
+  if (tid == 0) sm100::bulk_wait_read0();  // this CTA's last pushes have read its staging slots
   cluster.sync();  // no CTA leaves while another may still push into it
 }
 

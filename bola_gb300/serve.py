@@ -209,10 +209,25 @@ def summarize(recs):
     t_first = min(r["t_submit"] for r in recs)
     t_last = max(r["t_done"] for r in recs)
     berr = np.array([r["backward_error"] for r in recs])
-    paths = {}
+    paths, facts = {}, {}
     for r in recs:
         paths[r["path"]] = paths.get(r["path"], 0) + 1
+        f = r.get("factorization", "lu")
+        facts[f] = facts.get(f, 0) + 1
     return {"requests": len(recs), "solves_per_s": len(recs) / (t_last - t_first),
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "max_backward_error": float(berr.max()), "within_1e-14": int((berr <= 1e-14).sum()),
-            "errors": int(sum(1 for r in recs if r["status"] != 0)), "paths": paths}
+            "errors": int(sum(1 for r in recs if r["status"] != 0)), "paths": paths, "factorizations": facts}
+
+
+def knee(by_rate):
+    """The first offered rate whose served rate falls below 90 % of it (the
+    server saturates there), with the p99 latency on either side; None if it
+    kept up at every rate."""
+    rates = sorted(by_rate, key=float)
+    for i, r in enumerate(rates):
+        if by_rate[r]["solves_per_s"] < 0.9 * float(r):
+            prev = rates[i - 1] if i > 0 else None
+            return {"saturates_at_rate": float(r), "served_solves_per_s": by_rate[r]["solves_per_s"],
+                    "p99_ms": by_rate[r]["p99_ms"], "p99_ms_below": by_rate[prev]["p99_ms"] if prev else None}
+    return None
