@@ -524,29 +524,30 @@ struct alignas(16) TSlot {
 // (candidate l + 32 r sits in row r of lane l).  The pivot key is |v| with
 // its 8 lowest bits replaced by 255 - candidate, so that one warp reduction
 // finds the pivot (the lowest mantissa bits do not matter for the pivot's
-// quality; ties go to the lowest candidate; a NaN never wins).  Writes the
-// selected candidates in order to sel[] (on every lane) and returns their
-// count.  RECORD: the multipliers each selected row had before its selection
-// go to Lrec[t][s] (s < t), and the pivot rows' eliminated values in group
-// column k >= t to Urec[k * uk + t].
+// quality; ties go to the lowest candidate; a NaN never wins).  The column
+// loop is not unrolled (code size: the panel's phases would otherwise keep
+// missing the instruction cache); instead the current column always sits in
+// register slot 0 and the remaining ones shift down after each step.  Writes
+// the selected candidates in order to sel[] (shared memory, lane 0) and
+// returns their count.  RECORD: each candidate's multipliers go to
+// Lsm[candidate * TG + step] (shared), the selected rows' ones to Lrec[t][s]
+// (s < t), and the pivot rows' eliminated values in group column t + k to
+// Urec[(t + k) * uk + t].
 template <int RPL, bool RECORD>
-__device__ __forceinline__ int warp_gepp(float (&v)[RPL][TG], bool (&live)[RPL], int gw, int (&sel)[TG],
+__device__ __forceinline__ int warp_gepp(float (&v)[RPL][TG], bool (&live)[RPL], int gw, int *sel, float *Lsm,
                                          float (*Lrec)[TG], float *Urec, int uk) {
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  float lm[RPL][TG];
   int cnt = 0;
-#pragma unroll
-  for (int t = 0; t < TG; ++t) {
-    if (t >= gw) break;
+#pragma unroll 1
+  for (int t = 0; t < gw; ++t) {
     uint32_t key = 0u;
 #pragma unroll
     for (int r = 0; r < RPL; ++r) {
-      if (!live[r]) continue;
-      const float x = fabsf(v[r][t]);
+      const float x = fabsf(v[r][0]);
       const uint32_t a = x == x ? __float_as_uint(x) : 0u;
       const uint32_t k = (a & ~0xFFu) | (uint32_t)(255 - (lane + 32 * r));
-      key = k > key ? k : key;
+      key = (live[r] && k > key) ? k : key;
     }
     const uint32_t mk = __reduce_max_sync(FULL, key);
     if (mk == 0u) break;  // no live candidate left (a live one has a key >= 128)
@@ -561,33 +562,34 @@ __device__ __forceinline__ int warp_gepp(float (&v)[RPL][TG], bool (&live)[RPL],
         if (wr == r) x = v[r][k];
       pv[k] = __shfl_sync(FULL, x, wl);
     }
-    sel[t] = slot;
+    if (lane == 0) sel[t] = slot;
     if (lane == wl) {
 #pragma unroll
       for (int r = 0; r < RPL; ++r)
-        if (r == wr) {
-          live[r] = false;
-          if (RECORD) {
-#pragma unroll
-            for (int s = 0; s < t; ++s) Lrec[t][s] = lm[r][s];
-          }
-        }
+        if (r == wr) live[r] = false;
     }
-    if (RECORD && lane == 0) {
+    if (RECORD) {
+      if (lane < t) Lrec[t][lane] = Lsm[slot * TG + lane];
+      if (lane < TG && lane < gw - t) {
+        float x = pv[0];
 #pragma unroll
-      for (int k = t; k < TG; ++k) Urec[k * uk + t] = pv[k];
+        for (int k = 1; k < TG; ++k)
+          if (lane == k) x = pv[k];
+        Urec[(t + lane) * uk + t] = x;
+      }
     }
-    const float inv = pv[t] != 0.f ? __frcp_rn(pv[t]) : 0.f;
+    const float inv = pv[0] != 0.f ? __frcp_rn(pv[0]) : 0.f;
 #pragma unroll
     for (int r = 0; r < RPL; ++r) {
-      if (!live[r]) continue;
-      const float l = v[r][t] * inv;
-      if (RECORD) lm[r][t] = l;
+      const float l = v[r][0] * inv;
+      if (RECORD && live[r]) Lsm[(lane + 32 * r) * TG + t] = l;
 #pragma unroll
-      for (int k = t + 1; k < TG; ++k) v[r][k] = fmaf(-l, pv[k], v[r][k]);
+      for (int k = 1; k < TG; ++k) v[r][k - 1] = live[r] ? fmaf(-l, pv[k], v[r][k]) : v[r][k];
+      v[r][TG - 1] = 0.f;
     }
     ++cnt;
   }
+  __syncwarp();
   return cnt;
 }
 
@@ -636,6 +638,9 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
   __shared__ int32_t posin[SNB], at_[SNB], ipg[SNB];  // interchange bookkeeping (CTA 0)
   __shared__ int sfail;
   __shared__ TSlot stage[TG];              // this CTA's nominees, as they are pushed
+  __shared__ int32_t selw[TPT / 32][TG];   // pivot search outputs (candidate order)
+  __shared__ float Lsm[SMAXC * TG * TG];   // multipliers of the stacked nominees, per step
+  __shared__ float Linv[TG][TG];           // inverse of the group's unit-lower 8 x 8 block of L
   extern __shared__ __align__(16) unsigned char tp_raw[];
   const int RP = panel_pitch<float>(R);
   float *sp = reinterpret_cast<float *>(tp_raw);
@@ -697,14 +702,10 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
 #pragma unroll
         for (int k = 0; k < TG; ++k) v[r][k] = live[r] ? sp[(c0 + k) * RP + il] : 0.f;
       }
-      int sel[TG];
-      const int cnt = warp_gepp<TRPL, false>(v, live, gw, sel, nullptr, nullptr, 0);
+      const int cnt = warp_gepp<TRPL, false>(v, live, gw, selw[warp], nullptr, nullptr, nullptr, 0);
       if (lane < TG) {
-        int il = -1;
-#pragma unroll
-        for (int t = 0; t < TG; ++t)
-          if (t == lane && t < cnt) il = warp * 32 + (sel[t] & 31) + TPT * (sel[t] >> 5);
-        cand1[warp][lane] = il;
+        const int sl = selw[warp][lane];
+        cand1[warp][lane] = lane < cnt ? warp * 32 + (sl & 31) + TPT * (sl >> 5) : -1;
       }
     }
     __syncthreads();
@@ -722,23 +723,13 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
 #pragma unroll
         for (int k = 0; k < TG; ++k) v[r][k] = live[r] ? sp[(c0 + k) * RP + cil[r]] : 0.f;
       }
-      int sel[TG];
-      const int cnt = warp_gepp<NC1 / 32, false>(v, live, gw, sel, nullptr, nullptr, 0);
-#pragma unroll
-      for (int t = 0; t < TG; ++t) {
-        int il = -1;
-        if (t < cnt) {
-          const int sl = sel[t];
-          int x = cil[0];
-#pragma unroll
-          for (int r = 1; r < NC1 / 32; ++r)
-            if ((sl >> 5) == r) x = cil[r];
-          il = __shfl_sync(0xffffffffu, x, sl & 31);
-        }
-        if (lane == 0) cand2[t] = il;
+      const int cnt = warp_gepp<NC1 / 32, false>(v, live, gw, selw[0], nullptr, nullptr, nullptr, 0);
+      if (lane < TG) {
+        const int ci = selw[0][lane];
+        cand2[lane] = lane < cnt ? cand1[ci / TG][ci % TG] : -1;
       }
       // the previous group's bulk pushes have read the staging slots
-      if (lane == 0) sm100::bulk_wait_read0();
+      if (lane < C) sm100::bulk_wait_read0();
     }
     __syncthreads();
     // -- 3. push the nominees (columns pb..63): staged as gw slots, then one
@@ -760,10 +751,9 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
     }
     sm100::fence_proxy_async_smem();  // the staged slots, visible to the bulk copies
     __syncthreads();
-    if (tid == 0) {
-      for (int d = 0; d < C; ++d)
-        bulk_push(cluster_addr(&slots[(size_t)par * C * TG + cr * gw], d), stage, (uint32_t)(gw * sizeof(TSlot)),
-                  cluster_addr(&xbar[par], d));
+    if (tid < C) {  // lane d of warp 0 pushes into CTA d
+      bulk_push(cluster_addr(&slots[(size_t)par * C * TG + cr * gw], tid), stage, (uint32_t)(gw * sizeof(TSlot)),
+                cluster_addr(&xbar[par], tid));
       sm100::bulk_commit();
     }
     // -- 4. the previous group's update on the columns right of this group
@@ -793,7 +783,10 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
       break;
     }
     const TSlot *sl = slots + (size_t)par * C * TG;
-    // -- 5. the group's pivots from all nominees: the same in every CTA
+    // -- 5. the group's pivots from all nominees, the same in every CTA (warp
+    // 0), while the other warps bring every pushed row's columns right of the
+    // group up to date with the previous group's update (the pushed
+    // multipliers of that group are its first 8 values), in place
     if (warp == 0) {
       constexpr int NC3 = SMAXC * TG / 32;  // up to 128 candidates: 4 per lane
       float v[NC3][TG];
@@ -805,23 +798,40 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
 #pragma unroll
         for (int k = 0; k < TG; ++k) v[r][k] = live[r] ? sl[ci].v[c0 - pb + k] : 0.f;
       }
-      int sel[TG];
-      const int cnt = warp_gepp<NC3, true>(v, live, gw, sel, Lg, &UgT[ub][c0][0], TG);
+      const int cnt = warp_gepp<NC3, true>(v, live, gw, selw[0], Lsm, Lg, &UgT[ub][c0][0], TG);
       // the panel always has at least gw rows that are not pivots yet, so
       // cnt == gw; a shortfall would mean a corrupted exchange
       if (cnt < gw && lane == 0) atomicExch(err, 6);
+      if (lane < gw) {
+        const int s2 = selw[0][lane];
+        wslot[lane] = lane < cnt ? s2 : -1;
+        win[c0 + lane] = lane < cnt ? (int32_t)sl[s2].row : -1;
+      }
+      // the inverse of the group's unit-lower block of L: lane q forms column q
+      __syncwarp();
       if (lane < TG) {
-        int s2 = 0;
+        float col[TG];
 #pragma unroll
-        for (int t = 0; t < TG; ++t)
-          if (t == lane) s2 = sel[t];
-        if (lane < cnt) {
-          wslot[lane] = s2;
-          win[c0 + lane] = (int32_t)sl[s2].row;
-        } else if (lane < gw) {
-          wslot[lane] = -1;
-          win[c0 + lane] = -1;
+        for (int t = 0; t < TG; ++t) {
+          float x = t == lane ? 1.f : 0.f;
+#pragma unroll
+          for (int p = 0; p < t; ++p) x = fmaf(-Lg[t][p], col[p], x);
+          col[t] = t < lane ? 0.f : x;
         }
+#pragma unroll
+        for (int t = 0; t < TG; ++t) Linv[t][lane] = col[t];
+      }
+    } else if (g > 0) {
+      TSlot *slw = slots + (size_t)par * C * TG;
+      const float(*U)[TG] = UgT[ub ^ 1];
+      const int nk = SNB - c0 - gw;
+      for (int e = tid - 32; e < C * gw * nk; e += TPT - 32) {
+        const int ci = e / nk, k = c0 + gw + e % nk;
+        float l[TG];
+#pragma unroll
+        for (int s2 = 0; s2 < TG; ++s2) l[s2] = slw[ci].v[s2];
+        slw[ci].v[k - pb] = rank8(slw[ci].v[k - pb], l, *reinterpret_cast<const float4 *>(&U[k][0]),
+                                  *reinterpret_cast<const float4 *>(&U[k][4]));
       }
     }
     __syncthreads();
@@ -829,29 +839,15 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
       failed = true;
       break;
     }
-    // the pivots' U rows right of the group: the pushed rows brought up to
-    // date with the previous group's update, then eliminated within the group
-    for (int k = c0 + gw + tid; k < SNB; k += TPT) {
-      float u[TG];
+    // the pivots' U rows right of the group: U = Linv A' over the up-to-date
+    // pushed rows A', one (row, column) element per thread
+    for (int e = tid; e < gw * (SNB - c0 - gw); e += TPT) {
+      const int t = e % gw, k = c0 + gw + e / gw;
+      float u = 0.f;
 #pragma unroll
-      for (int t = 0; t < TG; ++t) {
-        u[t] = 0.f;
-        if (t >= gw) continue;
-        const TSlot &w = sl[wslot[t]];
-        float a = w.v[k - pb];
-        if (g > 0) {
-          float l[TG];
-#pragma unroll
-          for (int s2 = 0; s2 < TG; ++s2) l[s2] = w.v[s2];
-          a = rank8(a, l, *reinterpret_cast<const float4 *>(&UgT[ub ^ 1][k][0]),
-                    *reinterpret_cast<const float4 *>(&UgT[ub ^ 1][k][4]));
-        }
-#pragma unroll
-        for (int q = 0; q < t; ++q) a = fmaf(-Lg[t][q], u[q], a);
-        u[t] = a;
-      }
-      *reinterpret_cast<float4 *>(&UgT[ub][k][0]) = make_float4(u[0], u[1], u[2], u[3]);
-      *reinterpret_cast<float4 *>(&UgT[ub][k][4]) = make_float4(u[4], u[5], u[6], u[7]);
+      for (int q = 0; q < TG; ++q)
+        if (q <= t) u = fmaf(Linv[t][q], sl[wslot[q]].v[k - pb], u);
+      UgT[ub][k][t] = u;
     }
     if (tid < gw) {
       const float pv = UgT[ub][c0 + tid][tid];
@@ -859,7 +855,7 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
       const int row = win[c0 + tid];
       if (row >= r0 && row < r1) rstate[row - r0] = (int16_t)(c0 + tid);
     }
-    if (cr == 0 && tid == 0) {
+    if (cr == 0 && tid == TPT - 1) {
       for (int t = 0; t < gw; ++t) {
         const float pv = UgT[ub][c0 + t][t];
         if (pv == 0.f) atomicCAS(info, 0, col0 + c0 + t + 1);
@@ -871,20 +867,20 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
       }
     }
     __syncthreads();
-    // -- 6. this CTA's rows: pivot rows take their final values; the others
-    // their multipliers and the update of the next group's columns
+    // -- 6. this CTA's pivot rows take their final values (all threads, an
+    // element each); the other rows their multipliers and the update of the
+    // next group's columns
+    for (int e = tid; e < gw * (SNB - c0); e += TPT) {
+      const int t = e / (SNB - c0), k = c0 + e % (SNB - c0);
+      const int row = win[c0 + t];
+      if (row < r0 || row >= r1) continue;
+      sp[k * RP + (row - r0)] = k < c0 + t ? Lg[t][k - c0] : UgT[ub][k][t];
+    }
 #pragma unroll
     for (int r = 0; r < TRPL; ++r) {
       const int il = tid + TPT * r;
       if (il >= nr) continue;
-      const int st = rstate[il];
-      if (st >= 0 && st < c0) continue;  // the pivot of an earlier group: final
-      if (st >= c0) {
-        const int t = st - c0;
-        for (int s2 = 0; s2 < t; ++s2) sp[(c0 + s2) * RP + il] = Lg[t][s2];
-        for (int k = c0 + t; k < SNB; ++k) sp[k * RP + il] = UgT[ub][k][t];
-        continue;
-      }
+      if (rstate[il] >= 0) continue;  // a pivot row (of this group: written above)
       float l[TG];
 #pragma unroll
       for (int s2 = 0; s2 < TG; ++s2) {
@@ -928,7 +924,7 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
       for (int j = 0; j < jb; ++j) ipiv[j] = ipg[j];
     }
     __syncthreads();
-    if (track != nullptr && cr == 0 && tid == 0) {
+    if (track != nullptr && cr == 0 && tid == TPT - 1) {
       if (umin != ~0ull) {
         const uint64_t mx = (uint64_t)__double_as_longlong((double)__uint_as_float((uint32_t)umax));
         const uint64_t mn = (uint64_t)__double_as_longlong((double)__uint_as_float((uint32_t)umin));
@@ -977,7 +973,7 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
       }
     }
   }
-  if (tid == 0) sm100::bulk_wait_read0();  // this CTA's last pushes have read its staging slots
+  if (tid < C) sm100::bulk_wait_read0();  // this CTA's last pushes have read its staging slots
   cluster.sync();  // no CTA leaves while another may still push into it
 }
 
