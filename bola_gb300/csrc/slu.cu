@@ -2,17 +2,19 @@
 // counterpart; it preconditions the FP64 refinement in ir.cu).
 //
 // A (FP64) is scaled per 64-column block by a power of two (exact) and
-// rounded to an FP32 working matrix W.  Blocked right-looking LU with partial
-// pivoting and NB = 64 = the K of the tensor-core update:
-//   spanel_kernel   the (n-j) x 64 panel on a cluster of <=16 CTAs, the rows
-//                   held in shared memory; per column each CTA pushes its pivot
-//                   candidate (key + row) into every CTA's shared memory, so
-//                   a column costs one CTA barrier pair and one cluster
-//                   barrier.  It also writes L21 as the K-major A operand
-//                   (bf16, or tf32 hi/lo) of the update.
+// rounded to the working matrix W: FP32 (factor kinds 0-2) or FP64 (kind 3).
+// Blocked right-looking LU, NB = 64 = the K of the tensor-core update:
+//   tpanel_kernel   FP32 W: the (n-j) x 64 panel on a cluster of <= 16 CTAs,
+//                   rows in shared memory, pivots chosen by tournament over
+//                   groups of 8 columns (one cluster exchange per group);
+//   spanel_kernel   FP64 W: the same panel with column-by-column partial
+//                   pivoting (each CTA pushes its candidate row into every
+//                   CTA's shared memory with st.async, per column).
+//   Both write L21 as the update's K-major A operand (bf16, tf32 hi/lo, or
+//   the exact bf16 slices of the FP64-accurate factor).
 //   sswap_trsm      the 64 interchanges on every other column, U12 = L11^-1 A12
 //                   and the K-major B operand.
-//   tc_update       W22 -= L21 U12 on tcgen05 with FP32 accumulation in TMEM.
+//   tc_update / oz_update   W22 -= L21 U12 on tcgen05 (tc_update.cu, oz_update.cu).
 // Pivots are this algorithm's own; only the FP64 refinement decides accuracy.
 #include <cooperative_groups.h>
 #include <cuda_bf16.h>
@@ -46,11 +48,6 @@ __device__ __forceinline__ uint32_t cluster_addr(const void *local, int rank) {
   asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(sm100::smem_u32(local)), "r"(rank));
   return r;
 }
-__device__ __forceinline__ void st_async(uint32_t addr, float v, uint32_t bar) {
-  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(addr),
-               "r"(__float_as_uint(v)), "r"(bar)
-               : "memory");
-}
 __device__ __forceinline__ void st_async(uint32_t addr, double v, uint32_t bar) {
   asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];" ::"r"(addr),
                "l"(__double_as_longlong(v)), "r"(bar)
@@ -83,10 +80,6 @@ struct PKey {
 __device__ __forceinline__ bool pk_less(const PKey &x, const PKey &y) {
   return x.a != y.a ? x.a < y.a : (x.b != y.b ? x.b < y.b : x.c < y.c);
 }
-__device__ __forceinline__ PKey pk_make(float v, int g) {
-  v = fabsf(v);
-  return PKey{v == v ? __float_as_uint(v) : 0u, 0u, 0xFFFFFFFFu - (uint32_t)g};
-}
 __device__ __forceinline__ PKey pk_make(double v, int g) {
   // |v| and the NaN test on the bits: an FP64 comparison would take an FP64 pipe slot
   uint64_t u = (uint64_t)__double_as_longlong(v) & 0x7fffffffffffffffull;
@@ -101,30 +94,9 @@ __device__ __forceinline__ PKey pk_warp_max(const PKey &k) {
 }
 
 // ---- panel arithmetic ---------------------------------------------------------
-// The panel kernel works on elements of type S in shared memory, loaded from
-// and stored to W of type G, through these operations (the FP32 factor's
-// panel, and the FP64-accurate factor's).
-struct PanelF32 {
-  using S = float;
-  using G = float;
-  static constexpr bool kFP64 = false;
-  __device__ static S zero() { return 0.f; }
-  __device__ static S load(G x) { return x; }
-  __device__ static G store(S x) { return x; }
-  __device__ static S mul(S a, S b) { return a * b; }
-  __device__ static S fnms(S z, S x, S y) { return fmaf(-x, y, z); }
-  __device__ static bool is_zero(S p) { return p == 0.f; }
-  __device__ static S recip(S p) { return p == 0.f ? 0.f : 1.0f / p; }
-  __device__ static PKey key(S v, int g) { return pk_make(v, g); }
-  __device__ static double to_double(S v) { return (double)v; }
-  // |v| as bits ordered like |v|; NaN above +inf
-  __device__ static uint64_t abs_bits(S v) { return __float_as_uint(v) & 0x7fffffffu; }
-  __device__ static bool is_nan_bits(uint64_t b) { return b > 0x7f800000u; }
-  __device__ static uint64_t bits_to_double_bits(uint64_t b) {
-    return (uint64_t)__double_as_longlong((double)__uint_as_float((uint32_t)b));
-  }
-};
-
+// The column-by-column panel kernel works on elements of type S in shared
+// memory, loaded from and stored to W of type G, through these operations
+// (the FP64-accurate factor's panel).
 struct PanelF64 {
   using S = double;
   using G = double;
@@ -151,16 +123,9 @@ template <typename T>
 __host__ __device__ constexpr int panel_pitch(int64_t R) {
   return (int)(((R + (int64_t)(16 / sizeof(T))) / (int64_t)(16 / sizeof(T))) * (int64_t)(16 / sizeof(T)));
 }
-__device__ __forceinline__ void vload(float (&v)[4], const float *p) {
-  const float4 t = *reinterpret_cast<const float4 *>(p);
-  v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
-}
 __device__ __forceinline__ void vload(double (&v)[2], const double *p) {
   const double2 t = *reinterpret_cast<const double2 *>(p);
   v[0] = t.x; v[1] = t.y;
-}
-__device__ __forceinline__ void vstore(float *p, const float (&v)[4]) {
-  *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
 }
 __device__ __forceinline__ void vstore(double *p, const double (&v)[2]) {
   *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
