@@ -230,7 +230,7 @@ int chol_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int32_t *info
         return oz_update(st, m2, cols, lu.mapA[buf], lu.mapA64[buf], lu.cap_n, lu.cap_n, lu.ea[buf], lu.ea[buf],
                          W22 + boff * ldw, ldw, lu.err, boff, abort, true);
       else
-        return tc_update(st, lu.kind, m2, cols, lu.mapA[buf], lu.mapA[buf], lu.mapAlo[buf], lu.mapAlo[buf],
+        return tc_update(st, lu.kind, m2, cols, lu.mapA[buf], lu.mapA64[buf], lu.mapAlo[buf], lu.mapAlo64[buf],
                          W22 + boff * ldw, ldw, lu.err, boff, abort, true);
     };
     BOLA_TRY(update(lu.sp, nb_next, 0));  // the next panel's columns

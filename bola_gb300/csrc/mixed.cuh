@@ -224,7 +224,7 @@ struct MixedLU {
   // non-negative doubles, ordered like the values), [2] low word = abandon flag
   uint64_t *track = nullptr;
   CUtensorMap mapA[2], mapB, mapAlo[2], mapBlo;
-  CUtensorMap mapA64[2];  // kind 3: the A operand in 64-row boxes (the B side of a Cholesky update)
+  CUtensorMap mapA64[2], mapAlo64[2];  // the A operands in 64-row boxes (the B side of a Cholesky update)
   cudaStream_t sp = nullptr, su = nullptr;
   cudaEvent_t ev_in = nullptr, ev_sw = nullptr, ev_wide = nullptr, ev_done = nullptr;
   int reserve(int64_t n, int kind, cudaStream_t s);

@@ -1129,16 +1129,20 @@ int MixedLU::reserve(int64_t n_, int kind_, cudaStream_t s) {
   }
   const size_t esz = kind == 0 ? 2 : 4;
   const bool bf = kind == 0;
+  // A operands in 128-row boxes (the update's rows) and 64-row boxes (as the
+  // B side of a Cholesky update); B operands in 64-row boxes
   for (int b = 0; b < 2; ++b) {
     BOLA_TRY_CUDA(cudaMallocAsync(&aop[b], (size_t)n * SNB * esz, s));
     if (kind == 2) BOLA_TRY_CUDA(cudaMallocAsync(&aop_lo[b], (size_t)n * SNB * 4, s));
     BOLA_TRY(make_kmajor_map(&mapA[b], aop[b], n, bf));
     BOLA_TRY(make_kmajor_map(&mapAlo[b], kind == 2 ? aop_lo[b] : aop[b], n, bf));
+    BOLA_TRY(make_kmajor_map(&mapA64[b], aop[b], n, bf, 64));
+    BOLA_TRY(make_kmajor_map(&mapAlo64[b], kind == 2 ? aop_lo[b] : aop[b], n, bf, 64));
   }
   BOLA_TRY_CUDA(cudaMallocAsync(&bop, (size_t)n * SNB * esz, s));
   if (kind == 2) BOLA_TRY_CUDA(cudaMallocAsync(&bop_lo, (size_t)n * SNB * 4, s));
-  BOLA_TRY(make_kmajor_map(&mapB, bop, n, bf));
-  BOLA_TRY(make_kmajor_map(&mapBlo, kind == 2 ? bop_lo : bop, n, bf));
+  BOLA_TRY(make_kmajor_map(&mapB, bop, n, bf, 64));
+  BOLA_TRY(make_kmajor_map(&mapBlo, kind == 2 ? bop_lo : bop, n, bf, 64));
   return 0;
 }
 

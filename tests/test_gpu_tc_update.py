@@ -1,5 +1,10 @@
 """tcgen05 rank-64 update W -= A B^T against a torch FP32 reference of the
-same operation (bf16, tf32 and 3xTF32 operand forms)."""
+same operation (bf16, tf32 and 3xTF32 operand forms).
+
+Shapes cover both kernels: a leading dimension that is not a multiple of 4
+takes the one-tile-per-CTA kernel, the others the pipelined kernel, with
+partial row and column tiles, padding rows below m (which must stay
+untouched) and, at 4096, runs of several tiles per CTA."""
 import ctypes
 
 import pytest
@@ -22,7 +27,8 @@ def tf32_split(x):
 
 
 @pytest.mark.parametrize("kind", [0, 1, 2])
-@pytest.mark.parametrize("m,n,ldw", [(128, 128, 128), (300, 200, 301), (1000, 77, 1000), (2048, 2048, 2048)])
+@pytest.mark.parametrize("m,n,ldw", [(128, 128, 128), (300, 200, 301), (1000, 77, 1000), (500, 300, 516),
+                                   (2048, 2048, 2048), (4096, 4096, 4096)])
 def test_tc_update_matches_fp32_reference(kind, m, n, ldw):
     from bola_gb300 import _lib
     L = _lib.load()
