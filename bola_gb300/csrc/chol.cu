@@ -44,7 +44,7 @@ __device__ __forceinline__ bool factor_stopped(const int32_t *info, const uint64
 // gives up as the LU panel does.
 template <typename T>
 __global__ void __launch_bounds__(256)
-chol_dblock(T *W, int64_t ldw, int jb, int32_t col0, int32_t *info, uint64_t *track, double give_up) {
+chol_dblock(T *W, int64_t ldw, int jb, int32_t col0, int64_t n, int32_t *info, uint64_t *track, double give_up) {
   __shared__ T a[CNB][CNB + 1];
   __shared__ T dinv;
   __shared__ int stop;
@@ -95,7 +95,7 @@ chol_dblock(T *W, int64_t ldw, int jb, int32_t col0, int32_t *info, uint64_t *tr
     if (mn < track[1]) track[1] = mn;
     const double gmx = __longlong_as_double((long long)track[0]), gmn = __longlong_as_double((long long)track[1]);
     const double spread = gmn > 0.0 ? gmx / gmn : INFINITY;
-    if (!(spread < give_up)) *(volatile int32_t *)(track + 2) = 1;
+    if (give_up_now(spread, give_up, col0 + jb, n)) *(volatile int32_t *)(track + 2) = 1;
   }
 }
 
@@ -209,7 +209,7 @@ int chol_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int32_t *info
     {
       ProfScope prof(lu.sp, fp64 ? "chol_panel64" : "chol_panel", (double)mp * jb * jb / 2.0,
                      2.0 * sizeof(T) * (double)mp * jb, 2);
-      chol_dblock<T><<<1, 256, 0, lu.sp>>>(Wp, ldw, jb, (int32_t)j, info, track, give_up);
+      chol_dblock<T><<<1, 256, 0, lu.sp>>>(Wp, ldw, jb, (int32_t)j, n, info, track, give_up);
       if (mp > jb) {
         constexpr int CR = fp64 ? 64 : 128;
         chol_l21<T, CR><<<(unsigned)cdiv(mp - jb, CR), CR, 0, lu.sp>>>(

@@ -1028,7 +1028,9 @@ int dgesv_mixed_ws(Workspace &w, bool chol, int64_t n, int64_t nrhs, const doubl
   // where the mixed one would have done.  The FP64-accurate factor (kind 3)
   // refines anything its pivots leave below ~1e13.  The spread only grows as
   // pivots are added, so the factorisation itself gives up at the first panel
-  // that takes it over the limit, with the decision the whole factor would give.
+  // that takes it over the limit, with the decision the whole factor would
+  // give, or earlier when the spread is on course for 100 times the limit
+  // (give_up_now: log-linear extrapolation from a quarter of the columns on).
   const double limit = o.factor_kind == 0 ? 175.0 : o.factor_kind == 1 ? 1100.0 : o.factor_kind == 2 ? 4.5e4 : 1e13;
   const double give_up = (o.fallback_fp64 || o.escalate) ? limit : INFINITY;
   if (chol) {

@@ -190,6 +190,21 @@ int tc_update(cudaStream_t s, int kind, int64_t m, int64_t n, const CUtensorMap 
               const CUtensorMap &Alo, const CUtensorMap &Blo, float *W, int64_t ldw, int32_t *err, int64_t boff = 0,
               const int32_t *abort = nullptr, bool lower = false);
 
+// The give-up test of the low-precision factorisations, from the spread
+// max|u_kk| / min|u_kk| over the first `done` of `total` columns: the spread
+// has reached the limit, or, once a quarter of the columns are done, its
+// logarithm extrapolated linearly to the last column exceeds 100 times the
+// limit (on systems with geometric spectra log(spread) grows about linearly
+// with the columns factored: a kappa = 1e10 system at n = 8192 is called at
+// a quarter of its columns instead of at 62%, while kappa = 1e6 systems,
+// which the 3xTF32 factor refines, extrapolate below 2e4 at every step).  A
+// wrong call only costs time: the factorisation that follows solves the
+// system all the same.
+__device__ __forceinline__ bool give_up_now(double spread, double give_up, int64_t done, int64_t total) {
+  if (!(spread < give_up)) return true;
+  return 4 * done >= total && spread > 1.0 && log(spread) * ((double)total / (double)done) > log(100.0 * give_up);
+}
+
 // A kernel of an abandoned factorisation returns at once: *abort is read by
 // one thread and the decision shared, so a CTA's barriers stay uniform even
 // while another stream sets the flag.

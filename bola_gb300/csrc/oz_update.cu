@@ -19,17 +19,16 @@
 // accumulators, W -= 2^(eA + eB - 14) * sum_d 2^(-8d) acc_d, on the integer
 // pipe: GB300 retires only about two FP64 operations per clock per SM, so
 // the exact accumulators become one 64-bit fixed-point sum (unit 2^-40),
-// which integer bit operations turn into a double; the subtraction from W is
-// the only FP64 instruction per element.
+// converted to a double once and scaled through its exponent field; the
+// subtraction from W is the only FP64 arithmetic per element.
 //
-// Per CTA: a 128 x 64 tile of W.  A's slices (128 rows) and B's (64 rows)
-// arrive by TMA with 128-byte swizzle, and the FP64 tile of W itself by TMA
-// too (64 KB, in flight while the MMAs run); one thread issues the 26 x 4
-// tcgen05.mma (kind::f16, M = 128, N = 64, K = 16) into seven 64-column TMEM
-// accumulators; eight warps drain them with tcgen05.ld (warps w and w + 4
-// share TMEM lanes 32(w%4).. and split the 64 columns), update the W tile in
-// shared memory, and one TMA store writes it back.  W's leading dimension
-// must be even and its tile origins 16-byte aligned (TMA).
+// Tiles of W are 128 x 64.  A's slices (128 rows) and B's (64 rows) arrive
+// by TMA with 128-byte swizzle; one thread issues the 26 x 4 tcgen05.mma
+// (kind::f16, M = 128, N = 64, K = 16) into seven 64-column TMEM
+// accumulators, one per weight; sixteen warps drain them with tcgen05.ld
+// (the four warps with the same w % 4 share TMEM lanes 32(w%4).. and split
+// the 64 columns) and update W in place.  Warp-specialised and pipelined across the tiles a
+// CTA runs through (oz_update_pipe below).
 #include <cuda_bf16.h>
 
 #include "common.cuh"
@@ -47,30 +46,19 @@ constexpr int DMAX = 6;  // highest pair weight t + u kept
 constexpr int NPAIRS = 26;
 constexpr int A_BOX = OBM * 128;  // bytes of one A slice tile (128 rows x 64 bf16)
 constexpr int B_BOX = OBN * 128;  // bytes of one B slice tile
-constexpr int W_BOX = OBM * OBN * 8;  // the FP64 tile of W, column-major 128 x 64
-constexpr int OZ_SMEM = S * (A_BOX + B_BOX) + W_BOX + 1024;
 constexpr uint32_t OZ_IDESC = make_idesc(1u, OBM, OBN);
 constexpr int OZ_TMEM_COLS = 512;  // (DMAX + 1) * 64 = 448 columns used
 
-// T * 2^E as a double, T a 64-bit integer, rounded to nearest (ties away
-// from zero) with integer operations only; ldexp for results outside the
-// normal range.
+// T * 2^E as a double, T a 64-bit integer: one conversion (rounded to
+// nearest even), then the power of two added to the exponent field when the
+// result stays normal (exact); ldexp otherwise.
 __device__ __forceinline__ double fix_to_double(int64_t T, int E) {
+  const double x = (double)T;
+  const long long b = __double_as_longlong(x);
+  const int field = (int)((b >> 52) & 0x7FF) + E;
   if (T == 0) return 0.0;
-  const bool neg = T < 0;
-  uint64_t a = neg ? (uint64_t)(-T) : (uint64_t)T;
-  const int lz = __clzll((long long)a);
-  a <<= lz;                                   // leading one at bit 63
-  uint64_t m = (a >> 11) + ((a >> 10) & 1u);  // 53 significant bits, rounded
-  int e = 63 - lz;                            // T = a * 2^(e - 63)
-  if (m >> 53) {
-    m >>= 1;
-    e += 1;
-  }
-  const int field = 1023 + e + E;
-  if (field <= 0 || field >= 2047) return ldexp((double)T, E);
-  const uint64_t bits = ((uint64_t)neg << 63) | ((uint64_t)field << 52) | (m & ((1ull << 52) - 1));
-  return __longlong_as_double((long long)bits);
+  if (field <= 0 || field >= 2047) return ldexp(x, E);
+  return __longlong_as_double(b + ((long long)E << 52));
 }
 
 // 32 lanes x 16 consecutive 32-bit TMEM columns.
@@ -87,118 +75,237 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-constexpr int OZ_THREADS = 256;
+// ---- the update kernel ---------------------------------------------------------------
+// Each CTA runs through a short range of consecutive 128 x 64 tiles of W
+// (row-block-major, so most of them share A's rows).  Warp 0 streams A's
+// slices (once per row block, resident) and B's (a two-stage ring) through
+// TMA, and prefetches the tile of W into L2; warp 1 issues the MMA chains and
+// commits each weight's accumulator on its own mbarrier; sixteen epilogue warps
+// drain accumulator d as soon as its pairs are done and hand it back, so the
+// next tile's MMAs for weight d start while the epilogue still reads weights
+// d + 1 ... of this one.  The drain is a chain of dependent integer steps per
+// element, so it takes sixteen warps (four per SM sub-partition, 16 columns
+// each) to keep the sub-partitions issuing.  W is read and written directly by
+// the epilogue (a warp moves 32 consecutive rows of a column per access),
+// which keeps shared memory to A's and B's slices.  The accumulators combine into three 32-bit
+// partial sums (weights 0-1, 2-3 and 4-6) before the 64-bit fixed-point sum:
+// the same integer as adding every weight into 64 bits.
+constexpr int ZEPI = 16;                   // epilogue warps: four per TMEM lane quadrant
+constexpr int ZCOL = OBN / (ZEPI / 4);     // columns an epilogue warp drains
+constexpr int ZTHREADS = 64 + 32 * ZEPI;   // producer warp, MMA warp, epilogue
+constexpr int ZA_BYTES = S * A_BOX;        // A's slices of one row block
+constexpr int ZB_BYTES = S * B_BOX;        // B's slices of one tile (one ring stage)
+constexpr int ZSMEM = ZA_BYTES + 2 * ZB_BYTES + 1024;
 
-__global__ void __launch_bounds__(OZ_THREADS)
-oz_update_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-                 const __grid_constant__ CUtensorMap mapW, int64_t capA, int64_t capB, int64_t boff, int64_t m,
-                 int64_t n, const int32_t *__restrict__ eA, const int32_t *__restrict__ eB, int32_t *err,
-                 const int32_t *abort, int lower) {
-  // a Cholesky update leaves the tiles strictly above the diagonal alone
-  if (lower && boff + (int64_t)blockIdx.y * OBN >= (int64_t)blockIdx.x * OBM + OBM) return;
+// The next tile at or after linear index T (row-block-major, NT tiles per row
+// block) that a lower (Cholesky) update keeps; t1 if none before it.
+__device__ __forceinline__ int oz_next_tile(int T, int t1, int NT, int64_t boff, bool lower) {
+  for (; T < t1; ++T) {
+    const int i = T / NT, j = T % NT;
+    if (!lower || boff + (int64_t)j * OBN < (int64_t)i * OBM + OBM) return T;
+  }
+  return t1;
+}
+
+// An integer-valued float v with |v| <= 2^22, as an int (an FP32 add and an
+// integer subtract instead of a conversion instruction).
+__device__ __forceinline__ int small_int(float v) { return __float_as_int(v + 12582912.0f) - 0x4B400000; }
+
+__global__ void __launch_bounds__(ZTHREADS, 1)
+oz_update_pipe(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int64_t capA,
+               int64_t capB, int64_t boff, int64_t m, int64_t n, const int32_t *__restrict__ eA,
+               const int32_t *__restrict__ eB, double *__restrict__ W, int64_t ldw, int tpc, int32_t *err,
+               const int32_t *abort, int lower) {
   if (abandoned(abort)) return;
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t bar_load, bar_mma;
+  __shared__ uint64_t a_full, a_empty, b_full[2], b_empty[2], acc_full[DMAX + 1], acc_empty[DMAX + 1];
   __shared__ uint32_t tmem_slot;
-  __shared__ int ok_shared;
-  __shared__ int32_t ebs[OBN];
   uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint8_t *tileA = base;                // S tiles of A_BOX bytes
-  uint8_t *tileB = base + S * A_BOX;    // S tiles of B_BOX bytes
-  double *tileW = reinterpret_cast<double *>(base + S * (A_BOX + B_BOX));  // [64 columns][128 rows]
-
+  uint8_t *tileA = base;             // S slices of A_BOX bytes
+  uint8_t *tileB = base + ZA_BYTES;  // two stages of S slices of B_BOX bytes
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int64_t i0 = (int64_t)blockIdx.x * OBM, j0 = (int64_t)blockIdx.y * OBN;
+  const int NT = (int)cdiv(n, OBN), MT = (int)cdiv(m, OBM);
+  const int t0 = blockIdx.x * tpc, t1 = (int)imin((int64_t)MT * NT, (int64_t)t0 + tpc);
+  const bool low = lower != 0;
+  // bulk prefetches need 16-byte aligned column starts
+  const bool wpre = (ldw & 1) == 0 && (reinterpret_cast<uintptr_t>(W) & 15) == 0;
 
   if (tid == 0) {
-    mbar_init(&bar_load, 1);
-    mbar_init(&bar_mma, 1);
+    mbar_init(&a_full, 1);
+    mbar_init(&a_empty, 1);
+    for (int q = 0; q < 2; ++q) {
+      mbar_init(&b_full[q], 1);
+      mbar_init(&b_empty[q], 1);
+    }
+    for (int d = 0; d <= DMAX; ++d) {
+      mbar_init(&acc_full[d], 1);
+      mbar_init(&acc_empty[d], ZEPI);
+    }
     fence_mbar_init();
   }
-  if (warp == 0) {
+  if (warp == 1) {
     tmem_alloc(&tmem_slot, OZ_TMEM_COLS);
     tmem_relinquish();
   }
-  if (tid < OBN) ebs[tid] = j0 + tid < n ? eB[boff + j0 + tid] : 0;
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
 
-  if (tid == 0) {
-    ok_shared = 1;
-    mbar_arrive_expect_tx(&bar_load, S * (A_BOX + B_BOX) + W_BOX);
-    tma_load_2d(tileW, &mapW, (int32_t)i0, (int32_t)j0, &bar_load);
-    for (int t = 0; t < S; ++t) {
-      tma_load_2d(tileA + t * A_BOX, &mapA, 0, (int32_t)(t * capA + i0), &bar_load);
-      tma_load_2d(tileB + t * B_BOX, &mapB, 0, (int32_t)(t * capB + boff + j0), &bar_load);
-    }
-    if (!bounded_wait(&bar_load, 0)) {
-      ok_shared = 0;
-      atomicExch(err, 1);
-    } else {
-      tc_fence_after();
-      for (int d = 0; d <= DMAX; ++d) {  // accumulator d collects the pairs t + u = d
-        const uint32_t acc_addr = tmem + (uint32_t)(d * OBN);
-        uint32_t acc = 0;
-        for (int t = (d > S - 1 ? d - (S - 1) : 0); t <= d && t < S; ++t) {
-          const int u = d - t;
-          const uint64_t da = sw128_kmajor_desc(tileA + t * A_BOX);
-          const uint64_t db = sw128_kmajor_desc(tileB + u * B_BOX);
-#pragma unroll
-          for (int ks = 0; ks < 4; ++ks) {  // K = 64 as 4 x 16 bf16 (32 bytes each)
-            umma<0>(acc_addr, desc_advance(da, ks * 32), desc_advance(db, ks * 32), OZ_IDESC, acc);
-            acc = 1;
+  if (warp == 0) {
+    if (lane == 0) {  // -- producer
+      int k = 0, ai = -1, na = 0;
+      for (int T = oz_next_tile(t0, t1, NT, boff, low); T < t1; T = oz_next_tile(T + 1, t1, NT, boff, low), ++k) {
+        const int i = T / NT, j = T % NT;
+        if (i != ai) {
+          if (na > 0 && !bounded_wait(&a_empty, (uint32_t)(na - 1) & 1u)) {
+            atomicExch(err, 31);
+            break;
           }
+          mbar_arrive_expect_tx(&a_full, ZA_BYTES);
+          for (int t = 0; t < S; ++t)
+            tma_load_2d(tileA + t * A_BOX, &mapA, 0, (int32_t)(t * capA + (int64_t)i * OBM), &a_full);
+          ai = i;
+          ++na;
+        }
+        const int st = k & 1;
+        if (!bounded_wait(&b_empty[st], ((uint32_t)(k >> 1) & 1u) ^ 1u)) {
+          atomicExch(err, 32);
+          break;
+        }
+        mbar_arrive_expect_tx(&b_full[st], ZB_BYTES);
+        for (int u = 0; u < S; ++u)
+          tma_load_2d(tileB + st * ZB_BYTES + u * B_BOX, &mapB, 0, (int32_t)(u * capB + boff + (int64_t)j * OBN),
+                      &b_full[st]);
+        if (wpre) {  // W's tile into L2 ahead of the epilogue: one bulk prefetch per column
+          const int64_t r0 = (int64_t)i * OBM, cb = (int64_t)j * OBN;
+          const uint32_t bytes = (uint32_t)(imin(OBM, m - r0) * 8) & ~15u;
+          const int nc = (int)imin(OBN, n - cb);
+          if (bytes > 0)
+            for (int c = 0; c < nc; ++c) bulk_prefetch_l2(W + r0 + (cb + c) * ldw, bytes);
         }
       }
-      umma_commit(&bar_mma);
     }
-  }
-  __syncthreads();
-  if (ok_shared != 0) {
-    if (!bounded_wait(&bar_mma, 0)) {
-      atomicExch(err, 2);
-    } else {
-      tc_fence_after();
-      const int rl = (warp & 3) * 32 + lane;
-      const int64_t row = i0 + rl;
-      const int ea = row < m ? eA[row] : 0;
-      const int cbeg = (warp >> 2) * (OBN / 2);
-#pragma unroll 1
-      for (int c0 = cbeg; c0 < cbeg + OBN / 2; c0 += 16) {
-        // sum_d acc_d 2^(-8d) in units of 2^-40: |acc_0| <= 2^20, so |T| < 2^61
-        int64_t T[16];
+  } else if (warp == 1) {
+    if (lane == 0) {  // -- MMA issuer
+      int k = 0, ai = -1, na = 0;
+      bool ok = true;
+      for (int T = oz_next_tile(t0, t1, NT, boff, low); T < t1 && ok; ++k) {
+        const int i = T / NT;
+        const int Tn = oz_next_tile(T + 1, t1, NT, boff, low);
+        if (i != ai) {
+          if (!bounded_wait(&a_full, (uint32_t)na & 1u)) {
+            atomicExch(err, 33);
+            break;
+          }
+          ai = i;
+          ++na;
+        }
+        const int st = k & 1;
+        if (!bounded_wait(&b_full[st], (uint32_t)(k >> 1) & 1u)) {
+          atomicExch(err, 34);
+          break;
+        }
+        for (int d = 0; d <= DMAX; ++d) {  // accumulator d collects the pairs t + u = d
+          // the epilogue has read this accumulator for the previous tile
+          if (!bounded_wait(&acc_empty[d], ((uint32_t)k & 1u) ^ 1u)) {
+            atomicExch(err, 35);
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t acc_addr = tmem + (uint32_t)(d * OBN);
+          uint32_t acc = 0;
+          for (int t = (d > S - 1 ? d - (S - 1) : 0); t <= d && t < S; ++t) {
+            const uint64_t da = sw128_kmajor_desc(tileA + t * A_BOX);
+            const uint64_t db = sw128_kmajor_desc(tileB + st * ZB_BYTES + (d - t) * B_BOX);
 #pragma unroll
-        for (int q = 0; q < 16; ++q) T[q] = 0;
+            for (int ks = 0; ks < 4; ++ks) {  // K = 64 as 4 x 16 bf16 (32 bytes each)
+              umma<0>(acc_addr, desc_advance(da, ks * 32), desc_advance(db, ks * 32), OZ_IDESC, acc);
+              acc = 1;
+            }
+          }
+          umma_commit(&acc_full[d]);
+        }
+        if (!ok) break;
+        umma_commit(&b_empty[st]);
+        if (Tn >= t1 || Tn / NT != i) umma_commit(&a_empty);  // the next tile loads other rows of A
+        T = Tn;
+      }
+    }
+  } else {
+    // -- epilogue: warp w drains TMEM lanes 32 (w % 4).. (its tile rows), columns ZCOL h ..
+    const int ew = warp - 2, q = warp & 3, h = ew >> 2;
+    const int rl = q * 32 + lane;
+    int k = 0;
+    for (int T = oz_next_tile(t0, t1, NT, boff, low); T < t1; T = oz_next_tile(T + 1, t1, NT, boff, low), ++k) {
+      const int i = T / NT, j = T % NT;
+      const int64_t row = (int64_t)i * OBM + rl;
+      const int64_t c0 = (int64_t)j * OBN + h * ZCOL;  // this warp's first column
+      const int ncol = (int)imax(0, imin(ZCOL, n - c0));
+      int Z[ZCOL], Y[ZCOL], X[ZCOL];  // weights 0-1, 2-3, 4-6 (the partial sums below)
+      bool ok = true;
 #pragma unroll
-        for (int d = 0; d <= DMAX; ++d) {
+      for (int d = 0; d <= DMAX; ++d) {
+        ok = ok && __all_sync(0xffffffffu, bounded_wait(&acc_full[d], (uint32_t)k & 1u));
+        if (ok) tc_fence_after();
+        const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(d * OBN + h * ZCOL);
+#pragma unroll
+        for (int hb = 0; hb < ZCOL; hb += 16) {
           float v[16];
-          tmem_ld16(tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(d * OBN + c0), v);
+          if (ok) {
+            tmem_ld16(ta + hb, v);
+          } else {
 #pragma unroll
-          for (int q = 0; q < 16; ++q) {
-            const int64_t iv = (int64_t)__float2int_rn(v[q]);  // exact: |acc_d| < 2^23
-            T[q] += d <= 5 ? (iv << (8 * (5 - d))) : (iv >> (8 * (d - 5)));
+            for (int c = 0; c < 16; ++c) v[c] = 0.f;
+          }
+          // |acc_d| <= (pairs of weight d) * 64 * 2^14: <= 2^22 for d <= 3
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            const int cc = hb + c;
+            if (d == 0) Z[cc] = small_int(v[c]);
+            if (d == 1) Z[cc] = Z[cc] * 256 + small_int(v[c]);  // |Z| <= 2^28 + 2^21
+            if (d == 2) Y[cc] = small_int(v[c]);
+            if (d == 3) Y[cc] = Y[cc] * 256 + small_int(v[c]);  // |Y| <= 3 * 2^28 + 2^22
+            if (d == 4) X[cc] = __float2int_rn(v[c]);            // <= 5 * 2^20
+            if (d == 5) X[cc] = X[cc] * 256 + __float2int_rn(v[c]);
+            if (d == 6) X[cc] += __float2int_rn(v[c]) >> 8;      // |X| < 1.26 * 2^30
           }
         }
-        // rows and columns outside W are clipped by the TMA store
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          double *p = tileW + (c0 + q) * OBM + rl;
-          *p -= fix_to_double(T[q], ea + ebs[c0 + q] - 54);
+        if (ok) {  // the accumulator goes back to the MMA issuer
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&acc_empty[d]);
         }
       }
-      fence_proxy_async_smem();
+      if (!ok) {
+        if (lane == 0) atomicExch(err, 36);
+        break;
+      }
+      if (row < m) {
+        double *wp = W + row + c0 * ldw;  // (prefetched into L2 by the producer)
+        const int ea = eA[row];
+        const int32_t *eb = eB + boff + c0;
+        double x[ZCOL];
+#pragma unroll
+        for (int c = 0; c < ZCOL; ++c) {
+          // sum_d acc_d 2^(-8d) in units of 2^-40
+          const int64_t Tq = ((int64_t)Z[c] << 32) + ((int64_t)Y[c] << 16) + (int64_t)X[c];
+          x[c] = c < ncol ? fix_to_double(Tq, ea + eb[c] - 54) : 0.0;
+        }
+        // all of W's loads first (no store between them), then the stores
+        double w[ZCOL];
+#pragma unroll
+        for (int c = 0; c < ZCOL; ++c) w[c] = c < ncol ? wp[c * ldw] : 0.0;
+#pragma unroll
+        for (int c = 0; c < ZCOL; ++c)
+          if (c < ncol) wp[c * ldw] = w[c] - x[c];
+      }
     }
   }
   tc_fence_before();
   __syncthreads();
-  if (tid == 0 && ok_shared != 0) {
-    tma_store_2d(&mapW, tileW, (int32_t)i0, (int32_t)j0);
-    bulk_commit();
-    bulk_wait_read0();
-  }
-  if (warp == 0) tmem_dealloc(tmem, OZ_TMEM_COLS);
+  if (warp == 1) tmem_dealloc(tmem, OZ_TMEM_COLS);
 }
 
 // Slices of rows of an FP64 K-major matrix (rows x 64, ld 64): one warp per
@@ -218,19 +325,19 @@ int oz_update(cudaStream_t s, int64_t m, int64_t n, const CUtensorMap &A, const 
               int64_t capB, const int32_t *eA, const int32_t *eB, double *W, int64_t ldw, int32_t *err, int64_t boff,
               const int32_t *abort, bool lower) {
   if (m <= 0 || n <= 0) return 0;
-  if ((ldw & 1) != 0 || (reinterpret_cast<uintptr_t>(W) & 15) != 0)
-    return fail(BOLA_ERR_UNSUPPORTED, "oz_update: W needs an even leading dimension and a 16-byte aligned origin");
-  CUtensorMap mapW;
-  BOLA_TRY(make_fp64_tile_map(&mapW, W, m, n, ldw, OBM, OBN));
   static bool attr = false;
   if (!attr) {
-    BOLA_TRY_CUDA(cudaFuncSetAttribute(oz_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM));
+    BOLA_TRY_CUDA(cudaFuncSetAttribute(oz_update_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, ZSMEM));
     attr = true;
   }
-  const dim3 grid((unsigned)cdiv(m, OBM), (unsigned)cdiv(n, OBN));
+  const int64_t tiles = cdiv(m, OBM) * cdiv(n, OBN);
+  // runs of up to 8 tiles per CTA, but never fewer CTAs than twice the SMs
+  // (a narrow update, on the critical path, keeps one tile per CTA)
+  const int tpc = (int)imax(1, imin(8, tiles / (2 * (int64_t)num_sms())));
+  const unsigned grid = (unsigned)cdiv(tiles, tpc);
   ProfScope prof(s, "oz_update", 2.0 * (double)m * n * OK * NPAIRS, 16.0 * (double)m * n);
-  oz_update_kernel<<<grid, OZ_THREADS, OZ_SMEM, s>>>(A, B, mapW, capA, capB, boff, m, n, eA, eB, err, abort,
-                                                     lower ? 1 : 0);
+  oz_update_pipe<<<grid, ZTHREADS, ZSMEM, s>>>(A, B, capA, capB, boff, m, n, eA, eB, W, ldw, tpc, err, abort,
+                                               lower ? 1 : 0);
   BOLA_CHECK_LAUNCH();
   return 0;
 }

@@ -40,27 +40,6 @@ struct alignas(16) SSlot {
   T v[SNB];                  // the candidate row
 };
 
-// Asynchronous stores into another CTA's shared memory that complete by
-// adding their byte count to that CTA's mbarrier (st.async): the receiver
-// waits on its own mbarrier instead of a cluster-wide barrier.
-__device__ __forceinline__ uint32_t cluster_addr(const void *local, int rank) {
-  uint32_t r;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(sm100::smem_u32(local)), "r"(rank));
-  return r;
-}
-__device__ __forceinline__ void st_async(uint32_t addr, double v, uint32_t bar) {
-  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];" ::"r"(addr),
-               "l"(__double_as_longlong(v)), "r"(bar)
-               : "memory");
-}
-__device__ __forceinline__ void st_async4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d,
-                                          uint32_t bar) {
-  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(
-                   addr),
-               "r"(a), "r"(b), "r"(c), "r"(d), "r"(bar)
-               : "memory");
-}
-
 // Bulk copy of `bytes` (a multiple of 16) from this CTA's shared memory into
 // another CTA's (cluster addresses dst and bar), completing on the
 // receiver's mbarrier; the issuing thread commits it as a bulk group.
@@ -262,15 +241,15 @@ spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, 
         j1v = lane + 32 < jb ? PE(lane + 32, jl) : P::zero();
       }
       for (int d = warp; d < C; d += SPT / 32) {
-        const uint32_t rbar = cluster_addr(&xbar[par], d);
-        const uint32_t rs = cluster_addr(&slots[par][cr], d);
-        if (lane == 0) st_async4(rs, ck.a, ck.b, ck.c, 0u, rbar);
-        st_async(rs + 16 + lane * (uint32_t)sizeof(T), c0, rbar);
-        st_async(rs + 16 + (lane + 32) * (uint32_t)sizeof(T), c1, rbar);
+        const uint32_t rbar = sm100::cluster_addr(&xbar[par], d);
+        const uint32_t rs = sm100::cluster_addr(&slots[par][cr], d);
+        if (lane == 0) sm100::st_async4(rs, ck.a, ck.b, ck.c, 0u, rbar);
+        sm100::st_async(rs + 16 + lane * (uint32_t)sizeof(T), c0, rbar);
+        sm100::st_async(rs + 16 + (lane + 32) * (uint32_t)sizeof(T), c1, rbar);
         if (own_j) {
-          const uint32_t rj = cluster_addr(&rowj[par][0], d);
-          st_async(rj + lane * (uint32_t)sizeof(T), j0v, rbar);
-          st_async(rj + (lane + 32) * (uint32_t)sizeof(T), j1v, rbar);
+          const uint32_t rj = sm100::cluster_addr(&rowj[par][0], d);
+          sm100::st_async(rj + lane * (uint32_t)sizeof(T), j0v, rbar);
+          sm100::st_async(rj + (lane + 32) * (uint32_t)sizeof(T), j1v, rbar);
         }
       }
     }
@@ -387,7 +366,7 @@ spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, 
     }
     const double gmx = __longlong_as_double((long long)track[0]), gmn = __longlong_as_double((long long)track[1]);
     const double spread = gmn > 0.0 ? gmx / gmn : INFINITY;
-    if (!(spread < give_up)) *(volatile int32_t *)(track + 2) = 1;
+    if (give_up_now(spread, give_up, col0 + jb, col0 + mp)) *(volatile int32_t *)(track + 2) = 1;
   }
 
   // -- write back the panel and the update's A operand (rows below the panel)
@@ -717,8 +696,8 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
     sm100::fence_proxy_async_smem();  // the staged slots, visible to the bulk copies
     __syncthreads();
     if (tid < C) {  // lane d of warp 0 pushes into CTA d
-      bulk_push(cluster_addr(&slots[(size_t)par * C * TG + cr * gw], tid), stage, (uint32_t)(gw * sizeof(TSlot)),
-                cluster_addr(&xbar[par], tid));
+      bulk_push(sm100::cluster_addr(&slots[(size_t)par * C * TG + cr * gw], tid), stage, (uint32_t)(gw * sizeof(TSlot)),
+                sm100::cluster_addr(&xbar[par], tid));
       sm100::bulk_commit();
     }
     // -- 4. the previous group's update on the columns right of this group
@@ -898,7 +877,7 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
       }
       const double gmx = __longlong_as_double((long long)track[0]), gmn = __longlong_as_double((long long)track[1]);
       const double spread = gmn > 0.0 ? gmx / gmn : INFINITY;
-      if (!(spread < give_up)) *(volatile int32_t *)(track + 2) = 1;
+      if (give_up_now(spread, give_up, col0 + jb, col0 + mp)) *(volatile int32_t *)(track + 2) = 1;
     }
     // final position of each of this CTA's rows
     auto dest = [&](int il) -> int {
@@ -1063,7 +1042,9 @@ template <typename P>
 int launch_spanel(cudaStream_t s, typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0,
                   int32_t *info, int kind, void *aop, float *aop_lo, int32_t *aexp, int64_t cap, int32_t *plan,
                   uint64_t *track, double give_up, int32_t *err) {
-  const int C = (int)imin(SMAXC, imax(1, cdiv(mp, SPT)));
+  // FP64 panels are bound by the FP64 pipe of each CTA (~2 FMA per clock per
+  // SM): short ones spread over up to 16 CTAs of more than 64 rows each
+  const int C = (int)imin(SMAXC, imax(1, cdiv(mp, P::kFP64 ? 128 : SPT)));
   const int64_t R = cdiv(mp, C);
   const size_t smem = sizeof(typename P::S) * (size_t)jb * (size_t)panel_pitch<typename P::S>(R);
   if (smem > 200 * 1024) return fail(BOLA_ERR_UNSUPPORTED, "mixed LU: panel of %lld rows too tall", (long long)mp);

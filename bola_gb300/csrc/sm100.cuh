@@ -69,6 +69,34 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, const void 
                "r"(smem_u32(src)), "r"(x), "r"(y)
                : "memory");
 }
+// ---- distributed shared memory ---------------------------------------------------
+// The address of `local` (this CTA's shared memory) in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t cluster_addr(const void *local, int rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(local)), "r"(rank));
+  return r;
+}
+// Asynchronous stores into another CTA's shared memory that complete by
+// adding their byte count to that CTA's mbarrier (st.async): the receiver
+// waits on its own mbarrier instead of a cluster-wide barrier.
+__device__ __forceinline__ void st_async(uint32_t addr, double v, uint32_t bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];" ::"r"(addr),
+               "l"(__double_as_longlong(v)), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void st_async(uint32_t addr, long long v, uint32_t bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];" ::"r"(addr), "l"(v),
+               "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void st_async4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d,
+                                          uint32_t bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(
+                   addr),
+               "r"(a), "r"(b), "r"(c), "r"(d), "r"(bar)
+               : "memory");
+}
+
 // Hint: bring `bytes` (a multiple of 16) from a 16-byte aligned global address into L2.
 __device__ __forceinline__ void bulk_prefetch_l2(const void *p, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");

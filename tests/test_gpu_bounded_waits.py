@@ -29,3 +29,24 @@ def test_expired_waits_report_and_context_survives(oracle_lib):
     tc = torch.from_numpy(np.asfortranarray(c).ravel(order="F")).cuda()
     api.gemm("N", "N", 64, 64, 64, 1.0, ta, 64, tb, 64, 1.0, tc, 64)
     assert np.array_equal(tc.cpu().numpy().reshape(64, 64, order="F"), c1)
+
+
+@pytest.mark.parametrize("csize,nbytes", [(2, 2176), (16, 2176), (16, 528)])
+def test_cluster_exchange_probe(csize, nbytes):
+    """The exchange-latency probe completes (no wait expires) and gives a
+    plausible time per round: above the ~0.1 us of a shared-memory round
+    trip, far below a millisecond."""
+    from bola_gb300 import _lib
+    L = _lib.load()
+    us = ctypes.c_double(0.0)
+    st = L.bola_measure_cluster_exchange(csize, nbytes, ctypes.byref(us))
+    assert st == 0, L.bola_last_error()
+    assert 0.05 < us.value < 100.0, us.value
+
+
+def test_cluster_exchange_probe_rejects_bad_arguments():
+    from bola_gb300 import _lib
+    L = _lib.load()
+    us = ctypes.c_double(0.0)
+    assert L.bola_measure_cluster_exchange(17, 512, ctypes.byref(us)) == -1
+    assert L.bola_measure_cluster_exchange(4, 100, ctypes.byref(us)) == -2

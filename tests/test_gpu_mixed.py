@@ -149,15 +149,27 @@ def test_escalation_to_fp64_accurate_factor(kind):
 
 
 def test_give_up_decides_as_the_whole_factor_would():
-    """The 3xTF32 factor gives up at the first panel whose pivots push the
-    U-diagonal spread over its limit; the spread of the finished factor is at
-    least as large, so the decision is the same, only earlier."""
+    """The 3xTF32 factor gives up once the U-diagonal spread reaches its limit
+    or is on course for 100 times it (log-linear extrapolation from a quarter
+    of the columns on); the finished factor's spread does exceed the limit,
+    so the decision is the one the whole factor would give, only earlier."""
     n, nrhs = 2048, 2
     A, b = make_system(n, nrhs, 1e10, seed=11)
     _, early = solve(A, b, n, nrhs, 2, fallback=1)            # may give up
     _, full = solve(A, b, n, nrhs, 2, fallback=0, max_it=0)   # never gives up
     assert early.path == 2
-    assert 4.5e4 <= early.condition_estimate <= full.condition_estimate
+    assert full.condition_estimate >= 4.5e4
+    assert early.condition_estimate <= full.condition_estimate
+
+
+def test_no_early_give_up_where_the_factor_refines():
+    """kappa = 1e6: the spread never extrapolates past 100 times the limit, so
+    the 3xTF32 factor is kept and refinement reaches the tolerance."""
+    n, nrhs = 2048, 2
+    A, b = make_system(n, nrhs, 1e6, seed=11)
+    x, info = solve(A, b, n, nrhs, 2, fallback=1, escalate=1)
+    assert info.path in (0, 1)
+    assert berr(A, x, b, n, nrhs) <= 1e-14
 
 
 def test_escalated_answer_equals_the_fp64_factor_alone():

@@ -1,7 +1,8 @@
 """FP64-accurate rank-64 update on the bf16 tensor cores (exact slicing):
 exact on integer data; otherwise within 2^-44 * 64 * max|a_i.| * max|b_j.|
 of the FP64 product (the slicing works relative to each row's scale);
-ragged tile edges included."""
+ragged tile edges, an odd leading dimension (no L2 prefetch of W) and, at
+4096 x 2000, several tiles per CTA included."""
 import ctypes
 
 import numpy as np
@@ -27,7 +28,7 @@ def _run(A, B, W):
     return w.cpu().numpy().reshape(n, m).T
 
 
-@pytest.mark.parametrize("m,n", [(300, 200), (128, 64), (1000, 513)])
+@pytest.mark.parametrize("m,n", [(300, 200), (128, 64), (1000, 513), (1001, 700), (4096, 2000)])
 def test_integer_data_is_exact(m, n):
     rng = np.random.default_rng(m + n)
     A = rng.integers(-100, 101, size=(m, 64)).astype(np.float64)
