@@ -37,6 +37,10 @@ typedef void *bola_stream_t; /* cudaStream_t */
 #define BOLA_ERR_CUDA (-1000)        /* a CUDA runtime call failed */
 #define BOLA_ERR_NO_DEVICE (-1001)   /* no usable sm_103 device */
 #define BOLA_ERR_UNSUPPORTED (-1002) /* argument combination outside this library */
+/* Device-side *info of bola_dgetrf / bola_dgetrf2: a panel's bounded wait for
+ * another CTA of its cluster expired (the factor is unusable; the context
+ * stays usable).  Positive values keep their meaning (first zero pivot). */
+#define BOLA_INFO_WAIT_EXPIRED (-2000)
 
 /* Library identification and diagnostics. */
 const char *bola_version(void);
@@ -64,6 +68,15 @@ int bola_profile_read(int index, char *name, int name_len, int64_t *calls, int64
  * fractions of the FP64 kernels are stated against a peak measured on the
  * same device and clocks.  Synchronises the device. */
 int bola_measure_fp64_peak(double *gflops);
+
+/* Measures one exchange round of a cluster panel (no BOLA counterpart): csize
+ * (1..16) CTAs each copy `bytes` (16..8192, a multiple of 16) of shared memory
+ * into every CTA of the cluster with bulk copies that complete on the
+ * receiver's mbarrier, then wait for their own arrivals (bounded) and meet a
+ * CTA barrier.  *us_per_round gets the time per round (microseconds), the
+ * floor of the mixed LU panels' serial chain per pivot group.  Synchronises
+ * the device. */
+int bola_measure_cluster_exchange(int csize, int bytes, double *us_per_round);
 
 /* Self-test of the library's bounded waits (no BOLA counterpart): one kernel
  * waits on an mbarrier that nothing completes and on a device flag that
