@@ -125,6 +125,9 @@ def syrk(uplo, trans, n, k, alpha, a, lda, beta, c, ldc):
 
 # ---- LAPACK ------------------------------------------------------------------
 
+INFO_WAIT_EXPIRED = -2000  # BOLA_INFO_WAIT_EXPIRED
+
+
 def _bola_local_column(info, min_mn):
     # BOLA's messages number the failing column inside the 32-wide block that
     # failed once the matrix is blocked (getrf2 / potrf2 see only that block).
@@ -144,6 +147,8 @@ def getrf(m, n, a, lda, ipiv):
         raise BolaError(f"Argument 4 to getrf had an illegal value of {lda}")
     _check(status, "getrf")
     v = int(info.item())
+    if v == INFO_WAIT_EXPIRED:
+        raise RuntimeError("getrf: a panel's bounded wait on another CTA expired")
     if v > 0:
         raise BolaError(f"Matrix is singular. The pivot in column {_bola_local_column(v, min(m, n))} is zero.")
     return None
@@ -156,6 +161,8 @@ def getrf2(m, n, a, lda, ipiv):
         raise BolaError(f"Argument 4 to getrf2 had an illegal value of {lda}")
     _check(status, "getrf2")
     v = int(info.item())
+    if v == INFO_WAIT_EXPIRED:
+        raise RuntimeError("getrf2: a panel's bounded wait on another CTA expired")
     if v > 0:
         raise BolaError(f"Matrix is singular. The pivot in column {v} is zero.")
     return None
@@ -223,6 +230,15 @@ def profile_read():
         out[name.value.decode()] = {"calls": calls.value, "launches": launches.value, "ms": ms.value,
                                     "flops": fl.value, "bytes": by.value}
     return out
+
+
+def measure_cluster_exchange(csize, nbytes):
+    """Microseconds of one all-to-all exchange round among `csize` cluster CTAs
+    of `nbytes` each (bola_measure_cluster_exchange)."""
+    v = ctypes.c_double(0.0)
+    _check(_lib.load().bola_measure_cluster_exchange(int(csize), int(nbytes), ctypes.byref(v)),
+           "measure_cluster_exchange")
+    return v.value
 
 
 def measure_fp64_peak():

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "sm100.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -222,14 +223,19 @@ struct XSlot {
 };
 
 // The same unblocked LU as panel_lu (BOLA's iterative_getrf2), rows in shared
-// memory, with one split cluster barrier per column instead of a full one and
-// three rounds of remote reads.  Per column j:
+// memory, with no cluster-wide barrier per column: the candidates travel by
+// asynchronous remote stores that count their bytes on the receiver's
+// mbarrier (st.async).  Per column j:
 //   (a) this CTA's candidate in column j is found (BOLA's lane-ordered idamax
 //       keys), one CTA barrier;
 //   (b) every warp pushes the CTA's candidate row (and row j, if owned) into
-//       its share of the cluster's CTAs, one CTA barrier, cluster ARRIVE;
+//       its share of the cluster's CTAs, one CTA barrier;
 //   (c) the rank-1 update of pivot j-1 on columns j+1.. (deferred), while the
-//       other CTAs arrive; cluster WAIT;
+//       pushes land; a bounded wait on this CTA's own mbarrier for all of
+//       them (a CTA pushes column j+1 only after it has read column j's
+//       slots, which keeps the double-buffered slots and mbarrier phases
+//       safe; a push that never lands stops the panel with
+//       *info = BOLA_INFO_WAIT_EXPIRED instead of hanging);
 //   (d) every CTA picks the same winner from its own slots and brings the
 //       pushed rows up to date (the owner's same operation for pivot j-1 on
 //       columns > j), one CTA barrier; zero pivot -> stop as BOLA does;
@@ -249,11 +255,13 @@ panel_lu_split(double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_
   __shared__ double oldj[PNB];    // the old row j, up to date (goes to the pivot's place)
   __shared__ Cand wc[PT / 32];
   __shared__ double sinv;
+  __shared__ uint64_t xbar[2];  // completes when every CTA's push for a column has landed here
+  __shared__ int sfail;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double *data = reinterpret_cast<double *>(smem_raw);
 
   // Uniform across the cluster: the only writer of *info here acts after
-  // the cluster barriers that every CTA passes after this read.
+  // the cluster barrier that every CTA passes after this read.
   if (stop_flag(info)) return;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -266,15 +274,28 @@ panel_lu_split(double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_
     const int c = (int)(e / nr);
     el(c, il) = A[(r0 + il) + (int64_t)c * lda];
   }
+  if (tid == 0) {
+    sm100::mbar_init(&xbar[0], 1);
+    sm100::mbar_init(&xbar[1], 1);
+    sm100::fence_mbar_init();
+    sfail = 0;
+  }
   __syncthreads();
-  cluster.sync();  // every CTA runs before the first push
+  cluster.sync();  // every CTA runs, its mbarriers initialised, before the first push
 
+  // bytes that land in this CTA per column: a slot (header + row) from every
+  // CTA, row j from its owner
+  constexpr uint32_t SLOT_BYTES = 3 * 8 + PNB * 8, ROW_BYTES = PNB * 8;
+  const uint32_t xbytes = (uint32_t)C * SLOT_BYTES + ROW_BYTES;
   const int steps = (int)imin(mp, nb);
   bool failed = false;
   double inv = 0.0;
   for (int j = 0; j < steps; ++j) {
     const int par = j & 1;
     const double *pprev = piv[par ^ 1];
+    // this column's phase of xbar[par] (its previous phase, column j-2, was
+    // waited for by every thread): expect the pushes
+    if (tid == 0) sm100::mbar_arrive_expect_tx(&xbar[par], xbytes);
     // (a)
     Cand best = cand_none();
     for (int64_t il = tid; il < nr; il += PT) {
@@ -297,18 +318,18 @@ panel_lu_split(double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_
       const double cv = (gl >= 0 && lane < nb) ? el(lane, gl) : 0.0;
       const double jv = (own_j && lane < nb) ? el(lane, j - r0) : 0.0;
       for (int d = warp; d < C; d += PT / 32) {
-        XSlot *rs = cluster.map_shared_rank(&slots[par][cr], d);
+        const uint32_t rbar = sm100::cluster_addr(&xbar[par], d);
+        const uint32_t rs = sm100::cluster_addr(&slots[par][cr], d);
         if (lane == 0) {
-          rs->v = cb.v;
-          rs->key = cb.key;
-          rs->g = gl >= 0 ? j + cb.idx : -1;
+          sm100::st_async(rs + offsetof(XSlot, v), (long long)cb.v, rbar);
+          sm100::st_async(rs + offsetof(XSlot, key), (long long)cb.key, rbar);
+          sm100::st_async(rs + offsetof(XSlot, g), (long long)(gl >= 0 ? j + cb.idx : -1), rbar);
         }
-        rs->row[lane] = cv;
-        if (own_j) cluster.map_shared_rank(&rowj[par][0], d)[lane] = jv;
+        sm100::st_async(rs + (uint32_t)offsetof(XSlot, row) + 8u * lane, cv, rbar);
+        if (own_j) sm100::st_async(sm100::cluster_addr(&rowj[par][0], d) + 8u * lane, jv, rbar);
       }
     }
     __syncthreads();  // the rows are read before the deferred update changes them
-    cluster_arrive();
     // (c) pivot j-1 on columns j+1.., rows >= j
     if (j > 0 && j + 1 < nb && j - 1 < steps - 1) {
       const GerStep gs = ger_step(j - 1, nb, mp, lanes);
@@ -322,7 +343,15 @@ panel_lu_split(double *A, int64_t lda, int64_t mp, int nb, int32_t *ipiv, int32_
         }
       }
     }
-    cluster_wait();
+    // every CTA's push for this column has landed (bounded: a push that
+    // never lands stops the panel, never a hang)
+    if (!sm100::bounded_wait(&xbar[par], (uint32_t)(j >> 1) & 1u)) sfail = 1;
+    __syncthreads();
+    if (sfail) {
+      if (tid == 0) atomicCAS(info, 0, BOLA_INFO_WAIT_EXPIRED);
+      failed = true;
+      break;
+    }
     // (d) the winner, identical in every CTA
     Cand wk = cand_none();
     int ws = 0;
@@ -732,6 +761,7 @@ int bola_dgetrf(int64_t m, int64_t n, double *a, int64_t lda, int32_t *ipiv, int
   if (n < 0) return -2;
   if (lda < imax(m, 1)) return -4;  // "Argument 4 to getrf had an illegal value" (src/getrf.rs:41-43)
   if (imin(m, n) > INT32_MAX - 1) return -1;
+  if (info == nullptr) return -6;
   return getrf_blocked((cudaStream_t)stream, m, n, a, lda, ipiv, info);
 }
 
@@ -741,6 +771,7 @@ int bola_dgetrf2(int64_t m, int64_t n, double *a, int64_t lda, int32_t *ipiv, in
   if (m < 0) return -1;
   if (n < 0) return -2;
   if (lda < imax(m, 1)) return -4;  // src/getrf2.rs:43-45
+  if (info == nullptr) return -6;
   {
     ProfScope prof(s, "info_init");
     zero_i32<<<1, 1, 0, s>>>(info);
