@@ -7,11 +7,13 @@
 //   tpanel_kernel   FP32 W: the (n-j) x 64 panel on a cluster of <= 16 CTAs,
 //                   rows in shared memory, pivots chosen by tournament over
 //                   groups of 8 columns (one cluster exchange per group);
-//   spanel_kernel   FP64 W: the same panel with column-by-column partial
-//                   pivoting (each CTA pushes its candidate row into every
-//                   CTA's shared memory with st.async, per column).
-//   Both write L21 as the update's K-major A operand (bf16, tf32 hi/lo, or
-//   the exact bf16 slices of the FP64-accurate factor).
+//                   writes L21 as the update's K-major A operand (bf16 or
+//                   tf32 hi/lo).
+//   FP64 W (the FP64-accurate factor): the same tournament on FP32 copies
+//                   chooses the pivot rows (tpanel_kernel<double>), then
+//                   panel_top64 factors the selected block in FP64 and
+//                   panel_l21_64 the rows below it, writing L21's exact bf16
+//                   slices as the A operand.
 //   sswap_trsm      the 64 interchanges on every other column, U12 = L11^-1 A12
 //                   and the K-major B operand.
 //   tc_update / oz_update   W22 -= L21 U12 on tcgen05 (tc_update.cu, oz_update.cu).
@@ -31,14 +33,7 @@ namespace bola {
 namespace {
 
 constexpr int SNB = 64;   // panel width and update depth
-constexpr int SPT = 256;  // threads per panel CTA
 constexpr int SMAXC = 16;
-
-template <typename T>
-struct alignas(16) SSlot {
-  uint32_t k0, k1, k2, pad;  // pivot key (see PKey)
-  T v[SNB];                  // the candidate row
-};
 
 // Bulk copy of `bytes` (a multiple of 16) from this CTA's shared memory into
 // another CTA's (cluster addresses dst and bar), completing on the
@@ -50,51 +45,6 @@ __device__ __forceinline__ void bulk_push(uint32_t dst, const void *src, uint32_
       : "memory");
 }
 
-// Pivot key, compared lexicographically: the bits of |v| (high word, low
-// word; the low word is 0 for FP32) and ~row, so the largest magnitude wins
-// and ties go to the lowest row; a NaN never wins.
-struct PKey {
-  uint32_t a, b, c;
-};
-__device__ __forceinline__ bool pk_less(const PKey &x, const PKey &y) {
-  return x.a != y.a ? x.a < y.a : (x.b != y.b ? x.b < y.b : x.c < y.c);
-}
-__device__ __forceinline__ PKey pk_make(double v, int g) {
-  // |v| and the NaN test on the bits: an FP64 comparison would take an FP64 pipe slot
-  uint64_t u = (uint64_t)__double_as_longlong(v) & 0x7fffffffffffffffull;
-  u = u > 0x7ff0000000000000ull ? 0ull : u;
-  return PKey{(uint32_t)(u >> 32), (uint32_t)u, 0xFFFFFFFFu - (uint32_t)g};
-}
-__device__ __forceinline__ PKey pk_warp_max(const PKey &k) {
-  const uint32_t a = __reduce_max_sync(0xffffffffu, k.a);
-  const uint32_t b = __reduce_max_sync(0xffffffffu, k.a == a ? k.b : 0u);
-  const uint32_t c = __reduce_max_sync(0xffffffffu, (k.a == a && k.b == b) ? k.c : 0u);
-  return PKey{a, b, c};
-}
-
-// ---- panel arithmetic ---------------------------------------------------------
-// The column-by-column panel kernel works on elements of type S in shared
-// memory, loaded from and stored to W of type G, through these operations
-// (the FP64-accurate factor's panel).
-struct PanelF64 {
-  using S = double;
-  using G = double;
-  static constexpr bool kFP64 = true;
-  __device__ static S zero() { return 0.0; }
-  __device__ static S load(G x) { return x; }
-  __device__ static G store(S x) { return x; }
-  __device__ static S mul(S a, S b) { return a * b; }
-  __device__ static S fnms(S z, S x, S y) { return fma(-x, y, z); }
-  __device__ static bool is_zero(S p) { return !nonzero64(p); }
-  __device__ static S recip(S p) { return nonzero64(p) ? 1.0 / p : 0.0; }
-  __device__ static PKey key(S v, int g) { return pk_make(v, g); }
-  __device__ static double to_double(S v) { return v; }
-  __device__ static uint64_t abs_bits(S v) { return (uint64_t)__double_as_longlong(v) & 0x7fffffffffffffffull; }
-  __device__ static bool is_nan_bits(uint64_t b) { return b > 0x7ff0000000000000ull; }
-  __device__ static uint64_t bits_to_double_bits(uint64_t b) { return b; }
-};
-
-
 // Row pitch of a panel held in shared memory: at least R + 1 and a multiple
 // of the 16-byte vector (4 floats or 2 doubles), so that a lane can move V
 // consecutive rows of a column in one access.
@@ -102,333 +52,8 @@ template <typename T>
 __host__ __device__ constexpr int panel_pitch(int64_t R) {
   return (int)(((R + (int64_t)(16 / sizeof(T))) / (int64_t)(16 / sizeof(T))) * (int64_t)(16 / sizeof(T)));
 }
-__device__ __forceinline__ void vload(double (&v)[2], const double *p) {
-  const double2 t = *reinterpret_cast<const double2 *>(p);
-  v[0] = t.x; v[1] = t.y;
-}
-__device__ __forceinline__ void vstore(double *p, const double (&v)[2]) {
-  *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
-}
 
-// Panel LU of W[0:mp, 0:jb] (W points at the panel's top-left).  ipiv gets
-// global 1-based rows (col0 + local + 1).  CTA cr of the cluster owns panel
-// rows [cr*R, cr*R + R), kept in shared memory column-major with an odd
-// pitch (R + 1) so that both a thread walking its row and a warp walking a
-// column are conflict-free.
-//
-// Per column j: pivot search in column j, one CTA barrier, every warp pushes
-// the CTA's candidate row (and row j if the CTA owns it) into its share of
-// the CTAs with asynchronous remote stores that count their bytes on the
-// receiver's mbarrier (st.async), one CTA barrier; then, while the other
-// CTAs' pushes arrive, the rank-1 update of pivot j-1 on columns j+1..
-// (deferred from the previous column); a wait on this CTA's own mbarrier for
-// every CTA's push (no cluster-wide barrier: a CTA pushes column j+1 only
-// after it has read column j's slots, which is what makes the double-buffered
-// slots safe); every CTA picks the same winner from its own slots and brings
-// the pushed rows up to date (they left before pivot j-1's deferred update
-// reached their columns > j: the same fmaf the owner does); swap; one CTA
-// barrier; the update of column j+1 only (the next pivot column).
-// Multipliers of column j are scaled when column j+1 is searched.  Waits are
-// bounded: a push that never lands sets *err and ends the panel.
-
-template <typename P>
-__global__ void __launch_bounds__(SPT)
-spanel_kernel(typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0, int32_t *info, int kind,
-              void *aop, float *aop_lo, int32_t *aexp, int64_t cap, int64_t R, int32_t *plan, uint64_t *track,
-              double give_up, int32_t *err) {
-  cg::cluster_group cluster = cg::this_cluster();
-  // An abandoned factorisation: the flag was set by an earlier panel on this
-  // stream, so every CTA of the cluster reads the same value.  Identity
-  // pivots keep ipiv valid for the kernels after the factorisation that
-  // compose it (the factor itself is discarded).
-  if (track != nullptr && *(volatile const int32_t *)(track + 2) != 0) {
-    if (cluster.block_rank() == 0)
-      for (int t = threadIdx.x; t < jb; t += blockDim.x) ipiv[t] = col0 + t + 1;
-    return;
-  }
-  const int C = (int)cluster.num_blocks();
-  const int cr = (int)cluster.block_rank();
-  using T = typename P::S;
-  __shared__ SSlot<T> slots[2][SMAXC];
-  __shared__ T rowj[2][SNB];
-  __shared__ T piv[2][SNB];   // pivot rows, up to date (piv[par] = column j's)
-  __shared__ T oldj[SNB];     // the old row j, up to date (goes to the pivot's place)
-  __shared__ PKey wkey[SPT / 32];
-  __shared__ T sinv;          // 1 / pivot of the current column
-  __shared__ uint64_t xbar[2];  // completes when every CTA's push for a column has landed here
-  __shared__ int sfail;
-  extern __shared__ __align__(16) unsigned char sp_raw[];
-  T *sp = reinterpret_cast<T *>(sp_raw);
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int RP = panel_pitch<T>(R);
-  const int r0 = (int)(cr * R);
-  const int r1 = (int)imin(mp, r0 + R);
-  const int nr = r1 > r0 ? r1 - r0 : 0;
-  // element (row il, column c) of this CTA's rows, in shared memory
-  auto PE = [&](int c, int il) -> T & { return sp[c * RP + il]; };
-  const int ns = nr;
-
-  // a thread's rows, 16 columns at a time, all of those loads in flight together
-  for (int il0 = tid; il0 < ns; il0 += 2 * SPT) {
-    const int il1 = il0 + SPT;
-    for (int c0 = 0; c0 < jb; c0 += 16) {
-      typename P::G t0[16], t1[16];
-#pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        t0[c] = c0 + c < jb ? W[(r0 + il0) + (int64_t)(c0 + c) * ldw] : typename P::G(0);
-        t1[c] = (il1 < ns && c0 + c < jb) ? W[(r0 + il1) + (int64_t)(c0 + c) * ldw] : typename P::G(0);
-      }
-#pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        if (c0 + c >= jb) break;
-        sp[(c0 + c) * RP + il0] = P::load(t0[c]);
-        if (il1 < ns) sp[(c0 + c) * RP + il1] = P::load(t1[c]);
-      }
-    }
-  }
-  if (tid == 0) {
-    sm100::mbar_init(&xbar[0], 1);
-    sm100::mbar_init(&xbar[1], 1);
-    sm100::fence_mbar_init();
-    sfail = 0;
-  }
-  __syncthreads();
-  cluster.sync();  // every CTA runs, its mbarriers initialised, before the first push
-  // bytes that land in this CTA per column: a slot from every CTA, row j from its owner
-  constexpr uint32_t SLOT_BYTES = 16 + SNB * sizeof(T), ROW_BYTES = SNB * sizeof(T);
-  const uint32_t xbytes = (uint32_t)C * SLOT_BYTES + ROW_BYTES;
-  bool failed = false;
-
-  T inv = P::zero();  // 1 / pivot of the previous column
-  // |u_jj| of this panel's pivots as ordered integer bits (NaN ignored, as
-  // fmax/fmin ignore it): thread 0 of CTA 0 only, on the integer pipe
-  uint64_t umax = 0, umin = ~0ull;
-  for (int j = 0; j < jb; ++j) {
-    const int par = j & 1;
-    const T *pprev = piv[par ^ 1];
-    // this column's phase of xbar[par] (its previous phase, column j-2, was
-    // waited for by every thread): expect the pushes
-    if (tid == 0) sm100::mbar_arrive_expect_tx(&xbar[par], xbytes);
-    // -- the multipliers of column j-1, then this CTA's pivot candidate in
-    // column j: key = (|v| bits, ~row), max wins, ties -> lowest row
-    PKey best = PKey{0u, 0u, 0u};
-    for (int il = tid; il < nr; il += SPT) {
-      const int g = r0 + il;
-      if (j > 0 && g >= j) PE(j - 1, il) = P::mul(PE(j - 1, il), inv);
-      if (g < j) continue;
-      const PKey k = P::key(PE(j, il), g);
-      if (pk_less(best, k)) best = k;
-    }
-    best = pk_warp_max(best);
-    if (lane == 0) wkey[warp] = best;
-    __syncthreads();
-    // -- every warp pushes the candidate (and row j if owned) to its share of the CTAs
-    {
-      PKey ck = wkey[0];
-#pragma unroll
-      for (int w = 1; w < SPT / 32; ++w)
-        if (pk_less(ck, wkey[w])) ck = wkey[w];
-      const int gl = ck.c ? (int)(0xFFFFFFFFu - ck.c) - r0 : -1;  // local row of the candidate
-      const bool own_j = j >= r0 && j < r1;
-      const int jl = j - r0;
-      T c0 = P::zero(), c1 = P::zero(), j0v = P::zero(), j1v = P::zero();
-      if (gl >= 0) {
-        c0 = lane < jb ? PE(lane, gl) : P::zero();
-        c1 = lane + 32 < jb ? PE(lane + 32, gl) : P::zero();
-      }
-      if (own_j) {
-        j0v = lane < jb ? PE(lane, jl) : P::zero();
-        j1v = lane + 32 < jb ? PE(lane + 32, jl) : P::zero();
-      }
-      for (int d = warp; d < C; d += SPT / 32) {
-        const uint32_t rbar = sm100::cluster_addr(&xbar[par], d);
-        const uint32_t rs = sm100::cluster_addr(&slots[par][cr], d);
-        if (lane == 0) sm100::st_async4(rs, ck.a, ck.b, ck.c, 0u, rbar);
-        sm100::st_async(rs + 16 + lane * (uint32_t)sizeof(T), c0, rbar);
-        sm100::st_async(rs + 16 + (lane + 32) * (uint32_t)sizeof(T), c1, rbar);
-        if (own_j) {
-          const uint32_t rj = sm100::cluster_addr(&rowj[par][0], d);
-          sm100::st_async(rj + lane * (uint32_t)sizeof(T), j0v, rbar);
-          sm100::st_async(rj + (lane + 32) * (uint32_t)sizeof(T), j1v, rbar);
-        }
-      }
-    }
-    __syncthreads();  // the rows are read before the deferred update changes them
-    // -- the deferred rank-1 update of pivot j-1 on columns j+1..jb-1, rows >= j:
-    // lanes walk rows, warps take every 8th column; the pivot-row values sit
-    // in registers, so a thread's 8 loads are all in flight together
-    if (j > 0 && j + 1 < jb) {
-      T pr[8];
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const int c = j + 1 + warp + 8 * q;
-        pr[q] = c < jb ? pprev[c] : P::zero();
-      }
-      // 16-byte shared-memory accesses: a lane takes V consecutive rows
-      constexpr int V = 16 / (int)sizeof(T);
-      const int ib = j > r0 ? j - r0 : 0;
-      for (int il0 = (ib & ~(V - 1)) + lane * V; il0 < nr; il0 += 32 * V) {
-        T l[V];
-        vload(l, &sp[(j - 1) * RP + il0]);
-        bool on[V];
-#pragma unroll
-        for (int e = 0; e < V; ++e) on[e] = il0 + e >= ib && il0 + e < nr;
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int c = j + 1 + warp + 8 * q;
-          if (c >= jb) continue;
-          T v[V];
-          vload(v, &sp[c * RP + il0]);
-#pragma unroll
-          for (int e = 0; e < V; ++e)
-            if (on[e]) v[e] = P::fnms(v[e], l[e], pr[q]);
-          vstore(&sp[c * RP + il0], v);
-        }
-      }
-    }
-    // every CTA's push for this column has landed (bounded: a missing push
-    // sets the error flag and ends the panel, never a hang)
-    {
-      const bool ok = sm100::bounded_wait(&xbar[par], (uint32_t)(j >> 1) & 1u);
-      if (!ok) sfail = 1;
-      __syncthreads();
-      if (sfail) {
-        if (tid == 0) atomicExch(err, 5);
-        failed = true;
-        break;
-      }
-    }
-    // -- the winner, identical in every CTA: lane s reads slot s, warp max
-    PKey wk;
-    int ws = 0;
-    {
-      const PKey k = lane < C ? PKey{slots[par][lane].k0, slots[par][lane].k1, slots[par][lane].k2} : PKey{0u, 0u, 0u};
-      wk = pk_warp_max(k);
-      const unsigned m = __ballot_sync(0xffffffffu, lane < C && k.a == wk.a && k.b == wk.b && k.c == wk.c);
-      ws = m ? __ffs(m) - 1 : 0;
-    }
-    const int jp = wk.c ? (int)(0xFFFFFFFFu - wk.c) : j;
-    const T *raw = wk.c ? slots[par][ws].v : rowj[par];
-    T *pcur = piv[par];
-    // the pushed rows, brought up to date: columns > j still lack pivot j-1
-    if (tid < jb) {
-      T pv_ = raw[tid], ov = rowj[par][tid];
-      if (j > 0 && tid > j) {
-        pv_ = P::fnms(pv_, raw[j - 1], pprev[tid]);
-        ov = P::fnms(ov, rowj[par][j - 1], pprev[tid]);
-      }
-      pcur[tid] = pv_;
-      oldj[tid] = ov;
-      if (tid == j) sinv = P::recip(pv_);  // once per CTA, not once per thread
-    }
-    __syncthreads();
-    const T pv = pcur[j];
-    if (cr == 0 && tid == 0) {
-      ipiv[j] = col0 + jp + 1;
-      const uint64_t ab = P::abs_bits(pv);
-      if (!P::is_nan_bits(ab)) {
-        umax = ab > umax ? ab : umax;
-        umin = ab < umin ? ab : umin;
-      }
-    }
-    inv = sinv;
-    if (P::is_zero(pv)) {
-      if (cr == 0 && tid == 0) atomicCAS(info, 0, col0 + j + 1);
-    }
-    if (jp != j && tid < jb) {
-      if (j >= r0 && j < r1) PE(tid, j - r0) = pcur[tid];
-      if (jp >= r0 && jp < r1) PE(tid, jp - r0) = oldj[tid];
-    }
-    __syncthreads();
-    // -- the next pivot column now (the rest of this update is deferred);
-    // same row-to-thread map as the search, so no barrier before it
-    if (j + 1 < jb) {
-      const T pj1 = pcur[j + 1];
-      for (int il = tid; il < nr; il += SPT) {
-        if (r0 + il <= j) continue;
-        T &x = PE(j + 1, il);
-        x = P::fnms(x, P::mul(PE(j, il), inv), pj1);
-      }
-    }
-  }
-  if (!failed) {  // (after a failed exchange the error flag fails the whole call)
-  // the last column's multipliers
-  for (int il = tid; il < nr; il += SPT)
-    if (r0 + il >= jb) PE(jb - 1, il) = P::mul(PE(jb - 1, il), inv);
-  __syncthreads();
-  if (track != nullptr && cr == 0 && tid == 0) {
-    // the running extent of |u_ii| and the give-up test (the spread only grows
-    // as pivots are added, so giving up early decides as the whole factor would)
-    if (umin != ~0ull) {
-      const uint64_t mx = P::bits_to_double_bits(umax), mn = P::bits_to_double_bits(umin);
-      if (mx > track[0]) track[0] = mx;
-      if (mn < track[1]) track[1] = mn;
-    }
-    const double gmx = __longlong_as_double((long long)track[0]), gmn = __longlong_as_double((long long)track[1]);
-    const double spread = gmn > 0.0 ? gmx / gmn : INFINITY;
-    if (give_up_now(spread, give_up, col0 + jb, col0 + mp)) *(volatile int32_t *)(track + 2) = 1;
-  }
-
-  // -- write back the panel and the update's A operand (rows below the panel)
-  for (int il = tid; il < ns; il += SPT) {
-    typename P::G *wr = W + (r0 + il);
-#pragma unroll 8
-    for (int c = 0; c < jb; ++c) wr[(int64_t)c * ldw] = P::store(sp[c * RP + il]);
-  }
-  if (plan != nullptr && cr == 0 && warp == 0) {
-    // the panel's interchanges as "row rows[t] takes the old row src[t]",
-    // composed once here for the swap kernel that follows
-    __syncwarp();
-    SwapPlan p;
-    p.ix0 = 0;
-    p.i1 = col0 + 1;
-    p.i2 = col0 + jb;
-    p.i_inc = 1;
-    p.incx = 1;
-    const int cnt = compose_swaps_warp<4, int32_t>(p, ipiv, plan + 1, plan + 1 + 2 * SNB);
-    if (lane == 0) plan[0] = cnt;
-  }
-  if (aop != nullptr) {
-    for (int il = tid; il < nr; il += SPT) {
-      const int g = r0 + il;
-      if (g < jb) continue;
-      if constexpr (!P::kFP64) {
-        float v[SNB];
-#pragma unroll
-        for (int c = 0; c < SNB; ++c) v[c] = c < jb ? PE(c, il) : 0.f;
-        write_operand_row(kind, aop, aop_lo, g - jb, v);
-      } else {
-        // exact bf16 slices of the row (FP64 factor): exponent, then 8 K values at a time
-        uint64_t mb = 0;
-        for (int c = 0; c < jb; ++c) {
-          const uint64_t mc = oz_mag(P::to_double(PE(c, il)));
-          mb = mc > mb ? mc : mb;
-        }
-        const int e = oz_exponent(mb);
-        aexp[g - jb] = e;
-        __nv_bfloat16 *out = static_cast<__nv_bfloat16 *>(aop);
-        for (int c0 = 0; c0 < SNB; c0 += 8) {
-          __align__(16) __nv_bfloat16 q[OZ_SLICES][8];
-#pragma unroll
-          for (int u = 0; u < 8; ++u) {
-            __nv_bfloat16 t8[OZ_SLICES];
-            oz_slices(c0 + u < jb ? P::to_double(PE(c0 + u, il)) : 0.0, e, t8);
-#pragma unroll
-            for (int t = 0; t < OZ_SLICES; ++t) q[t][u] = t8[t];
-          }
-#pragma unroll
-          for (int t = 0; t < OZ_SLICES; ++t)
-            *reinterpret_cast<uint4 *>(out + ((int64_t)t * cap + (g - jb)) * SNB + c0) =
-                *reinterpret_cast<const uint4 *>(q[t]);
-        }
-      }
-    }
-  }
-  }
-  cluster.sync();  // no CTA leaves while another may still push into it
-}
-
-// ---- tournament panel (the FP32 factors) ----------------------------------------
+// ---- tournament panel (the FP32 factors; pivot selection of the FP64 one) ----------------------------------------
 // Partial pivoting exchanges the pivot candidates of every CTA once per
 // column, so a cluster panel pays 64 cluster round trips.  The FP32 factors
 // (kinds 0-2) select their pivots by tournament instead (TSLU, the panel
@@ -537,6 +162,41 @@ __device__ __forceinline__ int warp_gepp(float (&v)[RPL][TG], bool (&live)[RPL],
   return cnt;
 }
 
+// LAPACK's interchanges for a panel whose pivot of column j is panel row
+// win[j] (j < jb): ipg[j] = col0 + 1 + the position row j swaps with.  Rows
+// below the panel's first jb never move until they become a pivot; rows among
+// the first jb are tracked: at_[q] = the row now in position q < jb,
+// posin[x] = the position of original row x < jb.  One thread.
+__device__ __forceinline__ void pivots_to_interchanges(const int32_t *win, int jb, int32_t col0, int32_t *posin,
+                                                       int32_t *at_, int32_t *ipg) {
+  for (int x = 0; x < jb; ++x) posin[x] = at_[x] = x;
+  for (int j = 0; j < jb; ++j) {
+    const int x = win[j];
+    const int q = x < jb ? posin[x] : x;
+    ipg[j] = col0 + q + 1;
+    const int r = at_[j];
+    if (r != x) {
+      if (q < jb) at_[q] = r;
+      posin[r] = q;
+    }
+    at_[j] = x;
+    if (x < jb) posin[x] = j;
+  }
+}
+
+// The interchanges ipg (global, 1-based) as "row rows[t] takes the old row
+// src[t]" for the swap kernel: plan[0] = count, then rows, then src.  Warp 0.
+__device__ __forceinline__ void compose_panel_plan(const int32_t *ipg, int jb, int32_t col0, int32_t *plan) {
+  SwapPlan p;
+  p.ix0 = 0;
+  p.i1 = col0 + 1;
+  p.i2 = col0 + jb;
+  p.i_inc = 1;
+  p.incx = 1;
+  const int cnt = compose_swaps_warp<4, int32_t>(p, ipg, plan + 1, plan + 1 + 2 * SNB);
+  if ((threadIdx.x & 31) == 0) plan[0] = cnt;
+}
+
 // Dynamic shared memory of the tournament panel: the rows (column-major,
 // pitch RP, 64 columns, zero beyond jb), the double-buffered nominee slots
 // (C x TG per buffer) and the row states.
@@ -558,9 +218,17 @@ __device__ __forceinline__ float rank8(float a, const float (&l)[TG], const floa
   return a;
 }
 
+// G = float: the FP32 factors' panel (factored in place).  G = double: the
+// FP64-accurate factor's pivot selection only — the tournament runs on FP32
+// copies of the panel's values and writes the jb pivot rows (panel rows, in
+// column order) to winout; W, ipiv, info and the operands are left to the
+// FP64 kernels that follow (panel_top64, panel_l21_64).
+template <typename G>
 __global__ void __launch_bounds__(TPT, 1)
-tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0, int32_t *info, int kind,
-              void *aop, float *aop_lo, int64_t R, int32_t *plan, uint64_t *track, double give_up, int32_t *err) {
+tpanel_kernel(G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0, int32_t *info, int kind,
+              void *aop, float *aop_lo, int64_t R, int32_t *plan, uint64_t *track, double give_up, int32_t *err,
+              int32_t *winout) {
+  constexpr bool SEL = std::is_same<G, double>::value;
   cg::cluster_group cluster = cg::this_cluster();
   // an abandoned factorisation (flag set by an earlier panel on this stream,
   // so every CTA reads the same value): identity pivots keep ipiv valid
@@ -606,7 +274,7 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
       const int il = tid + TPT * r;
 #pragma unroll
       for (int c = 0; c < 32; ++c)
-        t[r][c] = (il < nr && c0 + c < jb) ? W[(r0 + il) + (int64_t)(c0 + c) * ldw] : 0.f;
+        t[r][c] = (il < nr && c0 + c < jb) ? (float)W[(r0 + il) + (int64_t)(c0 + c) * ldw] : 0.f;
     }
 #pragma unroll
     for (int r = 0; r < TRPL; ++r) {
@@ -802,7 +470,7 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
     if (cr == 0 && tid == TPT - 1) {
       for (int t = 0; t < gw; ++t) {
         const float pv = UgT[ub][c0 + t][t];
-        if (pv == 0.f) atomicCAS(info, 0, col0 + c0 + t + 1);
+        if (!SEL && pv == 0.f) atomicCAS(info, 0, col0 + c0 + t + 1);
         const uint64_t ab = __float_as_uint(pv) & 0x7fffffffu;
         if (ab <= 0x7f800000u) {
           umax = ab > umax ? ab : umax;
@@ -846,25 +514,14 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
     __syncthreads();
   }
   if (!failed) {
+    if constexpr (SEL) {
+      if (cr == 0)
+        for (int t = tid; t < jb; t += TPT) winout[t] = win[t];
+    } else {
     // -- the interchanges (CTA 0): LAPACK's sequence of row swaps that puts
-    // the pivot of column j in row j, from the pivot list.  Rows below the
-    // panel's first jb never move until they become a pivot; rows among the
-    // first jb are tracked: at_[q] = the row now in position q < jb,
-    // posin[x] = the position of original row x < jb.
+    // the pivot of column j in row j, from the pivot list
     if (cr == 0 && tid == 0) {
-      for (int x = 0; x < jb; ++x) posin[x] = at_[x] = x;
-      for (int j = 0; j < jb; ++j) {
-        const int x = win[j];
-        const int q = x < jb ? posin[x] : x;
-        ipg[j] = col0 + q + 1;
-        const int r = at_[j];
-        if (r != x) {
-          if (q < jb) at_[q] = r;
-          posin[r] = q;
-        }
-        at_[j] = x;
-        if (x < jb) posin[x] = j;
-      }
+      pivots_to_interchanges(win, jb, col0, posin, at_, ipg);
       for (int j = 0; j < jb; ++j) ipiv[j] = ipg[j];
     }
     __syncthreads();
@@ -891,21 +548,11 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
     for (int r = 0; r < TRPL; ++r) {
       const int il = tid + TPT * r;
       if (il >= nr) continue;
-      float *wr = W + dest(il);
+      G *wr = W + dest(il);
 #pragma unroll 8
       for (int c = 0; c < jb; ++c) wr[(int64_t)c * ldw] = sp[c * RP + il];
     }
-    if (plan != nullptr && cr == 0 && warp == 0) {
-      // the interchanges as "row rows[t] takes the old row src[t]" for the swap kernel
-      SwapPlan p;
-      p.ix0 = 0;
-      p.i1 = col0 + 1;
-      p.i2 = col0 + jb;
-      p.i_inc = 1;
-      p.incx = 1;
-      const int cnt = compose_swaps_warp<4, int32_t>(p, ipg, plan + 1, plan + 1 + 2 * SNB);
-      if (lane == 0) plan[0] = cnt;
-    }
+    if (plan != nullptr && cr == 0 && warp == 0) compose_panel_plan(ipg, jb, col0, plan);
     if (aop != nullptr) {  // rows below the panel's top: the update's K-major A operand
       for (int il = tid; il < nr; il += TPT) {
         const int dst = dest(il);
@@ -916,14 +563,16 @@ tpanel_kernel(float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t 
         write_operand_row(kind, aop, aop_lo, dst - jb, v);
       }
     }
+    }
   }
   if (tid < C) sm100::bulk_wait_read0();  // this CTA's last pushes have read its staging slots
   cluster.sync();  // no CTA leaves while another may still push into it
 }
 
-int launch_tpanel(cudaStream_t s, float *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0,
+template <typename G>
+int launch_tpanel(cudaStream_t s, G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0,
                   int32_t *info, int kind, void *aop, float *aop_lo, int32_t *plan, uint64_t *track, double give_up,
-                  int32_t *err) {
+                  int32_t *err, int32_t *winout = nullptr) {
   const int C = (int)imin(SMAXC, imax(1, cdiv(mp, TPT)));
   const int64_t R = cdiv(mp, C);
   // CTA 0 must hold the panel's first jb rows (the interchange bookkeeping)
@@ -932,8 +581,8 @@ int launch_tpanel(cudaStream_t s, float *W, int64_t ldw, int64_t mp, int jb, int
   const size_t smem = tpanel_smem(R, C);
   static bool attr = false;
   if (!attr) {
-    BOLA_TRY_CUDA(cudaFuncSetAttribute(tpanel_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    BOLA_TRY_CUDA(cudaFuncSetAttribute(tpanel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    BOLA_TRY_CUDA(cudaFuncSetAttribute(tpanel_kernel<G>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    BOLA_TRY_CUDA(cudaFuncSetAttribute(tpanel_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)tpanel_smem(TPT * TRPL, SMAXC)));
     attr = true;
   }
@@ -949,10 +598,295 @@ int launch_tpanel(cudaStream_t s, float *W, int64_t ldw, int64_t mp, int jb, int
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  ProfScope prof(s, "tpanel", (double)mp * jb * jb, 8.0 * (double)mp * jb);
-  BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, tpanel_kernel, W, ldw, mp, jb, ipiv, col0, info, kind, aop, aop_lo, R, plan,
-                                   track, give_up, err));
+  ProfScope prof(s, std::is_same<G, double>::value ? "tselect64" : "tpanel", (double)mp * jb * jb,
+                 8.0 * (double)mp * jb);
+  BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, tpanel_kernel<G>, W, ldw, mp, jb, ipiv, col0, info, kind, aop, aop_lo, R,
+                                   plan, track, give_up, err, winout));
   return 0;
+}
+
+// ---- the FP64-accurate factor's panel ------------------------------------------
+// Column-by-column partial pivoting in FP64 costs, per column, a cluster
+// exchange, four CTA barriers and the column's FP64 update confined to the
+// panel's CTAs.  The FP64-storage factor splits its panel instead, as
+// communication-avoiding LU (CALU) does:
+//   1. tpanel_kernel<double> chooses the jb pivot rows by tournament on FP32
+//      copies of the panel (W's column blocks are scaled to O(1), and FP32
+//      is ample for choosing pivots);
+//   2. panel_top64 factors the selected jb x jb block in FP64 with partial
+//      pivoting among its rows (CALU's final step), derives LAPACK's
+//      interchanges, moves the rows they displace and tracks the pivots;
+//   3. panel_l21_64 forms L21 = A21 U11^-1 in FP64 for every row below, on
+//      as many SMs as there are rows, and writes the update's operand (exact
+//      bf16 slices of each row of L21).
+
+// 1 / p for the FP64 panel's pivots without the long-latency division:
+// Newton's iteration for the reciprocal, r <- r (2 - p r), from the FP32
+// reciprocal as its seed (relative error 2^-23 -> 2^-46 -> below 2^-52 after
+// two steps); plain division where p or 1/p lies outside the range in which
+// the FP32 seed is a normal number.
+__device__ __forceinline__ double recip64(double p) {
+  const double ap = fabs(p);
+  if (!(ap > 1e-30 && ap < 1e30)) return 1.0 / p;
+  double r = (double)__frcp_rn((float)p);
+  r = r * fma(-p, r, 2.0);
+  r = r * fma(-p, r, 2.0);
+  return r;
+}
+
+// Step 2 of the panel above for one panel (Wp: its top-left, rows
+// col0.. of W).  One CTA of 256 threads; the block lives in shared memory and
+// its rows never move: a flag marks the rows that are pivots already, and
+// the pivot order is kept as a list.  Thread (q, g) owns block row q = tid %
+// 64 in the columns c = g (mod 4), g = tid / 64.  Per column k, after one
+// barrier every thread forms its row's multiplier and updates column k + 1;
+// after a second, warps 0-1 search column k + 1 and form the reciprocal of
+// its pivot while every thread updates its remaining columns (look-ahead:
+// the search and the reciprocal leave the critical path).
+__global__ void __launch_bounds__(256)
+panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int32_t *win_in, int32_t *plan,
+            int32_t *ipiv, int32_t *info, uint64_t *track, double give_up, int32_t *err) {
+  // an abandoned factorisation (flag set by an earlier panel on this stream):
+  // identity pivots keep ipiv valid for the kernels that compose it
+  if (track != nullptr && *(volatile const int32_t *)(track + 2) != 0) {
+    for (int t = threadIdx.x; t < jb; t += blockDim.x) ipiv[t] = col0 + t + 1;
+    return;
+  }
+  __shared__ double a[SNB][SNB + 1];  // a[c][q]: column c of block row q
+  __shared__ int32_t win[SNB], order[SNB], pivl[SNB], posin[SNB], at_[SNB], ipg[SNB], rows_s[2 * SNB],
+      src_s[2 * SNB];
+  __shared__ uint8_t isp[SNB];         // block row q is a pivot already
+  __shared__ double rinv_s[2];         // reciprocal of the pivot of column k (k & 1)
+  __shared__ int piv_s[2];             // block row of the pivot of column k (k & 1)
+  __shared__ uint64_t pkey[2][2];      // the two search warps' best keys (parity, warp)
+  __shared__ int pq[2][2];
+  __shared__ int bad, cnt_s;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int q = tid & (SNB - 1), g = tid >> 6;
+  if (tid == 0) bad = 0;
+  __syncthreads();
+  for (int t = tid; t < jb; t += 256) {
+    win[t] = win_in[t];
+    isp[t] = 0;
+    // a selection that did not finish (its exchange gave up and set the
+    // error word) leaves no valid list: stop here rather than index W with it
+    if (win[t] < 0 || win[t] >= mp) atomicExch(&bad, 1);
+  }
+  __syncthreads();
+  if (bad != 0) {
+    if (tid == 0) atomicExch(err, 7);
+    for (int t = tid; t < jb; t += 256) ipiv[t] = col0 + t + 1;
+    return;
+  }
+  // the selected rows, all of a thread's loads in flight together
+  {
+    constexpr int PER = SNB * SNB / 256;
+    double v[PER];
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+      const int e = tid + 256 * u, r = e % SNB, c = e / SNB;
+      v[u] = (r < jb && c < jb) ? Wp[win[r] + (int64_t)c * ldw] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+      const int e = tid + 256 * u;
+      a[e / SNB][e % SNB] = v[u];
+    }
+  }
+  __syncthreads();
+  uint64_t umax = 0, umin = ~0ull;  // |u_kk| bits (thread 0)
+  // the largest |a[c][r]| over rows r that are not pivots (ties: lowest r; a
+  // NaN never wins), by warps 0 and 1 (rows 32 w + lane); the result, with
+  // the reciprocal of the pivot, goes to slot par
+  auto search = [&](int c, int par) {
+    const int r = warp * 32 + lane;
+    uint64_t key = 0;
+    if (r < jb && !isp[r]) {
+      const uint64_t b = (uint64_t)__double_as_longlong(a[c][r]) & 0x7fffffffffffffffull;
+      key = b > 0x7ff0000000000000ull ? 0 : b;
+    }
+    int kr = r;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const uint64_t ok = __shfl_xor_sync(0xffffffffu, key, off);
+      const int orr = __shfl_xor_sync(0xffffffffu, kr, off);
+      if (ok > key || (ok == key && orr < kr)) {
+        key = ok;
+        kr = orr;
+      }
+    }
+    if (lane == 0) {
+      pkey[par][warp] = key;
+      pq[par][warp] = kr;
+    }
+    asm volatile("bar.sync 1, 64;" ::: "memory");  // warps 0 and 1
+    if (tid == 0) {
+      int p = pq[par][0];
+      if (pkey[par][1] > pkey[par][0]) p = pq[par][1];
+      // an all-zero (or all-NaN) column: the first row that is not a pivot yet
+      if ((pkey[par][0] | pkey[par][1]) == 0)
+        for (p = 0; p < jb && isp[p]; ++p) {
+        }
+      const double pv = a[c][p];
+      const uint64_t ab = (uint64_t)__double_as_longlong(pv) & 0x7fffffffffffffffull;
+      if (ab == 0) atomicCAS(info, 0, col0 + c + 1);
+      if (ab <= 0x7ff0000000000000ull) {
+        umax = ab > umax ? ab : umax;
+        umin = ab < umin ? ab : umin;
+      }
+      piv_s[par] = p;
+      rinv_s[par] = ab != 0 ? recip64(pv) : 0.0;
+    }
+  };
+  if (warp < 2) search(0, 0);
+  __syncthreads();
+  for (int k = 0; k < jb; ++k) {
+    const int par = k & 1;
+    const int p = piv_s[par];
+    const double ri = rinv_s[par];
+    // row q's multiplier and the update of column k + 1 (the next one searched)
+    const bool act = q < jb && !isp[q] && q != p;
+    double l = 0.0;
+    if (act) {
+      l = a[k][q] * ri;  // (all four threads of the row read a[k][q]; it is replaced after the barrier)
+      if (k + 1 < jb && ((k + 1) & 3) == g) a[k + 1][q] = fma(-l, a[k + 1][p], a[k + 1][q]);
+    }
+    if (tid == 0) {
+      isp[p] = 1;
+      order[k] = p;
+    }
+    __syncthreads();
+    if (k + 1 < jb && warp < 2) search(k + 1, par ^ 1);
+    if (act) {
+      if (g == 0) a[k][q] = l;
+      for (int c = ((k + 2 + 3 - g) & ~3) + g; c < jb; c += 4)  // c = g (mod 4), c >= k + 2
+        a[c][q] = fma(-l, a[c][p], a[c][q]);
+    }
+    __syncthreads();
+  }
+  // LAPACK's interchanges from the final pivot order, and the plan for the
+  // swap kernel
+  if (tid == 0) {
+    for (int t = 0; t < jb; ++t) pivl[t] = win[order[t]];  // panel row of the pivot of column t
+    pivots_to_interchanges(pivl, jb, col0, posin, at_, ipg);
+  }
+  __syncthreads();
+  if (warp == 0) compose_panel_plan(ipg, jb, col0, plan);
+  for (int t = tid; t < jb; t += 256) ipiv[t] = ipg[t];
+  __syncthreads();
+  // rows the interchanges move below the block: their panel columns, read
+  // before anything is written
+  if (tid == 0) cnt_s = plan[0];
+  for (int t = tid; t < 2 * SNB; t += 256) {
+    rows_s[t] = plan[1 + t] - col0;
+    src_s[t] = plan[1 + 2 * SNB + t] - col0;
+  }
+  __syncthreads();
+  const int cnt = cnt_s;
+  constexpr int MV = 2 * SNB * SNB / 256;
+  double mv[MV];
+#pragma unroll
+  for (int u = 0; u < MV; ++u) {
+    const int e = tid + 256 * u, t = e % (2 * SNB), c = e / (2 * SNB);
+    mv[u] = (t < cnt && c < jb && rows_s[t] >= jb) ? Wp[src_s[t] + (int64_t)c * ldw] : 0.0;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < MV; ++u) {
+    const int e = tid + 256 * u, t = e % (2 * SNB), c = e / (2 * SNB);
+    if (t < cnt && c < jb && rows_s[t] >= jb) Wp[rows_s[t] + (int64_t)c * ldw] = mv[u];
+  }
+  // the factored block in pivot order (unit-lower L11 below the diagonal, U11
+  // on and above)
+  for (int e = tid; e < jb * jb; e += 256) {
+    const int r = e % jb, c = e / jb;
+    Wp[r + (int64_t)c * ldw] = a[c][order[r]];
+  }
+  if (track != nullptr && tid == 0) {
+    // the running extent of |u_ii| and the give-up test
+    if (umin != ~0ull) {
+      if (umax > track[0]) track[0] = umax;
+      if (umin < track[1]) track[1] = umin;
+    }
+    const double gmx = __longlong_as_double((long long)track[0]), gmn = __longlong_as_double((long long)track[1]);
+    const double spread = gmn > 0.0 ? gmx / gmn : INFINITY;
+    if (give_up_now(spread, give_up, col0 + jb, col0 + mp)) *(volatile int32_t *)(track + 2) = 1;
+  }
+}
+
+// L21 = A21 U11^-1 (rows jb..mp-1 of the panel, after its interchanges) in
+// FP64, and the update's operand.  Two lanes per row, lane h holding columns
+// 2i + h: the substitution's chain runs over the columns, and every FP64
+// warp instruction has all 32 lanes busy (on GB300 an FP64 instruction takes
+// its full issue slot whatever the number of active lanes).  64 rows per CTA.
+constexpr int L21_ROWS = 64;
+__global__ void __launch_bounds__(128)
+panel_l21_64(double *Wp, int64_t ldw, int64_t mp, int jb, void *aop, int32_t *aexp, int64_t cap,
+             const int32_t *abort) {
+  if (abort != nullptr && *(volatile const int32_t *)abort != 0) return;  // set before this launch (same stream)
+  __shared__ double U[SNB][SNB];  // U[k][c], zero outside the upper triangle of the jb x jb block
+  __shared__ double rinv[SNB];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, h = lane & 1;
+  for (int e = tid; e < SNB * SNB; e += 128) {
+    const int k = e % SNB, c = e / SNB;
+    U[k][c] = (k <= c && c < jb) ? Wp[k + (int64_t)c * ldw] : 0.0;
+  }
+  __syncthreads();
+  if (tid < SNB) {
+    const double d = U[tid][tid];
+    rinv[tid] = (tid < jb && (__double_as_longlong(d) << 1) != 0) ? 1.0 / d : 0.0;
+  }
+  __syncthreads();
+  const int64_t r = jb + (int64_t)blockIdx.x * L21_ROWS + warp * 16 + (lane >> 1);
+  const bool live = r < mp;
+  double x[SNB / 2];
+#pragma unroll
+  for (int i = 0; i < SNB / 2; ++i) {
+    const int c = 2 * i + h;
+    x[i] = (live && c < jb) ? Wp[r + (int64_t)c * ldw] : 0.0;
+  }
+#pragma unroll
+  for (int k = 0; k < SNB; ++k) {
+    const int ik = k >> 1, hk = k & 1;
+    const double mine = x[ik] * rinv[k];  // (the owner's value is l_rk)
+    const double lk = __shfl_sync(0xffffffffu, mine, (lane & ~1) | hk);
+    if (h == hk) x[ik] = lk;
+#pragma unroll
+    for (int i = ik; i < SNB / 2; ++i) {
+      // column 2i + h > k: every i > ik, and at i == ik the odd column of an even k
+      if (i > ik || (hk == 0 && h == 1)) x[i] = fma(-lk, U[k][2 * i + h], x[i]);
+    }
+  }
+  if (live) {
+#pragma unroll
+    for (int i = 0; i < SNB / 2; ++i) {
+      const int c = 2 * i + h;
+      if (c < jb) Wp[r + (int64_t)c * ldw] = x[i];
+    }
+  }
+  if (aop != nullptr) {
+    // exact bf16 slices of the row: one exponent for its 64 values
+    uint64_t mb = 0;
+#pragma unroll
+    for (int i = 0; i < SNB / 2; ++i) {
+      const uint64_t m = oz_mag(x[i]);
+      mb = m > mb ? m : mb;
+    }
+    const uint64_t om = __shfl_xor_sync(0xffffffffu, mb, 1);  // the pair's other half of the row
+    mb = om > mb ? om : mb;
+    if (!live) return;
+    const int e = oz_exponent(mb);
+    const int64_t orow = r - jb;
+    if (h == 0) aexp[orow] = e;
+    __nv_bfloat16 *out = static_cast<__nv_bfloat16 *>(aop);
+#pragma unroll
+    for (int i = 0; i < SNB / 2; ++i) {
+      __nv_bfloat16 sl[OZ_SLICES];
+      oz_slices(x[i], e, sl);
+#pragma unroll
+      for (int t = 0; t < OZ_SLICES; ++t) out[((int64_t)t * cap + orow) * SNB + 2 * i + h] = sl[t];
+    }
+  }
 }
 
 // The panel's interchanges on all other columns, U12 = L11^-1 A12 on the
@@ -1038,41 +972,6 @@ __global__ void track_init(uint64_t *t) {
   t[2] = 0;                       // not abandoned
 }
 
-template <typename P>
-int launch_spanel(cudaStream_t s, typename P::G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0,
-                  int32_t *info, int kind, void *aop, float *aop_lo, int32_t *aexp, int64_t cap, int32_t *plan,
-                  uint64_t *track, double give_up, int32_t *err) {
-  // FP64 panels are bound by the FP64 pipe of each CTA (~2 FMA per clock per
-  // SM): short ones spread over up to 16 CTAs of more than 64 rows each
-  const int C = (int)imin(SMAXC, imax(1, cdiv(mp, P::kFP64 ? 128 : SPT)));
-  const int64_t R = cdiv(mp, C);
-  const size_t smem = sizeof(typename P::S) * (size_t)jb * (size_t)panel_pitch<typename P::S>(R);
-  if (smem > 200 * 1024) return fail(BOLA_ERR_UNSUPPORTED, "mixed LU: panel of %lld rows too tall", (long long)mp);
-  static bool attr = false;
-  if (!attr) {
-    BOLA_TRY_CUDA(cudaFuncSetAttribute(spanel_kernel<P>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    BOLA_TRY_CUDA(cudaFuncSetAttribute(spanel_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr = true;
-  }
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)C, 1, 1);
-  cfg.blockDim = dim3(SPT, 1, 1);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute attr1[1];
-  attr1[0].id = cudaLaunchAttributeClusterDimension;
-  attr1[0].val.clusterDim.x = (unsigned)C;
-  attr1[0].val.clusterDim.y = 1;
-  attr1[0].val.clusterDim.z = 1;
-  cfg.attrs = attr1;
-  cfg.numAttrs = 1;
-  ProfScope prof(s, P::kFP64 ? "spanel64" : "spanel", (double)mp * jb * jb,
-                 2.0 * sizeof(typename P::G) * (double)mp * jb);
-  BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, spanel_kernel<P>, W, ldw, mp, jb, ipiv, col0, info, kind, aop, aop_lo, aexp,
-                                   cap, R, plan, track, give_up, err));
-  return 0;
-}
-
 }  // namespace
 
 int MixedLU::reserve(int64_t n_, int kind_, cudaStream_t s) {
@@ -1092,7 +991,7 @@ int MixedLU::reserve(int64_t n_, int kind_, cudaStream_t s) {
   n = cap_n = n_;
   kind = kind_;
   BOLA_TRY_CUDA(cudaMallocAsync(&err, sizeof(int32_t), s));
-  BOLA_TRY_CUDA(cudaMallocAsync(&plan, sizeof(int32_t) * (1 + 4 * SNB), s));
+  BOLA_TRY_CUDA(cudaMallocAsync(&plan, sizeof(int32_t) * (1 + 5 * SNB), s));
   BOLA_TRY_CUDA(cudaMallocAsync(&track, 4 * sizeof(uint64_t), s));
   BOLA_TRY_CUDA(cudaMemsetAsync(err, 0, sizeof(int32_t), s));
   if (kind == 3) {
@@ -1153,12 +1052,8 @@ void MixedLU::destroy() {
 
 namespace {
 
-// Width of the panel starting at j: 64, or 48 for FP64 panels taller than
-// the cluster's shared memory holds at 64 columns (16 x 399 rows).
-int panel_width(bool fp64, int64_t n, int64_t j) {
-  const int64_t mp = n - j;
-  return (int)imin(fp64 && mp > SMAXC * 399 ? 48 : SNB, mp);
-}
+// Width of the panel starting at j.
+int panel_width(bool, int64_t n, int64_t j) { return (int)imin(SNB, n - j); }
 
 }  // namespace
 
@@ -1191,11 +1086,26 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
     const int64_t mp = n - j;
     const bool upd = j + jb < n;
     const int buf = (int)(k & 1);
-    if constexpr (fp64)
-      BOLA_TRY(launch_spanel<PanelF64>(lu.sp, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, lu.kind,
-                                       upd ? lu.aop[buf] : nullptr, nullptr, lu.ea[buf], lu.cap_n, lu.plan, track,
-                                       give_up, lu.err));
-    else
+    if constexpr (fp64) {
+      // pivot rows by tournament on FP32 copies, then the FP64 factorisation
+      // of the selected block and of the rows below it
+      double *Wp = W + j + j * ldw;
+      int32_t *win = lu.plan + 1 + 4 * SNB;
+      BOLA_TRY(launch_tpanel<double>(lu.sp, Wp, ldw, mp, jb, ipiv + j, (int32_t)j, info, lu.kind, nullptr, nullptr,
+                                     nullptr, track, give_up, lu.err, win));
+      {
+        ProfScope prof(lu.sp, "panel_top64", (double)jb * jb * jb * 2.0 / 3.0, 16.0 * (double)jb * jb);
+        panel_top64<<<1, 256, 0, lu.sp>>>(Wp, ldw, mp, jb, (int32_t)j, win, lu.plan, ipiv + j, info, track,
+                                          give_up, lu.err);
+      }
+      if (mp > jb) {
+        ProfScope prof(lu.sp, "panel_l21_64", (double)(mp - jb) * jb * jb, 16.0 * (double)(mp - jb) * jb);
+        panel_l21_64<<<(unsigned)cdiv(mp - jb, L21_ROWS), 128, 0, lu.sp>>>(Wp, ldw, mp, jb,
+                                                                           upd ? lu.aop[buf] : nullptr, lu.ea[buf],
+                                                                           lu.cap_n, abort);
+      }
+      BOLA_CHECK_LAUNCH();
+    } else
       BOLA_TRY(launch_tpanel(lu.sp, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, lu.kind,
                              upd ? lu.aop[buf] : nullptr, lu.aop_lo[buf], lu.plan, track, give_up, lu.err));
     // the row swaps reach every column: the previous wide update must be done
