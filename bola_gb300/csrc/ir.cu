@@ -331,25 +331,34 @@ __device__ __forceinline__ void block_product(float (&acc)[RH], const float (*A)
   }
 }
 
-// Spins until block k's words carry this launch's epoch, into X[kk][c].
+// Spins until block k's words carry this launch's epoch, into X[kk][c].  A
+// thread's words are all loaded at once (one L2 round trip, not one per
+// word); only those not yet published are polled again.
 template <int RH>
 __device__ __forceinline__ void take_block(const unsigned long long *xw, int64_t n, int nrhs, int64_t k0, int kbk,
                                            uint32_t epoch, float (*X)[4 * RH], int32_t *err) {
-  for (int e = threadIdx.x; e < TB * 4 * RH; e += 256) {
-    const int kk = e % TB, c = e / TB;
+  constexpr int PW = TB * 4 * RH / 256;  // words per thread
+  unsigned long long w[PW];
+#pragma unroll
+  for (int u = 0; u < PW; ++u) {
+    const int e = threadIdx.x + 256 * u, kk = e % TB, c = e / TB;
+    w[u] = (kk < kbk && c < nrhs) ? ld_word(xw + (k0 + kk) + (int64_t)c * n) : 0ull;
+  }
+#pragma unroll
+  for (int u = 0; u < PW; ++u) {
+    const int e = threadIdx.x + 256 * u, kk = e % TB, c = e / TB;
     float v = 0.f;
     if (kk < kbk && c < nrhs) {
       const unsigned long long *p = xw + (k0 + kk) + (int64_t)c * n;
-      unsigned long long w = ld_word(p);
       int polls = 0;
-      while ((uint32_t)(w >> 32) != epoch) {
+      while ((uint32_t)(w[u] >> 32) != epoch) {
         if (++polls > (1 << 20)) {
           atomicExch(err, 3);
           break;
         }
-        w = ld_word(p);
+        w[u] = ld_word(p);
       }
-      v = __uint_as_float((uint32_t)w);
+      v = __uint_as_float((uint32_t)w[u]);
     }
     X[kk][c] = v;
   }

@@ -89,24 +89,29 @@ struct alignas(16) TSlot {
   float v[SNB];                    // its values from column pb on: v[k] = column pb + k
 };
 
-// Partial pivoting over gw <= TG columns of the candidates a warp holds
-// (candidate l + 32 r sits in row r of lane l).  The pivot key is |v| with
-// its 8 lowest bits replaced by 255 - candidate, so that one warp reduction
-// finds the pivot (the lowest mantissa bits do not matter for the pivot's
-// quality; ties go to the lowest candidate; a NaN never wins).  The column
-// loop is not unrolled (code size: the panel's phases would otherwise keep
-// missing the instruction cache); instead the current column always sits in
-// register slot 0 and the remaining ones shift down after each step.  Writes
-// the selected candidates in order to sel[] (shared memory, lane 0) and
-// returns their count.  RECORD: each candidate's multipliers go to
-// Lsm[candidate * TG + step] (shared), the selected rows' ones to Lrec[t][s]
-// (s < t), and the pivot rows' eliminated values in group column t + k to
-// Urec[(t + k) * uk + t].
-template <int RPL, bool RECORD>
-__device__ __forceinline__ int warp_gepp(float (&v)[RPL][TG], bool (&live)[RPL], int gw, int *sel, float *Lsm,
-                                         float (*Lrec)[TG], float *Urec, int uk) {
-  constexpr unsigned FULL = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
+// Partial pivoting over gw <= TG columns of candidates held by the first NW
+// warps of the CTA: thread t (< 32 NW) holds candidate t + 32 NW r in row r
+// of v (r < RPL), the current column always in register slot 0 (the others
+// shift down after each step, which keeps the column loop rolled).  Pivot
+// key: |v| with its KB lowest bits replaced by (2^KB - 1 - candidate), so a
+// warp reduction and a maximum over the NW warps' results find the pivot
+// (the lowest mantissa bits do not matter for the pivot's quality; ties go
+// to the lowest candidate; a NaN never wins over a number).  Per step: the
+// warps' maxima meet in shared memory at one named barrier over the NW
+// warps, the pivot's owner publishes its row at a second, and every thread
+// updates its own candidates.  Writes the selected candidates in order to
+// sel[] and returns their count (the same in every thread).  RECORD: each
+// candidate's multipliers go to Lsm[candidate * TG + step], the selected
+// rows' ones to Lrec[t][s] (s < t), and the pivot rows' eliminated values in
+// group column t + k to Urec[(t + k) * uk + t].
+template <int RPL, int NW, bool RECORD>
+__device__ __forceinline__ int group_gepp(float (&v)[RPL][TG], bool (&live)[RPL], int gw, int32_t *sel, int bar,
+                                          uint32_t *wmax, float *prow, float *Lsm, float (*Lrec)[TG], float *Urec,
+                                          int uk) {
+  constexpr int NT = 32 * NW;
+  constexpr uint32_t MASK = RPL * NT <= 256 ? 0xFFu : 0x3FFu;  // candidate-index bits
+  static_assert(RPL * NT <= 1024, "too many candidates for the key");
+  const int t0 = threadIdx.x, lane = t0 & 31, w = t0 >> 5;
   int cnt = 0;
 #pragma unroll 1
   for (int t = 0; t < gw; ++t) {
@@ -115,50 +120,47 @@ __device__ __forceinline__ int warp_gepp(float (&v)[RPL][TG], bool (&live)[RPL],
     for (int r = 0; r < RPL; ++r) {
       const float x = fabsf(v[r][0]);
       const uint32_t a = x == x ? __float_as_uint(x) : 0u;
-      const uint32_t k = (a & ~0xFFu) | (uint32_t)(255 - (lane + 32 * r));
+      const uint32_t k = (a & ~MASK) | (MASK - (uint32_t)(t0 + NT * r));
       key = (live[r] && k > key) ? k : key;
     }
-    const uint32_t mk = __reduce_max_sync(FULL, key);
-    if (mk == 0u) break;  // no live candidate left (a live one has a key >= 128)
-    const int slot = 255 - (int)(mk & 0xFFu);
-    const int wl = slot & 31, wr = slot >> 5;
-    float pv[TG];
+    key = __reduce_max_sync(0xffffffffu, key);
+    if (lane == 0) wmax[w] = key;
+    asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(NT) : "memory");
+    uint32_t mk = wmax[0];
 #pragma unroll
-    for (int k = 0; k < TG; ++k) {
-      float x = v[0][k];
-#pragma unroll
-      for (int r = 1; r < RPL; ++r)
-        if (wr == r) x = v[r][k];
-      pv[k] = __shfl_sync(FULL, x, wl);
-    }
-    if (lane == 0) sel[t] = slot;
-    if (lane == wl) {
+    for (int i = 1; i < NW; ++i) mk = wmax[i] > mk ? wmax[i] : mk;
+    if (mk == 0u) break;  // no live candidate left (a live one has a key > 0)
+    const int ci = (int)(MASK - (mk & MASK));
+    if (t0 == ci % NT) {  // the owner publishes the pivot row and retires it
+      const int ro = ci / NT;
 #pragma unroll
       for (int r = 0; r < RPL; ++r)
-        if (r == wr) live[r] = false;
-    }
-    if (RECORD) {
-      if (lane < t) Lrec[t][lane] = Lsm[slot * TG + lane];
-      if (lane < TG && lane < gw - t) {
-        float x = pv[0];
+        if (r == ro) {
 #pragma unroll
-        for (int k = 1; k < TG; ++k)
-          if (lane == k) x = pv[k];
-        Urec[(t + lane) * uk + t] = x;
-      }
+          for (int k = 0; k < TG; ++k) prow[k] = v[r][k];
+          live[r] = false;
+        }
+      sel[t] = ci;
+    }
+    asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(NT) : "memory");
+    float pv[TG];
+#pragma unroll
+    for (int k = 0; k < TG; ++k) pv[k] = prow[k];
+    if (RECORD) {
+      if (t0 < t) Lrec[t][t0] = Lsm[ci * TG + t0];
+      if (t0 < TG && t0 < gw - t) Urec[(t + t0) * uk + t] = pv[t0];
     }
     const float inv = pv[0] != 0.f ? __frcp_rn(pv[0]) : 0.f;
 #pragma unroll
     for (int r = 0; r < RPL; ++r) {
       const float l = v[r][0] * inv;
-      if (RECORD && live[r]) Lsm[(lane + 32 * r) * TG + t] = l;
+      if (RECORD && live[r]) Lsm[(t0 + NT * r) * TG + t] = l;
 #pragma unroll
       for (int k = 1; k < TG; ++k) v[r][k - 1] = live[r] ? fmaf(-l, pv[k], v[r][k]) : v[r][k];
       v[r][TG - 1] = 0.f;
     }
     ++cnt;
   }
-  __syncwarp();
   return cnt;
 }
 
@@ -240,8 +242,9 @@ tpanel_kernel(G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
   const int C = (int)cluster.num_blocks();
   const int cr = (int)cluster.block_rank();
   __shared__ uint64_t xbar[2];             // completes when every CTA's nominees of a group have landed
-  __shared__ int32_t cand1[TPT / 32][TG];  // each warp's nominees (local rows, -1: none)
-  __shared__ int32_t cand2[TG];            // the CTA's nominees
+  __shared__ int32_t cand2[TG];            // the CTA's nominees (local rows, -1: none)
+  __shared__ uint32_t gwmax[TPT / 32];     // pivot searches: the warps' best keys
+  __shared__ float gprow[TG];              // pivot searches: the pivot row of the current step
   __shared__ int32_t win[SNB];             // panel row of the pivot of each column
   __shared__ int32_t wslot[TG];            // the group's pivots as slot indices
   __shared__ float Lg[TG][TG];             // the group pivots' multipliers within the group
@@ -250,7 +253,7 @@ tpanel_kernel(G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
   __shared__ int32_t posin[SNB], at_[SNB], ipg[SNB];  // interchange bookkeeping (CTA 0)
   __shared__ int sfail;
   __shared__ TSlot stage[TG];              // this CTA's nominees, as they are pushed
-  __shared__ int32_t selw[TPT / 32][TG];   // pivot search outputs (candidate order)
+  __shared__ int32_t selw[2][TG];          // pivot searches' outputs (candidate order): own rows, nominees
   __shared__ float Lsm[SMAXC * TG * TG];   // multipliers of the stacked nominees, per step
   __shared__ float Linv[TG][TG];           // inverse of the group's unit-lower 8 x 8 block of L
   extern __shared__ __align__(16) unsigned char tp_raw[];
@@ -303,45 +306,24 @@ tpanel_kernel(G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
     const int nv = SNB - pb;                // values pushed per nominee (a multiple of 8)
     const int nq = 1 + nv / 4;
     if (tid == 0) sm100::mbar_arrive_expect_tx(&xbar[par], (uint32_t)(C * gw * sizeof(TSlot)));
-    // -- 1. each warp's nominees from its own rows (the group's columns are current)
+    // -- 1-2. the CTA's nominees: partial pivoting over all of its rows on
+    // the group's columns (scratch copies in registers), every warp taking
+    // part in every step
     {
       float v[TRPL][TG];
       bool live[TRPL];
 #pragma unroll
       for (int r = 0; r < TRPL; ++r) {
-        const int il = warp * 32 + lane + TPT * r;
+        const int il = tid + TPT * r;
         live[r] = il < nr && rstate[il] < 0;
 #pragma unroll
         for (int k = 0; k < TG; ++k) v[r][k] = live[r] ? sp[(c0 + k) * RP + il] : 0.f;
       }
-      const int cnt = warp_gepp<TRPL, false>(v, live, gw, selw[warp], nullptr, nullptr, nullptr, 0);
-      if (lane < TG) {
-        const int sl = selw[warp][lane];
-        cand1[warp][lane] = lane < cnt ? warp * 32 + (sl & 31) + TPT * (sl >> 5) : -1;
-      }
-    }
-    __syncthreads();
-    // -- 2. the CTA's nominees from the warps' (warp 0)
-    if (warp == 0) {
-      constexpr int NC1 = (TPT / 32) * TG;  // 64 candidates: 2 per lane
-      float v[NC1 / 32][TG];
-      bool live[NC1 / 32];
-      int cil[NC1 / 32];
-#pragma unroll
-      for (int r = 0; r < NC1 / 32; ++r) {
-        const int ci = lane + 32 * r;
-        cil[r] = cand1[ci / TG][ci % TG];
-        live[r] = cil[r] >= 0;
-#pragma unroll
-        for (int k = 0; k < TG; ++k) v[r][k] = live[r] ? sp[(c0 + k) * RP + cil[r]] : 0.f;
-      }
-      const int cnt = warp_gepp<NC1 / 32, false>(v, live, gw, selw[0], nullptr, nullptr, nullptr, 0);
-      if (lane < TG) {
-        const int ci = selw[0][lane];
-        cand2[lane] = lane < cnt ? cand1[ci / TG][ci % TG] : -1;
-      }
+      const int cnt = group_gepp<TRPL, TPT / 32, false>(v, live, gw, selw[0], 1, gwmax, gprow, nullptr, nullptr,
+                                                        nullptr, 0);
+      if (tid < TG) cand2[tid] = tid < cnt ? selw[0][tid] : -1;
       // the previous group's bulk pushes have read the staging slots
-      if (lane < C) sm100::bulk_wait_read0();
+      if (tid < C) sm100::bulk_wait_read0();
     }
     __syncthreads();
     // -- 3. push the nominees (columns pb..63): staged as gw slots, then one
@@ -395,61 +377,61 @@ tpanel_kernel(G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
       break;
     }
     const TSlot *sl = slots + (size_t)par * C * TG;
-    // -- 5. the group's pivots from all nominees, the same in every CTA (warp
-    // 0), while the other warps bring every pushed row's columns right of the
-    // group up to date with the previous group's update (the pushed
-    // multipliers of that group are its first 8 values), in place
-    if (warp == 0) {
-      constexpr int NC3 = SMAXC * TG / 32;  // up to 128 candidates: 4 per lane
-      float v[NC3][TG];
-      bool live[NC3];
+    // -- 5. the group's pivots from all nominees, the same in every CTA
+    // (warps 0-3, one candidate per lane)
+    if (warp < 4) {
+      float v[1][TG];
+      bool live[1];
+      live[0] = tid < C * gw && sl[tid].row != 0xFFFFFFFFu;
 #pragma unroll
-      for (int r = 0; r < NC3; ++r) {
-        const int ci = lane + 32 * r;
-        live[r] = ci < C * gw && sl[ci].row != 0xFFFFFFFFu;
-#pragma unroll
-        for (int k = 0; k < TG; ++k) v[r][k] = live[r] ? sl[ci].v[c0 - pb + k] : 0.f;
-      }
-      const int cnt = warp_gepp<NC3, true>(v, live, gw, selw[0], Lsm, Lg, &UgT[ub][c0][0], TG);
-      // the panel always has at least gw rows that are not pivots yet, so
-      // cnt == gw; a shortfall would mean a corrupted exchange
-      if (cnt < gw && lane == 0) atomicExch(err, 6);
-      if (lane < gw) {
-        const int s2 = selw[0][lane];
-        wslot[lane] = lane < cnt ? s2 : -1;
-        win[c0 + lane] = lane < cnt ? (int32_t)sl[s2].row : -1;
-      }
-      // the inverse of the group's unit-lower block of L: lane q forms column q
-      __syncwarp();
-      if (lane < TG) {
-        float col[TG];
-#pragma unroll
-        for (int t = 0; t < TG; ++t) {
-          float x = t == lane ? 1.f : 0.f;
-#pragma unroll
-          for (int p = 0; p < t; ++p) x = fmaf(-Lg[t][p], col[p], x);
-          col[t] = t < lane ? 0.f : x;
+      for (int k = 0; k < TG; ++k) v[0][k] = live[0] ? sl[tid].v[c0 - pb + k] : 0.f;
+      const int cnt = group_gepp<1, 4, true>(v, live, gw, selw[1], 2, gwmax, gprow, Lsm, Lg, &UgT[ub][c0][0], TG);
+      if (warp == 0) {
+        // the panel always has at least gw rows that are not pivots yet, so
+        // cnt == gw; a shortfall would mean a corrupted exchange
+        if (cnt < gw && lane == 0) atomicExch(err, 6);
+        if (lane < gw) {
+          const int s2 = selw[1][lane];
+          wslot[lane] = lane < cnt ? s2 : -1;
+          win[c0 + lane] = lane < cnt ? (int32_t)sl[s2].row : -1;
         }
+        // the inverse of the group's unit-lower block of L: lane q forms column q
+        __syncwarp();
+        if (lane < TG) {
+          float col[TG];
 #pragma unroll
-        for (int t = 0; t < TG; ++t) Linv[t][lane] = col[t];
-      }
-    } else if (g > 0) {
-      TSlot *slw = slots + (size_t)par * C * TG;
-      const float(*U)[TG] = UgT[ub ^ 1];
-      const int nk = SNB - c0 - gw;
-      for (int e = tid - 32; e < C * gw * nk; e += TPT - 32) {
-        const int ci = e / nk, k = c0 + gw + e % nk;
-        float l[TG];
+          for (int t = 0; t < TG; ++t) {
+            float x = t == lane ? 1.f : 0.f;
 #pragma unroll
-        for (int s2 = 0; s2 < TG; ++s2) l[s2] = slw[ci].v[s2];
-        slw[ci].v[k - pb] = rank8(slw[ci].v[k - pb], l, *reinterpret_cast<const float4 *>(&U[k][0]),
-                                  *reinterpret_cast<const float4 *>(&U[k][4]));
+            for (int p = 0; p < t; ++p) x = fmaf(-Lg[t][p], col[p], x);
+            col[t] = t < lane ? 0.f : x;
+          }
+#pragma unroll
+          for (int t = 0; t < TG; ++t) Linv[t][lane] = col[t];
+        }
       }
     }
     __syncthreads();
     if (win[c0 + gw - 1] < 0) {  // (err is set) leave the group loop uniformly
       failed = true;
       break;
+    }
+    // the pivots' pushed rows, brought up to date on the columns right of the
+    // group with the previous group's update (their multipliers of that group
+    // are the first 8 pushed values), in place
+    if (g > 0) {
+      TSlot *slw = slots + (size_t)par * C * TG;
+      const float(*U)[TG] = UgT[ub ^ 1];
+      const int nk = SNB - c0 - gw;
+      for (int e = tid; e < gw * nk; e += TPT) {
+        const int ci = wslot[e / nk], k = c0 + gw + e % nk;
+        float l[TG];
+#pragma unroll
+        for (int s2 = 0; s2 < TG; ++s2) l[s2] = slw[ci].v[s2];
+        slw[ci].v[k - pb] = rank8(slw[ci].v[k - pb], l, *reinterpret_cast<const float4 *>(&U[k][0]),
+                                  *reinterpret_cast<const float4 *>(&U[k][4]));
+      }
+      __syncthreads();
     }
     // the pivots' U rows right of the group: U = Linv A' over the up-to-date
     // pushed rows A', one (row, column) element per thread
@@ -623,27 +605,33 @@ int launch_tpanel(cudaStream_t s, G *W, int64_t ldw, int64_t mp, int jb, int32_t
 // 1 / p for the FP64 panel's pivots without the long-latency division:
 // Newton's iteration for the reciprocal, r <- r (2 - p r), from the FP32
 // reciprocal as its seed (relative error 2^-23 -> 2^-46 -> below 2^-52 after
-// two steps); plain division where p or 1/p lies outside the range in which
+// two steps); plain division where |p| lies outside [2^-100, 2^101), so that
 // the FP32 seed is a normal number.
 __device__ __forceinline__ double recip64(double p) {
-  const double ap = fabs(p);
-  if (!(ap > 1e-30 && ap < 1e30)) return 1.0 / p;
+  const int e = (int)(((uint64_t)__double_as_longlong(p) >> 52) & 0x7FF);  // biased exponent (integer pipe)
+  if (e < 1023 - 100 || e > 1023 + 100) return 1.0 / p;
   double r = (double)__frcp_rn((float)p);
   r = r * fma(-p, r, 2.0);
   r = r * fma(-p, r, 2.0);
   return r;
 }
 
-// Step 2 of the panel above for one panel (Wp: its top-left, rows
-// col0.. of W).  One CTA of 256 threads; the block lives in shared memory and
-// its rows never move: a flag marks the rows that are pivots already, and
-// the pivot order is kept as a list.  Thread (q, g) owns block row q = tid %
-// 64 in the columns c = g (mod 4), g = tid / 64.  Per column k, after one
-// barrier every thread forms its row's multiplier and updates column k + 1;
-// after a second, warps 0-1 search column k + 1 and form the reciprocal of
-// its pivot while every thread updates its remaining columns (look-ahead:
-// the search and the reciprocal leave the critical path).
-__global__ void __launch_bounds__(256)
+// Step 2 of the panel above for one panel (Wp: its top-left, rows col0.. of
+// W).  One CTA of 8 warps; the block's rows live in shared memory and never
+// move (each row remembers the column it became the pivot of).  Block row q
+// belongs to lanes 4q .. 4q + 3; lane h of the quad updates columns
+// c = h (mod 4), so every FP64 warp instruction has 32 busy lanes.  On GB300
+// a warp's other instructions wait while its FP64 instruction is dispatched
+// (~64 cycles), so two warps share each sub-partition: one's shared-memory
+// and integer work overlaps the other's FP64 work.  Per column k (a rolled
+// loop: an unrolled one misses the instruction cache): the pivot from the
+// warps' keys at a named barrier, its lane forms 1 / pivot, a second
+// barrier, then every row forms its multiplier, updates column k + 1 and
+// publishes its key for the next search before its other columns' FMAs.
+constexpr int T64_LPR = 4;                       // lanes per block row
+constexpr int T64_THREADS = SNB * T64_LPR;       // 256
+constexpr int T64_WARPS = T64_THREADS / 32;      // 8
+__global__ void __launch_bounds__(T64_THREADS, 1)
 panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int32_t *win_in, int32_t *plan,
             int32_t *ipiv, int32_t *info, uint64_t *track, double give_up, int32_t *err) {
   // an abandoned factorisation (flag set by an earlier panel on this stream):
@@ -652,22 +640,18 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
     for (int t = threadIdx.x; t < jb; t += blockDim.x) ipiv[t] = col0 + t + 1;
     return;
   }
-  __shared__ double a[SNB][SNB + 1];  // a[c][q]: column c of block row q
+  __shared__ double a[SNB][SNB + 1];  // a[q][c]: block row q, column c
   __shared__ int32_t win[SNB], order[SNB], pivl[SNB], posin[SNB], at_[SNB], ipg[SNB], rows_s[2 * SNB],
       src_s[2 * SNB];
-  __shared__ uint8_t isp[SNB];         // block row q is a pivot already
-  __shared__ double rinv_s[2];         // reciprocal of the pivot of column k (k & 1)
-  __shared__ int piv_s[2];             // block row of the pivot of column k (k & 1)
-  __shared__ uint64_t pkey[2][2];      // the two search warps' best keys (parity, warp)
-  __shared__ int pq[2][2];
+  __shared__ double rinv_s[2];             // 1 / the pivot of column k (k & 1)
+  __shared__ uint32_t wkey[2][T64_WARPS];  // the warps' best keys for column k (k & 1)
   __shared__ int bad, cnt_s;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int q = tid & (SNB - 1), g = tid >> 6;
+  const int q = tid / T64_LPR, h = tid % T64_LPR;
   if (tid == 0) bad = 0;
   __syncthreads();
-  for (int t = tid; t < jb; t += 256) {
+  for (int t = tid; t < jb; t += T64_THREADS) {
     win[t] = win_in[t];
-    isp[t] = 0;
     // a selection that did not finish (its exchange gave up and set the
     // error word) leaves no valid list: stop here rather than index W with it
     if (win[t] < 0 || win[t] >= mp) atomicExch(&bad, 1);
@@ -675,132 +659,155 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
   __syncthreads();
   if (bad != 0) {
     if (tid == 0) atomicExch(err, 7);
-    for (int t = tid; t < jb; t += 256) ipiv[t] = col0 + t + 1;
+    for (int t = tid; t < jb; t += T64_THREADS) ipiv[t] = col0 + t + 1;
     return;
   }
   // the selected rows, all of a thread's loads in flight together
   {
-    constexpr int PER = SNB * SNB / 256;
+    constexpr int PER = SNB * SNB / T64_THREADS;
     double v[PER];
 #pragma unroll
     for (int u = 0; u < PER; ++u) {
-      const int e = tid + 256 * u, r = e % SNB, c = e / SNB;
+      const int e = tid + T64_THREADS * u, r = e % SNB, c = e / SNB;
       v[u] = (r < jb && c < jb) ? Wp[win[r] + (int64_t)c * ldw] : 0.0;
     }
 #pragma unroll
     for (int u = 0; u < PER; ++u) {
-      const int e = tid + 256 * u;
-      a[e / SNB][e % SNB] = v[u];
+      const int e = tid + T64_THREADS * u;
+      a[e % SNB][e / SNB] = v[u];
     }
   }
-  __syncthreads();
+  const bool rowok = q < jb;
+  int mystep = -1;                  // the column this row is the pivot of
   uint64_t umax = 0, umin = ~0ull;  // |u_kk| bits (thread 0)
-  // the largest |a[c][r]| over rows r that are not pivots (ties: lowest r; a
-  // NaN never wins), by warps 0 and 1 (rows 32 w + lane); the result, with
-  // the reciprocal of the pivot, goes to slot par
-  auto search = [&](int c, int par) {
-    const int r = warp * 32 + lane;
-    uint64_t key = 0;
-    if (r < jb && !isp[r]) {
-      const uint64_t b = (uint64_t)__double_as_longlong(a[c][r]) & 0x7fffffffffffffffull;
-      key = b > 0x7ff0000000000000ull ? 0 : b;
+  // this row's key in column k (v: its value there) if it may still pivot:
+  // the high word of |v| with the row in its 7 low bits (>= 64 for every
+  // candidate, so a zero column still yields a pivot; a NaN counts as zero)
+  auto publish = [&](double v, int k) {
+    uint32_t key = 0u;
+    if (rowok && mystep < 0 && h == k % T64_LPR && k < jb) {
+      const uint64_t b = (uint64_t)__double_as_longlong(v) & 0x7fffffffffffffffull;
+      const uint32_t hi = b > 0x7ff0000000000000ull ? 0u : (uint32_t)(b >> 32);
+      key = (hi & ~127u) | (uint32_t)(127 - q);
     }
-    int kr = r;
+    key = __reduce_max_sync(0xffffffffu, key);
+    if (lane == 0) wkey[k & 1][warp] = key;
+  };
+  __syncthreads();
+  publish(a[q][0], 0);
+#pragma unroll 1
+  for (int k = 0; k < jb; ++k) {
+    const int par = k & 1, hk = k % T64_LPR;
+    asm volatile("bar.sync 1, %0;" ::"r"(T64_THREADS) : "memory");
+    uint32_t mk = wkey[par][0];
+#pragma unroll
+    for (int w = 1; w < T64_WARPS; ++w) mk = wkey[par][w] > mk ? wkey[par][w] : mk;
+    const int p = 127 - (int)(mk & 127u);
+    if (q == p) {
+      mystep = k;
+      if (h == hk) {  // the lane of column k: 1 / pivot, the pivot order, info and the pivots' extent
+        const double pv = a[p][k];
+        const uint64_t ab = (uint64_t)__double_as_longlong(pv) & 0x7fffffffffffffffull;
+        rinv_s[par] = ab != 0 ? recip64(pv) : 0.0;
+        order[k] = p;
+        if (ab == 0) atomicCAS(info, 0, col0 + k + 1);
+        if (ab <= 0x7ff0000000000000ull) {
+          umax = ab > umax ? ab : umax;
+          umin = ab < umin ? ab : umin;
+        }
+      }
+    }
+    asm volatile("bar.sync 1, %0;" ::"r"(T64_THREADS) : "memory");
+    const bool act = rowok && mystep < 0;
+    const double l = act ? a[q][k] * rinv_s[par] : 0.0;
+    __syncwarp();  // the quad has read a[q][k] before it becomes the multiplier
+    double v1 = 0.0;
+    if (act) {
+      if (h == hk) a[q][k] = l;
+      // column k + 1 first: the next search reads it
+      if (k + 1 < jb && h == (k + 1) % T64_LPR) {
+        v1 = fma(-l, a[p][k + 1], a[q][k + 1]);
+        a[q][k + 1] = v1;
+      }
+    }
+    publish(v1, k + 1);
+    // the row's other columns c = 4u + h >= k + 2: the same trip count in
+    // every lane of the warp (a per-lane start would split the warp into
+    // paths that each dispatch their own FP64 instructions), 4 columns at a
+    // time with all of their loads issued before the FMAs
+    for (int u0 = (k + 2) / T64_LPR; u0 < SNB / T64_LPR; u0 += 4) {
+      double pr[4], xr[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int c = T64_LPR * (u0 + u) + h;
+        const bool on = act && u0 + u < SNB / T64_LPR && c >= k + 2 && c < jb;
+        pr[u] = on ? a[p][c] : 0.0;
+        xr[u] = on ? a[q][c] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int c = T64_LPR * (u0 + u) + h;
+        if (act && u0 + u < SNB / T64_LPR && c >= k + 2 && c < jb) a[q][c] = fma(-l, pr[u], xr[u]);
+      }
+    }
+  }
+  // the pivots' extent lives with the lanes that saw them: fold into thread 0
+  {
+    __syncthreads();
+    uint64_t mx = umax, mn = umin;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-      const uint64_t ok = __shfl_xor_sync(0xffffffffu, key, off);
-      const int orr = __shfl_xor_sync(0xffffffffu, kr, off);
-      if (ok > key || (ok == key && orr < kr)) {
-        key = ok;
-        kr = orr;
-      }
+      const uint64_t o1 = __shfl_xor_sync(0xffffffffu, mx, off), o2 = __shfl_xor_sync(0xffffffffu, mn, off);
+      mx = o1 > mx ? o1 : mx;
+      mn = o2 < mn ? o2 : mn;
     }
+    __shared__ uint64_t wx[T64_WARPS], wn[T64_WARPS];
     if (lane == 0) {
-      pkey[par][warp] = key;
-      pq[par][warp] = kr;
+      wx[warp] = mx;
+      wn[warp] = mn;
     }
-    asm volatile("bar.sync 1, 64;" ::: "memory");  // warps 0 and 1
-    if (tid == 0) {
-      int p = pq[par][0];
-      if (pkey[par][1] > pkey[par][0]) p = pq[par][1];
-      // an all-zero (or all-NaN) column: the first row that is not a pivot yet
-      if ((pkey[par][0] | pkey[par][1]) == 0)
-        for (p = 0; p < jb && isp[p]; ++p) {
-        }
-      const double pv = a[c][p];
-      const uint64_t ab = (uint64_t)__double_as_longlong(pv) & 0x7fffffffffffffffull;
-      if (ab == 0) atomicCAS(info, 0, col0 + c + 1);
-      if (ab <= 0x7ff0000000000000ull) {
-        umax = ab > umax ? ab : umax;
-        umin = ab < umin ? ab : umin;
+    __syncthreads();
+    if (tid == 0)
+      for (int w = 0; w < T64_WARPS; ++w) {
+        umax = wx[w] > umax ? wx[w] : umax;
+        umin = wn[w] < umin ? wn[w] : umin;
       }
-      piv_s[par] = p;
-      rinv_s[par] = ab != 0 ? recip64(pv) : 0.0;
-    }
-  };
-  if (warp < 2) search(0, 0);
-  __syncthreads();
-  for (int k = 0; k < jb; ++k) {
-    const int par = k & 1;
-    const int p = piv_s[par];
-    const double ri = rinv_s[par];
-    // row q's multiplier and the update of column k + 1 (the next one searched)
-    const bool act = q < jb && !isp[q] && q != p;
-    double l = 0.0;
-    if (act) {
-      l = a[k][q] * ri;  // (all four threads of the row read a[k][q]; it is replaced after the barrier)
-      if (k + 1 < jb && ((k + 1) & 3) == g) a[k + 1][q] = fma(-l, a[k + 1][p], a[k + 1][q]);
-    }
-    if (tid == 0) {
-      isp[p] = 1;
-      order[k] = p;
-    }
-    __syncthreads();
-    if (k + 1 < jb && warp < 2) search(k + 1, par ^ 1);
-    if (act) {
-      if (g == 0) a[k][q] = l;
-      for (int c = ((k + 2 + 3 - g) & ~3) + g; c < jb; c += 4)  // c = g (mod 4), c >= k + 2
-        a[c][q] = fma(-l, a[c][p], a[c][q]);
-    }
-    __syncthreads();
   }
-  // LAPACK's interchanges from the final pivot order, and the plan for the
-  // swap kernel
   if (tid == 0) {
     for (int t = 0; t < jb; ++t) pivl[t] = win[order[t]];  // panel row of the pivot of column t
     pivots_to_interchanges(pivl, jb, col0, posin, at_, ipg);
   }
   __syncthreads();
   if (warp == 0) compose_panel_plan(ipg, jb, col0, plan);
-  for (int t = tid; t < jb; t += 256) ipiv[t] = ipg[t];
+  for (int t = tid; t < jb; t += T64_THREADS) ipiv[t] = ipg[t];
   __syncthreads();
   // rows the interchanges move below the block: their panel columns, read
   // before anything is written
   if (tid == 0) cnt_s = plan[0];
-  for (int t = tid; t < 2 * SNB; t += 256) {
+  for (int t = tid; t < 2 * SNB; t += T64_THREADS) {
     rows_s[t] = plan[1 + t] - col0;
     src_s[t] = plan[1 + 2 * SNB + t] - col0;
   }
   __syncthreads();
   const int cnt = cnt_s;
-  constexpr int MV = 2 * SNB * SNB / 256;
+  constexpr int MV = 2 * SNB * SNB / T64_THREADS;
   double mv[MV];
 #pragma unroll
   for (int u = 0; u < MV; ++u) {
-    const int e = tid + 256 * u, t = e % (2 * SNB), c = e / (2 * SNB);
+    const int e = tid + T64_THREADS * u, t = e % (2 * SNB), c = e / (2 * SNB);
     mv[u] = (t < cnt && c < jb && rows_s[t] >= jb) ? Wp[src_s[t] + (int64_t)c * ldw] : 0.0;
   }
   __syncthreads();
 #pragma unroll
   for (int u = 0; u < MV; ++u) {
-    const int e = tid + 256 * u, t = e % (2 * SNB), c = e / (2 * SNB);
+    const int e = tid + T64_THREADS * u, t = e % (2 * SNB), c = e / (2 * SNB);
     if (t < cnt && c < jb && rows_s[t] >= jb) Wp[rows_s[t] + (int64_t)c * ldw] = mv[u];
   }
   // the factored block in pivot order (unit-lower L11 below the diagonal, U11
   // on and above)
-  for (int e = tid; e < jb * jb; e += 256) {
+  for (int e = tid; e < jb * jb; e += T64_THREADS) {
     const int r = e % jb, c = e / jb;
-    Wp[r + (int64_t)c * ldw] = a[c][order[r]];
+    Wp[r + (int64_t)c * ldw] = a[order[r]][c];
   }
   if (track != nullptr && tid == 0) {
     // the running extent of |u_ii| and the give-up test
@@ -815,52 +822,58 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
 }
 
 // L21 = A21 U11^-1 (rows jb..mp-1 of the panel, after its interchanges) in
-// FP64, and the update's operand.  Two lanes per row, lane h holding columns
-// 2i + h: the substitution's chain runs over the columns, and every FP64
+// FP64, and the update's operand.  Eight lanes per row, lane h holding
+// columns 8i + h: the substitution's chain runs over the columns, every FP64
 // warp instruction has all 32 lanes busy (on GB300 an FP64 instruction takes
-// its full issue slot whatever the number of active lanes).  64 rows per CTA.
-constexpr int L21_ROWS = 64;
-__global__ void __launch_bounds__(128)
+// its full issue slot whatever the number of active lanes), and 32 rows make
+// a CTA of 8 warps, two per sub-partition, so that one warp's shared-memory
+// and shuffle work overlaps the other's FP64 dispatch.  U11 is held as a
+// packed upper triangle (16.6 KB), small enough for a CTA to share an SM
+// with the update kernel that runs beside the panel.
+constexpr int L21_LPR = 8;                       // lanes per row
+constexpr int L21_ROWS = 32;                     // rows per CTA
+constexpr int L21_THREADS = L21_ROWS * L21_LPR;  // 256
+constexpr int L21_NX = SNB / L21_LPR;            // values per lane
+__host__ __device__ constexpr int tri_off(int k) { return k * SNB - k * (k - 1) / 2; }  // row k of the packed U
+__global__ void __launch_bounds__(L21_THREADS)
 panel_l21_64(double *Wp, int64_t ldw, int64_t mp, int jb, void *aop, int32_t *aexp, int64_t cap,
              const int32_t *abort) {
   if (abort != nullptr && *(volatile const int32_t *)abort != 0) return;  // set before this launch (same stream)
-  __shared__ double U[SNB][SNB];  // U[k][c], zero outside the upper triangle of the jb x jb block
+  __shared__ double U[SNB * (SNB + 1) / 2];  // U[tri_off(k) + c - k] = u_kc, c >= k (zero outside the jb x jb block)
   __shared__ double rinv[SNB];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, h = lane & 1;
-  for (int e = tid; e < SNB * SNB; e += 128) {
-    const int k = e % SNB, c = e / SNB;
-    U[k][c] = (k <= c && c < jb) ? Wp[k + (int64_t)c * ldw] : 0.0;
-  }
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, h = lane & (L21_LPR - 1);
+  for (int k = warp; k < SNB; k += L21_THREADS / 32)
+    for (int c = k + lane; c < SNB; c += 32) U[tri_off(k) + c - k] = (c < jb) ? Wp[k + (int64_t)c * ldw] : 0.0;
   __syncthreads();
   if (tid < SNB) {
-    const double d = U[tid][tid];
+    const double d = U[tri_off(tid)];
     rinv[tid] = (tid < jb && (__double_as_longlong(d) << 1) != 0) ? 1.0 / d : 0.0;
   }
   __syncthreads();
-  const int64_t r = jb + (int64_t)blockIdx.x * L21_ROWS + warp * 16 + (lane >> 1);
+  const int64_t r = jb + (int64_t)blockIdx.x * L21_ROWS + warp * (32 / L21_LPR) + lane / L21_LPR;
   const bool live = r < mp;
-  double x[SNB / 2];
+  double x[L21_NX];
 #pragma unroll
-  for (int i = 0; i < SNB / 2; ++i) {
-    const int c = 2 * i + h;
+  for (int i = 0; i < L21_NX; ++i) {
+    const int c = L21_LPR * i + h;
     x[i] = (live && c < jb) ? Wp[r + (int64_t)c * ldw] : 0.0;
   }
 #pragma unroll
   for (int k = 0; k < SNB; ++k) {
-    const int ik = k >> 1, hk = k & 1;
+    const int ik = k / L21_LPR, hk = k % L21_LPR;
     const double mine = x[ik] * rinv[k];  // (the owner's value is l_rk)
-    const double lk = __shfl_sync(0xffffffffu, mine, (lane & ~1) | hk);
+    const double lk = __shfl_sync(0xffffffffu, mine, (lane & ~(L21_LPR - 1)) | hk);
     if (h == hk) x[ik] = lk;
 #pragma unroll
-    for (int i = ik; i < SNB / 2; ++i) {
-      // column 2i + h > k: every i > ik, and at i == ik the odd column of an even k
-      if (i > ik || (hk == 0 && h == 1)) x[i] = fma(-lk, U[k][2 * i + h], x[i]);
+    for (int i = ik; i < L21_NX; ++i) {
+      // column 4i + h > k: every i > ik, and at i == ik the lanes after the owner
+      if (i > ik || h > hk) x[i] = fma(-lk, U[tri_off(k) + L21_LPR * i + h - k], x[i]);
     }
   }
   if (live) {
 #pragma unroll
-    for (int i = 0; i < SNB / 2; ++i) {
-      const int c = 2 * i + h;
+    for (int i = 0; i < L21_NX; ++i) {
+      const int c = L21_LPR * i + h;
       if (c < jb) Wp[r + (int64_t)c * ldw] = x[i];
     }
   }
@@ -868,23 +881,26 @@ panel_l21_64(double *Wp, int64_t ldw, int64_t mp, int jb, void *aop, int32_t *ae
     // exact bf16 slices of the row: one exponent for its 64 values
     uint64_t mb = 0;
 #pragma unroll
-    for (int i = 0; i < SNB / 2; ++i) {
+    for (int i = 0; i < L21_NX; ++i) {
       const uint64_t m = oz_mag(x[i]);
       mb = m > mb ? m : mb;
     }
-    const uint64_t om = __shfl_xor_sync(0xffffffffu, mb, 1);  // the pair's other half of the row
-    mb = om > mb ? om : mb;
+#pragma unroll
+    for (int off = 1; off < L21_LPR; off <<= 1) {  // the row's other lanes
+      const uint64_t om = __shfl_xor_sync(0xffffffffu, mb, off);
+      mb = om > mb ? om : mb;
+    }
     if (!live) return;
     const int e = oz_exponent(mb);
     const int64_t orow = r - jb;
     if (h == 0) aexp[orow] = e;
     __nv_bfloat16 *out = static_cast<__nv_bfloat16 *>(aop);
 #pragma unroll
-    for (int i = 0; i < SNB / 2; ++i) {
+    for (int i = 0; i < L21_NX; ++i) {
       __nv_bfloat16 sl[OZ_SLICES];
       oz_slices(x[i], e, sl);
 #pragma unroll
-      for (int t = 0; t < OZ_SLICES; ++t) out[((int64_t)t * cap + orow) * SNB + 2 * i + h] = sl[t];
+      for (int t = 0; t < OZ_SLICES; ++t) out[((int64_t)t * cap + orow) * SNB + L21_LPR * i + h] = sl[t];
     }
   }
 }
@@ -1095,12 +1111,12 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
                                      nullptr, track, give_up, lu.err, win));
       {
         ProfScope prof(lu.sp, "panel_top64", (double)jb * jb * jb * 2.0 / 3.0, 16.0 * (double)jb * jb);
-        panel_top64<<<1, 256, 0, lu.sp>>>(Wp, ldw, mp, jb, (int32_t)j, win, lu.plan, ipiv + j, info, track,
+        panel_top64<<<1, T64_THREADS, 0, lu.sp>>>(Wp, ldw, mp, jb, (int32_t)j, win, lu.plan, ipiv + j, info, track,
                                           give_up, lu.err);
       }
       if (mp > jb) {
         ProfScope prof(lu.sp, "panel_l21_64", (double)(mp - jb) * jb * jb, 16.0 * (double)(mp - jb) * jb);
-        panel_l21_64<<<(unsigned)cdiv(mp - jb, L21_ROWS), 128, 0, lu.sp>>>(Wp, ldw, mp, jb,
+        panel_l21_64<<<(unsigned)cdiv(mp - jb, L21_ROWS), L21_THREADS, 0, lu.sp>>>(Wp, ldw, mp, jb,
                                                                            upd ? lu.aop[buf] : nullptr, lu.ea[buf],
                                                                            lu.cap_n, abort);
       }

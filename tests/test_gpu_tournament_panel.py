@@ -52,6 +52,13 @@ def check(A, n, kind):
     return res, np.abs(np.tril(F, -1)).max(), np.abs(Um).max() / np.abs(A).max()
 
 
+def gepp_growth(A):
+    """max|U| / max|A| of column-by-column partial pivoting (LAPACK's getrf via SciPy)."""
+    sl = pytest.importorskip("scipy.linalg")
+    _, _, U = sl.lu(A)
+    return np.abs(U).max() / np.abs(A).max()
+
+
 @pytest.mark.parametrize("kind", [0, 1, 2])
 @pytest.mark.parametrize("n", [64, 200, 1000, 2048])
 def test_tournament_lu_factors(kind, n):
@@ -59,7 +66,9 @@ def test_tournament_lu_factors(kind, n):
     res, lmax, growth = check(A, n, kind)
     assert res <= TOL[kind], res
     assert lmax <= 8.0, lmax  # partial pivoting would give 1; tournament pivoting stays within a few
-    assert growth <= 100.0, growth
+    # tournament pivoting's growth stays within a small factor of partial
+    # pivoting's on the same matrix (about 70 for these at n = 1000, 2048)
+    assert growth <= 3.0 * gepp_growth(A), (growth, gepp_growth(A))
 
 
 def test_tournament_lu_ragged_sizes_and_ties():
