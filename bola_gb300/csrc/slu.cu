@@ -617,17 +617,20 @@ __device__ __forceinline__ double recip64(double p) {
 }
 
 // Step 2 of the panel above for one panel (Wp: its top-left, rows col0.. of
-// W).  One CTA of 8 warps; the block's rows live in shared memory and never
-// move (each row remembers the column it became the pivot of).  Block row q
-// belongs to lanes 4q .. 4q + 3; lane h of the quad updates columns
-// c = h (mod 4), so every FP64 warp instruction has 32 busy lanes.  On GB300
-// a warp's other instructions wait while its FP64 instruction is dispatched
-// (~64 cycles), so two warps share each sub-partition: one's shared-memory
-// and integer work overlaps the other's FP64 work.  Per column k (a rolled
-// loop: an unrolled one misses the instruction cache): the pivot from the
-// warps' keys at a named barrier, its lane forms 1 / pivot, a second
-// barrier, then every row forms its multiplier, updates column k + 1 and
-// publishes its key for the next search before its other columns' FMAs.
+// W).  One CTA of 8 warps; the block lives in shared memory and is factored
+// with row interchanges as LAPACK does (the pivot row moves to position k),
+// so the rows still to be eliminated are positions k + 1 .. and a warp
+// whose rows are all done stops issuing.  Position q belongs to lanes
+// 4q .. 4q + 3; lane h updates columns c = h (mod 4), so every FP64 warp
+// instruction has 32 busy lanes.  On GB300 a warp's other instructions wait
+// while its FP64 instruction is dispatched (~64 cycles), so two warps share
+// each sub-partition: one's shared-memory and integer work overlaps the
+// other's FP64 work.  Per column k (a rolled loop: an unrolled one misses
+// the instruction cache): the pivot from the warps' keys at a named barrier,
+// the swap of positions k and p (the thread of column k also forms 1 /
+// pivot), a second barrier, then every remaining row forms its multiplier,
+// updates column k + 1 and publishes its key for the next search before its
+// other columns' FMAs.
 constexpr int T64_LPR = 4;                       // lanes per block row
 constexpr int T64_THREADS = SNB * T64_LPR;       // 256
 constexpr int T64_WARPS = T64_THREADS / 32;      // 8
@@ -640,8 +643,8 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
     for (int t = threadIdx.x; t < jb; t += blockDim.x) ipiv[t] = col0 + t + 1;
     return;
   }
-  __shared__ double a[SNB][SNB + 1];  // a[q][c]: block row q, column c
-  __shared__ int32_t win[SNB], order[SNB], pivl[SNB], posin[SNB], at_[SNB], ipg[SNB], rows_s[2 * SNB],
+  __shared__ double a[SNB][SNB + 1];  // a[q][c]: the row now in position q, column c
+  __shared__ int32_t win[SNB], rowid[SNB], pivl[SNB], posin[SNB], at_[SNB], ipg[SNB], rows_s[2 * SNB],
       src_s[2 * SNB];
   __shared__ double rinv_s[2];             // 1 / the pivot of column k (k & 1)
   __shared__ uint32_t wkey[2][T64_WARPS];  // the warps' best keys for column k (k & 1)
@@ -652,6 +655,7 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
   __syncthreads();
   for (int t = tid; t < jb; t += T64_THREADS) {
     win[t] = win_in[t];
+    rowid[t] = t;
     // a selection that did not finish (its exchange gave up and set the
     // error word) leaves no valid list: stop here rather than index W with it
     if (win[t] < 0 || win[t] >= mp) atomicExch(&bad, 1);
@@ -677,15 +681,14 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
       a[e % SNB][e / SNB] = v[u];
     }
   }
-  const bool rowok = q < jb;
-  int mystep = -1;                  // the column this row is the pivot of
-  uint64_t umax = 0, umin = ~0ull;  // |u_kk| bits (thread 0)
-  // this row's key in column k (v: its value there) if it may still pivot:
-  // the high word of |v| with the row in its 7 low bits (>= 64 for every
-  // candidate, so a zero column still yields a pivot; a NaN counts as zero)
+  uint64_t umax = 0, umin = ~0ull;  // |u_kk| bits (the thread of column k)
+  // the key of position q in column k (v: its value there) if it is still to
+  // be eliminated: the high word of |v| with the position in its 7 low bits
+  // (>= 64 for every candidate, so a zero column still yields a pivot; a NaN
+  // counts as zero)
   auto publish = [&](double v, int k) {
     uint32_t key = 0u;
-    if (rowok && mystep < 0 && h == k % T64_LPR && k < jb) {
+    if (q >= k && q < jb && h == k % T64_LPR && k < jb) {
       const uint64_t b = (uint64_t)__double_as_longlong(v) & 0x7fffffffffffffffull;
       const uint32_t hi = b > 0x7ff0000000000000ull ? 0u : (uint32_t)(b >> 32);
       key = (hi & ~127u) | (uint32_t)(127 - q);
@@ -703,22 +706,36 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
 #pragma unroll
     for (int w = 1; w < T64_WARPS; ++w) mk = wkey[par][w] > mk ? wkey[par][w] : mk;
     const int p = 127 - (int)(mk & 127u);
-    if (q == p) {
-      mystep = k;
-      if (h == hk) {  // the lane of column k: 1 / pivot, the pivot order, info and the pivots' extent
+    // positions k and p trade rows: thread t swaps column t; the thread of
+    // column k first forms 1 / pivot and records the pivot
+    if (tid < jb) {
+      if (tid == k) {
         const double pv = a[p][k];
         const uint64_t ab = (uint64_t)__double_as_longlong(pv) & 0x7fffffffffffffffull;
         rinv_s[par] = ab != 0 ? recip64(pv) : 0.0;
-        order[k] = p;
         if (ab == 0) atomicCAS(info, 0, col0 + k + 1);
         if (ab <= 0x7ff0000000000000ull) {
           umax = ab > umax ? ab : umax;
           umin = ab < umin ? ab : umin;
         }
+        if (p != k) {
+          const int t = rowid[k];
+          rowid[k] = rowid[p];
+          rowid[p] = t;
+        }
+      }
+      if (p != k) {
+        const double t = a[k][tid];
+        a[k][tid] = a[p][tid];
+        a[p][tid] = t;
       }
     }
     asm volatile("bar.sync 1, %0;" ::"r"(T64_THREADS) : "memory");
-    const bool act = rowok && mystep < 0;
+    if ((warp + 1) * (32 / T64_LPR) - 1 <= k) {  // every row of this warp is done: no candidate for k + 1
+      if (lane == 0) wkey[par ^ 1][warp] = 0u;
+      continue;
+    }
+    const bool act = q > k && q < jb;
     const double l = act ? a[q][k] * rinv_s[par] : 0.0;
     __syncwarp();  // the quad has read a[q][k] before it becomes the multiplier
     double v1 = 0.0;
@@ -726,7 +743,7 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
       if (h == hk) a[q][k] = l;
       // column k + 1 first: the next search reads it
       if (k + 1 < jb && h == (k + 1) % T64_LPR) {
-        v1 = fma(-l, a[p][k + 1], a[q][k + 1]);
+        v1 = fma(-l, a[k][k + 1], a[q][k + 1]);
         a[q][k + 1] = v1;
       }
     }
@@ -741,7 +758,7 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
       for (int u = 0; u < 4; ++u) {
         const int c = T64_LPR * (u0 + u) + h;
         const bool on = act && u0 + u < SNB / T64_LPR && c >= k + 2 && c < jb;
-        pr[u] = on ? a[p][c] : 0.0;
+        pr[u] = on ? a[k][c] : 0.0;
         xr[u] = on ? a[q][c] : 0.0;
       }
 #pragma unroll
@@ -774,7 +791,7 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
       }
   }
   if (tid == 0) {
-    for (int t = 0; t < jb; ++t) pivl[t] = win[order[t]];  // panel row of the pivot of column t
+    for (int t = 0; t < jb; ++t) pivl[t] = win[rowid[t]];  // panel row of the pivot of column t
     pivots_to_interchanges(pivl, jb, col0, posin, at_, ipg);
   }
   __syncthreads();
@@ -803,11 +820,10 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
     const int e = tid + T64_THREADS * u, t = e % (2 * SNB), c = e / (2 * SNB);
     if (t < cnt && c < jb && rows_s[t] >= jb) Wp[rows_s[t] + (int64_t)c * ldw] = mv[u];
   }
-  // the factored block in pivot order (unit-lower L11 below the diagonal, U11
-  // on and above)
+  // the factored block (unit-lower L11 below the diagonal, U11 on and above)
   for (int e = tid; e < jb * jb; e += T64_THREADS) {
     const int r = e % jb, c = e / jb;
-    Wp[r + (int64_t)c * ldw] = a[order[r]][c];
+    Wp[r + (int64_t)c * ldw] = a[r][c];
   }
   if (track != nullptr && tid == 0) {
     // the running extent of |u_ii| and the give-up test
