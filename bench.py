@@ -334,8 +334,7 @@ def run_ours(args, rank, world, device):
             xcache[(c2, nbytes)] = api.measure_cluster_exchange(max(2, c2), nbytes)
         return xcache[(c2, nbytes)]
 
-    roof = roofline_for(dom_name, dom, peak_fp64, n=n, exchange_us=exchange_us,
-                        sms=torch.cuda.get_device_properties(device).multi_processor_count)
+    roof = roofline_for(dom_name, dom, peak_fp64, n=n, exchange_us=exchange_us)
     kernels = {k: {"scopes": v["calls"], "launches": v["launches"], "ms": round(v["ms"], 3),
                    "share": round(v["ms"] / prof_total, 4),
                    "tflops": round(v["flops"] / max(v["ms"], 1e-9) / 1e9, 4) if v["flops"] else None,
@@ -588,57 +587,49 @@ def run_serve(args, device):
 
 
 # DRAM bytes (read + write) per algorithmic byte, from the ncu captures
-# summarised under profiles/ (n=4096 cases): spanel 0.79 MB read for a
-# 2752 x 64 FP32 panel whose algorithmic read + write is 1.41 MB; tc_update
-# 33.2 MB for a 2752^2 step with 60.6 MB algorithmic (writes still in L2);
-# oz_update 71.1 MB for 121 MB.
-TRAFFIC_PER_ALGORITHMIC_BYTE = {"spanel": 0.56, "tc_update": 0.55, "oz_update": 0.59}
+# summarised under profiles/ (n=4096 cases): the tournament panel 0.82 MB read
+# for a 2816 x 64 FP32 panel whose algorithmic read + write is 1.44 MB;
+# tc_update 49.4 MB for a 3392 x 3328 step with 90.3 MB algorithmic (writes
+# still in L2); oz_update 129.4 MB for 180.6 MB.
+TRAFFIC_PER_ALGORITHMIC_BYTE = {"tpanel": 0.57, "tc_update": 0.55, "oz_update": 0.72}
 
 
-# Cluster panels of the mixed LU, as slu.cu schedules them: (mp, jb, C, R)
-# per panel of an n x n factorisation.  FP64 panels (kind 3) take 48 columns
-# while taller than 16 x 399 rows and spread over CTAs of >= ~128 rows; the
-# FP32 tournament panel uses CTAs of up to 256 threads x 2 rows.
-def panel_schedule(n, fp64):
+# The tournament panels of the mixed LU as slu.cu schedules them: (mp, jb, C,
+# R) per panel of an n x n factorisation, 64 columns, CTAs of up to 256
+# threads x 2 rows.  The same kernel selects the FP64-accurate factor's
+# pivots (tselect64) on the same schedule.
+def panel_schedule(n):
     out, j = [], 0
     while j < n:
         mp = n - j
-        jb = min(48 if (fp64 and mp > 16 * 399) else 64, mp)
-        C = min(16, max(1, -(-mp // (128 if fp64 else 256))))
+        jb = min(64, mp)
+        C = min(16, max(1, -(-mp // 256)))
         out.append((mp, jb, C, -(-mp // C)))
         j += jb
     return out
 
 
-TSLOT_BYTES = 16 + 64 * 4   # a tournament nominee pushed between CTAs (FP32 panel)
-SSLOT_BYTES = 16 + 64 * 8   # a candidate row pushed per column (FP64 panel)
+TSLOT_BYTES = 16 + 64 * 4   # a tournament nominee pushed between CTAs
 
 
-def panel_floor(name, n, exchange_us, peak_fp64_gflops, sms):
-    """Lower bound (us) of one factorisation's panels and its unit count.
-    spanel64: per column, the larger of one cluster exchange round (measured,
-    at the panel's cluster size) and the column's FP64 work per CTA (rank-1
-    update of R rows over the remaining columns) at the measured per-SM DFMA
-    rate.  tpanel: per group of 8 columns, the larger of one exchange round
-    of 8 nominees and the group's FP32 work per CTA (rank-8 update of R rows
-    over the remaining columns) at 128 FMA per clock per SM, 2.07 GHz."""
-    fp64 = name == "spanel64"
-    fma_sm = (peak_fp64_gflops * 1e9 / 2.0 / sms) if fp64 else 128 * 2.07e9
+def panel_floor(n, exchange_us):
+    """Lower bound (us) of one factorisation's tournament panels and their
+    unit count: per group of 8 columns, the larger of one exchange round of 8
+    nominees at the panel's cluster size (measured) and the group's FP32 work
+    per CTA (rank-8 update of R rows over the remaining columns) at 128 FMA
+    per clock per SM, 2.07 GHz."""
+    fma_sm = 128 * 2.07e9
     total, units = 0.0, 0
-    for mp, jb, C, R in panel_schedule(n, fp64):
-        x = exchange_us(C, SSLOT_BYTES if fp64 else 8 * TSLOT_BYTES)
-        if fp64:
-            for t in range(jb):
-                total += max(x, 1e6 * R * (jb - t - 1) / fma_sm)
-                units += 1
-        else:
-            for g0 in range(0, jb, 8):
-                total += max(x, 1e6 * R * 8 * (64 - g0) / fma_sm)
-                units += 1
-    return total, units, len(panel_schedule(n, fp64))
+    sched = panel_schedule(n)
+    for mp, jb, C, R in sched:
+        x = exchange_us(C, 8 * TSLOT_BYTES)
+        for g0 in range(0, jb, 8):
+            total += max(x, 1e6 * R * 8 * (64 - g0) / fma_sm)
+            units += 1
+    return total, units, len(sched)
 
 
-def roofline_for(name, v, peak_fp64_gflops, n=None, exchange_us=None, sms=None):
+def roofline_for(name, v, peak_fp64_gflops, n=None, exchange_us=None):
     """The dominant kernel's achieved rate against its bounding peak.
     FP64 kernels: DFMA peak measured in this run.  Tensor-core update: HBM
     (it reads and writes the FP32 trailing matrix once per step).  Cluster
@@ -666,23 +657,19 @@ def roofline_for(name, v, peak_fp64_gflops, n=None, exchange_us=None, sms=None):
         # algorithmic bytes of this run's average launch
         out["traffic"] = round(ratio * per_launch)
         out["algorithmic_bytes_per_launch"] = round(per_launch)
-    if name in ("spanel64", "tpanel") and n and exchange_us and sms:
-        floor_us, units, panels = panel_floor(name, n, exchange_us, peak_fp64_gflops, sms)
+    if name in ("tpanel", "tselect64") and n and exchange_us:
+        floor_us, units, panels = panel_floor(n, exchange_us)
         facts = max(v["launches"], 1) / panels  # factorisations in the timed region
         ach_unit = 1e3 * v["ms"] / facts / units
         floor_unit = floor_us / units
-        unit = "us per panel column" if name == "spanel64" else "us per pivot group of 8 columns"
         hbm_part = {k: out[k] for k in ("achieved", "peak", "unit", "frac", "traffic")}
         out = {"kernel": name, "bound": "latency", "achieved": round(ach_unit, 3), "peak": round(floor_unit, 3),
-               "unit": unit, "frac": round(floor_unit / ach_unit, 4), "traffic": hbm_part["traffic"],
-               "floor": ("per column: max(one cluster exchange round of a 528-byte candidate slot at the panel's "
-                         "cluster size, measured by bola_measure_cluster_exchange; the column's FP64 work per CTA "
-                         "at the measured per-SM DFMA rate)" if name == "spanel64" else
-                         "per group: max(one cluster exchange round of 8 nominees (2176 bytes) at the panel's "
+               "unit": "us per pivot group of 8 columns", "frac": round(floor_unit / ach_unit, 4),
+               "traffic": hbm_part["traffic"],
+               "floor": ("per group: max(one cluster exchange round of 8 nominees (2176 bytes) at the panel's "
                          "cluster size, measured by bola_measure_cluster_exchange; the group's FP32 work per CTA "
                          "at 128 FMA/clock/SM)"),
-               "exchange_round_us": {str(c): round(exchange_us(c, SSLOT_BYTES if name == "spanel64"
-                                                               else 8 * TSLOT_BYTES), 3) for c in (2, 4, 8, 16)},
+               "exchange_round_us": {str(c): round(exchange_us(c, 8 * TSLOT_BYTES), 3) for c in (2, 4, 8, 16)},
                "factorisations": round(facts, 2), "hbm": hbm_part}
         if name == "tpanel":
             out["note"] = ("launches of an abandoned 3xTF32 factorisation return at once and are averaged in, "

@@ -27,6 +27,7 @@ SIGNATURES = {
     "bola_profile_count": (_int, []),
     "bola_profile_read": (_int, [_int, ctypes.c_char_p, _int, _p, _p, _p, _p, _p]),
     "bola_measure_fp64_peak": (_int, [_p]),
+    "bola_measure_dmma_peak": (_int, [_p]),
     "bola_measure_cluster_exchange": (_int, [_int, _int, _p]),
     "bola_selftest_bounded_waits": (_int, [_p, ctypes.c_uint32, _p]),
     "bola_idamax": (_int, [_i64, _p, _p, _p]),

@@ -1,5 +1,6 @@
-// calibrate.cu — probes of the device the library runs on: FP64 throughput,
-// the latency of one cluster exchange round, and a bounded-wait self-test.
+// calibrate.cu — probes of the device the library runs on: FP64 throughput
+// (DFMA on the FP64 pipe, and DMMA on the tensor cores for comparison), the
+// latency of one cluster exchange round, and a bounded-wait self-test.
 //
 // The FP64 rate of a GB300 is far below its tensor rates and not a number to
 // take from a datasheet, so roofline fractions of the FP64 kernels are stated
@@ -28,8 +29,63 @@ __global__ void dfma_probe(double *sink, int iters, double a, double b) {
   if (s == 12345.678) sink[0] = s;  // keeps the loop alive; never true for these inputs
 }
 
+// The same measurement through the FP64 tensor-core instruction (DMMA,
+// mma.sync m8n8k4 f64): eight independent accumulator tiles per warp.
+__global__ void dmma_probe(double *sink, int iters, double a0, double b0) {
+  const double a = a0 + threadIdx.x * 1e-12, b = b0 - threadIdx.x * 1e-12;
+  double c[8][2];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) c[i][0] = c[i][1] = 1e-3 * i;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                   : "+d"(c[i][0]), "+d"(c[i][1])
+                   : "d"(a), "d"(b));
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) s = __dadd_rn(s, __dadd_rn(c[i][0], c[i][1]));
+  if (s == 12345.678) sink[0] = s;  // keeps the loop alive; never true for these inputs
+}
+
 }  // namespace
 }  // namespace bola
+
+extern "C" int bola_measure_dmma_peak(double *gflops) {
+  using namespace bola;
+  if (gflops == nullptr) return -1;
+  double *sink = nullptr;
+  BOLA_TRY_CUDA(cudaMalloc(&sink, 64));
+  const int sms = num_sms();
+  const dim3 grid(4 * sms), block(256);
+  const int iters = 2048;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  dmma_probe<<<grid, block>>>(sink, 16, 1.0000001, 1e-9);
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; ++rep) {
+    cudaEventRecord(e0);
+    dmma_probe<<<grid, block>>>(sink, iters, 1.0000001, 1e-9);
+    cudaEventRecord(e1);
+    cudaError_t e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess) {
+      cudaFree(sink);
+      return cuda_fail(e, "dmma_probe");
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(sink);
+  // 8 x 8 x 4 multiply-adds per warp instruction
+  const double flops = 2.0 * 256.0 * 8.0 * iters * (double)grid.x * (block.x / 32);
+  *gflops = flops / (best * 1e6);
+  return 0;
+}
 
 extern "C" int bola_measure_fp64_peak(double *gflops) {
   using namespace bola;

@@ -69,6 +69,12 @@ int bola_profile_read(int index, char *name, int name_len, int64_t *calls, int64
  * same device and clocks.  Synchronises the device. */
 int bola_measure_fp64_peak(double *gflops);
 
+/* The same FP64 throughput measurement through the tensor cores' FP64 MMA
+ * (mma.sync m8n8k4 f64, eight independent tiles per warp, every SM), so the
+ * choice of DFMA for the FP64 kernels rests on a measurement on this device.
+ * Synchronises the device.  No BOLA counterpart. */
+int bola_measure_dmma_peak(double *gflops);
+
 /* Measures one exchange round of a cluster panel (no BOLA counterpart): csize
  * (1..16) CTAs each copy `bytes` (16..8192, a multiple of 16) of shared memory
  * into every CTA of the cluster with bulk copies that complete on the

@@ -50,3 +50,15 @@ def test_cluster_exchange_probe_rejects_bad_arguments():
     us = ctypes.c_double(0.0)
     assert L.bola_measure_cluster_exchange(17, 512, ctypes.byref(us)) == -1
     assert L.bola_measure_cluster_exchange(4, 100, ctypes.byref(us)) == -2
+
+
+def test_fp64_throughput_probes():
+    """DFMA and DMMA probes both run and give plausible FP64 rates (GB300:
+    about 1.2 TFLOP/s through DFMA)."""
+    from bola_gb300 import _lib
+    L = _lib.load()
+    v = ctypes.c_double(0.0)
+    assert L.bola_measure_fp64_peak(ctypes.byref(v)) == 0, L.bola_last_error()
+    assert 100.0 < v.value < 20000.0, v.value
+    assert L.bola_measure_dmma_peak(ctypes.byref(v)) == 0, L.bola_last_error()
+    assert 10.0 < v.value < 20000.0, v.value
