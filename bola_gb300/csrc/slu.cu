@@ -351,20 +351,37 @@ tpanel_kernel(G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
       sm100::bulk_commit();
     }
     // -- 4. the previous group's update on the columns right of this group
+    // (a thread's rows and 4 columns at a time: 8 independent chains of the
+    // 8 dependent FMAs of rank8 in flight; SNB - c0 - TG is a multiple of 8)
     if (g > 0) {
       const float(*U)[TG] = UgT[ub ^ 1];
+      bool on[TRPL];
+      float l[TRPL][TG];
 #pragma unroll
       for (int r = 0; r < TRPL; ++r) {
         const int il = tid + TPT * r;
-        if (il >= nr || rstate[il] >= 0) continue;
-        float l[TG];
+        on[r] = il < nr && rstate[il] < 0;
 #pragma unroll
-        for (int s2 = 0; s2 < TG; ++s2) l[s2] = sp[(pb + s2) * RP + il];
-        for (int k = c0 + TG; k < SNB; ++k) {
-          const float4 u0 = *reinterpret_cast<const float4 *>(&U[k][0]);
-          const float4 u1 = *reinterpret_cast<const float4 *>(&U[k][4]);
-          sp[k * RP + il] = rank8(sp[k * RP + il], l, u0, u1);
+        for (int s2 = 0; s2 < TG; ++s2) l[r][s2] = on[r] ? sp[(pb + s2) * RP + il] : 0.f;
+      }
+      for (int k0 = c0 + TG; k0 < SNB; k0 += 4) {
+        float x[TRPL][4];
+#pragma unroll
+        for (int r = 0; r < TRPL; ++r)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) x[r][j] = on[r] ? sp[(k0 + j) * RP + tid + TPT * r] : 0.f;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const float4 u0 = *reinterpret_cast<const float4 *>(&U[k0 + j][0]);
+          const float4 u1 = *reinterpret_cast<const float4 *>(&U[k0 + j][4]);
+#pragma unroll
+          for (int r = 0; r < TRPL; ++r) x[r][j] = rank8(x[r][j], l[r], u0, u1);
         }
+#pragma unroll
+        for (int r = 0; r < TRPL; ++r)
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            if (on[r]) sp[(k0 + j) * RP + tid + TPT * r] = x[r][j];
       }
     }
     // every CTA's nominees have landed (bounded: a missing push sets the
@@ -470,27 +487,41 @@ tpanel_kernel(G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
       if (row < r0 || row >= r1) continue;
       sp[k * RP + (row - r0)] = k < c0 + t ? Lg[t][k - c0] : UgT[ub][k][t];
     }
+    // (a thread's rows side by side, so that their dependent chains overlap;
+    // pivot rows, of this group or earlier, are left as they are)
+    {
+      bool on[TRPL];
+      float l[TRPL][TG];
 #pragma unroll
-    for (int r = 0; r < TRPL; ++r) {
-      const int il = tid + TPT * r;
-      if (il >= nr) continue;
-      if (rstate[il] >= 0) continue;  // a pivot row (of this group: written above)
-      float l[TG];
+      for (int r = 0; r < TRPL; ++r) {
+        const int il = tid + TPT * r;
+        on[r] = il < nr && rstate[il] < 0;
+      }
 #pragma unroll
       for (int s2 = 0; s2 < TG; ++s2) {
-        l[s2] = 0.f;
-        if (s2 >= gw) continue;
-        float a = sp[(c0 + s2) * RP + il];
 #pragma unroll
-        for (int q = 0; q < s2; ++q) a = fmaf(-l[q], UgT[ub][c0 + s2][q], a);
-        l[s2] = a * invp[s2];
-        sp[(c0 + s2) * RP + il] = l[s2];
+        for (int r = 0; r < TRPL; ++r) {
+          const int il = tid + TPT * r;
+          const bool live = on[r] && s2 < gw;
+          float a = live ? sp[(c0 + s2) * RP + il] : 0.f;
+#pragma unroll
+          for (int q = 0; q < s2; ++q) a = fmaf(-l[r][q], UgT[ub][c0 + s2][q], a);
+          l[r][s2] = live ? a * invp[s2] : 0.f;
+          if (live) sp[(c0 + s2) * RP + il] = l[r][s2];
+        }
       }
-      const int k1 = (int)imin(SNB, c0 + 2 * TG);
-      for (int k = c0 + TG; k < k1; ++k) {
-        const float4 u0 = *reinterpret_cast<const float4 *>(&UgT[ub][k][0]);
-        const float4 u1 = *reinterpret_cast<const float4 *>(&UgT[ub][k][4]);
-        sp[k * RP + il] = rank8(sp[k * RP + il], l, u0, u1);
+      if (c0 + TG < SNB) {  // the next group's 8 columns
+#pragma unroll
+        for (int j = 0; j < TG; ++j) {
+          const int k = c0 + TG + j;
+          const float4 u0 = *reinterpret_cast<const float4 *>(&UgT[ub][k][0]);
+          const float4 u1 = *reinterpret_cast<const float4 *>(&UgT[ub][k][4]);
+#pragma unroll
+          for (int r = 0; r < TRPL; ++r) {
+            const int il = tid + TPT * r;
+            if (on[r]) sp[k * RP + il] = rank8(sp[k * RP + il], l[r], u0, u1);
+          }
+        }
       }
     }
     __syncthreads();
