@@ -186,17 +186,40 @@ __device__ __forceinline__ void pivots_to_interchanges(const int32_t *win, int j
   }
 }
 
-// The interchanges ipg (global, 1-based) as "row rows[t] takes the old row
-// src[t]" for the swap kernel: plan[0] = count, then rows, then src.  Warp 0.
-__device__ __forceinline__ void compose_panel_plan(const int32_t *ipg, int jb, int32_t col0, int32_t *plan) {
-  SwapPlan p;
-  p.ix0 = 0;
-  p.i1 = col0 + 1;
-  p.i2 = col0 + jb;
-  p.i_inc = 1;
-  p.incx = 1;
-  const int cnt = compose_swaps_warp<4, int32_t>(p, ipg, plan + 1, plan + 1 + 2 * SNB);
-  if ((threadIdx.x & 31) == 0) plan[0] = cnt;
+// The panel's row interchanges as "row rows[t] takes the old row src[t]"
+// (global rows) for the swap kernel: plan[0] = count, then rows, then src.
+// From the final state of pivots_to_interchanges (no replay of the swaps):
+// position q < jb takes its pivot pivl[q], and each of the first jb rows
+// that is not a pivot goes to the position posin[x] >= jb it was displaced
+// to.  One warp; entries are compacted with ballots.
+__device__ __forceinline__ void list_panel_moves(const int32_t *pivl, const int32_t *posin, int jb, int32_t col0,
+                                                 int32_t *plan) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  for (int q0 = 0; q0 < jb; q0 += 32) {
+    const int q = q0 + lane;
+    const bool mv = q < jb && pivl[q] != q;
+    const unsigned m = __ballot_sync(FULL, mv);
+    if (mv) {
+      const int slot = base + __popc(m & ((1u << lane) - 1u));
+      plan[1 + slot] = col0 + q;
+      plan[1 + 2 * SNB + slot] = col0 + pivl[q];
+    }
+    base += __popc(m);
+  }
+  for (int x0 = 0; x0 < jb; x0 += 32) {
+    const int x = x0 + lane;
+    const bool mv = x < jb && posin[x] >= jb;
+    const unsigned m = __ballot_sync(FULL, mv);
+    if (mv) {
+      const int slot = base + __popc(m & ((1u << lane) - 1u));
+      plan[1 + slot] = col0 + posin[x];
+      plan[1 + 2 * SNB + slot] = col0 + x;
+    }
+    base += __popc(m);
+  }
+  if (lane == 0) plan[0] = base;
 }
 
 // Dynamic shared memory of the tournament panel: the rows (column-major,
@@ -565,7 +588,7 @@ tpanel_kernel(G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
 #pragma unroll 8
       for (int c = 0; c < jb; ++c) wr[(int64_t)c * ldw] = sp[c * RP + il];
     }
-    if (plan != nullptr && cr == 0 && warp == 0) compose_panel_plan(ipg, jb, col0, plan);
+    if (plan != nullptr && cr == 0 && warp == 0) list_panel_moves(win, posin, jb, col0, plan);
     if (aop != nullptr) {  // rows below the panel's top: the update's K-major A operand
       for (int il = tid; il < nr; il += TPT) {
         const int dst = dest(il);
@@ -826,7 +849,7 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
     pivots_to_interchanges(pivl, jb, col0, posin, at_, ipg);
   }
   __syncthreads();
-  if (warp == 0) compose_panel_plan(ipg, jb, col0, plan);
+  if (warp == 0) list_panel_moves(pivl, posin, jb, col0, plan);
   for (int t = tid; t < jb; t += T64_THREADS) ipiv[t] = ipg[t];
   __syncthreads();
   // rows the interchanges move below the block: their panel columns, read
