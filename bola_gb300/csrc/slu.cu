@@ -164,36 +164,40 @@ __device__ __forceinline__ int group_gepp(float (&v)[RPL][TG], bool (&live)[RPL]
   return cnt;
 }
 
-// LAPACK's interchanges for a panel whose pivot of column j is panel row
-// win[j] (j < jb): ipg[j] = col0 + 1 + the position row j swaps with.  Rows
+// LAPACK's interchanges for a panel whose pivot of column j is panel row x
+// (j < jb), one column at a time in column order: interchange_step returns
+// ipiv's entry for column j (col0 + 1 + the position row j swaps with).  Rows
 // below the panel's first jb never move until they become a pivot; rows among
 // the first jb are tracked: at_[q] = the row now in position q < jb,
-// posin[x] = the position of original row x < jb.  One thread.
-__device__ __forceinline__ void pivots_to_interchanges(const int32_t *win, int jb, int32_t col0, int32_t *posin,
-                                                       int32_t *at_, int32_t *ipg) {
+// posin[x] = the position of original row x < jb (interchanges_init: the
+// identity).  One thread; a column's step needs only the pivots before it, so
+// the kernels run the steps while the later columns are still being factored.
+__device__ __forceinline__ void interchanges_init(int jb, int32_t *posin, int32_t *at_) {
   for (int x = 0; x < jb; ++x) posin[x] = at_[x] = x;
-  for (int j = 0; j < jb; ++j) {
-    const int x = win[j];
-    const int q = x < jb ? posin[x] : x;
-    ipg[j] = col0 + q + 1;
-    const int r = at_[j];
-    if (r != x) {
-      if (q < jb) at_[q] = r;
-      posin[r] = q;
-    }
-    at_[j] = x;
-    if (x < jb) posin[x] = j;
+}
+__device__ __forceinline__ int32_t interchange_step(int j, int x, int jb, int32_t col0, int32_t *posin,
+                                                    int32_t *at_) {
+  const int q = x < jb ? posin[x] : x;
+  const int r = at_[j];
+  if (r != x) {
+    if (q < jb) at_[q] = r;
+    posin[r] = q;
   }
+  at_[j] = x;
+  if (x < jb) posin[x] = j;
+  return col0 + q + 1;
 }
 
 // The panel's row interchanges as "row rows[t] takes the old row src[t]"
 // (global rows) for the swap kernel: plan[0] = count, then rows, then src.
-// From the final state of pivots_to_interchanges (no replay of the swaps):
+// From the final state of the interchange steps (no replay of the swaps):
 // position q < jb takes its pivot pivl[q], and each of the first jb rows
 // that is not a pivot goes to the position posin[x] >= jb it was displaced
-// to.  One warp; entries are compacted with ballots.
+// to.  One warp; entries are compacted with ballots.  With rows_s != nullptr
+// the list also goes to shared memory, as panel rows (rows_s, src_s, *cnt_s).
 __device__ __forceinline__ void list_panel_moves(const int32_t *pivl, const int32_t *posin, int jb, int32_t col0,
-                                                 int32_t *plan) {
+                                                 int32_t *plan, int32_t *rows_s = nullptr, int32_t *src_s = nullptr,
+                                                 int *cnt_s = nullptr) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   int base = 0;
@@ -205,6 +209,10 @@ __device__ __forceinline__ void list_panel_moves(const int32_t *pivl, const int3
       const int slot = base + __popc(m & ((1u << lane) - 1u));
       plan[1 + slot] = col0 + q;
       plan[1 + 2 * SNB + slot] = col0 + pivl[q];
+      if (rows_s != nullptr) {
+        rows_s[slot] = q;
+        src_s[slot] = pivl[q];
+      }
     }
     base += __popc(m);
   }
@@ -216,10 +224,17 @@ __device__ __forceinline__ void list_panel_moves(const int32_t *pivl, const int3
       const int slot = base + __popc(m & ((1u << lane) - 1u));
       plan[1 + slot] = col0 + posin[x];
       plan[1 + 2 * SNB + slot] = col0 + x;
+      if (rows_s != nullptr) {
+        rows_s[slot] = posin[x];
+        src_s[slot] = x;
+      }
     }
     base += __popc(m);
   }
-  if (lane == 0) plan[0] = base;
+  if (lane == 0) {
+    plan[0] = base;
+    if (cnt_s != nullptr) *cnt_s = base;
+  }
 }
 
 // Dynamic shared memory of the tournament panel: the rows (column-major,
@@ -250,9 +265,8 @@ __device__ __forceinline__ float rank8(float a, const float (&l)[TG], const floa
 // FP64 kernels that follow (panel_top64, panel_l21_64).
 template <typename G>
 __global__ void __launch_bounds__(TPT, 1)
-tpanel_kernel(G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0, int32_t *info, int kind,
-              void *aop, float *aop_lo, int64_t R, int32_t *plan, uint64_t *track, double give_up, int32_t *err,
-              int32_t *winout) {
+tpanel_kernel(G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0, int32_t *info, int64_t R,
+              int32_t *plan, uint64_t *track, double give_up, int32_t *err, int32_t *winout) {
   constexpr bool SEL = std::is_same<G, double>::value;
   cg::cluster_group cluster = cg::this_cluster();
   // an abandoned factorisation (flag set by an earlier panel on this stream,
@@ -273,7 +287,7 @@ tpanel_kernel(G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
   __shared__ float Lg[TG][TG];             // the group pivots' multipliers within the group
   __shared__ __align__(16) float UgT[2][SNB][TG];  // U rows of a group's pivots, transposed (two groups)
   __shared__ float invp[TG];
-  __shared__ int32_t posin[SNB], at_[SNB], ipg[SNB];  // interchange bookkeeping (CTA 0)
+  __shared__ int32_t posin[SNB], at_[SNB];  // interchange bookkeeping (CTA 0)
   __shared__ int sfail;
   __shared__ TSlot stage[TG];              // this CTA's nominees, as they are pushed
   __shared__ int32_t selw[2][TG];          // pivot searches' outputs (candidate order): own rows, nominees
@@ -450,6 +464,11 @@ tpanel_kernel(G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
           for (int t = 0; t < TG; ++t) Linv[t][lane] = col[t];
         }
       }
+    } else if (!SEL && cr == 0 && tid == TPT / 2) {
+      // meanwhile (warps 4-7 are idle): LAPACK's interchanges for the
+      // previous group's pivots
+      if (g == 0) interchanges_init(jb, posin, at_);
+      for (int j = c0 - TG; j >= 0 && j < c0; ++j) ipiv[j] = interchange_step(j, win[j], jb, col0, posin, at_);
     }
     __syncthreads();
     if (win[c0 + gw - 1] < 0) {  // (err is set) leave the group loop uniformly
@@ -554,13 +573,10 @@ tpanel_kernel(G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
       if (cr == 0)
         for (int t = tid; t < jb; t += TPT) winout[t] = win[t];
     } else {
-    // -- the interchanges (CTA 0): LAPACK's sequence of row swaps that puts
-    // the pivot of column j in row j, from the pivot list
-    if (cr == 0 && tid == 0) {
-      pivots_to_interchanges(win, jb, col0, posin, at_, ipg);
-      for (int j = 0; j < jb; ++j) ipiv[j] = ipg[j];
-    }
-    __syncthreads();
+    // -- the last group's interchanges (CTA 0; the earlier groups' ran
+    // during the searches that followed them)
+    if (cr == 0 && tid == TPT / 2)
+      for (int j = (ngroups - 1) * TG; j < jb; ++j) ipiv[j] = interchange_step(j, win[j], jb, col0, posin, at_);
     if (track != nullptr && cr == 0 && tid == TPT - 1) {
       if (umin != ~0ull) {
         const uint64_t mx = (uint64_t)__double_as_longlong((double)__uint_as_float((uint32_t)umax));
@@ -572,45 +588,65 @@ tpanel_kernel(G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
       const double spread = gmn > 0.0 ? gmx / gmn : INFINITY;
       if (give_up_now(spread, give_up, col0 + jb, col0 + mp)) *(volatile int32_t *)(track + 2) = 1;
     }
-    // final position of each of this CTA's rows
-    auto dest = [&](int il) -> int {
-      const int st = rstate[il];
-      if (st >= 0) return st;
-      if (cr == 0 && il < jb) return posin[il];
-      return r0 + il;
-    };
-    // -- write back the panel, each row to its final position
+    __syncthreads();
+    // -- write back the panel: first every row where it started, as float4
+    // runs of 4 rows (a warp writes 512 contiguous bytes of a column; R is a
+    // multiple of 4, so runs start 16-byte aligned in W when W and ldw allow);
+    // the rows that move (the pivots, and CTA 0's first jb rows that are not
+    // pivots) are written again to their final positions after the cluster
+    // barrier below, so that those writes land last
+    const bool vec = (ldw & 3) == 0 && (reinterpret_cast<uintptr_t>(W) & 15) == 0 && (R & 3) == 0;
+    if (vec) {
+      const int nq4 = nr / 4;
+      for (int e = tid; e < nq4 * jb; e += TPT) {
+        const int il0 = 4 * (e % nq4), c = e / nq4;
+        *reinterpret_cast<float4 *>(&W[(r0 + il0) + (int64_t)c * ldw]) =
+            *reinterpret_cast<const float4 *>(&sp[c * RP + il0]);
+      }
+      for (int e = tid; e < (nr - 4 * nq4) * jb; e += TPT) {
+        const int il = 4 * nq4 + e % (nr - 4 * nq4), c = e / (nr - 4 * nq4);
+        W[(r0 + il) + (int64_t)c * ldw] = sp[c * RP + il];
+      }
+    } else {
 #pragma unroll
-    for (int r = 0; r < TRPL; ++r) {
-      const int il = tid + TPT * r;
-      if (il >= nr) continue;
-      G *wr = W + dest(il);
+      for (int r = 0; r < TRPL; ++r) {
+        const int il = tid + TPT * r;
+        if (il >= nr) continue;
 #pragma unroll 8
-      for (int c = 0; c < jb; ++c) wr[(int64_t)c * ldw] = sp[c * RP + il];
-    }
-    if (plan != nullptr && cr == 0 && warp == 0) list_panel_moves(win, posin, jb, col0, plan);
-    if (aop != nullptr) {  // rows below the panel's top: the update's K-major A operand
-      for (int il = tid; il < nr; il += TPT) {
-        const int dst = dest(il);
-        if (dst < jb) continue;
-        float v[SNB];
-#pragma unroll
-        for (int c = 0; c < SNB; ++c) v[c] = c < jb ? sp[c * RP + il] : 0.f;
-        write_operand_row(kind, aop, aop_lo, dst - jb, v);
+        for (int c = 0; c < jb; ++c) W[(r0 + il) + (int64_t)c * ldw] = sp[c * RP + il];
       }
     }
+    if (plan != nullptr && cr == 0 && warp == 0) list_panel_moves(win, posin, jb, col0, plan);
     }
   }
   if (tid < C) sm100::bulk_wait_read0();  // this CTA's last pushes have read its staging slots
   cluster.sync();  // no CTA leaves while another may still push into it
+  if constexpr (!SEL) {
+    if (!failed) {
+      // the rows that move, over their first write: the pivot of column t
+      // (panel row win[t]) to position t, lanes on consecutive t; CTA 0's
+      // first jb rows that are not pivots to where the interchanges put them
+      for (int e = tid; e < jb * jb; e += TPT) {
+        const int t = e % jb, c = e / jb, x = win[t];
+        if (x >= r0 && x < r1) W[t + (int64_t)c * ldw] = sp[c * RP + (x - r0)];
+      }
+      if (cr == 0)
+        for (int e = tid; e < jb * jb; e += TPT) {
+          const int il = e % jb, c = e / jb;
+          if (rstate[il] < 0) W[posin[il] + (int64_t)c * ldw] = sp[c * RP + il];
+        }
+    }
+  }
 }
 
 template <typename G>
 int launch_tpanel(cudaStream_t s, G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0,
-                  int32_t *info, int kind, void *aop, float *aop_lo, int32_t *plan, uint64_t *track, double give_up,
-                  int32_t *err, int32_t *winout = nullptr) {
+                  int32_t *info, int32_t *plan, uint64_t *track, double give_up, int32_t *err,
+                  int32_t *winout = nullptr) {
   const int C = (int)imin(SMAXC, imax(1, cdiv(mp, TPT)));
-  const int64_t R = cdiv(mp, C);
+  // rows per CTA, a multiple of 4 (the write-back's float4 runs); C <= 16
+  // keeps the last CTA's share positive: mp > 256 (C - 1) > 4 C (C - 1)
+  const int64_t R = cdiv(cdiv(mp, C), 4) * 4;
   // CTA 0 must hold the panel's first jb rows (the interchange bookkeeping)
   if (R > (int64_t)TPT * TRPL || R < jb)
     return fail(BOLA_ERR_UNSUPPORTED, "mixed LU: panel of %lld x %d not supported", (long long)mp, jb);
@@ -636,8 +672,8 @@ int launch_tpanel(cudaStream_t s, G *W, int64_t ldw, int64_t mp, int jb, int32_t
   cfg.numAttrs = 1;
   ProfScope prof(s, std::is_same<G, double>::value ? "tselect64" : "tpanel", (double)mp * jb * jb,
                  8.0 * (double)mp * jb);
-  BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, tpanel_kernel<G>, W, ldw, mp, jb, ipiv, col0, info, kind, aop, aop_lo, R,
-                                   plan, track, give_up, err, winout));
+  BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, tpanel_kernel<G>, W, ldw, mp, jb, ipiv, col0, info, R, plan, track,
+                                   give_up, err, winout));
   return 0;
 }
 
@@ -698,8 +734,7 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
     return;
   }
   __shared__ double a[SNB][SNB + 1];  // a[q][c]: the row now in position q, column c
-  __shared__ int32_t win[SNB], rowid[SNB], pivl[SNB], posin[SNB], at_[SNB], ipg[SNB], rows_s[2 * SNB],
-      src_s[2 * SNB];
+  __shared__ int32_t win[SNB], rowid[SNB], pivl[SNB], posin[SNB], at_[SNB], rows_s[2 * SNB], src_s[2 * SNB];
   __shared__ double rinv_s[2];             // 1 / the pivot of column k (k & 1)
   __shared__ uint32_t wkey[2][T64_WARPS];  // the warps' best keys for column k (k & 1)
   __shared__ int bad, cnt_s;
@@ -750,6 +785,8 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
     key = __reduce_max_sync(0xffffffffu, key);
     if (lane == 0) wkey[k & 1][warp] = key;
   };
+  if (tid == 0) interchanges_init(jb, posin, at_);
+  int jdone = 0;  // (thread 0) columns whose interchange is done
   __syncthreads();
   publish(a[q][0], 0);
 #pragma unroll 1
@@ -787,6 +824,15 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
     asm volatile("bar.sync 1, %0;" ::"r"(T64_THREADS) : "memory");
     if ((warp + 1) * (32 / T64_LPR) - 1 <= k) {  // every row of this warp is done: no candidate for k + 1
       if (lane == 0) wkey[par ^ 1][warp] = 0u;
+      // warp 0, idle from column 7 on, runs LAPACK's interchanges for the
+      // columns whose pivot row is final (positions 0..k), two per column
+      // until it has caught up
+      if (tid == 0)
+        for (int u = 0; u < 2 && jdone <= k; ++u, ++jdone) {
+          const int x = win[rowid[jdone]];
+          pivl[jdone] = x;
+          ipiv[jdone] = interchange_step(jdone, x, jb, col0, posin, at_);
+        }
       continue;
     }
     const bool act = q > k && q < jb;
@@ -822,9 +868,10 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
       }
     }
   }
-  // the pivots' extent lives with the lanes that saw them: fold into thread 0
+  // the pivots' extent lives with the lanes that saw them: per warp here,
+  // into thread 0 at the end
+  __shared__ uint64_t wx[T64_WARPS], wn[T64_WARPS];
   {
-    __syncthreads();
     uint64_t mx = umax, mn = umin;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -832,34 +879,23 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
       mx = o1 > mx ? o1 : mx;
       mn = o2 < mn ? o2 : mn;
     }
-    __shared__ uint64_t wx[T64_WARPS], wn[T64_WARPS];
     if (lane == 0) {
       wx[warp] = mx;
       wn[warp] = mn;
     }
-    __syncthreads();
-    if (tid == 0)
-      for (int w = 0; w < T64_WARPS; ++w) {
-        umax = wx[w] > umax ? wx[w] : umax;
-        umin = wn[w] < umin ? wn[w] : umin;
-      }
   }
-  if (tid == 0) {
-    for (int t = 0; t < jb; ++t) pivl[t] = win[rowid[t]];  // panel row of the pivot of column t
-    pivots_to_interchanges(pivl, jb, col0, posin, at_, ipg);
-  }
+  if (tid == 0)  // the interchanges still to run (the last columns, or all of a narrow block)
+    for (; jdone < jb; ++jdone) {
+      const int x = win[rowid[jdone]];
+      pivl[jdone] = x;
+      ipiv[jdone] = interchange_step(jdone, x, jb, col0, posin, at_);
+    }
   __syncthreads();
-  if (warp == 0) list_panel_moves(pivl, posin, jb, col0, plan);
-  for (int t = tid; t < jb; t += T64_THREADS) ipiv[t] = ipg[t];
+  // the moves of rows, to the swap kernel (plan) and to this CTA (rows_s, src_s)
+  if (warp == 0) list_panel_moves(pivl, posin, jb, col0, plan, rows_s, src_s, &cnt_s);
   __syncthreads();
   // rows the interchanges move below the block: their panel columns, read
   // before anything is written
-  if (tid == 0) cnt_s = plan[0];
-  for (int t = tid; t < 2 * SNB; t += T64_THREADS) {
-    rows_s[t] = plan[1 + t] - col0;
-    src_s[t] = plan[1 + 2 * SNB + t] - col0;
-  }
-  __syncthreads();
   const int cnt = cnt_s;
   constexpr int MV = 2 * SNB * SNB / T64_THREADS;
   double mv[MV];
@@ -881,6 +917,10 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
   }
   if (track != nullptr && tid == 0) {
     // the running extent of |u_ii| and the give-up test
+    for (int w = 0; w < T64_WARPS; ++w) {
+      umax = wx[w] > umax ? wx[w] : umax;
+      umin = wn[w] < umin ? wn[w] : umin;
+    }
     if (umin != ~0ull) {
       if (umax > track[0]) track[0] = umax;
       if (umin < track[1]) track[1] = umin;
@@ -975,16 +1015,69 @@ panel_l21_64(double *Wp, int64_t ldw, int64_t mp, int jb, void *aop, int32_t *ae
   }
 }
 
+// Rows r0 .. r0 + 63 of the update's K-major A operand (kinds 0-2) from the
+// factored panel: operand row r is row j + 64 + r of W's columns j .. j + 63
+// (final once the panel kernel has written them back), rounded as
+// write_operand_row rounds.  The 64 x 64 tile is read a column at a time and
+// written a row at a time, both coalesced, through t (64 x 64, columns
+// XOR-swizzled by the row so that both passes are free of bank conflicts).
+__device__ __forceinline__ void operand_tile(const float *W, int64_t ldw, int64_t j, int64_t m2, int64_t r0,
+                                             int kind, void *op, float *op_lo, float *t) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int rows = (int)imin(SNB, m2 - r0);
+  const float *src = W + (j + SNB + r0) + j * ldw;
+  constexpr int PER = SNB * SNB / 256;
+  float v[PER];
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int e = tid + 256 * q, r = e % SNB, c = e / SNB;
+    v[q] = r < rows ? src[r + (int64_t)c * ldw] : 0.f;
+  }
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int e = tid + 256 * q, r = e % SNB, c = e / SNB;
+    t[r * SNB + (c ^ (r & 31))] = v[q];
+  }
+  __syncthreads();
+  for (int r = warp; r < rows; r += 8) {
+    const float a = t[r * SNB + (lane ^ (r & 31))], b = t[r * SNB + ((lane + 32) ^ (r & 31))];
+    const int64_t orow = r0 + r;
+    if (kind == 0) {
+      __nv_bfloat16 *d = static_cast<__nv_bfloat16 *>(op) + orow * SNB;
+      d[lane] = __float2bfloat16_rn(a);
+      d[lane + 32] = __float2bfloat16_rn(b);
+    } else {
+      float *d = static_cast<float *>(op) + orow * SNB;
+      const float ha = tf32_round(a), hb = tf32_round(b);
+      d[lane] = ha;
+      d[lane + 32] = hb;
+      if (kind == 2) {
+        float *dl = op_lo + orow * SNB;
+        dl[lane] = tf32_round(a - ha);
+        dl[lane + 32] = tf32_round(b - hb);
+      }
+    }
+  }
+}
+
 // The panel's interchanges on all other columns, U12 = L11^-1 A12 on the
-// right ones and their K-major B operand.  A warp per column.
+// right ones and their K-major B operand: a warp per column, ncta CTAs.  The
+// FP32 factors' CTAs from ncta on write the A operand of the update (aop:
+// operand_tile, one 64-row tile each).
 template <typename T>
 __global__ void __launch_bounds__(256)
 sswap_trsm(T *W, int64_t ldw, int64_t n, int64_t j, int jb, const int32_t *plan, int kind, void *bop,
-           float *bop_lo, int32_t *bexp, int64_t cap, const int32_t *abort) {
+           float *bop_lo, int32_t *bexp, int64_t cap, const int32_t *abort, int ncta, void *aop, float *aop_lo) {
   if (abort != nullptr && *(volatile const int32_t *)abort != 0) return;  // set before this launch (same stream)
   __shared__ int32_t rows[2 * SNB], src[2 * SNB];
-  __shared__ T L[SNB * SNB];
+  __shared__ __align__(16) T L[SNB * SNB];
   __shared__ int cnt;
+  if constexpr (std::is_same<T, float>::value) {
+    if ((int)blockIdx.x >= ncta) {
+      operand_tile(W, ldw, j, n - j - jb, (int64_t)((int)blockIdx.x - ncta) * SNB, kind, aop, aop_lo, L);
+      return;
+    }
+  }
   // the interchanges, composed once by the panel kernel
   if (threadIdx.x == 0) cnt = plan[0];
   for (int t = threadIdx.x; t < 2 * SNB; t += blockDim.x) {
@@ -1177,8 +1270,8 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
       // of the selected block and of the rows below it
       double *Wp = W + j + j * ldw;
       int32_t *win = lu.plan + 1 + 4 * SNB;
-      BOLA_TRY(launch_tpanel<double>(lu.sp, Wp, ldw, mp, jb, ipiv + j, (int32_t)j, info, lu.kind, nullptr, nullptr,
-                                     nullptr, track, give_up, lu.err, win));
+      BOLA_TRY(launch_tpanel<double>(lu.sp, Wp, ldw, mp, jb, ipiv + j, (int32_t)j, info, nullptr, track, give_up,
+                                     lu.err, win));
       {
         ProfScope prof(lu.sp, "panel_top64", (double)jb * jb * jb * 2.0 / 3.0, 16.0 * (double)jb * jb);
         panel_top64<<<1, T64_THREADS, 0, lu.sp>>>(Wp, ldw, mp, jb, (int32_t)j, win, lu.plan, ipiv + j, info, track,
@@ -1192,17 +1285,21 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
       }
       BOLA_CHECK_LAUNCH();
     } else
-      BOLA_TRY(launch_tpanel(lu.sp, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, lu.kind,
-                             upd ? lu.aop[buf] : nullptr, lu.aop_lo[buf], lu.plan, track, give_up, lu.err));
+      BOLA_TRY(launch_tpanel(lu.sp, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, lu.plan, track,
+                             give_up, lu.err));
     // the row swaps reach every column: the previous wide update must be done
     if (wide_pending) BOLA_TRY_CUDA(cudaStreamWaitEvent(lu.sp, lu.ev_wide, 0));
     wide_pending = false;
     const int64_t others = n - jb;
     if (others > 0) {
       ProfScope prof(lu.sp, fp64 ? "sswap_trsm64" : "sswap_trsm", (double)jb * jb * (double)(n - j - jb));
-      sswap_trsm<T><<<(unsigned)cdiv(others, 8), 256, 0, lu.sp>>>(W, ldw, n, j, jb, lu.plan, lu.kind,
-                                                                    upd ? lu.bop : nullptr, fp64 ? nullptr : lu.bop_lo,
-                                                                    fp64 ? lu.eb : nullptr, lu.cap_n, abort);
+      // (the FP32 factors: one more CTA per 64 rows below the panel writes
+      // the update's A operand)
+      const int ncta = (int)cdiv(others, 8);
+      const int nop = (!fp64 && upd) ? (int)cdiv(mp - jb, SNB) : 0;
+      sswap_trsm<T><<<(unsigned)(ncta + nop), 256, 0, lu.sp>>>(
+          W, ldw, n, j, jb, lu.plan, lu.kind, upd ? lu.bop : nullptr, fp64 ? nullptr : lu.bop_lo,
+          fp64 ? lu.eb : nullptr, lu.cap_n, abort, ncta, fp64 ? nullptr : lu.aop[buf], fp64 ? nullptr : lu.aop_lo[buf]);
       BOLA_CHECK_LAUNCH();
     }
     if (!upd) continue;

@@ -205,8 +205,9 @@ template <int KIND, int NPASS>
 __global__ void __launch_bounds__(PTHREADS, 1)
 tc_update_pipe(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                const __grid_constant__ CUtensorMap mapAlo, const __grid_constant__ CUtensorMap mapBlo,
-               const __grid_constant__ CUtensorMap mapW, int64_t m, int64_t n, int64_t boff, int tpc,
-               int32_t *err, const int32_t *abort, int lower) {
+               const __grid_constant__ CUtensorMap mapW, const __grid_constant__ CUtensorMap mapWs, int64_t m,
+               int64_t n, int64_t boff, int tpc, int32_t *err, const int32_t *abort, int lower, float *W,
+               int64_t ldw) {
   using Cfg = PCfg<KIND, NPASS>;
   if (abandoned(abort)) return;
   extern __shared__ uint8_t smem_raw[];
@@ -341,11 +342,22 @@ tc_update_pipe(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
         if (lane == 0) mbar_arrive(&acc_empty[st]);
 #pragma unroll
         for (int c = 0; c < 32; ++c) Ws[(h * 32 + c) * BM + r] -= v[c];
+        // the last 1-3 rows when m is not a multiple of 4: the tile store
+        // (mapWs) covers m & ~3 rows only — a TMA store clips the innermost
+        // dimension at 16-byte granularity, and the rows past m belong to the
+        // caller (ldw > m) — so these go by plain stores
+        const int64_t row = (int64_t)i * BM + r;
+        if (row >= (m & ~(int64_t)3) && row < m) {
+          for (int c = 0; c < 32; ++c) {
+            const int64_t col = (int64_t)j * PBN + h * 32 + c;
+            if (col < n) W[row + col * ldw] = Ws[(h * 32 + c) * BM + r];
+          }
+        }
       }
       fence_proxy_async_smem();
       if (epilogue_bar_any(!ok)) break;  // the epilogue warps only
       if (ew == 0 && lane == 0) {
-        tma_store_2d(&mapW, Ws, i * BM, j * PBN);  // rows and columns outside W are clipped
+        tma_store_2d(&mapWs, Ws, i * BM, j * PBN);  // rows (past m & ~3) and columns outside W are clipped
         bulk_commit();
         bulk_wait_read0();
         mbar_arrive(&w_empty[st]);
@@ -446,10 +458,13 @@ int tc_update(cudaStream_t s, int kind, int64_t m, int64_t n, const CUtensorMap 
               const int32_t *abort, bool lower) {
   if (m <= 0 || n <= 0) return 0;
   ProfScope prof(s, "tc_update", 2.0 * (double)m * n * KDIM * (kind == 2 ? 3 : 1), 8.0 * (double)m * n);
-  if ((ldw & 3) == 0 && (reinterpret_cast<uintptr_t>(W) & 15) == 0) {
-    // the pipelined kernel: W's tiles move by TMA (16-byte aligned rows)
-    CUtensorMap mapW;
+  if ((ldw & 3) == 0 && (reinterpret_cast<uintptr_t>(W) & 15) == 0 && m >= 4) {
+    // the pipelined kernel: W's tiles move by TMA (16-byte aligned rows);
+    // loads see all m rows, the tile store m & ~3 of them (the rest are
+    // stored by the epilogue threads)
+    CUtensorMap mapW, mapWs;
     BOLA_TRY(make_fp32_tile_map(&mapW, W, m, n, ldw));
+    BOLA_TRY(make_fp32_tile_map(&mapWs, W, m & ~(int64_t)3, n, ldw));
     const int64_t tiles = cdiv(m, BM) * cdiv(n, PBN);
     // runs of up to 8 tiles per CTA, but never fewer CTAs than twice the SMs
     // (a narrow update, on the critical path, keeps one tile per CTA)
@@ -464,8 +479,8 @@ int tc_update(cudaStream_t s, int kind, int64_t m, int64_t n, const CUtensorMap 
           cudaFuncSetAttribute(tc_update_pipe<KIND, NPASS>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM)); \
       attr = true;                                                                                              \
     }                                                                                                           \
-    tc_update_pipe<KIND, NPASS><<<grid, PTHREADS, Cfg::SMEM, s>>>(A, B, Alo, Blo, mapW, m, n, boff, tpc, err, abort, \
-                                                                  lower ? 1 : 0);                               \
+    tc_update_pipe<KIND, NPASS><<<grid, PTHREADS, Cfg::SMEM, s>>>(A, B, Alo, Blo, mapW, mapWs, m, n, boff, tpc, err, \
+                                                                  abort, lower ? 1 : 0, W, ldw);                \
   } while (0)
     if (kind == 0) BOLA_TCP(0, 1);
     else if (kind == 1) BOLA_TCP(1, 1);

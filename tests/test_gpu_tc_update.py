@@ -4,7 +4,9 @@ same operation (bf16, tf32 and 3xTF32 operand forms).
 Shapes cover both kernels: a leading dimension that is not a multiple of 4
 takes the one-tile-per-CTA kernel, the others the pipelined kernel, with
 partial row and column tiles, padding rows below m (which must stay
-untouched) and, at 4096, runs of several tiles per CTA."""
+untouched, also when m is not a multiple of 4: the pipelined kernel's tile
+store stops at m & ~3 and the last rows go by plain stores) and, at 4096,
+runs of several tiles per CTA."""
 import ctypes
 
 import pytest
@@ -28,6 +30,7 @@ def tf32_split(x):
 
 @pytest.mark.parametrize("kind", [0, 1, 2])
 @pytest.mark.parametrize("m,n,ldw", [(128, 128, 128), (300, 200, 301), (1000, 77, 1000), (500, 300, 516),
+                                   (501, 300, 516), (1023, 130, 1028), (3, 64, 8),
                                    (2048, 2048, 2048), (4096, 4096, 4096)])
 def test_tc_update_matches_fp32_reference(kind, m, n, ldw):
     from bola_gb300 import _lib

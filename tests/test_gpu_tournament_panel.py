@@ -89,3 +89,27 @@ def test_tournament_lu_zero_column_reports_info():
     W = torch.from_numpy(A.astype(np.float32).ravel(order="F").copy()).cuda()
     _, info = factor(W, n, 2)
     assert info == 78
+
+
+@pytest.mark.parametrize("n,ldw", [(1001, 1004), (333, 336), (2050, 2056)])
+def test_tournament_lu_padded_leading_dimension(n, ldw):
+    """ldw > n, a multiple of 4 (the panel's float4 write-back runs) with n
+    not one (ragged last runs); the padding rows keep their values."""
+    from bola_gb300 import _lib
+    L = _lib.load()
+    A = wl.uniform_matrix(n, n, seed=n, lo=-1.0, hi=1.0)
+    buf = np.full((ldw, n), 7.25, dtype=np.float32)
+    buf[:n] = A.astype(np.float32)
+    W = torch.from_numpy(buf.ravel(order="F").copy()).cuda()
+    ipiv = torch.zeros(n, dtype=torch.int32, device="cuda")
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    st = L.bola_sgetrf_mixed(2, n, _p(W), ldw, _p(ipiv), _p(info),
+                             ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == 0 and int(info.item()) == 0
+    out = W.cpu().numpy().reshape(ldw, n, order="F")
+    assert np.all(out[n:] == 7.25)
+    # the same factors as with ldw = n
+    W2 = torch.from_numpy(A.astype(np.float32).ravel(order="F").copy()).cuda()
+    ipiv2, _ = factor(W2, n, 2)
+    assert np.array_equal(ipiv.cpu().numpy(), ipiv2)
+    assert np.array_equal(out[:n], W2.cpu().numpy().reshape(n, n, order="F"))
