@@ -332,35 +332,40 @@ __device__ __forceinline__ void block_product(float (&acc)[RH], const float (*A)
 }
 
 // Spins until block k's words carry this launch's epoch, into X[kk][c].  A
-// thread's words are all loaded at once (one L2 round trip, not one per
-// word); only those not yet published are polled again.
+// thread's words are loaded together, and each pass polls again all of
+// those not yet published, together: one L2 round trip per pass, not one
+// per word.
 template <int RH>
 __device__ __forceinline__ void take_block(const unsigned long long *xw, int64_t n, int nrhs, int64_t k0, int kbk,
                                            uint32_t epoch, float (*X)[4 * RH], int32_t *err) {
   constexpr int PW = TB * 4 * RH / 256;  // words per thread
   unsigned long long w[PW];
+  bool need[PW];
 #pragma unroll
   for (int u = 0; u < PW; ++u) {
     const int e = threadIdx.x + 256 * u, kk = e % TB, c = e / TB;
-    w[u] = (kk < kbk && c < nrhs) ? ld_word(xw + (k0 + kk) + (int64_t)c * n) : 0ull;
+    need[u] = kk < kbk && c < nrhs;
+    w[u] = need[u] ? ld_word(xw + (k0 + kk) + (int64_t)c * n) : 0ull;
+  }
+  for (int polls = 0;; ++polls) {
+    bool done = true;
+#pragma unroll
+    for (int u = 0; u < PW; ++u) done = done && (!need[u] || (uint32_t)(w[u] >> 32) == epoch);
+    if (done) break;
+    if (polls >= (1 << 20)) {
+      atomicExch(err, 3);
+      break;
+    }
+#pragma unroll
+    for (int u = 0; u < PW; ++u) {
+      const int e = threadIdx.x + 256 * u, kk = e % TB, c = e / TB;
+      if (need[u] && (uint32_t)(w[u] >> 32) != epoch) w[u] = ld_word(xw + (k0 + kk) + (int64_t)c * n);
+    }
   }
 #pragma unroll
   for (int u = 0; u < PW; ++u) {
     const int e = threadIdx.x + 256 * u, kk = e % TB, c = e / TB;
-    float v = 0.f;
-    if (kk < kbk && c < nrhs) {
-      const unsigned long long *p = xw + (k0 + kk) + (int64_t)c * n;
-      int polls = 0;
-      while ((uint32_t)(w[u] >> 32) != epoch) {
-        if (++polls > (1 << 20)) {
-          atomicExch(err, 3);
-          break;
-        }
-        w[u] = ld_word(p);
-      }
-      v = __uint_as_float((uint32_t)w[u]);
-    }
-    X[kk][c] = v;
+    X[kk][c] = need[u] ? __uint_as_float((uint32_t)w[u]) : 0.f;
   }
 }
 
@@ -1052,16 +1057,21 @@ int dgesv_mixed_ws(Workspace &w, bool chol, int64_t n, int64_t nrhs, const doubl
       BOLA_TRY(chol_lu_form<float>(s, n, (float *)w.W, n, (float *)w.dg));
     }
   } else if (fp64) {
-    BOLA_TRY(w.lu.factor64(s, (double *)w.W, ldW, w.ipiv, w.info, give_up));
+    BOLA_TRY(w.lu.factor64(s, (double *)w.W, ldW, w.ipiv, w.info, give_up, n > TB ? w.perm : nullptr));
   } else {
-    BOLA_TRY(w.lu.factor(s, (float *)w.W, n, w.ipiv, w.info, give_up));
+    BOLA_TRY(w.lu.factor(s, (float *)w.W, n, w.ipiv, w.info, give_up, n > TB ? w.perm : nullptr));
   }
-  {
+  // the row permutation: kept by the LU's swap kernels for n > 64 (there is
+  // no swap kernel when the whole matrix is one panel)
+  if (chol || n <= TB) {
     ProfScope prof(s, "mixed_perm");
     if (chol)
       iota_perm<<<(unsigned)cdiv(n, 256), 256, 0, s>>>(n, w.perm);
     else
       compose_perm<<<1, 1024, sizeof(int32_t) * n, s>>>(n, w.ipiv, w.perm);
+  }
+  {
+    ProfScope prof(s, "diag_inverses");
     const unsigned nb = (unsigned)cdiv(n, TB);
     if (fp64) {
       diag_block_inverses<double><<<nb, TB, 0, s>>>(n, (const double *)w.W, ldW, (double *)w.Dl, (double *)w.Du);

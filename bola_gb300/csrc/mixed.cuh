@@ -250,9 +250,13 @@ struct MixedLU {
   // give_up: the factorisation is abandoned (its kernels return at once) as
   // soon as max|u_ii| / min|u_ii| over the pivots so far is not below it;
   // INFINITY never gives up.  abandoned() on the host tells afterwards.
-  int factor(cudaStream_t s, float *W, int64_t ldw, int32_t *ipiv, int32_t *info, double give_up = INFINITY);
+  // perm (optional, n > 64): perm[i] = the original row in position i once
+  // ipiv's interchanges are applied, kept by the swap kernels as they go.
+  int factor(cudaStream_t s, float *W, int64_t ldw, int32_t *ipiv, int32_t *info, double give_up = INFINITY,
+             int32_t *perm = nullptr);
   // The same for an FP64 W (kind 3).
-  int factor64(cudaStream_t s, double *W, int64_t ldw, int32_t *ipiv, int32_t *info, double give_up = INFINITY);
+  int factor64(cudaStream_t s, double *W, int64_t ldw, int32_t *ipiv, int32_t *info, double give_up = INFINITY,
+               int32_t *perm = nullptr);
   // Cholesky W = L L^T of the lower triangle of an SPD W (chol.cu): L in the
   // lower triangle; *info = the first column whose pivot is not positive.
   int factor_chol(cudaStream_t s, float *W, int64_t ldw, int32_t *info, double give_up = INFINITY);

@@ -1067,7 +1067,8 @@ __device__ __forceinline__ void operand_tile(const float *W, int64_t ldw, int64_
 template <typename T>
 __global__ void __launch_bounds__(256)
 sswap_trsm(T *W, int64_t ldw, int64_t n, int64_t j, int jb, const int32_t *plan, int kind, void *bop,
-           float *bop_lo, int32_t *bexp, int64_t cap, const int32_t *abort, int ncta, void *aop, float *aop_lo) {
+           float *bop_lo, int32_t *bexp, int64_t cap, const int32_t *abort, int ncta, void *aop, float *aop_lo,
+           int32_t *perm) {
   if (abort != nullptr && *(volatile const int32_t *)abort != 0) return;  // set before this launch (same stream)
   __shared__ int32_t rows[2 * SNB], src[2 * SNB];
   __shared__ __align__(16) T L[SNB * SNB];
@@ -1099,6 +1100,16 @@ sswap_trsm(T *W, int64_t ldw, int64_t n, int64_t j, int jb, const int32_t *plan,
   }
   __syncthreads();
   const int lane = threadIdx.x & 31;
+  if (perm != nullptr && blockIdx.x == 0 && threadIdx.x < 32) {
+    // the same moves on the row permutation (warp 0 of CTA 0, besides its column)
+    int32_t pv[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) pv[e] = lane + 32 * e < cnt ? perm[src[lane + 32 * e]] : 0;
+    __syncwarp();
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+      if (lane + 32 * e < cnt) perm[rows[lane + 32 * e]] = pv[e];
+  }
   const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (w >= n - jb) return;
   const int64_t col = w < j ? w : w + jb;
@@ -1145,6 +1156,10 @@ sswap_trsm(T *W, int64_t ldw, int64_t n, int64_t j, int jb, const int32_t *plan,
 }
 
 __global__ void zero_i32(int32_t *p) { *p = 0; }
+__global__ void iota32(int64_t n, int32_t *p) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = (int32_t)i;
+}
 __global__ void track_init(uint64_t *t) {
   t[0] = 0;                       // max |u_ii| = +0
   t[1] = 0x7ff0000000000000ull;   // min |u_ii| = +inf
@@ -1244,7 +1259,7 @@ int panel_width(bool, int64_t n, int64_t j) { return (int)imin(SNB, n - j); }
 // overlaps panel k+1; the swaps of step k+1 wait for it.
 template <typename T>
 static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int32_t *ipiv, int32_t *info,
-                            double give_up) {
+                            double give_up, int32_t *perm) {
   constexpr bool fp64 = std::is_same<T, double>::value;
   const int64_t n = lu.n;
   BOLA_TRY_CUDA(cudaEventRecord(lu.ev_in, s));
@@ -1252,6 +1267,7 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
   BOLA_TRY_CUDA(cudaStreamWaitEvent(lu.su, lu.ev_in, 0));
   zero_i32<<<1, 1, 0, lu.sp>>>(info);
   track_init<<<1, 1, 0, lu.sp>>>(lu.track);
+  if (perm != nullptr) iota32<<<(unsigned)cdiv(n, 256), 256, 0, lu.sp>>>(n, perm);
   BOLA_CHECK_LAUNCH();
   // su's first kernels read the flag too: they must see it initialised
   BOLA_TRY_CUDA(cudaEventRecord(lu.ev_in, lu.sp));
@@ -1299,7 +1315,8 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
       const int nop = (!fp64 && upd) ? (int)cdiv(mp - jb, SNB) : 0;
       sswap_trsm<T><<<(unsigned)(ncta + nop), 256, 0, lu.sp>>>(
           W, ldw, n, j, jb, lu.plan, lu.kind, upd ? lu.bop : nullptr, fp64 ? nullptr : lu.bop_lo,
-          fp64 ? lu.eb : nullptr, lu.cap_n, abort, ncta, fp64 ? nullptr : lu.aop[buf], fp64 ? nullptr : lu.aop_lo[buf]);
+          fp64 ? lu.eb : nullptr, lu.cap_n, abort, ncta, fp64 ? nullptr : lu.aop[buf], fp64 ? nullptr : lu.aop_lo[buf],
+          perm);
       BOLA_CHECK_LAUNCH();
     }
     if (!upd) continue;
@@ -1329,12 +1346,14 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
   return 0;
 }
 
-int MixedLU::factor(cudaStream_t s, float *W, int64_t ldw, int32_t *ipiv, int32_t *info, double give_up) {
-  return factor_lookahead<float>(*this, s, W, ldw, ipiv, info, give_up);
+int MixedLU::factor(cudaStream_t s, float *W, int64_t ldw, int32_t *ipiv, int32_t *info, double give_up,
+                    int32_t *perm) {
+  return factor_lookahead<float>(*this, s, W, ldw, ipiv, info, give_up, perm);
 }
 
-int MixedLU::factor64(cudaStream_t s, double *W, int64_t ldw, int32_t *ipiv, int32_t *info, double give_up) {
-  return factor_lookahead<double>(*this, s, W, ldw, ipiv, info, give_up);
+int MixedLU::factor64(cudaStream_t s, double *W, int64_t ldw, int32_t *ipiv, int32_t *info, double give_up,
+                      int32_t *perm) {
+  return factor_lookahead<double>(*this, s, W, ldw, ipiv, info, give_up, perm);
 }
 
 }  // namespace bola
