@@ -189,3 +189,15 @@ def test_escalation_not_taken_when_refinement_converges():
     x, info = solve(A, b, n, nrhs, 2, fallback=1, escalate=1)
     assert info.path in (0, 1)
     assert berr(A, x, b, n, nrhs) <= 1e-14
+
+
+@pytest.mark.parametrize("n,nrhs", [(300, 3), (1001, 16), (4500, 20)])
+def test_triangular_solves_with_an_odd_block_count(n, nrhs):
+    """The FP32 triangular solves take 64-row blocks two at a time: an odd
+    number of blocks leaves the last pair with one block; 20 right-hand sides
+    take the 32-wide form.  The refinement still reaches 1e-14 by plain IR."""
+    A, b = make_system(n, nrhs, 1e2, seed=13)
+    x, info = solve(A, b, n, nrhs, 2)
+    assert info.path == 0, (info.path, info.iterations)
+    assert info.iterations <= 4
+    assert berr(A, x, b, n, nrhs) <= 1e-14
