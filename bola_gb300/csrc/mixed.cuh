@@ -234,7 +234,7 @@ struct MixedLU {
   float *aop_lo[2] = {nullptr, nullptr}, *bop_lo = nullptr;
   int32_t *ea[2] = {nullptr, nullptr}, *eb = nullptr;  // kind 3: row exponents of the sliced operands
   int32_t *err = nullptr;
-  int32_t *plan = nullptr;  // the current panel's composed interchanges: count, rows[128], src[128];
+  int32_t *plan = nullptr;  // every panel's moves of rows (count, rows[128], src[128], per panel);
                             // then the FP64 panel's pivot rows (64)
   // running extent of |u_ii| over the panels done: [0] max, [1] min (bits of
   // non-negative doubles, ordered like the values), [2] low word = abandon flag

@@ -34,6 +34,8 @@ namespace {
 
 constexpr int SNB = 64;   // panel width and update depth
 constexpr int SMAXC = 16;
+// a panel's moves of rows for the swap kernels: count, rows[128], src[128] (+ spare)
+constexpr int PLAN_STRIDE = 1 + 4 * SNB;
 
 // Bulk copy of `bytes` (a multiple of 16) from this CTA's shared memory into
 // another CTA's (cluster addresses dst and bar), completing on the
@@ -1060,9 +1062,11 @@ __device__ __forceinline__ void operand_tile(const float *W, int64_t ldw, int64_
   }
 }
 
-// The panel's interchanges on all other columns, U12 = L11^-1 A12 on the
-// right ones and their K-major B operand: a warp per column, ncta CTAs.  The
-// FP32 factors' CTAs from ncta on write the A operand of the update (aop:
+// The panel's interchanges on the columns right of it, U12 = L11^-1 A12 and
+// its K-major B operand: a warp per column, ncta CTAs (the finished columns
+// left of the panel take the interchanges once, when the factorisation is
+// done: apply_left_swaps).  CTA 0 also applies them to the row permutation.
+// The FP32 factors' CTAs from ncta on write the A operand of the update (aop:
 // operand_tile, one 64-row tile each).
 template <typename T>
 __global__ void __launch_bounds__(256)
@@ -1111,8 +1115,8 @@ sswap_trsm(T *W, int64_t ldw, int64_t n, int64_t j, int jb, const int32_t *plan,
       if (lane + 32 * e < cnt) perm[rows[lane + 32 * e]] = pv[e];
   }
   const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (w >= n - jb) return;
-  const int64_t col = w < j ? w : w + jb;
+  if (w >= n - j - jb) return;
+  const int64_t col = j + jb + w;
   T *cp = W + col * ldw;
   T v[4];
 #pragma unroll
@@ -1122,7 +1126,6 @@ sswap_trsm(T *W, int64_t ldw, int64_t n, int64_t j, int jb, const int32_t *plan,
   for (int e = 0; e < 4; ++e)
     if (lane + 32 * e < cnt) cp[rows[lane + 32 * e]] = v[e];
   __syncwarp();
-  if (col < j + jb) return;
   T b0 = lane < jb ? cp[j + lane] : T(0);
   T b1 = lane + 32 < jb ? cp[j + lane + 32] : T(0);
   // rows 0..31 take updates from k < 32 only: two loops, so that no warp
@@ -1152,6 +1155,62 @@ sswap_trsm(T *W, int64_t ldw, int64_t n, int64_t j, int jb, const int32_t *plan,
       oz_split_pair(lane < jb ? (double)b0 : 0.0, lane + 32 < jb ? (double)b1 : 0.0, lane, col - j - jb, cap,
                     static_cast<__nv_bfloat16 *>(bop), bexp);
     }
+  }
+}
+
+// Once the factorisation is done: every panel's interchanges on the columns
+// left of it (the finished L), deferred from the swap kernel.  CTA k takes
+// column block k: the moves of panels k+1.. (plans[k'], as the swap kernel
+// took them) composed in shared memory into one gather — arr[i] = the
+// position, relative to the first row below the block, that the row ending
+// in position i held after panel k — then each column's rows below the block
+// are read once and the moved ones written back.
+template <typename T>
+__global__ void __launch_bounds__(512)
+apply_left_swaps(T *W, int64_t ldw, int64_t n, const int32_t *plans, const int32_t *abort) {
+  if (abort != nullptr && *(volatile const int32_t *)abort != 0) return;
+  extern __shared__ __align__(16) unsigned char als_raw[];
+  constexpr int NT = 512, U = 16;
+  const int k = blockIdx.x, K = (int)cdiv(n, SNB);
+  const int64_t base = (int64_t)(k + 1) * SNB;
+  const int m = (int)(n - base);
+  int32_t *arr = reinterpret_cast<int32_t *>(als_raw);
+  T *col = reinterpret_cast<T *>(als_raw + ((sizeof(int32_t) * (size_t)m + 15) & ~(size_t)15));
+  for (int i = threadIdx.x; i < m; i += NT) arr[i] = i;
+  __syncthreads();
+  for (int kp = k + 1; kp < K; ++kp) {
+    const int32_t *pl = plans + (int64_t)kp * PLAN_STRIDE;
+    const int cnt = pl[0];
+    int v = 0, dst = -1;
+    if ((int)threadIdx.x < cnt) {
+      v = arr[pl[1 + 2 * SNB + threadIdx.x] - base];
+      dst = (int)(pl[1 + threadIdx.x] - base);
+    }
+    __syncthreads();
+    if (dst >= 0) arr[dst] = v;
+    __syncthreads();
+  }
+  for (int c = k * SNB; c < (k + 1) * SNB && c < n; ++c) {
+    T *cp = W + base + (int64_t)c * ldw;
+    for (int i0 = 0; i0 < m; i0 += NT * U) {  // a thread's loads in flight together
+      T r[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = i0 + (int)threadIdx.x + NT * u;
+        r[u] = i < m ? cp[i] : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = i0 + (int)threadIdx.x + NT * u;
+        if (i < m) col[i] = r[u];
+      }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < m; i += NT) {
+      const int sidx = arr[i];
+      if (sidx != i) cp[i] = col[sidx];
+    }
+    __syncthreads();
   }
 }
 
@@ -1185,7 +1244,7 @@ int MixedLU::reserve(int64_t n_, int kind_, cudaStream_t s) {
   n = cap_n = n_;
   kind = kind_;
   BOLA_TRY_CUDA(cudaMallocAsync(&err, sizeof(int32_t), s));
-  BOLA_TRY_CUDA(cudaMallocAsync(&plan, sizeof(int32_t) * (1 + 5 * SNB), s));
+  BOLA_TRY_CUDA(cudaMallocAsync(&plan, sizeof(int32_t) * ((size_t)PLAN_STRIDE * cdiv(n, SNB) + SNB), s));
   BOLA_TRY_CUDA(cudaMallocAsync(&track, 4 * sizeof(uint64_t), s));
   BOLA_TRY_CUDA(cudaMemsetAsync(err, 0, sizeof(int32_t), s));
   if (kind == 3) {
@@ -1281,16 +1340,17 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
     const int64_t mp = n - j;
     const bool upd = j + jb < n;
     const int buf = (int)(k & 1);
+    int32_t *plan_k = lu.plan + k * PLAN_STRIDE;  // this panel's moves, kept for apply_left_swaps
     if constexpr (fp64) {
       // pivot rows by tournament on FP32 copies, then the FP64 factorisation
       // of the selected block and of the rows below it
       double *Wp = W + j + j * ldw;
-      int32_t *win = lu.plan + 1 + 4 * SNB;
+      int32_t *win = lu.plan + (int64_t)PLAN_STRIDE * cdiv(lu.cap_n, SNB);
       BOLA_TRY(launch_tpanel<double>(lu.sp, Wp, ldw, mp, jb, ipiv + j, (int32_t)j, info, nullptr, track, give_up,
                                      lu.err, win));
       {
         ProfScope prof(lu.sp, "panel_top64", (double)jb * jb * jb * 2.0 / 3.0, 16.0 * (double)jb * jb);
-        panel_top64<<<1, T64_THREADS, 0, lu.sp>>>(Wp, ldw, mp, jb, (int32_t)j, win, lu.plan, ipiv + j, info, track,
+        panel_top64<<<1, T64_THREADS, 0, lu.sp>>>(Wp, ldw, mp, jb, (int32_t)j, win, plan_k, ipiv + j, info, track,
                                           give_up, lu.err);
       }
       if (mp > jb) {
@@ -1301,20 +1361,19 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
       }
       BOLA_CHECK_LAUNCH();
     } else
-      BOLA_TRY(launch_tpanel(lu.sp, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, lu.plan, track,
+      BOLA_TRY(launch_tpanel(lu.sp, W + j + j * ldw, ldw, mp, jb, ipiv + j, (int32_t)j, info, plan_k, track,
                              give_up, lu.err));
     // the row swaps reach every column: the previous wide update must be done
     if (wide_pending) BOLA_TRY_CUDA(cudaStreamWaitEvent(lu.sp, lu.ev_wide, 0));
     wide_pending = false;
-    const int64_t others = n - jb;
-    if (others > 0) {
+    if (n > jb) {  // (also the last panel: its moves reach the row permutation)
       ProfScope prof(lu.sp, fp64 ? "sswap_trsm64" : "sswap_trsm", (double)jb * jb * (double)(n - j - jb));
       // (the FP32 factors: one more CTA per 64 rows below the panel writes
       // the update's A operand)
-      const int ncta = (int)cdiv(others, 8);
+      const int ncta = (int)imax(1, cdiv(n - j - jb, 8));
       const int nop = (!fp64 && upd) ? (int)cdiv(mp - jb, SNB) : 0;
       sswap_trsm<T><<<(unsigned)(ncta + nop), 256, 0, lu.sp>>>(
-          W, ldw, n, j, jb, lu.plan, lu.kind, upd ? lu.bop : nullptr, fp64 ? nullptr : lu.bop_lo,
+          W, ldw, n, j, jb, plan_k, lu.kind, upd ? lu.bop : nullptr, fp64 ? nullptr : lu.bop_lo,
           fp64 ? lu.eb : nullptr, lu.cap_n, abort, ncta, fp64 ? nullptr : lu.aop[buf], fp64 ? nullptr : lu.aop_lo[buf],
           perm);
       BOLA_CHECK_LAUNCH();
@@ -1339,6 +1398,18 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
       BOLA_TRY_CUDA(cudaEventRecord(lu.ev_wide, lu.su));
       wide_pending = true;
     }
+  }
+  // the interchanges on the columns left of each panel, all at once
+  if (n > SNB) {
+    ProfScope prof(lu.sp, "left_swaps");
+    const size_t smem = ((sizeof(int32_t) * (size_t)(n - SNB) + 15) & ~(size_t)15) + sizeof(T) * (size_t)(n - SNB);
+    static size_t attr = 0;
+    if (smem > attr) {
+      BOLA_TRY_CUDA(cudaFuncSetAttribute(apply_left_swaps<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      attr = smem;
+    }
+    apply_left_swaps<T><<<(unsigned)(cdiv(n, SNB) - 1), 512, smem, lu.sp>>>(W, ldw, n, lu.plan, abort);
+    BOLA_CHECK_LAUNCH();
   }
   if (wide_pending) BOLA_TRY_CUDA(cudaStreamWaitEvent(lu.sp, lu.ev_wide, 0));
   BOLA_TRY_CUDA(cudaEventRecord(lu.ev_done, lu.sp));
