@@ -687,9 +687,10 @@ int launch_tpanel(cudaStream_t s, G *W, int64_t ldw, int64_t mp, int jb, int32_t
 //   1. tpanel_kernel<double> chooses the jb pivot rows by tournament on FP32
 //      copies of the panel (W's column blocks are scaled to O(1), and FP32
 //      is ample for choosing pivots);
-//   2. panel_top64 factors the selected jb x jb block in FP64 with partial
-//      pivoting among its rows (CALU's final step), derives LAPACK's
-//      interchanges, moves the rows they displace and tracks the pivots;
+//   2. panel_top64 factors the selected jb x jb block in FP64 in the
+//      tournament's pivot order without further pivoting (CALU's final
+//      step), derives LAPACK's interchanges, moves the rows they displace
+//      and tracks the pivots;
 //   3. panel_l21_64 forms L21 = A21 U11^-1 in FP64 for every row below, on
 //      as many SMs as there are rows, and writes the update's operand (exact
 //      bf16 slices of each row of L21).
@@ -709,24 +710,25 @@ __device__ __forceinline__ double recip64(double p) {
 }
 
 // Step 2 of the panel above for one panel (Wp: its top-left, rows col0.. of
-// W).  One CTA of 8 warps; the block lives in shared memory and is factored
-// with row interchanges as LAPACK does (the pivot row moves to position k),
-// so the rows still to be eliminated are positions k + 1 .. and a warp
-// whose rows are all done stops issuing.  Position q belongs to lanes
-// 4q .. 4q + 3; lane h updates columns c = h (mod 4), so every FP64 warp
-// instruction has 32 busy lanes.  On GB300 a warp's other instructions wait
-// while its FP64 instruction is dispatched (~64 cycles), so two warps share
-// each sub-partition: one's shared-memory and integer work overlaps the
-// other's FP64 work.  Per column k (a rolled loop: an unrolled one misses
-// the instruction cache): the pivot from the warps' keys at a named barrier,
-// the swap of positions k and p (the thread of column k also forms 1 /
-// pivot), a second barrier, then every remaining row forms its multiplier,
-// updates column k + 1 and publishes its key for the next search before its
-// other columns' FMAs.
+// W).  The tournament has fixed the pivot order (row win[q] is the pivot of
+// column q, chosen by partial pivoting among the nominees), so the selected
+// block is factored without pivoting in that order, as CALU's last step
+// does: no search, no row exchange, one barrier per column.  One CTA of 8
+// warps, the block in shared memory; row q belongs to lanes 4q .. 4q + 3,
+// lane h updating columns c = h (mod 4), so every FP64 warp instruction has
+// 32 busy lanes, and a warp whose rows are all done stops issuing.  On GB300
+// a warp's other instructions wait while its FP64 instruction is dispatched
+// (~64 cycles), so two warps share each sub-partition.  Per column k (a
+// rolled loop: an unrolled one misses the instruction cache): every
+// remaining row forms its multiplier and updates column k + 1 first; the
+// owner of the next pivot forms its reciprocal while the rows' other columns
+// are updated.  Then LAPACK's interchanges (from the pivot list), the rows
+// they displace below the block, the block itself and the pivots' spread.
 constexpr int T64_LPR = 4;                       // lanes per block row
 constexpr int T64_THREADS = SNB * T64_LPR;       // 256
-constexpr int T64_WARPS = T64_THREADS / 32;      // 8
-__global__ void __launch_bounds__(T64_THREADS, 1)
+constexpr int T64_WARPS = T64_THREADS / 32;      // 8 warps with rows
+constexpr int T64_BLOCK = T64_THREADS + 32;      // and the reciprocal warp
+__global__ void __launch_bounds__(T64_BLOCK, 1)
 panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int32_t *win_in, int32_t *plan,
             int32_t *ipiv, int32_t *info, uint64_t *track, double give_up, int32_t *err) {
   // an abandoned factorisation (flag set by an earlier panel on this stream):
@@ -735,10 +737,9 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
     for (int t = threadIdx.x; t < jb; t += blockDim.x) ipiv[t] = col0 + t + 1;
     return;
   }
-  __shared__ double a[SNB][SNB + 1];  // a[q][c]: the row now in position q, column c
-  __shared__ int32_t win[SNB], rowid[SNB], pivl[SNB], posin[SNB], at_[SNB], rows_s[2 * SNB], src_s[2 * SNB];
-  __shared__ double rinv_s[2];             // 1 / the pivot of column k (k & 1)
-  __shared__ uint32_t wkey[2][T64_WARPS];  // the warps' best keys for column k (k & 1)
+  __shared__ double a[SNB][SNB + 1];  // a[q][c]: the pivot row of column q (panel row win[q]), column c
+  __shared__ int32_t win[SNB], pivl[SNB], posin[SNB], at_[SNB], rows_s[2 * SNB], src_s[2 * SNB];
+  __shared__ double rinv_s[2];  // 1 / the pivot of column k (k & 1)
   __shared__ int bad, cnt_s;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int q = tid / T64_LPR, h = tid % T64_LPR;
@@ -746,7 +747,6 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
   __syncthreads();
   for (int t = tid; t < jb; t += T64_THREADS) {
     win[t] = win_in[t];
-    rowid[t] = t;
     // a selection that did not finish (its exchange gave up and set the
     // error word) leaves no valid list: stop here rather than index W with it
     if (win[t] < 0 || win[t] >= mp) atomicExch(&bad, 1);
@@ -758,7 +758,7 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
     return;
   }
   // the selected rows, all of a thread's loads in flight together
-  {
+  if (tid < T64_THREADS) {
     constexpr int PER = SNB * SNB / T64_THREADS;
     double v[PER];
 #pragma unroll
@@ -772,84 +772,62 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
       a[e % SNB][e / SNB] = v[u];
     }
   }
-  uint64_t umax = 0, umin = ~0ull;  // |u_kk| bits (the thread of column k)
-  // the key of position q in column k (v: its value there) if it is still to
-  // be eliminated: the high word of |v| with the position in its 7 low bits
-  // (>= 64 for every candidate, so a zero column still yields a pivot; a NaN
-  // counts as zero)
-  auto publish = [&](double v, int k) {
-    uint32_t key = 0u;
-    if (q >= k && q < jb && h == k % T64_LPR && k < jb) {
-      const uint64_t b = (uint64_t)__double_as_longlong(v) & 0x7fffffffffffffffull;
-      const uint32_t hi = b > 0x7ff0000000000000ull ? 0u : (uint32_t)(b >> 32);
-      key = (hi & ~127u) | (uint32_t)(127 - q);
+  uint64_t umax = 0, umin = ~0ull;  // |u_kk| bits (the threads that formed the pivots' reciprocals)
+  // 1 / the pivot of column k into rinv_s[k & 1], with the pivots' extent and
+  // the first zero pivot
+  auto pivot = [&](double pv, int k) {
+    const uint64_t ab = (uint64_t)__double_as_longlong(pv) & 0x7fffffffffffffffull;
+    rinv_s[k & 1] = ab != 0 ? recip64(pv) : 0.0;
+    if (ab == 0) atomicCAS(info, 0, col0 + k + 1);
+    if (ab <= 0x7ff0000000000000ull) {
+      umax = ab > umax ? ab : umax;
+      umin = ab < umin ? ab : umin;
     }
-    key = __reduce_max_sync(0xffffffffu, key);
-    if (lane == 0) wkey[k & 1][warp] = key;
   };
+  const bool rwarp = warp == T64_WARPS;  // the reciprocal warp (no rows)
   if (tid == 0) interchanges_init(jb, posin, at_);
-  int jdone = 0;  // (thread 0) columns whose interchange is done
   __syncthreads();
-  publish(a[q][0], 0);
+  if (rwarp && lane == 0) pivot(a[0][0], 0);
+  int jdone = 0;  // (thread 0) columns whose interchange is done
 #pragma unroll 1
   for (int k = 0; k < jb; ++k) {
-    const int par = k & 1, hk = k % T64_LPR;
-    asm volatile("bar.sync 1, %0;" ::"r"(T64_THREADS) : "memory");
-    uint32_t mk = wkey[par][0];
-#pragma unroll
-    for (int w = 1; w < T64_WARPS; ++w) mk = wkey[par][w] > mk ? wkey[par][w] : mk;
-    const int p = 127 - (int)(mk & 127u);
-    // positions k and p trade rows: thread t swaps column t; the thread of
-    // column k first forms 1 / pivot and records the pivot
-    if (tid < jb) {
-      if (tid == k) {
-        const double pv = a[p][k];
-        const uint64_t ab = (uint64_t)__double_as_longlong(pv) & 0x7fffffffffffffffull;
-        rinv_s[par] = ab != 0 ? recip64(pv) : 0.0;
-        if (ab == 0) atomicCAS(info, 0, col0 + k + 1);
-        if (ab <= 0x7ff0000000000000ull) {
-          umax = ab > umax ? ab : umax;
-          umin = ab < umin ? ab : umin;
-        }
-        if (p != k) {
-          const int t = rowid[k];
-          rowid[k] = rowid[p];
-          rowid[p] = t;
-        }
+    const int hk = k % T64_LPR;
+    // column k's pivot row and reciprocal are final
+    asm volatile("bar.sync 1, %0;" ::"r"(T64_BLOCK) : "memory");
+    if (rwarp) {
+      // the next pivot, once its row's warp has updated it (named barrier 2:
+      // that warp arrives, this one waits), while the rows' other columns are
+      // updated; the dependent FP64 chain of the reciprocal stays off the
+      // row warps
+      if (k + 1 < jb) {
+        asm volatile("bar.sync 2, 64;" ::: "memory");
+        if (lane == 0) pivot(a[k + 1][k + 1], k + 1);
       }
-      if (p != k) {
-        const double t = a[k][tid];
-        a[k][tid] = a[p][tid];
-        a[p][tid] = t;
-      }
+      continue;
     }
-    asm volatile("bar.sync 1, %0;" ::"r"(T64_THREADS) : "memory");
-    if ((warp + 1) * (32 / T64_LPR) - 1 <= k) {  // every row of this warp is done: no candidate for k + 1
-      if (lane == 0) wkey[par ^ 1][warp] = 0u;
+    if ((warp + 1) * (32 / T64_LPR) - 1 <= k) {  // every row of this warp is done
       // warp 0, idle from column 7 on, runs LAPACK's interchanges for the
-      // columns whose pivot row is final (positions 0..k), two per column
-      // until it has caught up
+      // pivots, two per column until it has caught up
       if (tid == 0)
         for (int u = 0; u < 2 && jdone <= k; ++u, ++jdone) {
-          const int x = win[rowid[jdone]];
-          pivl[jdone] = x;
-          ipiv[jdone] = interchange_step(jdone, x, jb, col0, posin, at_);
+          pivl[jdone] = win[jdone];
+          ipiv[jdone] = interchange_step(jdone, win[jdone], jb, col0, posin, at_);
         }
       continue;
     }
     const bool act = q > k && q < jb;
-    const double l = act ? a[q][k] * rinv_s[par] : 0.0;
+    const double l = act ? a[q][k] * rinv_s[k & 1] : 0.0;
     __syncwarp();  // the quad has read a[q][k] before it becomes the multiplier
-    double v1 = 0.0;
     if (act) {
       if (h == hk) a[q][k] = l;
-      // column k + 1 first: the next search reads it
-      if (k + 1 < jb && h == (k + 1) % T64_LPR) {
-        v1 = fma(-l, a[k][k + 1], a[q][k + 1]);
-        a[q][k + 1] = v1;
-      }
+      // column k + 1 first: the next pivot
+      if (k + 1 < jb && h == (k + 1) % T64_LPR) a[q][k + 1] = fma(-l, a[k][k + 1], a[q][k + 1]);
     }
-    publish(v1, k + 1);
+    if (k + 1 < jb && warp == (k + 1) / (32 / T64_LPR)) {  // the next pivot's warp hands it over
+      __threadfence_block();
+      __syncwarp();
+      asm volatile("bar.arrive 2, 64;" ::: "memory");
+    }
     // the row's other columns c = 4u + h >= k + 2: the same trip count in
     // every lane of the warp (a per-lane start would split the warp into
     // paths that each dispatch their own FP64 instructions), 4 columns at a
@@ -872,7 +850,7 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
   }
   // the pivots' extent lives with the lanes that saw them: per warp here,
   // into thread 0 at the end
-  __shared__ uint64_t wx[T64_WARPS], wn[T64_WARPS];
+  __shared__ uint64_t wx[T64_WARPS + 1], wn[T64_WARPS + 1];
   {
     uint64_t mx = umax, mn = umin;
 #pragma unroll
@@ -888,9 +866,8 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
   }
   if (tid == 0)  // the interchanges still to run (the last columns, or all of a narrow block)
     for (; jdone < jb; ++jdone) {
-      const int x = win[rowid[jdone]];
-      pivl[jdone] = x;
-      ipiv[jdone] = interchange_step(jdone, x, jb, col0, posin, at_);
+      pivl[jdone] = win[jdone];
+      ipiv[jdone] = interchange_step(jdone, win[jdone], jb, col0, posin, at_);
     }
   __syncthreads();
   // the moves of rows, to the swap kernel (plan) and to this CTA (rows_s, src_s)
@@ -901,25 +878,26 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
   const int cnt = cnt_s;
   constexpr int MV = 2 * SNB * SNB / T64_THREADS;
   double mv[MV];
+  const bool rowt = tid < T64_THREADS;
 #pragma unroll
   for (int u = 0; u < MV; ++u) {
     const int e = tid + T64_THREADS * u, t = e % (2 * SNB), c = e / (2 * SNB);
-    mv[u] = (t < cnt && c < jb && rows_s[t] >= jb) ? Wp[src_s[t] + (int64_t)c * ldw] : 0.0;
+    mv[u] = (rowt && t < cnt && c < jb && rows_s[t] >= jb) ? Wp[src_s[t] + (int64_t)c * ldw] : 0.0;
   }
   __syncthreads();
 #pragma unroll
   for (int u = 0; u < MV; ++u) {
     const int e = tid + T64_THREADS * u, t = e % (2 * SNB), c = e / (2 * SNB);
-    if (t < cnt && c < jb && rows_s[t] >= jb) Wp[rows_s[t] + (int64_t)c * ldw] = mv[u];
+    if (rowt && t < cnt && c < jb && rows_s[t] >= jb) Wp[rows_s[t] + (int64_t)c * ldw] = mv[u];
   }
   // the factored block (unit-lower L11 below the diagonal, U11 on and above)
-  for (int e = tid; e < jb * jb; e += T64_THREADS) {
+  for (int e = tid; e < jb * jb; e += T64_BLOCK) {
     const int r = e % jb, c = e / jb;
     Wp[r + (int64_t)c * ldw] = a[r][c];
   }
   if (track != nullptr && tid == 0) {
     // the running extent of |u_ii| and the give-up test
-    for (int w = 0; w < T64_WARPS; ++w) {
+    for (int w = 0; w <= T64_WARPS; ++w) {
       umax = wx[w] > umax ? wx[w] : umax;
       umin = wn[w] < umin ? wn[w] : umin;
     }
@@ -1350,7 +1328,7 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
                                      lu.err, win));
       {
         ProfScope prof(lu.sp, "panel_top64", (double)jb * jb * jb * 2.0 / 3.0, 16.0 * (double)jb * jb);
-        panel_top64<<<1, T64_THREADS, 0, lu.sp>>>(Wp, ldw, mp, jb, (int32_t)j, win, plan_k, ipiv + j, info, track,
+        panel_top64<<<1, T64_BLOCK, 0, lu.sp>>>(Wp, ldw, mp, jb, (int32_t)j, win, plan_k, ipiv + j, info, track,
                                           give_up, lu.err);
       }
       if (mp > jb) {
