@@ -233,6 +233,7 @@ struct MixedLU {
   void *aop[2] = {nullptr, nullptr}, *bop = nullptr;
   float *aop_lo[2] = {nullptr, nullptr}, *bop_lo = nullptr;
   int32_t *ea[2] = {nullptr, nullptr}, *eb = nullptr;  // kind 3: row exponents of the sliced operands
+  double *sel = nullptr;  // kind 3: the current panel's pivot rows (64 x 64, row-major), from the selection
   int32_t *err = nullptr;
   int32_t *plan = nullptr;  // every panel's moves of rows (count, rows[128], src[128], per panel);
                             // then the FP64 panel's pivot rows (64)

@@ -11,11 +11,12 @@
 //                   tf32 hi/lo).
 //   FP64 W (the FP64-accurate factor): the same tournament on FP32 copies
 //                   chooses the pivot rows (tpanel_kernel<double>), then
-//                   panel_top64 factors the selected block in FP64 and
-//                   panel_l21_64 the rows below it, writing L21's exact bf16
-//                   slices as the A operand.
-//   sswap_trsm      the 64 interchanges on every other column, U12 = L11^-1 A12
-//                   and the K-major B operand.
+//                   panel_lu64 factors the panel in FP64 in that pivot order
+//                   on as many SMs as it has 64-row slices, writing L21's
+//                   exact bf16 slices as the A operand.
+//   sswap_trsm      the 64 interchanges on the columns right of the panel,
+//                   U12 = L11^-1 A12 and the K-major B operand (the columns
+//                   left of it take them at the end: apply_left_swaps).
 //   tc_update / oz_update   W22 -= L21 U12 on tcgen05 (tc_update.cu, oz_update.cu).
 // Pivots are this algorithm's own; only the FP64 refinement decides accuracy.
 #include <cooperative_groups.h>
@@ -263,12 +264,13 @@ __device__ __forceinline__ float rank8(float a, const float (&l)[TG], const floa
 // G = float: the FP32 factors' panel (factored in place).  G = double: the
 // FP64-accurate factor's pivot selection only — the tournament runs on FP32
 // copies of the panel's values and writes the jb pivot rows (panel rows, in
-// column order) to winout; W, ipiv, info and the operands are left to the
-// FP64 kernels that follow (panel_top64, panel_l21_64).
+// column order) to winout and their FP64 values (columns of the panel) to
+// sel, 64 x 64 row-major; W, ipiv, info and the operands are left to the
+// FP64 kernel that follows (panel_lu64).
 template <typename G>
 __global__ void __launch_bounds__(TPT, 1)
 tpanel_kernel(G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0, int32_t *info, int64_t R,
-              int32_t *plan, uint64_t *track, double give_up, int32_t *err, int32_t *winout) {
+              int32_t *plan, uint64_t *track, double give_up, int32_t *err, int32_t *winout, G *sel) {
   constexpr bool SEL = std::is_same<G, double>::value;
   cg::cluster_group cluster = cg::this_cluster();
   // an abandoned factorisation (flag set by an earlier panel on this stream,
@@ -574,6 +576,11 @@ tpanel_kernel(G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
     if constexpr (SEL) {
       if (cr == 0)
         for (int t = tid; t < jb; t += TPT) winout[t] = win[t];
+      // the pivot rows' FP64 values, each CTA its own rows
+      for (int e = tid; e < jb * jb; e += TPT) {
+        const int t = e / jb, c = e % jb, row = win[t];
+        if (row >= r0 && row < r1) sel[t * SNB + c] = W[row + (int64_t)c * ldw];
+      }
     } else {
     // -- the last group's interchanges (CTA 0; the earlier groups' ran
     // during the searches that followed them)
@@ -644,7 +651,7 @@ tpanel_kernel(G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0
 template <typename G>
 int launch_tpanel(cudaStream_t s, G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0,
                   int32_t *info, int32_t *plan, uint64_t *track, double give_up, int32_t *err,
-                  int32_t *winout = nullptr) {
+                  int32_t *winout = nullptr, G *sel = nullptr) {
   const int C = (int)imin(SMAXC, imax(1, cdiv(mp, TPT)));
   // rows per CTA, a multiple of 4 (the write-back's float4 runs); C <= 16
   // keeps the last CTA's share positive: mp > 256 (C - 1) > 4 C (C - 1)
@@ -675,7 +682,7 @@ int launch_tpanel(cudaStream_t s, G *W, int64_t ldw, int64_t mp, int jb, int32_t
   ProfScope prof(s, std::is_same<G, double>::value ? "tselect64" : "tpanel", (double)mp * jb * jb,
                  8.0 * (double)mp * jb);
   BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, tpanel_kernel<G>, W, ldw, mp, jb, ipiv, col0, info, R, plan, track,
-                                   give_up, err, winout));
+                                   give_up, err, winout, sel));
   return 0;
 }
 
@@ -687,13 +694,12 @@ int launch_tpanel(cudaStream_t s, G *W, int64_t ldw, int64_t mp, int jb, int32_t
 //   1. tpanel_kernel<double> chooses the jb pivot rows by tournament on FP32
 //      copies of the panel (W's column blocks are scaled to O(1), and FP32
 //      is ample for choosing pivots);
-//   2. panel_top64 factors the selected jb x jb block in FP64 in the
-//      tournament's pivot order without further pivoting (CALU's final
-//      step), derives LAPACK's interchanges, moves the rows they displace
-//      and tracks the pivots;
-//   3. panel_l21_64 forms L21 = A21 U11^-1 in FP64 for every row below, on
-//      as many SMs as there are rows, and writes the update's operand (exact
-//      bf16 slices of each row of L21).
+//   2. panel_lu64 factors the panel in FP64 in the tournament's pivot order
+//      without further pivoting (CALU's final step): the selected block and
+//      the rows below it, on one CTA per 64 rows, each factoring the block
+//      itself; it derives LAPACK's interchanges, puts the rows they displace
+//      below the block, tracks the pivots and writes the update's operand
+//      (exact bf16 slices of each row of L21).
 
 // 1 / p for the FP64 panel's pivots without the long-latency division:
 // Newton's iteration for the reciprocal, r <- r (2 - p r), from the FP32
@@ -709,91 +715,129 @@ __device__ __forceinline__ double recip64(double p) {
   return r;
 }
 
-// Step 2 of the panel above for one panel (Wp: its top-left, rows col0.. of
-// W).  The tournament has fixed the pivot order (row win[q] is the pivot of
-// column q, chosen by partial pivoting among the nominees), so the selected
-// block is factored without pivoting in that order, as CALU's last step
-// does: no search, no row exchange, one barrier per column.  One CTA of 8
-// warps, the block in shared memory; row q belongs to lanes 4q .. 4q + 3,
-// lane h updating columns c = h (mod 4), so every FP64 warp instruction has
-// 32 busy lanes, and a warp whose rows are all done stops issuing.  On GB300
-// a warp's other instructions wait while its FP64 instruction is dispatched
-// (~64 cycles), so two warps share each sub-partition.  Per column k (a
-// rolled loop: an unrolled one misses the instruction cache): every
-// remaining row forms its multiplier and updates column k + 1 first; the
-// owner of the next pivot forms its reciprocal while the rows' other columns
-// are updated.  Then LAPACK's interchanges (from the pivot list), the rows
-// they displace below the block, the block itself and the pivots' spread.
-constexpr int T64_LPR = 4;                       // lanes per block row
-constexpr int T64_THREADS = SNB * T64_LPR;       // 256
-constexpr int T64_WARPS = T64_THREADS / 32;      // 8 warps with rows
-constexpr int T64_BLOCK = T64_THREADS + 32;      // and the reciprocal warp
-__global__ void __launch_bounds__(T64_BLOCK, 1)
-panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int32_t *win_in, int32_t *plan,
-            int32_t *ipiv, int32_t *info, uint64_t *track, double give_up, int32_t *err) {
+// Steps 2 and 3 of the panel above in one launch (Wp: the panel's top-left,
+// rows col0.. of W).  The tournament has fixed the pivot order (row win[q]
+// is the pivot of column q, chosen by partial pivoting among the nominees),
+// so the panel is factored without further pivoting, as CALU's last step
+// does: the selected block and every row below it go through the same 64
+// right-looking steps.  CTA i < nA takes the panel's rows at positions
+// 64 + 64 i .. 127 + 64 i that are not pivots (they stay where they are);
+// the last CTA takes the first 64 rows that are not pivots (they move to the
+// pivots' old positions).  Every CTA factors the 64 x 64 block itself, with
+// the same arithmetic (so the same U11 everywhere), from the copy of the
+// pivot rows that the selection made (sel): no CTA reads a part of W that
+// another one writes.  Rows in shared memory, four lanes per row, lane h
+// updating columns c = h (mod 4), so every FP64 warp instruction has 32 busy
+// lanes; warps 0-7 hold the block (a warp whose rows are done stops
+// issuing), warps 8-15 the rows below, warp 16 forms the next pivot's
+// reciprocal behind a named barrier while the rows update.  On GB300 a
+// warp's other instructions wait while its FP64 instruction is dispatched
+// (~64 cycles), so several warps share each sub-partition.  Per column k (a
+// rolled loop: an unrolled one misses the instruction cache): every row's
+// multiplier, its column k + 1 first, then its other columns.  The last CTA
+// also derives LAPACK's interchanges (on warp 0 once its block rows are
+// done), the swap plan, the block and the pivots' spread; every CTA writes
+// its rows' L21 and their exact bf16 slices (the update's A operand).
+constexpr int PL_LPR = 4;                          // lanes per row
+constexpr int PL_ROWS = 2 * SNB;                   // block rows + rows below
+constexpr int PL_RWARPS = PL_ROWS * PL_LPR / 32;   // 16 warps with rows
+constexpr int PL_BWARPS = SNB * PL_LPR / 32;       // 8 of them the block's
+constexpr int PL_THREADS = PL_RWARPS * 32 + 32;    // and the reciprocal warp: 544
+constexpr size_t PL_SMEM = sizeof(double) * PL_ROWS * (SNB + 1);
+__global__ void __launch_bounds__(PL_THREADS, 1)
+panel_lu64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int32_t *win_in, const double *sel,
+           int32_t *plan, int32_t *ipiv, int32_t *info, uint64_t *track, double give_up, int32_t *err, void *aop,
+           int32_t *aexp, int64_t cap) {
+  const int nA = (int)gridDim.x - 1;
+  const bool top = (int)blockIdx.x == nA;
   // an abandoned factorisation (flag set by an earlier panel on this stream):
   // identity pivots keep ipiv valid for the kernels that compose it
   if (track != nullptr && *(volatile const int32_t *)(track + 2) != 0) {
-    for (int t = threadIdx.x; t < jb; t += blockDim.x) ipiv[t] = col0 + t + 1;
+    if (top)
+      for (int t = threadIdx.x; t < jb; t += blockDim.x) ipiv[t] = col0 + t + 1;
     return;
   }
-  __shared__ double a[SNB][SNB + 1];  // a[q][c]: the pivot row of column q (panel row win[q]), column c
+  extern __shared__ __align__(16) double pl_raw[];
+  double(*a)[SNB + 1] = reinterpret_cast<double(*)[SNB + 1]>(pl_raw);  // rows 0..63: the block; 64 + i: slot i
   __shared__ int32_t win[SNB], pivl[SNB], posin[SNB], at_[SNB], rows_s[2 * SNB], src_s[2 * SNB];
-  __shared__ double rinv_s[2];  // 1 / the pivot of column k (k & 1)
-  __shared__ int bad, cnt_s;
+  __shared__ int32_t slot[SNB];  // panel position of slot i's row (-1: none)
+  __shared__ double rinv_s[2];   // 1 / the pivot of column k (k & 1)
+  __shared__ int bad;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int q = tid / T64_LPR, h = tid % T64_LPR;
+  const int q = tid / PL_LPR, h = tid % PL_LPR;
+  const int64_t base = top ? 0 : SNB + (int64_t)blockIdx.x * SNB;  // panel position of slot 0
   if (tid == 0) bad = 0;
+  if (tid < SNB) slot[tid] = 0;
   __syncthreads();
-  for (int t = tid; t < jb; t += T64_THREADS) {
-    win[t] = win_in[t];
+  for (int t = tid; t < jb; t += PL_THREADS) {
+    const int w = win_in[t];
+    win[t] = w;
     // a selection that did not finish (its exchange gave up and set the
     // error word) leaves no valid list: stop here rather than index W with it
-    if (win[t] < 0 || win[t] >= mp) atomicExch(&bad, 1);
+    if (w < 0 || w >= mp) atomicExch(&bad, 1);
+    else if (w >= base && w < base + SNB) slot[w - base] = -1;  // a pivot: not one of this CTA's rows
   }
   __syncthreads();
   if (bad != 0) {
-    if (tid == 0) atomicExch(err, 7);
-    for (int t = tid; t < jb; t += T64_THREADS) ipiv[t] = col0 + t + 1;
+    if (top) {
+      if (tid == 0) atomicExch(err, 7);
+      for (int t = tid; t < jb; t += PL_THREADS) ipiv[t] = col0 + t + 1;
+    }
     return;
   }
-  // the selected rows, all of a thread's loads in flight together
-  if (tid < T64_THREADS) {
-    constexpr int PER = SNB * SNB / T64_THREADS;
+  if (tid < SNB) {
+    const int64_t p = base + tid;
+    slot[tid] = (slot[tid] == 0 && p < mp && (!top || tid < jb)) ? (int32_t)p : -1;
+  }
+  __syncthreads();
+  // the block (from sel) and this CTA's rows (from W), all of a thread's
+  // loads in flight together
+  if (tid < PL_RWARPS * 32) {
+    constexpr int PER = PL_ROWS * SNB / (PL_RWARPS * 32);  // 16
     double v[PER];
 #pragma unroll
     for (int u = 0; u < PER; ++u) {
-      const int e = tid + T64_THREADS * u, r = e % SNB, c = e / SNB;
-      v[u] = (r < jb && c < jb) ? Wp[win[r] + (int64_t)c * ldw] : 0.0;
+      const int e = tid + PL_RWARPS * 32 * u;
+      if (e < SNB * SNB) {
+        const int r = e / SNB, c = e % SNB;
+        v[u] = (r < jb && c < jb) ? sel[r * SNB + c] : 0.0;
+      } else {
+        const int r = (e - SNB * SNB) % SNB, c = (e - SNB * SNB) / SNB;
+        const int s2 = slot[r];
+        v[u] = (s2 >= 0 && c < jb) ? Wp[s2 + (int64_t)c * ldw] : 0.0;
+      }
     }
 #pragma unroll
     for (int u = 0; u < PER; ++u) {
-      const int e = tid + T64_THREADS * u;
-      a[e % SNB][e / SNB] = v[u];
+      const int e = tid + PL_RWARPS * 32 * u;
+      if (e < SNB * SNB)
+        a[e / SNB][e % SNB] = v[u];
+      else
+        a[SNB + (e - SNB * SNB) % SNB][(e - SNB * SNB) / SNB] = v[u];
     }
   }
-  uint64_t umax = 0, umin = ~0ull;  // |u_kk| bits (the threads that formed the pivots' reciprocals)
+  uint64_t umax = 0, umin = ~0ull;  // |u_kk| bits (the reciprocal warp's lane 0)
   // 1 / the pivot of column k into rinv_s[k & 1], with the pivots' extent and
   // the first zero pivot
   auto pivot = [&](double pv, int k) {
     const uint64_t ab = (uint64_t)__double_as_longlong(pv) & 0x7fffffffffffffffull;
     rinv_s[k & 1] = ab != 0 ? recip64(pv) : 0.0;
-    if (ab == 0) atomicCAS(info, 0, col0 + k + 1);
+    if (ab == 0 && top) atomicCAS(info, 0, col0 + k + 1);
     if (ab <= 0x7ff0000000000000ull) {
       umax = ab > umax ? ab : umax;
       umin = ab < umin ? ab : umin;
     }
   };
-  const bool rwarp = warp == T64_WARPS;  // the reciprocal warp (no rows)
-  if (tid == 0) interchanges_init(jb, posin, at_);
+  const bool rwarp = warp == PL_RWARPS;  // the reciprocal warp (no rows)
+  if (top && tid == 0) interchanges_init(jb, posin, at_);
   __syncthreads();
   if (rwarp && lane == 0) pivot(a[0][0], 0);
-  int jdone = 0;  // (thread 0) columns whose interchange is done
+  int jdone = 0;  // (thread 0 of the last CTA) columns whose interchange is done
 #pragma unroll 1
   for (int k = 0; k < jb; ++k) {
-    const int hk = k % T64_LPR;
+    const int hk = k % PL_LPR;
     // column k's pivot row and reciprocal are final
-    asm volatile("bar.sync 1, %0;" ::"r"(T64_BLOCK) : "memory");
+    asm volatile("bar.sync 1, %0;" ::"r"(PL_THREADS) : "memory");
     if (rwarp) {
       // the next pivot, once its row's warp has updated it (named barrier 2:
       // that warp arrives, this one waits), while the rows' other columns are
@@ -805,25 +849,25 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
       }
       continue;
     }
-    if ((warp + 1) * (32 / T64_LPR) - 1 <= k) {  // every row of this warp is done
+    if (warp < PL_BWARPS && (warp + 1) * (32 / PL_LPR) - 1 <= k) {  // every block row of this warp is done
       // warp 0, idle from column 7 on, runs LAPACK's interchanges for the
       // pivots, two per column until it has caught up
-      if (tid == 0)
+      if (top && tid == 0)
         for (int u = 0; u < 2 && jdone <= k; ++u, ++jdone) {
           pivl[jdone] = win[jdone];
           ipiv[jdone] = interchange_step(jdone, win[jdone], jb, col0, posin, at_);
         }
       continue;
     }
-    const bool act = q > k && q < jb;
+    const bool act = q >= SNB || (q > k && q < jb);  // (rows below: every step; an empty slot holds zeros)
     const double l = act ? a[q][k] * rinv_s[k & 1] : 0.0;
     __syncwarp();  // the quad has read a[q][k] before it becomes the multiplier
     if (act) {
       if (h == hk) a[q][k] = l;
       // column k + 1 first: the next pivot
-      if (k + 1 < jb && h == (k + 1) % T64_LPR) a[q][k + 1] = fma(-l, a[k][k + 1], a[q][k + 1]);
+      if (k + 1 < jb && h == (k + 1) % PL_LPR) a[q][k + 1] = fma(-l, a[k][k + 1], a[q][k + 1]);
     }
-    if (k + 1 < jb && warp == (k + 1) / (32 / T64_LPR)) {  // the next pivot's warp hands it over
+    if (k + 1 < jb && warp == (k + 1) / (32 / PL_LPR)) {  // the next pivot's warp hands it over
       __threadfence_block();
       __syncwarp();
       asm volatile("bar.arrive 2, 64;" ::: "memory");
@@ -832,165 +876,84 @@ panel_top64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int
     // every lane of the warp (a per-lane start would split the warp into
     // paths that each dispatch their own FP64 instructions), 4 columns at a
     // time with all of their loads issued before the FMAs
-    for (int u0 = (k + 2) / T64_LPR; u0 < SNB / T64_LPR; u0 += 4) {
+    for (int u0 = (k + 2) / PL_LPR; u0 < SNB / PL_LPR; u0 += 4) {
       double pr[4], xr[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        const int c = T64_LPR * (u0 + u) + h;
-        const bool on = act && u0 + u < SNB / T64_LPR && c >= k + 2 && c < jb;
+        const int c = PL_LPR * (u0 + u) + h;
+        const bool on = act && u0 + u < SNB / PL_LPR && c >= k + 2 && c < jb;
         pr[u] = on ? a[k][c] : 0.0;
         xr[u] = on ? a[q][c] : 0.0;
       }
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        const int c = T64_LPR * (u0 + u) + h;
-        if (act && u0 + u < SNB / T64_LPR && c >= k + 2 && c < jb) a[q][c] = fma(-l, pr[u], xr[u]);
+        const int c = PL_LPR * (u0 + u) + h;
+        if (act && u0 + u < SNB / PL_LPR && c >= k + 2 && c < jb) a[q][c] = fma(-l, pr[u], xr[u]);
       }
     }
   }
-  // the pivots' extent lives with the lanes that saw them: per warp here,
-  // into thread 0 at the end
-  __shared__ uint64_t wx[T64_WARPS + 1], wn[T64_WARPS + 1];
-  {
-    uint64_t mx = umax, mn = umin;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      const uint64_t o1 = __shfl_xor_sync(0xffffffffu, mx, off), o2 = __shfl_xor_sync(0xffffffffu, mn, off);
-      mx = o1 > mx ? o1 : mx;
-      mn = o2 < mn ? o2 : mn;
-    }
-    if (lane == 0) {
-      wx[warp] = mx;
-      wn[warp] = mn;
-    }
-  }
-  if (tid == 0)  // the interchanges still to run (the last columns, or all of a narrow block)
+  if (top && tid == 0)  // the interchanges still to run (the last columns, or all of a narrow block)
     for (; jdone < jb; ++jdone) {
       pivl[jdone] = win[jdone];
       ipiv[jdone] = interchange_step(jdone, win[jdone], jb, col0, posin, at_);
     }
   __syncthreads();
-  // the moves of rows, to the swap kernel (plan) and to this CTA (rows_s, src_s)
-  if (warp == 0) list_panel_moves(pivl, posin, jb, col0, plan, rows_s, src_s, &cnt_s);
-  __syncthreads();
-  // rows the interchanges move below the block: their panel columns, read
-  // before anything is written
-  const int cnt = cnt_s;
-  constexpr int MV = 2 * SNB * SNB / T64_THREADS;
-  double mv[MV];
-  const bool rowt = tid < T64_THREADS;
-#pragma unroll
-  for (int u = 0; u < MV; ++u) {
-    const int e = tid + T64_THREADS * u, t = e % (2 * SNB), c = e / (2 * SNB);
-    mv[u] = (rowt && t < cnt && c < jb && rows_s[t] >= jb) ? Wp[src_s[t] + (int64_t)c * ldw] : 0.0;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int u = 0; u < MV; ++u) {
-    const int e = tid + T64_THREADS * u, t = e % (2 * SNB), c = e / (2 * SNB);
-    if (rowt && t < cnt && c < jb && rows_s[t] >= jb) Wp[rows_s[t] + (int64_t)c * ldw] = mv[u];
-  }
-  // the factored block (unit-lower L11 below the diagonal, U11 on and above)
-  for (int e = tid; e < jb * jb; e += T64_BLOCK) {
-    const int r = e % jb, c = e / jb;
-    Wp[r + (int64_t)c * ldw] = a[r][c];
-  }
-  if (track != nullptr && tid == 0) {
-    // the running extent of |u_ii| and the give-up test
-    for (int w = 0; w <= T64_WARPS; ++w) {
-      umax = wx[w] > umax ? wx[w] : umax;
-      umin = wn[w] < umin ? wn[w] : umin;
-    }
-    if (umin != ~0ull) {
-      if (umax > track[0]) track[0] = umax;
-      if (umin < track[1]) track[1] = umin;
-    }
-    const double gmx = __longlong_as_double((long long)track[0]), gmn = __longlong_as_double((long long)track[1]);
-    const double spread = gmn > 0.0 ? gmx / gmn : INFINITY;
-    if (give_up_now(spread, give_up, col0 + jb, col0 + mp)) *(volatile int32_t *)(track + 2) = 1;
-  }
-}
-
-// L21 = A21 U11^-1 (rows jb..mp-1 of the panel, after its interchanges) in
-// FP64, and the update's operand.  Eight lanes per row, lane h holding
-// columns 8i + h: the substitution's chain runs over the columns, every FP64
-// warp instruction has all 32 lanes busy (on GB300 an FP64 instruction takes
-// its full issue slot whatever the number of active lanes), and 32 rows make
-// a CTA of 8 warps, two per sub-partition, so that one warp's shared-memory
-// and shuffle work overlaps the other's FP64 dispatch.  U11 is held as a
-// packed upper triangle (16.6 KB), small enough for a CTA to share an SM
-// with the update kernel that runs beside the panel.
-constexpr int L21_LPR = 8;                       // lanes per row
-constexpr int L21_ROWS = 32;                     // rows per CTA
-constexpr int L21_THREADS = L21_ROWS * L21_LPR;  // 256
-constexpr int L21_NX = SNB / L21_LPR;            // values per lane
-__host__ __device__ constexpr int tri_off(int k) { return k * SNB - k * (k - 1) / 2; }  // row k of the packed U
-__global__ void __launch_bounds__(L21_THREADS)
-panel_l21_64(double *Wp, int64_t ldw, int64_t mp, int jb, void *aop, int32_t *aexp, int64_t cap,
-             const int32_t *abort) {
-  if (abort != nullptr && *(volatile const int32_t *)abort != 0) return;  // set before this launch (same stream)
-  __shared__ double U[SNB * (SNB + 1) / 2];  // U[tri_off(k) + c - k] = u_kc, c >= k (zero outside the jb x jb block)
-  __shared__ double rinv[SNB];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, h = lane & (L21_LPR - 1);
-  for (int k = warp; k < SNB; k += L21_THREADS / 32)
-    for (int c = k + lane; c < SNB; c += 32) U[tri_off(k) + c - k] = (c < jb) ? Wp[k + (int64_t)c * ldw] : 0.0;
-  __syncthreads();
-  if (tid < SNB) {
-    const double d = U[tri_off(tid)];
-    rinv[tid] = (tid < jb && (__double_as_longlong(d) << 1) != 0) ? 1.0 / d : 0.0;
-  }
-  __syncthreads();
-  const int64_t r = jb + (int64_t)blockIdx.x * L21_ROWS + warp * (32 / L21_LPR) + lane / L21_LPR;
-  const bool live = r < mp;
-  double x[L21_NX];
-#pragma unroll
-  for (int i = 0; i < L21_NX; ++i) {
-    const int c = L21_LPR * i + h;
-    x[i] = (live && c < jb) ? Wp[r + (int64_t)c * ldw] : 0.0;
-  }
-#pragma unroll
-  for (int k = 0; k < SNB; ++k) {
-    const int ik = k / L21_LPR, hk = k % L21_LPR;
-    const double mine = x[ik] * rinv[k];  // (the owner's value is l_rk)
-    const double lk = __shfl_sync(0xffffffffu, mine, (lane & ~(L21_LPR - 1)) | hk);
-    if (h == hk) x[ik] = lk;
-#pragma unroll
-    for (int i = ik; i < L21_NX; ++i) {
-      // column 4i + h > k: every i > ik, and at i == ik the lanes after the owner
-      if (i > ik || h > hk) x[i] = fma(-lk, U[tri_off(k) + L21_LPR * i + h - k], x[i]);
-    }
-  }
-  if (live) {
-#pragma unroll
-    for (int i = 0; i < L21_NX; ++i) {
-      const int c = L21_LPR * i + h;
-      if (c < jb) Wp[r + (int64_t)c * ldw] = x[i];
-    }
-  }
-  if (aop != nullptr) {
-    // exact bf16 slices of the row: one exponent for its 64 values
+  if (top && warp == 0) list_panel_moves(pivl, posin, jb, col0, plan, rows_s, src_s);
+  // -- this CTA's rows: L21 to their final positions (the last CTA's to
+  // where the interchanges put them) and their exact bf16 slices, one
+  // exponent per row
+  if (q >= SNB && warp < PL_RWARPS) {
+    const int i = q - SNB, s2 = slot[i];
+    double x[SNB / PL_LPR];
     uint64_t mb = 0;
 #pragma unroll
-    for (int i = 0; i < L21_NX; ++i) {
-      const uint64_t m = oz_mag(x[i]);
+    for (int u = 0; u < SNB / PL_LPR; ++u) {
+      x[u] = a[q][PL_LPR * u + h];
+      const uint64_t m = oz_mag(x[u]);
       mb = m > mb ? m : mb;
     }
 #pragma unroll
-    for (int off = 1; off < L21_LPR; off <<= 1) {  // the row's other lanes
+    for (int off = 1; off < PL_LPR; off <<= 1) {  // the row's other lanes
       const uint64_t om = __shfl_xor_sync(0xffffffffu, mb, off);
       mb = om > mb ? om : mb;
     }
-    if (!live) return;
-    const int e = oz_exponent(mb);
-    const int64_t orow = r - jb;
-    if (h == 0) aexp[orow] = e;
-    __nv_bfloat16 *out = static_cast<__nv_bfloat16 *>(aop);
+    if (s2 >= 0) {
+      const int64_t fp = top ? posin[s2] : s2;
 #pragma unroll
-    for (int i = 0; i < L21_NX; ++i) {
-      __nv_bfloat16 sl[OZ_SLICES];
-      oz_slices(x[i], e, sl);
+      for (int u = 0; u < SNB / PL_LPR; ++u) {
+        const int c = PL_LPR * u + h;
+        if (c < jb) Wp[fp + (int64_t)c * ldw] = x[u];
+      }
+      if (aop != nullptr) {
+        const int e = oz_exponent(mb);
+        const int64_t orow = fp - jb;
+        if (h == 0) aexp[orow] = e;
+        __nv_bfloat16 *out = static_cast<__nv_bfloat16 *>(aop);
 #pragma unroll
-      for (int t = 0; t < OZ_SLICES; ++t) out[((int64_t)t * cap + orow) * SNB + L21_LPR * i + h] = sl[t];
+        for (int u = 0; u < SNB / PL_LPR; ++u) {
+          __nv_bfloat16 sl[OZ_SLICES];
+          oz_slices(x[u], e, sl);
+#pragma unroll
+          for (int t = 0; t < OZ_SLICES; ++t) out[((int64_t)t * cap + orow) * SNB + PL_LPR * u + h] = sl[t];
+        }
+      }
+    }
+  }
+  if (top) {
+    // the factored block (unit-lower L11 below the diagonal, U11 on and above)
+    for (int e = tid; e < jb * jb; e += PL_THREADS) {
+      const int r = e % jb, c = e / jb;
+      Wp[r + (int64_t)c * ldw] = a[r][c];
+    }
+    if (track != nullptr && rwarp && lane == 0) {
+      // the running extent of |u_ii| and the give-up test
+      if (umin != ~0ull) {
+        if (umax > track[0]) track[0] = umax;
+        if (umin < track[1]) track[1] = umin;
+      }
+      const double gmx = __longlong_as_double((long long)track[0]), gmn = __longlong_as_double((long long)track[1]);
+      const double spread = gmn > 0.0 ? gmx / gmn : INFINITY;
+      if (give_up_now(spread, give_up, col0 + jb, col0 + mp)) *(volatile int32_t *)(track + 2) = 1;
     }
   }
 }
@@ -1235,6 +1198,7 @@ int MixedLU::reserve(int64_t n_, int kind_, cudaStream_t s) {
     }
     BOLA_TRY_CUDA(cudaMallocAsync(&bop, (size_t)OZ_SLICES * n * SNB * 2, s));
     BOLA_TRY_CUDA(cudaMallocAsync(&eb, sizeof(int32_t) * n, s));
+    BOLA_TRY_CUDA(cudaMallocAsync(&sel, sizeof(double) * SNB * SNB, s));
     BOLA_TRY(make_kmajor_map(&mapB, bop, OZ_SLICES * n, true, 64));
     return 0;
   }
@@ -1262,7 +1226,8 @@ void MixedLU::release(cudaStream_t s) {
                    reinterpret_cast<void **>(&aop_lo[1]), reinterpret_cast<void **>(&bop_lo),
                    reinterpret_cast<void **>(&err), reinterpret_cast<void **>(&plan), reinterpret_cast<void **>(&track),
                    reinterpret_cast<void **>(&ea[0]),
-                   reinterpret_cast<void **>(&ea[1]), reinterpret_cast<void **>(&eb)}) {
+                   reinterpret_cast<void **>(&ea[1]), reinterpret_cast<void **>(&eb),
+                   reinterpret_cast<void **>(&sel)}) {
     if (*p) cudaFreeAsync(*p, s);
     *p = nullptr;
   }
@@ -1325,17 +1290,19 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
       double *Wp = W + j + j * ldw;
       int32_t *win = lu.plan + (int64_t)PLAN_STRIDE * cdiv(lu.cap_n, SNB);
       BOLA_TRY(launch_tpanel<double>(lu.sp, Wp, ldw, mp, jb, ipiv + j, (int32_t)j, info, nullptr, track, give_up,
-                                     lu.err, win));
+                                     lu.err, win, lu.sel));
       {
-        ProfScope prof(lu.sp, "panel_top64", (double)jb * jb * jb * 2.0 / 3.0, 16.0 * (double)jb * jb);
-        panel_top64<<<1, T64_BLOCK, 0, lu.sp>>>(Wp, ldw, mp, jb, (int32_t)j, win, plan_k, ipiv + j, info, track,
-                                          give_up, lu.err);
-      }
-      if (mp > jb) {
-        ProfScope prof(lu.sp, "panel_l21_64", (double)(mp - jb) * jb * jb, 16.0 * (double)(mp - jb) * jb);
-        panel_l21_64<<<(unsigned)cdiv(mp - jb, L21_ROWS), L21_THREADS, 0, lu.sp>>>(Wp, ldw, mp, jb,
-                                                                           upd ? lu.aop[buf] : nullptr, lu.ea[buf],
-                                                                           lu.cap_n, abort);
+        ProfScope prof(lu.sp, "panel_lu64", (double)jb * jb * jb * 2.0 / 3.0 + (double)(mp - jb) * jb * jb,
+                       16.0 * (double)mp * jb);
+        static bool attr = false;
+        if (!attr) {
+          BOLA_TRY_CUDA(cudaFuncSetAttribute(panel_lu64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PL_SMEM));
+          attr = true;
+        }
+        const unsigned nA = mp > jb ? (unsigned)cdiv(mp - jb, SNB) : 0u;
+        panel_lu64<<<nA + 1, PL_THREADS, PL_SMEM, lu.sp>>>(Wp, ldw, mp, jb, (int32_t)j, win, lu.sel, plan_k, ipiv + j,
+                                                          info, track, give_up, lu.err, upd ? lu.aop[buf] : nullptr,
+                                                          lu.ea[buf], lu.cap_n);
       }
       BOLA_CHECK_LAUNCH();
     } else
