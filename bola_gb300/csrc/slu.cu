@@ -721,12 +721,13 @@ __device__ __forceinline__ double recip64(double p) {
 // so the panel is factored without further pivoting, as CALU's last step
 // does: the selected block and every row below it go through the same 64
 // right-looking steps.  CTA i < nA takes the panel's rows at positions
-// 64 + 64 i .. 127 + 64 i that are not pivots (they stay where they are);
-// the last CTA takes the first 64 rows that are not pivots (they move to the
-// pivots' old positions).  Every CTA factors the 64 x 64 block itself, with
-// the same arithmetic (so the same U11 everywhere), from the copy of the
-// pivot rows that the selection made (sel): no CTA reads a part of W that
-// another one writes.  Rows in shared memory, four lanes per row, lane h
+// 64 (i + 1) .. 64 (i + 1) + 63 that are not pivots (they stay where they
+// are); the last CTA takes the first 64 rows that are not pivots (they move
+// to the pivots' old positions).  (128 rows a CTA, on half the SMs, measured
+// slower: each CTA's FP64 pipe bounds it.)  Every CTA factors the 64 x 64
+// block itself, with the same arithmetic (so the same U11 everywhere), from
+// the copy of the pivot rows that the selection made (sel): no CTA reads a
+// part of W that another one writes.  Rows in shared memory, four lanes per row, lane h
 // updating columns c = h (mod 4), so every FP64 warp instruction has 32 busy
 // lanes; warps 0-7 hold the block (a warp whose rows are done stops
 // issuing), warps 8-15 the rows below, warp 16 forms the next pivot's
@@ -739,7 +740,8 @@ __device__ __forceinline__ double recip64(double p) {
 // done), the swap plan, the block and the pivots' spread; every CTA writes
 // its rows' L21 and their exact bf16 slices (the update's A operand).
 constexpr int PL_LPR = 4;                          // lanes per row
-constexpr int PL_ROWS = 2 * SNB;                   // block rows + rows below
+constexpr int PL_SLOTS = SNB;                      // rows below the block per CTA
+constexpr int PL_ROWS = SNB + PL_SLOTS;            // block rows + rows below
 constexpr int PL_RWARPS = PL_ROWS * PL_LPR / 32;   // 16 warps with rows
 constexpr int PL_BWARPS = SNB * PL_LPR / 32;       // 8 of them the block's
 constexpr int PL_THREADS = PL_RWARPS * 32 + 32;    // and the reciprocal warp: 544
@@ -760,14 +762,14 @@ panel_lu64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int3
   extern __shared__ __align__(16) double pl_raw[];
   double(*a)[SNB + 1] = reinterpret_cast<double(*)[SNB + 1]>(pl_raw);  // rows 0..63: the block; 64 + i: slot i
   __shared__ int32_t win[SNB], pivl[SNB], posin[SNB], at_[SNB], rows_s[2 * SNB], src_s[2 * SNB];
-  __shared__ int32_t slot[SNB];  // panel position of slot i's row (-1: none)
+  __shared__ int32_t slot[PL_SLOTS];  // panel position of slot i's row (-1: none)
   __shared__ double rinv_s[2];   // 1 / the pivot of column k (k & 1)
   __shared__ int bad;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int q = tid / PL_LPR, h = tid % PL_LPR;
-  const int64_t base = top ? 0 : SNB + (int64_t)blockIdx.x * SNB;  // panel position of slot 0
+  const int64_t base = top ? 0 : PL_SLOTS + (int64_t)blockIdx.x * PL_SLOTS;  // panel position of slot 0
   if (tid == 0) bad = 0;
-  if (tid < SNB) slot[tid] = 0;
+  if (tid < PL_SLOTS) slot[tid] = 0;
   __syncthreads();
   for (int t = tid; t < jb; t += PL_THREADS) {
     const int w = win_in[t];
@@ -775,7 +777,7 @@ panel_lu64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int3
     // a selection that did not finish (its exchange gave up and set the
     // error word) leaves no valid list: stop here rather than index W with it
     if (w < 0 || w >= mp) atomicExch(&bad, 1);
-    else if (w >= base && w < base + SNB) slot[w - base] = -1;  // a pivot: not one of this CTA's rows
+    else if (w >= base && w < base + PL_SLOTS) slot[w - base] = -1;  // a pivot: not one of this CTA's rows
   }
   __syncthreads();
   if (bad != 0) {
@@ -785,9 +787,9 @@ panel_lu64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int3
     }
     return;
   }
-  if (tid < SNB) {
+  if (tid < PL_SLOTS) {
     const int64_t p = base + tid;
-    slot[tid] = (slot[tid] == 0 && p < mp && (!top || tid < jb)) ? (int32_t)p : -1;
+    slot[tid] = (slot[tid] == 0 && p < mp) ? (int32_t)p : -1;
   }
   __syncthreads();
   // the block (from sel) and this CTA's rows (from W), all of a thread's
@@ -802,7 +804,7 @@ panel_lu64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int3
         const int r = e / SNB, c = e % SNB;
         v[u] = (r < jb && c < jb) ? sel[r * SNB + c] : 0.0;
       } else {
-        const int r = (e - SNB * SNB) % SNB, c = (e - SNB * SNB) / SNB;
+        const int r = (e - SNB * SNB) % PL_SLOTS, c = (e - SNB * SNB) / PL_SLOTS;
         const int s2 = slot[r];
         v[u] = (s2 >= 0 && c < jb) ? Wp[s2 + (int64_t)c * ldw] : 0.0;
       }
@@ -813,7 +815,7 @@ panel_lu64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int3
       if (e < SNB * SNB)
         a[e / SNB][e % SNB] = v[u];
       else
-        a[SNB + (e - SNB * SNB) % SNB][(e - SNB * SNB) / SNB] = v[u];
+        a[SNB + (e - SNB * SNB) % PL_SLOTS][(e - SNB * SNB) / PL_SLOTS] = v[u];
     }
   }
   uint64_t umax = 0, umin = ~0ull;  // |u_kk| bits (the reciprocal warp's lane 0)
@@ -918,7 +920,7 @@ panel_lu64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int3
       mb = om > mb ? om : mb;
     }
     if (s2 >= 0) {
-      const int64_t fp = top ? posin[s2] : s2;
+      const int64_t fp = s2 < jb ? posin[s2] : s2;  // (only the last CTA has rows among the first jb)
 #pragma unroll
       for (int u = 0; u < SNB / PL_LPR; ++u) {
         const int c = PL_LPR * u + h;
@@ -1299,7 +1301,7 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
           BOLA_TRY_CUDA(cudaFuncSetAttribute(panel_lu64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PL_SMEM));
           attr = true;
         }
-        const unsigned nA = mp > jb ? (unsigned)cdiv(mp - jb, SNB) : 0u;
+        const unsigned nA = mp > PL_SLOTS ? (unsigned)cdiv(mp - PL_SLOTS, PL_SLOTS) : 0u;
         panel_lu64<<<nA + 1, PL_THREADS, PL_SMEM, lu.sp>>>(Wp, ldw, mp, jb, (int32_t)j, win, lu.sel, plan_k, ipiv + j,
                                                           info, track, give_up, lu.err, upd ? lu.aop[buf] : nullptr,
                                                           lu.ea[buf], lu.cap_n);
