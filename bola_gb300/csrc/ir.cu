@@ -7,8 +7,8 @@
 //   x0 = S U^-1 L^-1 P b          FP32 triangular solves
 //   repeat: r = b - A x           FP64 (the exact DGEMM)
 //           berr = max_rhs ||r||_inf / (||A||_inf ||x||_inf + ||b||_inf)
-//           stop when berr <= tol; on stall (berr not halving) switch to
-//           GMRES-IR, and when that stalls too, to the plain FP64 path
+//           stop when berr <= tol; on a sweep gaining less than ~3x switch
+//           to GMRES-IR, and when that stalls too, to the plain FP64 path
 //           d = S U^-1 L^-1 P (r / ||r||) * ||r||;  x += d    (FP64 update)
 // The residual, the update and the backward-error test are the only FP64
 // steps.  Each FP32 triangular solve is one launch: a dataflow over 64-row
@@ -1137,7 +1137,13 @@ int dgesv_mixed_ws(Workspace &w, bool chol, int64_t n, int64_t nrhs, const doubl
           to_gmres = o.gmres != 0;
           break;
         }
-        if (o.gmres && rate > 0.05) {  // converging slowly: Krylov acceleration pays
+        // converging slowly: Krylov acceleration pays.  A plain sweep and a
+        // GMRES step cost about the same (two triangular solves and an
+        // FP64-accurate product); GMRES(24) took ~13 of them for the seven
+        // digits left at kappa = 1e6 (n = 8192), i.e. ~1.9 per digit, and a
+        // plain sweep at rate r gains log10(1 / r) digits: the break-even is
+        // r ~ 0.3 (kappa = 1e6: r ~ 0.2, plain IR 28.7 against 30.6 ms)
+        if (o.gmres && rate > 0.3) {
           to_gmres = true;
           break;
         }
