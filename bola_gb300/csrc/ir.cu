@@ -30,24 +30,41 @@ constexpr int TB = 64;      // triangular-solve block (= LU block)
 constexpr int MAXRHS = 32;  // right-hand sides per refinement sweep
 
 // ---- scaling and conversion -------------------------------------------------------
-__global__ void colblock_scale(int64_t n, const double *__restrict__ A, int64_t lda, double *scale) {
-  // one CTA per 64-column block: scale = 2^-e with max|a| in [2^(e-1), 2^e)
-  __shared__ double red[32];
-  const int64_t c0 = (int64_t)blockIdx.x * TB;
-  const int64_t c1 = imin(n, c0 + TB);
+// Per 64-column block the largest |a| (a CTA per block and slice of rows,
+// every thread's loads of 4 columns in flight together), folded with 64-bit
+// atomics into mbits as the bits of a non-negative double (they order like
+// the values; mbits starts at zero); colblock_finish then turns it in place
+// into the block's scale 2^-e with max|a| in [2^(e-1), 2^e).  A NaN is
+// passed over, as fmax does.
+__global__ void __launch_bounds__(256)
+colblock_max(int64_t n, const double *__restrict__ A, int64_t lda, unsigned long long *mbits) {
+  __shared__ double red[8];
+  const int64_t c0 = (int64_t)blockIdx.x * TB, c1 = imin(n, c0 + TB);
+  const int64_t rs = cdiv(n, (int64_t)gridDim.y), r0 = (int64_t)blockIdx.y * rs, r1 = imin(n, r0 + rs);
   double m = 0.0;
-  for (int64_t c = c0; c < c1; ++c)
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, fabs(A[i + c * lda]));
+  for (int64_t c = c0; c < c1; c += 4)
+    for (int64_t i = r0 + threadIdx.x; i < r1; i += 256) {
+      double v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) v[u] = c + u < c1 ? fabs(A[i + (c + u) * lda]) : 0.0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) m = fmax(m, v[u]);
+    }
   for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double mm = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mm = fmax(mm, red[w]);
-    int e = 0;
-    frexp(mm, &e);
-    scale[blockIdx.x] = (mm > 0.0 && isfinite(mm)) ? ldexp(1.0, -e) : 1.0;
+    for (int w = 1; w < 8; ++w) m = fmax(m, red[w]);
+    atomicMax(mbits + blockIdx.x, (unsigned long long)__double_as_longlong(m));
   }
+}
+__global__ void colblock_finish(int64_t nb, double *scale) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  const double mm = scale[b];  // (the bits colblock_max left)
+  int e = 0;
+  frexp(mm, &e);
+  scale[b] = (mm > 0.0 && isfinite(mm)) ? ldexp(1.0, -e) : 1.0;
 }
 
 // W = A S rounded to T (exact for T = double: S is a power of two per block).
@@ -667,6 +684,7 @@ struct Workspace {
   double *hn = nullptr;                              // per-column 2-norms (GMRES)
   int32_t *ipiv = nullptr, *perm = nullptr, *info = nullptr;
   bool chol = false;           // the current factor is a Cholesky (in LU form)
+  bool split_kept = false;     // oz holds this call's A already (a solve handed on within one call)
   double *dscale = nullptr;    // its row scale D (W = D A D)
   void *dg = nullptr;          // scratch: the diagonal of L (8-byte elements)
   float *Mc = nullptr;         // FP32 factors: Dinv times the coupling blocks, lower then upper
@@ -1016,15 +1034,20 @@ int dgesv_mixed_ws(Workspace &w, bool chol, int64_t n, int64_t nrhs, const doubl
     else
       convert_sym_lower<float><<<(unsigned)cdiv(n * n, 256), 256, 0, s>>>(n, a, lda, w.dscale, (float *)w.W, n);
   } else {
-    ProfScope prof(s, "mixed_convert", 0.0, 12.0 * (double)n * n, 2);
-    colblock_scale<<<(unsigned)cdiv(n, TB), 512, 0, s>>>(n, a, lda, w.scale);
+    ProfScope prof(s, "mixed_convert", 0.0, 12.0 * (double)n * n, 3);
+    BOLA_TRY_CUDA(cudaMemsetAsync(w.scale, 0, sizeof(double) * cdiv(n, TB), s));
+    colblock_max<<<dim3((unsigned)cdiv(n, TB), (unsigned)imin(16, cdiv(n, 256))), 256, 0, s>>>(
+        n, a, lda, reinterpret_cast<unsigned long long *>(w.scale));
+    colblock_finish<<<(unsigned)cdiv(cdiv(n, TB), 256), 256, 0, s>>>(cdiv(n, TB), w.scale);
     if (fp64)
       convert_scaled<double><<<(unsigned)cdiv(n * n, 256), 256, 0, s>>>(n, a, lda, w.scale, (double *)w.W, ldW);
     else
       convert_scaled<float><<<(unsigned)cdiv(n * n, 256), 256, 0, s>>>(n, a, lda, w.scale, (float *)w.W, n);
   }
   BOLA_CHECK_LAUNCH();
-  BOLA_TRY(w.oz.split(s, a, lda, w.rowsum));  // A's digit planes and its row sums
+  // A's digit planes and its row sums (once per call: a solve handed on to
+  // another factor within the same call keeps them)
+  if (!w.split_kept) BOLA_TRY(w.oz.split(s, a, lda, w.rowsum));
   {
     ProfScope prof(s, "mixed_norms", 0.0, 8.0 * (double)n * nr, 2);
     max_of<<<1, 1024, 0, s>>>(n, w.rowsum, nrm + 3 * nr);
@@ -1101,7 +1124,10 @@ int dgesv_mixed_ws(Workspace &w, bool chol, int64_t n, int64_t nrhs, const doubl
     // a pivot that is not positive: A is not SPD at this precision (or at
     // all) and no FP64-accurate Cholesky is left to try; the mixed LU takes
     // over with the same options
-    BOLA_TRY(dgesv_mixed_ws(w, false, n, nrhs, a, lda, b, ldb, x, ldx, &o, out, s));
+    w.split_kept = true;
+    const int st = dgesv_mixed_ws(w, false, n, nrhs, a, lda, b, ldb, x, ldx, &o, out, s);
+    w.split_kept = false;
+    BOLA_TRY(st);
     if (out) out->factor_info = finfo;
     return 0;
   }
@@ -1177,7 +1203,10 @@ int dgesv_mixed_ws(Workspace &w, bool chol, int64_t n, int64_t nrhs, const doubl
     o3.factor_kind = 3;
     o3.escalate = 0;
     bola_mixed_info i3;
-    BOLA_TRY(dgesv_mixed_ws(w, chol, n, nrhs, a, lda, b, ldb, x, ldx, &o3, &i3, s));
+    w.split_kept = true;
+    const int st = dgesv_mixed_ws(w, chol, n, nrhs, a, lda, b, ldb, x, ldx, &o3, &i3, s);
+    w.split_kept = false;
+    BOLA_TRY(st);
     i3.iterations += info_out.iterations;
     i3.gmres_iterations += info_out.gmres_iterations;
     if (i3.path != 2) i3.path = 3;
