@@ -180,7 +180,7 @@ __device__ __forceinline__ void write_slices_row(const double (&v)[64], int64_t 
 // somewhere in the tile) are updated: the trailing update of a Cholesky.
 int oz_update(cudaStream_t s, int64_t m, int64_t n, const CUtensorMap &A, const CUtensorMap &B, int64_t capA,
               int64_t capB, const int32_t *eA, const int32_t *eB, double *W, int64_t ldw, int32_t *err,
-              int64_t boff = 0, const int32_t *abort = nullptr, bool lower = false);
+              int64_t boff = 0, const int32_t *abort = nullptr, bool lower = false, bool pdl = false);
 
 // W(m x n, column-major, ld ldw) -= A * B^T on tcgen05 (kind 0 bf16, 1 tf32,
 // 2 3xTF32 with the lo maps); *err is set non-zero if a bounded wait expired.
@@ -188,7 +188,7 @@ int oz_update(cudaStream_t s, int64_t m, int64_t n, const CUtensorMap &A, const 
 // lower: only tiles reaching the diagonal or below it (as oz_update).
 int tc_update(cudaStream_t s, int kind, int64_t m, int64_t n, const CUtensorMap &A, const CUtensorMap &B,
               const CUtensorMap &Alo, const CUtensorMap &Blo, float *W, int64_t ldw, int32_t *err, int64_t boff = 0,
-              const int32_t *abort = nullptr, bool lower = false);
+              const int32_t *abort = nullptr, bool lower = false, bool pdl = false);
 
 // The give-up test of the low-precision factorisations, from the spread
 // max|u_kk| / min|u_kk| over the first `done` of `total` columns: the spread
@@ -204,6 +204,29 @@ __device__ __forceinline__ bool give_up_now(double spread, double give_up, int64
   if (!(spread < give_up)) return true;
   return 4 * done >= total && spread > 1.0 && log(spread) * ((double)total / (double)done) > log(100.0 * give_up);
 }
+
+// Launch configuration of a factorisation step's kernel; pdl: a programmatic
+// dependent of the previous kernel on the stream (the kernel calls
+// sm100::grid_dependency_wait() before it reads what that kernel wrote), so
+// the step's kernels follow each other without the launch gap.
+struct StepLaunch {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[2];
+  StepLaunch(dim3 grid, dim3 block, size_t smem, cudaStream_t s, bool pdl) {
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = at;
+    cfg.numAttrs = 0;
+    if (pdl) add_pdl();
+  }
+  void add_pdl() {
+    at[cfg.numAttrs].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[cfg.numAttrs].val.programmaticStreamSerializationAllowed = 1;
+    ++cfg.numAttrs;
+  }
+};
 
 // A kernel of an abandoned factorisation returns at once: *abort is read by
 // one thread and the decision shared, so a CTA's barriers stay uniform even

@@ -116,6 +116,7 @@ oz_update_pipe(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
                int64_t capB, int64_t boff, int64_t m, int64_t n, const int32_t *__restrict__ eA,
                const int32_t *__restrict__ eB, double *__restrict__ W, int64_t ldw, int tpc, int32_t *err,
                const int32_t *abort, int lower) {
+  sm100::grid_dependency_wait();
   if (abandoned(abort)) return;
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t a_full, a_empty, b_full[2], b_empty[2], acc_full[DMAX + 1], acc_empty[DMAX + 1];
@@ -323,7 +324,7 @@ __global__ void oz_split_rows(int64_t rows, const double *__restrict__ X, int64_
 
 int oz_update(cudaStream_t s, int64_t m, int64_t n, const CUtensorMap &A, const CUtensorMap &B, int64_t capA,
               int64_t capB, const int32_t *eA, const int32_t *eB, double *W, int64_t ldw, int32_t *err, int64_t boff,
-              const int32_t *abort, bool lower) {
+              const int32_t *abort, bool lower, bool pdl) {
   if (m <= 0 || n <= 0) return 0;
   static bool attr = false;
   if (!attr) {
@@ -336,8 +337,9 @@ int oz_update(cudaStream_t s, int64_t m, int64_t n, const CUtensorMap &A, const 
   const int tpc = (int)imax(1, imin(8, tiles / (2 * (int64_t)num_sms())));
   const unsigned grid = (unsigned)cdiv(tiles, tpc);
   ProfScope prof(s, "oz_update", 2.0 * (double)m * n * OK * NPAIRS, 16.0 * (double)m * n);
-  oz_update_pipe<<<grid, ZTHREADS, ZSMEM, s>>>(A, B, capA, capB, boff, m, n, eA, eB, W, ldw, tpc, err, abort,
-                                               lower ? 1 : 0);
+  StepLaunch L(dim3(grid), dim3(ZTHREADS), ZSMEM, s, pdl);
+  BOLA_TRY_CUDA(cudaLaunchKernelEx(&L.cfg, oz_update_pipe, A, B, capA, capB, boff, m, n, eA, eB, W, ldw, tpc, err,
+                                   abort, lower ? 1 : 0));
   BOLA_CHECK_LAUNCH();
   return 0;
 }

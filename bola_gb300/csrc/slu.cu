@@ -272,6 +272,7 @@ __global__ void __launch_bounds__(TPT, 1)
 tpanel_kernel(G *W, int64_t ldw, int64_t mp, int jb, int32_t *ipiv, int32_t col0, int32_t *info, int64_t R,
               int32_t *plan, uint64_t *track, double give_up, int32_t *err, int32_t *winout, G *sel) {
   constexpr bool SEL = std::is_same<G, double>::value;
+  sm100::grid_dependency_wait();
   cg::cluster_group cluster = cg::this_cluster();
   // an abandoned factorisation (flag set by an earlier panel on this stream,
   // so every CTA reads the same value): identity pivots keep ipiv valid
@@ -672,13 +673,15 @@ int launch_tpanel(cudaStream_t s, G *W, int64_t ldw, int64_t mp, int jb, int32_t
   cfg.blockDim = dim3(TPT, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
-  cudaLaunchAttribute at[1];
+  cudaLaunchAttribute at[2];  // the cluster; a programmatic dependent of the previous step's kernel
   at[0].id = cudaLaunchAttributeClusterDimension;
   at[0].val.clusterDim.x = (unsigned)C;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
+  at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[1].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = 2;
   ProfScope prof(s, std::is_same<G, double>::value ? "tselect64" : "tpanel", (double)mp * jb * jb,
                  8.0 * (double)mp * jb);
   BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, tpanel_kernel<G>, W, ldw, mp, jb, ipiv, col0, info, R, plan, track,
@@ -750,6 +753,7 @@ __global__ void __launch_bounds__(PL_THREADS, 1)
 panel_lu64(double *Wp, int64_t ldw, int64_t mp, int jb, int32_t col0, const int32_t *win_in, const double *sel,
            int32_t *plan, int32_t *ipiv, int32_t *info, uint64_t *track, double give_up, int32_t *err, void *aop,
            int32_t *aexp, int64_t cap) {
+  sm100::grid_dependency_wait();
   const int nA = (int)gridDim.x - 1;
   const bool top = (int)blockIdx.x == nA;
   // an abandoned factorisation (flag set by an earlier panel on this stream):
@@ -1016,6 +1020,7 @@ __global__ void __launch_bounds__(256)
 sswap_trsm(T *W, int64_t ldw, int64_t n, int64_t j, int jb, const int32_t *plan, int kind, void *bop,
            float *bop_lo, int32_t *bexp, int64_t cap, const int32_t *abort, int ncta, void *aop, float *aop_lo,
            int32_t *perm) {
+  sm100::grid_dependency_wait();
   if (abort != nullptr && *(volatile const int32_t *)abort != 0) return;  // set before this launch (same stream)
   __shared__ int32_t rows[2 * SNB], src[2 * SNB];
   __shared__ __align__(16) T L[SNB * SNB];
@@ -1302,9 +1307,10 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
           attr = true;
         }
         const unsigned nA = mp > PL_SLOTS ? (unsigned)cdiv(mp - PL_SLOTS, PL_SLOTS) : 0u;
-        panel_lu64<<<nA + 1, PL_THREADS, PL_SMEM, lu.sp>>>(Wp, ldw, mp, jb, (int32_t)j, win, lu.sel, plan_k, ipiv + j,
-                                                          info, track, give_up, lu.err, upd ? lu.aop[buf] : nullptr,
-                                                          lu.ea[buf], lu.cap_n);
+        StepLaunch L(dim3(nA + 1), dim3(PL_THREADS), PL_SMEM, lu.sp, true);
+        BOLA_TRY_CUDA(cudaLaunchKernelEx(&L.cfg, panel_lu64, Wp, ldw, mp, jb, (int32_t)j, (const int32_t *)win,
+                                         (const double *)lu.sel, plan_k, ipiv + j, info, track, give_up, lu.err,
+                                         upd ? lu.aop[buf] : nullptr, lu.ea[buf], lu.cap_n));
       }
       BOLA_CHECK_LAUNCH();
     } else
@@ -1319,23 +1325,28 @@ static int factor_lookahead(MixedLU &lu, cudaStream_t s, T *W, int64_t ldw, int3
       // the update's A operand)
       const int ncta = (int)imax(1, cdiv(n - j - jb, 8));
       const int nop = (!fp64 && upd) ? (int)cdiv(mp - jb, SNB) : 0;
-      sswap_trsm<T><<<(unsigned)(ncta + nop), 256, 0, lu.sp>>>(
-          W, ldw, n, j, jb, plan_k, lu.kind, upd ? lu.bop : nullptr, fp64 ? nullptr : lu.bop_lo,
-          fp64 ? lu.eb : nullptr, lu.cap_n, abort, ncta, fp64 ? nullptr : lu.aop[buf], fp64 ? nullptr : lu.aop_lo[buf],
-          perm);
+      StepLaunch L(dim3((unsigned)(ncta + nop)), dim3(256), 0, lu.sp, true);
+      BOLA_TRY_CUDA(cudaLaunchKernelEx(
+          &L.cfg, sswap_trsm<T>, W, ldw, n, (int64_t)j, jb, (const int32_t *)plan_k, lu.kind,
+          upd ? (void *)lu.bop : nullptr, fp64 ? (float *)nullptr : lu.bop_lo, fp64 ? lu.eb : (int32_t *)nullptr,
+          lu.cap_n, abort, ncta, fp64 ? (void *)nullptr : lu.aop[buf], fp64 ? (float *)nullptr : lu.aop_lo[buf],
+          perm));
       BOLA_CHECK_LAUNCH();
     }
     if (!upd) continue;
     const int64_t m2 = mp - jb, n2 = n - j - jb;
     const int64_t nb_next = imin((int64_t)panel_width(fp64, n, j + jb), n2);
     T *W22 = W + (j + jb) + (j + jb) * ldw;
+    // (the next panel's columns follow the swap kernel on sp as its
+    // programmatic dependent; the rest go to su)
     auto update = [&](cudaStream_t st, int64_t cols, int64_t boff) -> int {
+      const bool pdl = st == lu.sp;
       if constexpr (fp64)
         return oz_update(st, m2, cols, lu.mapA[buf], lu.mapB, lu.cap_n, lu.cap_n, lu.ea[buf], lu.eb,
-                         W22 + boff * ldw, ldw, lu.err, boff, abort);
+                         W22 + boff * ldw, ldw, lu.err, boff, abort, false, pdl);
       else
         return tc_update(st, lu.kind, m2, cols, lu.mapA[buf], lu.mapB, lu.mapAlo[buf], lu.mapBlo,
-                         W22 + boff * ldw, ldw, lu.err, boff, abort);
+                         W22 + boff * ldw, ldw, lu.err, boff, abort, false, pdl);
     };
     BOLA_TRY(update(lu.sp, nb_next, 0));  // the next panel's columns
     if (n2 > nb_next) {

@@ -209,6 +209,7 @@ tc_update_pipe(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
                int64_t n, int64_t boff, int tpc, int32_t *err, const int32_t *abort, int lower, float *W,
                int64_t ldw) {
   using Cfg = PCfg<KIND, NPASS>;
+  sm100::grid_dependency_wait();
   if (abandoned(abort)) return;
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t a_full, a_empty, b_full[2], b_empty[2], w_full[2], w_empty[2], acc_full[2], acc_empty[2];
@@ -455,7 +456,7 @@ int make_fp32_tile_map(CUtensorMap *map, const float *ptr, int64_t rows, int64_t
 
 int tc_update(cudaStream_t s, int kind, int64_t m, int64_t n, const CUtensorMap &A, const CUtensorMap &B,
               const CUtensorMap &Alo, const CUtensorMap &Blo, float *W, int64_t ldw, int32_t *err, int64_t boff,
-              const int32_t *abort, bool lower) {
+              const int32_t *abort, bool lower, bool pdl) {
   if (m <= 0 || n <= 0) return 0;
   ProfScope prof(s, "tc_update", 2.0 * (double)m * n * KDIM * (kind == 2 ? 3 : 1), 8.0 * (double)m * n);
   if ((ldw & 3) == 0 && (reinterpret_cast<uintptr_t>(W) & 15) == 0 && m >= 4) {
@@ -479,8 +480,9 @@ int tc_update(cudaStream_t s, int kind, int64_t m, int64_t n, const CUtensorMap 
           cudaFuncSetAttribute(tc_update_pipe<KIND, NPASS>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM)); \
       attr = true;                                                                                              \
     }                                                                                                           \
-    tc_update_pipe<KIND, NPASS><<<grid, PTHREADS, Cfg::SMEM, s>>>(A, B, Alo, Blo, mapW, mapWs, m, n, boff, tpc, err, \
-                                                                  abort, lower ? 1 : 0, W, ldw);                \
+    StepLaunch L(dim3(grid), dim3(PTHREADS), Cfg::SMEM, s, pdl);                                                \
+    BOLA_TRY_CUDA(cudaLaunchKernelEx(&L.cfg, tc_update_pipe<KIND, NPASS>, A, B, Alo, Blo, mapW, mapWs, m, n, boff,  \
+                                     tpc, err, abort, lower ? 1 : 0, W, ldw));                                  \
   } while (0)
     if (kind == 0) BOLA_TCP(0, 1);
     else if (kind == 1) BOLA_TCP(1, 1);
