@@ -20,8 +20,13 @@
 #include <mutex>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 #include "mixed.cuh"
+#include "sm100.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace bola {
 namespace {
@@ -280,20 +285,46 @@ __device__ __forceinline__ void st_release(int32_t *p, int v) {
 
 // Blocked triangular solve with nrhs <= 32 right-hand sides (n x nrhs, ld n)
 // in ONE launch, as a dataflow over the 64-row blocks.  LOWER: unit-lower L,
-// blocks solved top to bottom; else U, bottom to top.  Each CTA takes the
-// next block in solve order from an atomic ticket, so it only ever waits for
-// blocks held by CTAs that started before it (no co-residency assumption).
+// blocks solved top to bottom; else U, bottom to top.  CTAs run in clusters
+// of TCL: each cluster takes the next TCL blocks in solve order from an
+// atomic ticket, so it only ever waits for blocks held by clusters that
+// started before it (no co-residency assumption beyond the cluster's own).
 // A solved block is published as 64-bit words (value bits, launch epoch):
 // a reader spins on the words themselves, so one round trip to L2 both
 // signals and delivers a block, and a writer needs no release fence (each
-// word is written atomically and carries its own epoch).  The CTA folds in
-// the blocks solved before its predecessor as they appear,
-//   acc -= T[blk, k] x_k              (the tile of W is loaded before the wait)
-// applies the inverse of its diagonal block, c = Dinv acc, and then needs
-// only one 64 x 64 product once its predecessor p is published:
-//   x_blk = c - M x_p,   M = Dinv T[blk, p]   (precomputed per factorisation).
-// Waits are bounded: on expiry *err is set (the host fails the solve) and the
-// CTA goes on, so that every later wait still ends.
+// word is written atomically and carries its own epoch).  Inside a cluster
+// the block also goes straight to the shared memory of the next TNP CTAs
+// (one bulk copy each, completing on the receiver's mbarrier), so that a
+// link between neighbours costs a shared-memory push, not an L2 round trip.
+// Block blk at position t in solve order folds in the blocks solved before
+// its last TNP predecessors as they appear,
+//   acc -= T[blk, k] x_k              (tile and words of the next block in
+//                                      flight during this block's product)
+// and then, with c = Dinv acc formed before any predecessor is needed,
+//   x_blk = c - sum_{d=1..TNP} C_d x_{t-d},   C_d = Dinv T[blk, t-d]
+// (C_d precomputed per factorisation).  The chain between consecutive
+// blocks is then one 64 x 64 product and a push; a block's words on L2 are
+// needed TNP links after they are written.  Waits are bounded: on expiry
+// *err is set (the host fails the solve) and the CTA goes on, so that every
+// later wait still ends.
+constexpr int TCL = 8;  // blocks (CTAs) per cluster of the FP32 solve
+constexpr int TNP = 3;  // predecessors coupled through C_d
+
+// bytes from this CTA's shared memory into another CTA's of the cluster,
+// completing on that CTA's mbarrier (dst and bar: cluster addresses)
+__device__ __forceinline__ void bulk_push_cluster(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "r"(sm100::smem_u32(src)), "r"(bytes), "r"(bar)
+      : "memory");
+}
+// bytes from global memory into this CTA's shared memory, completing on bar
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   sm100::smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(sm100::smem_u32(bar))
+               : "memory");
+}
 __device__ __forceinline__ unsigned long long ld_word(const unsigned long long *p) {
   unsigned long long v;
   asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
@@ -303,15 +334,17 @@ __device__ __forceinline__ void st_word(unsigned long long *p, unsigned long lon
   asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-// M[b] = Dinv_b T_b (column-major 64 x 64), T_b the block coupling block b
-// to its predecessor in solve order: L[b, b-1] (lower), U[b, b+1] (upper).
+// C_d[b] = Dinv_b T[b, k] (column-major 64 x 64), k the block d places
+// before b in solve order (d = blockIdx.y + 1): L[b, b - d] (lower),
+// U[b, b + d] (upper).  C holds C_d for all blocks at C + ((d-1) nb + b) 4096.
 template <bool LOWER>
 __global__ void __launch_bounds__(256)
-couple_blocks(int64_t n, const float *__restrict__ W, int64_t ldw, const float *__restrict__ Dinv, float *M) {
+couple_blocks(int64_t n, const float *__restrict__ W, int64_t ldw, const float *__restrict__ Dinv, float *C) {
   __shared__ float D[TB][TB + 1], T[TB][TB + 1];
   const int nb = (int)cdiv(n, TB);
-  const int b = blockIdx.x;
-  const int k = LOWER ? b - 1 : b + 1;
+  const int b = blockIdx.x, d = (int)blockIdx.y + 1;
+  float *outp = C + ((int64_t)(d - 1) * nb + b) * TB * TB;
+  const int k = LOWER ? b - d : b + d;
   if (k < 0 || k >= nb) return;
   const int64_t i0 = (int64_t)b * TB, k0 = (int64_t)k * TB;
   const int kb = (int)imin(TB, n - i0), kbk = (int)imin(TB, n - k0);
@@ -326,157 +359,237 @@ couple_blocks(int64_t n, const float *__restrict__ W, int64_t ldw, const float *
     float v = 0.f;
 #pragma unroll 16
     for (int q = 0; q < TB; ++q) v = fmaf(D[r][q], T[q][c], v);
-    M[(int64_t)b * TB * TB + e] = v;
+    outp[e] = v;
   }
 }
 
-// acc[c] (c < RH) -= sum_kk A[kk][r] X[kk][g RH + c]
+// acc[c] (c < RH) -= sum_kk A[kk][r] X[kk][g RH + c]: two partial sums (even
+// and odd kk) per output, so that each FMA chain is 32 long, not 64
 template <int RH>
-__device__ __forceinline__ void block_product(float (&acc)[RH], const float (*A)[TB + 4], const float (*X)[4 * RH],
-                                              int r, int g) {
+__device__ __forceinline__ void block_product(float (&acc)[RH], const float (*A)[TB], const float (*X)[4 * RH], int r,
+                                              int g) {
+  float p[2][RH];
+#pragma unroll
+  for (int c = 0; c < RH; ++c) p[0][c] = p[1][c] = 0.f;
 #pragma unroll 8
   for (int kk = 0; kk < TB; ++kk) {
     const float a = A[kk][r];
 #pragma unroll
     for (int c = 0; c < RH; c += 4) {
       const float4 x = *reinterpret_cast<const float4 *>(&X[kk][g * RH + c]);
-      acc[c] = fmaf(-a, x.x, acc[c]);
-      acc[c + 1] = fmaf(-a, x.y, acc[c + 1]);
-      acc[c + 2] = fmaf(-a, x.z, acc[c + 2]);
-      acc[c + 3] = fmaf(-a, x.w, acc[c + 3]);
+      float *q = p[kk & 1];
+      q[c] = fmaf(a, x.x, q[c]);
+      q[c + 1] = fmaf(a, x.y, q[c + 1]);
+      q[c + 2] = fmaf(a, x.z, q[c + 2]);
+      q[c + 3] = fmaf(a, x.w, q[c + 3]);
     }
   }
+#pragma unroll
+  for (int c = 0; c < RH; ++c) acc[c] -= p[0][c] + p[1][c];
 }
 
-// Spins until block k's words carry this launch's epoch, into X[kk][c].  A
-// thread's words are loaded together, and each pass polls again all of
-// those not yet published, together: one L2 round trip per pass, not one
-// per word.
+// A thread's share of one published block's words: loaded together, then
+// polled again together (all those not yet published) until every one
+// carries this launch's epoch: one L2 round trip per pass, not one per word.
 template <int RH>
-__device__ __forceinline__ void take_block(const unsigned long long *xw, int64_t n, int nrhs, int64_t k0, int kbk,
-                                           uint32_t epoch, float (*X)[4 * RH], int32_t *err) {
-  constexpr int PW = TB * 4 * RH / 256;  // words per thread
+struct BlockWords {
+  static constexpr int PW = TB * 4 * RH / 256;  // words per thread
   unsigned long long w[PW];
-  bool need[PW];
-#pragma unroll
-  for (int u = 0; u < PW; ++u) {
-    const int e = threadIdx.x + 256 * u, kk = e % TB, c = e / TB;
-    need[u] = kk < kbk && c < nrhs;
-    w[u] = need[u] ? ld_word(xw + (k0 + kk) + (int64_t)c * n) : 0ull;
+  __device__ __forceinline__ bool need(int u, int kbk, int nrhs) const {
+    const int e = threadIdx.x + 256 * u;
+    return e % TB < kbk && e / TB < nrhs;
   }
-  for (int polls = 0;; ++polls) {
-    bool done = true;
+  __device__ __forceinline__ void load(const unsigned long long *xw, int64_t n, int nrhs, int64_t k0, int kbk) {
 #pragma unroll
-    for (int u = 0; u < PW; ++u) done = done && (!need[u] || (uint32_t)(w[u] >> 32) == epoch);
-    if (done) break;
-    if (polls >= (1 << 20)) {
-      atomicExch(err, 3);
-      break;
+    for (int u = 0; u < PW; ++u) {
+      const int e = threadIdx.x + 256 * u, kk = e % TB, c = e / TB;
+      w[u] = need(u, kbk, nrhs) ? ld_word(xw + (k0 + kk) + (int64_t)c * n) : 0ull;
+    }
+  }
+  // spins until the words carry epoch, then writes them to X[kk][c]
+  __device__ __forceinline__ void take(const unsigned long long *xw, int64_t n, int nrhs, int64_t k0, int kbk,
+                                       uint32_t epoch, float (*X)[4 * RH], int32_t *err) {
+    for (int polls = 0;; ++polls) {
+      bool done = true;
+#pragma unroll
+      for (int u = 0; u < PW; ++u) done = done && (!need(u, kbk, nrhs) || (uint32_t)(w[u] >> 32) == epoch);
+      if (done) break;
+      if (polls >= (1 << 20)) {
+        atomicExch(err, 3);
+        break;
+      }
+#pragma unroll
+      for (int u = 0; u < PW; ++u) {
+        const int e = threadIdx.x + 256 * u, kk = e % TB, c = e / TB;
+        if (need(u, kbk, nrhs) && (uint32_t)(w[u] >> 32) != epoch) w[u] = ld_word(xw + (k0 + kk) + (int64_t)c * n);
+      }
     }
 #pragma unroll
     for (int u = 0; u < PW; ++u) {
       const int e = threadIdx.x + 256 * u, kk = e % TB, c = e / TB;
-      if (need[u] && (uint32_t)(w[u] >> 32) != epoch) w[u] = ld_word(xw + (k0 + kk) + (int64_t)c * n);
+      X[kk][c] = need(u, kbk, nrhs) ? __uint_as_float((uint32_t)w[u]) : 0.f;
     }
   }
-#pragma unroll
-  for (int u = 0; u < PW; ++u) {
-    const int e = threadIdx.x + 256 * u, kk = e % TB, c = e / TB;
-    X[kk][c] = need[u] ? __uint_as_float((uint32_t)w[u]) : 0.f;
-  }
+};
+
+// dynamic shared memory of trsv_words: the operands Dinv, C_1..C_TNP; two
+// fold tiles; two fold blocks; the TNP pushed predecessors
+template <int RH>
+constexpr size_t trsv_words_smem() {
+  return sizeof(float) * ((size_t)(TNP + 1) * TB * TB + 2 * TB * TB + (2 + TNP) * TB * 4 * RH);
 }
 
 template <bool LOWER, int RH>
 __global__ void __launch_bounds__(256)
 trsv_words(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, const float *__restrict__ Dinv,
-           const float *__restrict__ M, const float *__restrict__ y, float *out, unsigned long long *xw,
+           const float *__restrict__ C, const float *__restrict__ y, float *out, unsigned long long *xw,
            int32_t *ticket, uint32_t epoch, int32_t *err) {
-  __shared__ __align__(16) float A[TB][TB + 4];   // a 64 x 64 operand, A[kk][r] = operand(r, kk)
-  __shared__ __align__(16) float X[TB][4 * RH];   // X[kk][c]
+  extern __shared__ __align__(128) float tsm[];
+  using Tile = float[TB][TB];      // Tile[kk][r] = operand(r, kk), the column-major 64 x 64 block
+  using Blk = float[TB][4 * RH];   // Blk[kk][c]
+  Tile *Op = reinterpret_cast<Tile *>(tsm);          // Op[0] = Dinv, Op[d] = C_d
+  Tile *A = Op + TNP + 1;                            // fold tiles (alternating)
+  Blk *X = reinterpret_cast<Blk *>(A + 2);           // fold blocks (alternating); X[0] later stages this block
+  Blk *Xp = X + 2;                                   // Xp[d-1]: the block d before, pushed by its CTA
+  __shared__ __align__(8) uint64_t xbar[TNP];        // complete when those pushes have landed
+  __shared__ __align__(8) uint64_t obar;             // complete when the operands have landed
   __shared__ int sb;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
   const int tid = threadIdx.x;
   const int nb = (int)cdiv(n, TB);
-  if (tid == 0) sb = atomicAdd(ticket, 1);
+  constexpr uint32_t XBYTES = sizeof(Blk), OBYTES = sizeof(Tile);
+  if (tid == 0) {
+#pragma unroll
+    for (int d = 0; d < TNP; ++d) sm100::mbar_init(&xbar[d], 1);
+    sm100::mbar_init(&obar, 1);
+    sm100::fence_mbar_init();
+    if (rank == 0) sb = atomicAdd(ticket, 1);
+  }
+  cluster.sync();  // every CTA's barriers initialised; the cluster's ticket taken
+  if (tid == 0 && rank != 0) sb = *cluster.map_shared_rank(&sb, 0);
   __syncthreads();
-  const int t = sb;
+  const int t = sb * TCL + rank;  // position in solve order
+  const bool live = t < nb;
   const int b = LOWER ? t : nb - 1 - t;
+  if (tid == 0 && live) {
+    // the pushes from the CTAs before, inside the cluster; the operands
+#pragma unroll
+    for (int d = 1; d <= TNP; ++d)
+      if (rank >= d) sm100::mbar_arrive_expect_tx(&xbar[d - 1], XBYTES);
+    const int nops = 1 + (t < TNP ? t : TNP);
+    sm100::mbar_arrive_expect_tx(&obar, OBYTES * nops);
+    bulk_load(Op[0], Dinv + (int64_t)b * TB * TB, OBYTES, &obar);
+    for (int d = 1; d < nops; ++d) bulk_load(Op[d], C + ((int64_t)(d - 1) * nb + b) * TB * TB, OBYTES, &obar);
+  }
   const int64_t i0 = (int64_t)b * TB;
-  const int kb = (int)imin(TB, n - i0);
+  const int kb = live ? (int)imin(TB, n - i0) : 0;
   const int r = tid & (TB - 1), g = tid >> 6;  // row of the block, right-hand-side group (4 groups of RH)
-  float acc[RH];
-#pragma unroll
-  for (int c = 0; c < RH; ++c) {
-    const int cc = g * RH + c;
-    acc[c] = (cc < nrhs && r < kb) ? y[i0 + r + (int64_t)cc * n] : 0.f;
-  }
-  constexpr int PER = TB * TB / 256;
-  // the blocks solved before the predecessor
-  for (int sidx = 0; sidx + 1 < t; ++sidx) {
-    const int k = LOWER ? sidx : nb - 1 - sidx;
-    const int64_t k0 = (int64_t)k * TB;
-    const int kbk = (int)imin(TB, n - k0);
-    float lv[PER];
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      const int e = tid + 256 * q;
-      const int rr = e % TB, kk = e / TB;
-      lv[q] = (rr < kb && kk < kbk) ? W[(i0 + rr) + (k0 + kk) * ldw] : 0.f;
-    }
-    take_block<RH>(xw, n, nrhs, k0, kbk, epoch, X, err);
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      const int e = tid + 256 * q;
-      A[e / TB][e % TB] = lv[q];
-    }
-    __syncthreads();
-    block_product<RH>(acc, A, X, r, g);
-    __syncthreads();
-  }
-  // c = Dinv acc: acc into X as a 64 x (4 RH) operand, Dinv into A
-#pragma unroll
-  for (int c = 0; c < RH; ++c) X[r][g * RH + c] = acc[c];
-  const float *D = Dinv + (int64_t)b * TB * TB;
-#pragma unroll
-  for (int q = 0; q < PER; ++q) {
-    const int e = tid + 256 * q;
-    A[e / TB][e % TB] = D[e];
-  }
-  __syncthreads();
-  float cv[RH];
-#pragma unroll
-  for (int c = 0; c < RH; ++c) cv[c] = 0.f;
-  block_product<RH>(cv, A, X, r, g);  // cv = -Dinv acc
-  __syncthreads();
-  if (t > 0) {
-    // the predecessor: x = c - M x_p
-    const int p = LOWER ? b - 1 : b + 1;
-    const int64_t p0 = (int64_t)p * TB;
-    const int kbp = (int)imin(TB, n - p0);
-    const float *Mb = M + (int64_t)b * TB * TB;
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      const int e = tid + 256 * q;
-      A[e / TB][e % TB] = Mb[e];
-    }
-    take_block<RH>(xw, n, nrhs, p0, kbp, epoch, X, err);
-    __syncthreads();
-#pragma unroll
-    for (int c = 0; c < RH; ++c) cv[c] = -cv[c];
-    block_product<RH>(cv, A, X, r, g);
-  } else {
-#pragma unroll
-    for (int c = 0; c < RH; ++c) cv[c] = -cv[c];
-  }
-  if (r < kb) {
+  if (live) {
+    float acc[RH];
 #pragma unroll
     for (int c = 0; c < RH; ++c) {
       const int cc = g * RH + c;
-      if (cc >= nrhs) continue;
-      const int64_t idx = i0 + r + (int64_t)cc * n;
-      out[idx] = cv[c];
-      st_word(xw + idx, ((unsigned long long)epoch << 32) | __float_as_uint(cv[c]));
+      acc[c] = (cc < nrhs && r < kb) ? y[i0 + r + (int64_t)cc * n] : 0.f;
+    }
+    constexpr int PER = TB * TB / 256;
+    // the blocks solved before the last TNP predecessors; block sidx + 1's
+    // tile and words are requested before block sidx's product
+    const int nf = t - TNP;
+    auto tile_load = [&](float (&lv)[PER], int sidx) {
+      const int64_t k0 = (int64_t)(LOWER ? sidx : nb - 1 - sidx) * TB;
+      const int kbk = (int)imin(TB, n - k0);
+#pragma unroll
+      for (int q = 0; q < PER; ++q) {
+        const int e = tid + 256 * q;
+        const int rr = e % TB, kk = e / TB;
+        lv[q] = (rr < kb && kk < kbk) ? W[(i0 + rr) + (k0 + kk) * ldw] : 0.f;
+      }
+    };
+    float lv[PER];
+    BlockWords<RH> wd;
+    if (nf > 0) {
+      tile_load(lv, 0);
+      const int64_t k0 = (int64_t)(LOWER ? 0 : nb - 1) * TB;
+      wd.load(xw, n, nrhs, k0, (int)imin(TB, n - k0));
+    }
+    for (int sidx = 0; sidx < nf; ++sidx) {
+      const int64_t k0 = (int64_t)(LOWER ? sidx : nb - 1 - sidx) * TB;
+      const int kbk = (int)imin(TB, n - k0);
+      const int h = sidx & 1;
+      wd.take(xw, n, nrhs, k0, kbk, epoch, X[h], err);
+#pragma unroll
+      for (int q = 0; q < PER; ++q) {
+        const int e = tid + 256 * q;
+        A[h][e / TB][e % TB] = lv[q];
+      }
+      if (sidx + 1 < nf) {
+        tile_load(lv, sidx + 1);
+        const int64_t k1 = (int64_t)(LOWER ? sidx + 1 : nb - 2 - sidx) * TB;
+        wd.load(xw, n, nrhs, k1, (int)imin(TB, n - k1));
+      }
+      __syncthreads();  // (also: every thread is past the product that last read A[h], X[h])
+      block_product<RH>(acc, A[h], X[h], r, g);
+    }
+    // c = Dinv acc: acc into X[0] as a 64 x (4 RH) operand
+    __syncthreads();  // every thread is past the last fold's product
+#pragma unroll
+    for (int c = 0; c < RH; ++c) X[0][r][g * RH + c] = acc[c];
+    if (!__syncthreads_and(sm100::bounded_wait(&obar, 0u)) && tid == 0) atomicExch(err, 3);
+    float cv[RH];
+#pragma unroll
+    for (int c = 0; c < RH; ++c) cv[c] = 0.f;
+    block_product<RH>(cv, Op[0], X[0], r, g);  // cv = -Dinv acc
+#pragma unroll
+    for (int c = 0; c < RH; ++c) cv[c] = -cv[c];
+    // the TNP predecessors, furthest first: x = c - sum_d C_d x_{t-d}, each
+    // from the push of its CTA (same cluster) or from its published words
+    // (an earlier cluster), into X[1] (the last fold read X[(nf-1)&1] and
+    // every thread is past that)
+#pragma unroll
+    for (int d = TNP; d >= 1; --d) {
+      if (t < d) continue;
+      if (rank >= d) {
+        if (!__syncthreads_and(sm100::bounded_wait(&xbar[d - 1], 0u)) && tid == 0) atomicExch(err, 3);
+        block_product<RH>(cv, Op[d], Xp[d - 1], r, g);
+      } else {
+        const int64_t p0 = (int64_t)(LOWER ? b - d : b + d) * TB;
+        const int kbp = (int)imin(TB, n - p0);
+        __syncthreads();  // every thread is past the product that last read X[1]
+        wd.load(xw, n, nrhs, p0, kbp);
+        wd.take(xw, n, nrhs, p0, kbp, epoch, X[1], err);
+        __syncthreads();
+        block_product<RH>(cv, Op[d], X[1], r, g);
+      }
+    }
+    if (r < kb) {
+#pragma unroll
+      for (int c = 0; c < RH; ++c) {
+        const int cc = g * RH + c;
+        if (cc >= nrhs) continue;
+        const int64_t idx = i0 + r + (int64_t)cc * n;
+        st_word(xw + idx, ((unsigned long long)epoch << 32) | __float_as_uint(cv[c]));
+        out[idx] = cv[c];
+      }
+    }
+    if (rank + 1 < TCL && t + 1 < nb) {  // to the next TNP CTAs of the cluster (their Xp[d-1])
+      __syncthreads();  // every thread is past the Dinv product, the last to read X[0]
+#pragma unroll
+      for (int c = 0; c < RH; ++c) X[0][r][g * RH + c] = cv[c];
+      sm100::fence_proxy_async_smem();  // the staged block, visible to the bulk copies
+      __syncthreads();
+      if (tid == 0) {
+#pragma unroll
+        for (int d = 1; d <= TNP; ++d)
+          if (rank + d < TCL && t + d < nb)
+            bulk_push_cluster(sm100::cluster_addr(&Xp[d - 1][0][0], rank + d), &X[0][0][0], XBYTES,
+                              sm100::cluster_addr(&xbar[d - 1], rank + d));
+        sm100::bulk_commit();
+        sm100::bulk_wait_read0();
+      }
     }
   }
+  cluster.sync();  // no CTA leaves while one before may still push into it
 }
 
 // The FP64 form of the same dataflow, for the FP64-storage factor.  GB300's
@@ -547,7 +660,8 @@ struct TrsvSync {
   int32_t *flags = nullptr, *ticket = nullptr, *err = nullptr;
   int32_t epoch = 0;
   unsigned long long *xw = nullptr;  // published blocks of the FP32 solves (value, epoch)
-  const float *Ml = nullptr, *Mu = nullptr;  // Dinv times the coupling block, per 64-row block
+  // Dinv times the blocks 1..TNP places back in solve order, per 64-row block (lower, upper factor)
+  const float *Cl = nullptr, *Cu = nullptr;
 };
 
 // y (right-hand sides) -> out (solution); y is not modified.
@@ -572,9 +686,30 @@ int trsv(cudaStream_t s, bool lower, int64_t n, int nrhs, const float *W, int64_
   const unsigned nb = (unsigned)cdiv(n, TB);
   const uint32_t epoch = (uint32_t)++sync.epoch;
   BOLA_TRY_CUDA(cudaMemsetAsync(sync.ticket, 0, sizeof(int32_t), s));
-  const float *M = lower ? sync.Ml : sync.Mu;
-#define BOLA_TRSV(LW, RH) \
-  trsv_words<LW, RH><<<nb, 256, 0, s>>>(n, nrhs, W, ldw, Dinv, M, y, out, sync.xw, sync.ticket, epoch, sync.err)
+  const float *C = lower ? sync.Cl : sync.Cu;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(cdiv(nb, TCL) * TCL));
+  cfg.blockDim = dim3(256);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = TCL;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+#define BOLA_TRSV(LW, RH)                                                                                    \
+  do {                                                                                                       \
+    static bool attr_set = false;                                                                            \
+    if (!attr_set) {                                                                                         \
+      BOLA_TRY_CUDA(cudaFuncSetAttribute(trsv_words<LW, RH>, cudaFuncAttributeMaxDynamicSharedMemorySize,    \
+                                         (int)trsv_words_smem<RH>()));                                       \
+      attr_set = true;                                                                                       \
+    }                                                                                                        \
+    cfg.dynamicSmemBytes = trsv_words_smem<RH>();                                                            \
+    BOLA_TRY_CUDA(cudaLaunchKernelEx(&cfg, trsv_words<LW, RH>, n, nrhs, W, ldw, Dinv, C, y, out, sync.xw,    \
+                                     sync.ticket, epoch, sync.err));                                         \
+  } while (0)
   if (nrhs <= 16) {
     if (lower) BOLA_TRSV(true, 4);
     else BOLA_TRSV(false, 4);
@@ -588,12 +723,12 @@ int trsv(cudaStream_t s, bool lower, int64_t n, int nrhs, const float *W, int64_
 }
 
 // Dinv times the coupling blocks of the FP32 factor's L and U (once per factorisation).
-int couple(cudaStream_t s, int64_t n, const float *W, int64_t ldw, const float *Dl, const float *Du, float *Ml,
-           float *Mu) {
-  ProfScope prof(s, "trsv_couple", 4.0 * (double)cdiv(n, TB) * TB * TB * TB, 0.0, 2);
+int couple(cudaStream_t s, int64_t n, const float *W, int64_t ldw, const float *Dl, const float *Du, float *Cl,
+           float *Cu) {
+  ProfScope prof(s, "trsv_couple", 2.0 * TNP * 2 * (double)cdiv(n, TB) * TB * TB * TB, 0.0, 2);
   const unsigned nb = (unsigned)cdiv(n, TB);
-  couple_blocks<true><<<nb, 256, 0, s>>>(n, W, ldw, Dl, Ml);
-  couple_blocks<false><<<nb, 256, 0, s>>>(n, W, ldw, Du, Mu);
+  couple_blocks<true><<<dim3(nb, TNP), 256, 0, s>>>(n, W, ldw, Dl, Cl);
+  couple_blocks<false><<<dim3(nb, TNP), 256, 0, s>>>(n, W, ldw, Du, Cu);
   BOLA_CHECK_LAUNCH();
   return 0;
 }
@@ -687,7 +822,7 @@ struct Workspace {
   bool split_kept = false;     // oz holds this call's A already (a solve handed on within one call)
   double *dscale = nullptr;    // its row scale D (W = D A D)
   void *dg = nullptr;          // scratch: the diagonal of L (8-byte elements)
-  float *Mc = nullptr;         // FP32 factors: Dinv times the coupling blocks, lower then upper
+  float *Mc = nullptr;         // FP32 factors: Dinv times the coupling blocks (M lower, M upper, N lower, N upper)
   TrsvSync ts;  // dataflow triangular solves
   MixedLU lu;
   OzMatrix oz;  // A's digit planes: the FP64-accurate products of the refinement
@@ -710,7 +845,7 @@ void ws_free(Workspace &w) {
   w.dg = nullptr;
   w.Mc = nullptr;
   w.ts.xw = nullptr;
-  w.ts.Ml = w.ts.Mu = nullptr;
+  w.ts.Cl = w.ts.Cu = nullptr;
   w.n = w.nrhs = w.bytes = 0;
 }
 
@@ -749,12 +884,12 @@ int ws_reserve(Workspace &w, int64_t n, int64_t nrhs, int kind, cudaStream_t s) 
     BOLA_TRY(alloc(&w.hn, sizeof(double) * MAXRHS));
     BOLA_TRY(alloc(&w.ts.flags, sizeof(int32_t) * cdiv(n, TB) * MAXRHS));
     BOLA_TRY(alloc(&w.ts.ticket, sizeof(int32_t) * 2));
-    BOLA_TRY(alloc(&w.Mc, sizeof(float) * 2 * cdiv(n, TB) * TB * TB));
+    BOLA_TRY(alloc(&w.Mc, sizeof(float) * 2 * TNP * cdiv(n, TB) * TB * TB));
     BOLA_TRY(alloc(&w.ts.xw, sizeof(unsigned long long) * n * MAXRHS));
     // the published words start from epoch 0, which no launch uses
     BOLA_TRY_CUDA(cudaMemset(w.ts.xw, 0, sizeof(unsigned long long) * n * MAXRHS));
-    w.ts.Ml = w.Mc;
-    w.ts.Mu = w.Mc + cdiv(n, TB) * TB * TB;
+    w.ts.Cl = w.Mc;
+    w.ts.Cu = w.Mc + TNP * cdiv(n, TB) * TB * TB;
     w.ts.err = w.ts.ticket + 1;
     BOLA_TRY_CUDA(cudaMemset(w.ts.flags, 0, sizeof(int32_t) * cdiv(n, TB) * MAXRHS));
     BOLA_TRY_CUDA(cudaMemset(w.ts.ticket, 0, sizeof(int32_t) * 2));
@@ -1102,7 +1237,7 @@ int dgesv_mixed_ws(Workspace &w, bool chol, int64_t n, int64_t nrhs, const doubl
     } else {
       diag_block_inverses<float><<<nb, TB, 0, s>>>(n, (const float *)w.W, n, (float *)w.Dl, (float *)w.Du);
       BOLA_TRY(couple(s, n, (const float *)w.W, n, (const float *)w.Dl, (const float *)w.Du,
-                      const_cast<float *>(w.ts.Ml), const_cast<float *>(w.ts.Mu)));
+                      const_cast<float *>(w.ts.Cl), const_cast<float *>(w.ts.Cu)));
       diag_extent<float><<<1, 1024, 0, s>>>(n, (const float *)w.W, n, w.norms + 5 * MAXRHS);
     }
   }
