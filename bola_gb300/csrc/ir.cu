@@ -294,8 +294,9 @@ __device__ __forceinline__ void st_release(int32_t *p, int v) {
 // signals and delivers a block, and a writer needs no release fence (each
 // word is written atomically and carries its own epoch).  Inside a cluster
 // the block also goes straight to the shared memory of the next TNP CTAs
-// (one bulk copy each, completing on the receiver's mbarrier), so that a
-// link between neighbours costs a shared-memory push, not an L2 round trip.
+// (asynchronous remote stores completing on the receiver's mbarrier), so
+// that a link between neighbours costs a shared-memory push, not an L2
+// round trip.
 // Block blk at position t in solve order folds in the blocks solved before
 // its last TNP predecessors as they appear,
 //   acc -= T[blk, k] x_k              (tile and words of the next block in
@@ -310,14 +311,6 @@ __device__ __forceinline__ void st_release(int32_t *p, int v) {
 constexpr int TCL = 8;  // blocks (CTAs) per cluster of the FP32 solve
 constexpr int TNP = 3;  // predecessors coupled through C_d
 
-// bytes from this CTA's shared memory into another CTA's of the cluster,
-// completing on that CTA's mbarrier (dst and bar: cluster addresses)
-__device__ __forceinline__ void bulk_push_cluster(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-      "r"(sm100::smem_u32(src)), "r"(bytes), "r"(bar)
-      : "memory");
-}
 // bytes from global memory into this CTA's shared memory, completing on bar
 __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
@@ -449,7 +442,7 @@ trsv_words(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, const 
   using Blk = float[TB][4 * RH];   // Blk[kk][c]
   Tile *Op = reinterpret_cast<Tile *>(tsm);          // Op[0] = Dinv, Op[d] = C_d
   Tile *A = Op + TNP + 1;                            // fold tiles (alternating)
-  Blk *X = reinterpret_cast<Blk *>(A + 2);           // fold blocks (alternating); X[0] later stages this block
+  Blk *X = reinterpret_cast<Blk *>(A + 2);           // fold blocks (alternating)
   Blk *Xp = X + 2;                                   // Xp[d-1]: the block d before, pushed by its CTA
   __shared__ __align__(8) uint64_t xbar[TNP];        // complete when those pushes have landed
   __shared__ __align__(8) uint64_t obar;             // complete when the operands have landed
@@ -562,6 +555,18 @@ trsv_words(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, const 
         block_product<RH>(cv, Op[d], X[1], r, g);
       }
     }
+    // to the next TNP CTAs of the cluster (their Xp[d-1]): each thread stores
+    // its row's values straight from registers (st.async, completing on the
+    // receiver's mbarrier); then the words, for the CTAs of later clusters
+#pragma unroll
+    for (int d = 1; d <= TNP; ++d) {
+      if (rank + d >= TCL || t + d >= nb) break;
+      const uint32_t bar = sm100::cluster_addr(&xbar[d - 1], rank + d);
+#pragma unroll
+      for (int c = 0; c < RH; c += 4)
+        sm100::st_async4(sm100::cluster_addr(&Xp[d - 1][r][g * RH + c], rank + d), __float_as_uint(cv[c]),
+                         __float_as_uint(cv[c + 1]), __float_as_uint(cv[c + 2]), __float_as_uint(cv[c + 3]), bar);
+    }
     if (r < kb) {
 #pragma unroll
       for (int c = 0; c < RH; ++c) {
@@ -570,22 +575,6 @@ trsv_words(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, const 
         const int64_t idx = i0 + r + (int64_t)cc * n;
         st_word(xw + idx, ((unsigned long long)epoch << 32) | __float_as_uint(cv[c]));
         out[idx] = cv[c];
-      }
-    }
-    if (rank + 1 < TCL && t + 1 < nb) {  // to the next TNP CTAs of the cluster (their Xp[d-1])
-      __syncthreads();  // every thread is past the Dinv product, the last to read X[0]
-#pragma unroll
-      for (int c = 0; c < RH; ++c) X[0][r][g * RH + c] = cv[c];
-      sm100::fence_proxy_async_smem();  // the staged block, visible to the bulk copies
-      __syncthreads();
-      if (tid == 0) {
-#pragma unroll
-        for (int d = 1; d <= TNP; ++d)
-          if (rank + d < TCL && t + d < nb)
-            bulk_push_cluster(sm100::cluster_addr(&Xp[d - 1][0][0], rank + d), &X[0][0][0], XBYTES,
-                              sm100::cluster_addr(&xbar[d - 1], rank + d));
-        sm100::bulk_commit();
-        sm100::bulk_wait_read0();
       }
     }
   }
@@ -704,6 +693,9 @@ int trsv(cudaStream_t s, bool lower, int64_t n, int nrhs, const float *W, int64_
     if (!attr_set) {                                                                                         \
       BOLA_TRY_CUDA(cudaFuncSetAttribute(trsv_words<LW, RH>, cudaFuncAttributeMaxDynamicSharedMemorySize,    \
                                          (int)trsv_words_smem<RH>()));                                       \
+      if (TCL > 8)                                                                                           \
+        BOLA_TRY_CUDA(                                                                                       \
+            cudaFuncSetAttribute(trsv_words<LW, RH>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));    \
       attr_set = true;                                                                                       \
     }                                                                                                        \
     cfg.dynamicSmemBytes = trsv_words_smem<RH>();                                                            \
