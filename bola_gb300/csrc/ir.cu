@@ -309,7 +309,7 @@ __device__ __forceinline__ void st_release(int32_t *p, int v) {
 // *err is set (the host fails the solve) and the CTA goes on, so that every
 // later wait still ends.
 constexpr int TCL = 8;  // blocks (CTAs) per cluster of the FP32 solve
-constexpr int TNP = 3;  // predecessors coupled through C_d
+constexpr int TNP = 6;  // predecessors coupled through C_d
 
 // bytes from global memory into this CTA's shared memory, completing on bar
 __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
@@ -356,48 +356,93 @@ couple_blocks(int64_t n, const float *__restrict__ W, int64_t ldw, const float *
   }
 }
 
-// acc[c] (c < RH) -= sum_kk A[kk][r] X[kk][g RH + c]: two partial sums (even
-// and odd kk) per output, so that each FMA chain is 32 long, not 64
+// acc[c] (c < RH) -= sum_kk A[kk][r] X[kk][g RH + c].
+// RH = 4 (16 right-hand sides): K is split in four; thread (ks, rg, cg) =
+// (tid / 64, tid % 16, tid / 16 % 4) forms the 4 x 4 partial product of rows
+// 4 rg.., right-hand sides 4 cg.. over kk in [16 ks, 16 ks + 16) from two
+// 16-byte loads and 16 independent FMAs a step; the partials meet in red
+// (red[(ks 16 + c) 64 + r]) and thread (r, g) subtracts their sum, slices in
+// order.  Other RH: thread (r, g) runs the sum itself, two partial sums (even
+// and odd kk).  The caller has synchronised the CTA since red was last read.
 template <int RH>
-__device__ __forceinline__ void block_product(float (&acc)[RH], const float (*A)[TB], const float (*X)[4 * RH], int r,
-                                              int g) {
-  float p[2][RH];
+__device__ __forceinline__ void block_product(float (&acc)[RH], const float (*A)[TB], const float (*X)[4 * RH],
+                                              float *red, int r, int g) {
+  if constexpr (RH == 4) {
+    const int tid = threadIdx.x, ks = tid >> 6, rg = tid & 15, cg = (tid >> 4) & 3;
+    float p[4][4];
 #pragma unroll
-  for (int c = 0; c < RH; ++c) p[0][c] = p[1][c] = 0.f;
-#pragma unroll 8
-  for (int kk = 0; kk < TB; ++kk) {
-    const float a = A[kk][r];
+    for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int c = 0; c < RH; c += 4) {
-      const float4 x = *reinterpret_cast<const float4 *>(&X[kk][g * RH + c]);
-      float *q = p[kk & 1];
-      q[c] = fmaf(a, x.x, q[c]);
-      q[c + 1] = fmaf(a, x.y, q[c + 1]);
-      q[c + 2] = fmaf(a, x.z, q[c + 2]);
-      q[c + 3] = fmaf(a, x.w, q[c + 3]);
+      for (int j = 0; j < 4; ++j) p[i][j] = 0.f;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const int kk = ks * 16 + q;
+      const float4 a = *reinterpret_cast<const float4 *>(&A[kk][4 * rg]);
+      const float4 x = *reinterpret_cast<const float4 *>(&X[kk][4 * cg]);
+      const float av[4] = {a.x, a.y, a.z, a.w}, xv[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) p[i][j] = fmaf(av[i], xv[j], p[i][j]);
     }
-  }
 #pragma unroll
-  for (int c = 0; c < RH; ++c) acc[c] -= p[0][c] + p[1][c];
+    for (int j = 0; j < 4; ++j)
+      *reinterpret_cast<float4 *>(&red[(ks * 16 + 4 * cg + j) * TB + 4 * rg]) =
+          make_float4(p[0][j], p[1][j], p[2][j], p[3][j]);
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int col = 4 * g + c;
+      acc[c] -= ((red[col * TB + r] + red[(16 + col) * TB + r]) + red[(32 + col) * TB + r]) + red[(48 + col) * TB + r];
+    }
+  } else {
+    float p[2][RH];
+#pragma unroll
+    for (int c = 0; c < RH; ++c) p[0][c] = p[1][c] = 0.f;
+#pragma unroll 8
+    for (int kk = 0; kk < TB; ++kk) {
+      const float a = A[kk][r];
+#pragma unroll
+      for (int c = 0; c < RH; c += 4) {
+        const float4 x = *reinterpret_cast<const float4 *>(&X[kk][g * RH + c]);
+        float *q = p[kk & 1];
+        q[c] = fmaf(a, x.x, q[c]);
+        q[c + 1] = fmaf(a, x.y, q[c + 1]);
+        q[c + 2] = fmaf(a, x.z, q[c + 2]);
+        q[c + 3] = fmaf(a, x.w, q[c + 3]);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < RH; ++c) acc[c] -= p[0][c] + p[1][c];
+  }
 }
 
-// A thread's share of one published block's words: loaded together, then
-// polled again together (all those not yet published) until every one
-// carries this launch's epoch: one L2 round trip per pass, not one per word.
+// A thread's share of one published block's words (row tid % 64, the RH
+// right-hand sides of group tid / 64): loaded together, then polled again
+// together (all those not yet published) until every one carries this
+// launch's epoch: one L2 round trip per pass, not one per word.  A warp's
+// loads of one right-hand side are 32 consecutive rows; its stores to X are
+// 16 bytes a thread.
 template <int RH>
 struct BlockWords {
-  static constexpr int PW = TB * 4 * RH / 256;  // words per thread
-  unsigned long long w[PW];
+  unsigned long long w[RH];
   __device__ __forceinline__ bool need(int u, int kbk, int nrhs) const {
-    const int e = threadIdx.x + 256 * u;
-    return e % TB < kbk && e / TB < nrhs;
+    return (int)(threadIdx.x % TB) < kbk && (int)(threadIdx.x / TB) * RH + u < nrhs;
+  }
+  __device__ __forceinline__ const unsigned long long *at(const unsigned long long *xw, int64_t n, int64_t k0,
+                                                          int u) const {
+    return xw + (k0 + threadIdx.x % TB) + (int64_t)((threadIdx.x / TB) * RH + u) * n;
   }
   __device__ __forceinline__ void load(const unsigned long long *xw, int64_t n, int nrhs, int64_t k0, int kbk) {
 #pragma unroll
-    for (int u = 0; u < PW; ++u) {
-      const int e = threadIdx.x + 256 * u, kk = e % TB, c = e / TB;
-      w[u] = need(u, kbk, nrhs) ? ld_word(xw + (k0 + kk) + (int64_t)c * n) : 0ull;
-    }
+    for (int u = 0; u < RH; ++u) w[u] = need(u, kbk, nrhs) ? ld_word(at(xw, n, k0, u)) : 0ull;
+  }
+  // requests again the words that did not yet carry epoch when they came back
+  __device__ __forceinline__ void refresh(const unsigned long long *xw, int64_t n, int nrhs, int64_t k0, int kbk,
+                                          uint32_t epoch) {
+#pragma unroll
+    for (int u = 0; u < RH; ++u)
+      if (need(u, kbk, nrhs) && (uint32_t)(w[u] >> 32) != epoch) w[u] = ld_word(at(xw, n, k0, u));
   }
   // spins until the words carry epoch, then writes them to X[kk][c]
   __device__ __forceinline__ void take(const unsigned long long *xw, int64_t n, int nrhs, int64_t k0, int kbk,
@@ -405,31 +450,36 @@ struct BlockWords {
     for (int polls = 0;; ++polls) {
       bool done = true;
 #pragma unroll
-      for (int u = 0; u < PW; ++u) done = done && (!need(u, kbk, nrhs) || (uint32_t)(w[u] >> 32) == epoch);
+      for (int u = 0; u < RH; ++u) done = done && (!need(u, kbk, nrhs) || (uint32_t)(w[u] >> 32) == epoch);
       if (done) break;
       if (polls >= (1 << 20)) {
         atomicExch(err, 3);
         break;
       }
 #pragma unroll
-      for (int u = 0; u < PW; ++u) {
-        const int e = threadIdx.x + 256 * u, kk = e % TB, c = e / TB;
-        if (need(u, kbk, nrhs) && (uint32_t)(w[u] >> 32) != epoch) w[u] = ld_word(xw + (k0 + kk) + (int64_t)c * n);
-      }
+      for (int u = 0; u < RH; ++u)
+        if (need(u, kbk, nrhs) && (uint32_t)(w[u] >> 32) != epoch) w[u] = ld_word(at(xw, n, k0, u));
     }
+    float *row = &X[threadIdx.x % TB][(threadIdx.x / TB) * RH];
 #pragma unroll
-    for (int u = 0; u < PW; ++u) {
-      const int e = threadIdx.x + 256 * u, kk = e % TB, c = e / TB;
-      X[kk][c] = need(u, kbk, nrhs) ? __uint_as_float((uint32_t)w[u]) : 0.f;
+    for (int u = 0; u < RH; u += 4) {
+      float4 v;
+      v.x = need(u, kbk, nrhs) ? __uint_as_float((uint32_t)w[u]) : 0.f;
+      v.y = need(u + 1, kbk, nrhs) ? __uint_as_float((uint32_t)w[u + 1]) : 0.f;
+      v.z = need(u + 2, kbk, nrhs) ? __uint_as_float((uint32_t)w[u + 2]) : 0.f;
+      v.w = need(u + 3, kbk, nrhs) ? __uint_as_float((uint32_t)w[u + 3]) : 0.f;
+      *reinterpret_cast<float4 *>(row + u) = v;
     }
   }
 };
 
 // dynamic shared memory of trsv_words: the operands Dinv, C_1..C_TNP; two
-// fold tiles; two fold blocks; the TNP pushed predecessors
+// fold tiles; two fold blocks; the TNP pushed predecessors; (RH = 4) the
+// products' reduction buffer
 template <int RH>
 constexpr size_t trsv_words_smem() {
-  return sizeof(float) * ((size_t)(TNP + 1) * TB * TB + 2 * TB * TB + (2 + TNP) * TB * 4 * RH);
+  return sizeof(float) * ((size_t)(TNP + 1) * TB * TB + 2 * TB * TB + (2 + TNP) * TB * 4 * RH +
+                          (RH == 4 ? 4 * 16 * TB : 0));
 }
 
 template <bool LOWER, int RH>
@@ -444,6 +494,7 @@ trsv_words(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, const 
   Tile *A = Op + TNP + 1;                            // fold tiles (alternating)
   Blk *X = reinterpret_cast<Blk *>(A + 2);           // fold blocks (alternating)
   Blk *Xp = X + 2;                                   // Xp[d-1]: the block d before, pushed by its CTA
+  float *red = reinterpret_cast<float *>(Xp + TNP);  // (RH = 4) partial products
   __shared__ __align__(8) uint64_t xbar[TNP];        // complete when those pushes have landed
   __shared__ __align__(8) uint64_t obar;             // complete when the operands have landed
   __shared__ int sb;
@@ -465,12 +516,13 @@ trsv_words(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, const 
   const int t = sb * TCL + rank;  // position in solve order
   const bool live = t < nb;
   const int b = LOWER ? t : nb - 1 - t;
+  const int kc = t < TNP ? t : TNP;  // predecessors coupled through C_d
   if (tid == 0 && live) {
     // the pushes from the CTAs before, inside the cluster; the operands
 #pragma unroll
     for (int d = 1; d <= TNP; ++d)
       if (rank >= d) sm100::mbar_arrive_expect_tx(&xbar[d - 1], XBYTES);
-    const int nops = 1 + (t < TNP ? t : TNP);
+    const int nops = 1 + kc;
     sm100::mbar_arrive_expect_tx(&obar, OBYTES * nops);
     bulk_load(Op[0], Dinv + (int64_t)b * TB * TB, OBYTES, &obar);
     for (int d = 1; d < nops; ++d) bulk_load(Op[d], C + ((int64_t)(d - 1) * nb + b) * TB * TB, OBYTES, &obar);
@@ -486,9 +538,9 @@ trsv_words(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, const 
       acc[c] = (cc < nrhs && r < kb) ? y[i0 + r + (int64_t)cc * n] : 0.f;
     }
     constexpr int PER = TB * TB / 256;
-    // the blocks solved before the last TNP predecessors; block sidx + 1's
-    // tile and words are requested before block sidx's product
-    const int nf = t - TNP;
+    // the blocks solved before the coupled predecessors; each block's tile
+    // and words are requested two folds before its own
+    const int nf = t - kc;
     auto tile_load = [&](float (&lv)[PER], int sidx) {
       const int64_t k0 = (int64_t)(LOWER ? sidx : nb - 1 - sidx) * TB;
       const int kbk = (int)imin(TB, n - k0);
@@ -499,61 +551,91 @@ trsv_words(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, const 
         lv[q] = (rr < kb && kk < kbk) ? W[(i0 + rr) + (k0 + kk) * ldw] : 0.f;
       }
     };
-    float lv[PER];
-    BlockWords<RH> wd;
-    if (nf > 0) {
-      tile_load(lv, 0);
-      const int64_t k0 = (int64_t)(LOWER ? 0 : nb - 1) * TB;
-      wd.load(xw, n, nrhs, k0, (int)imin(TB, n - k0));
-    }
-    for (int sidx = 0; sidx < nf; ++sidx) {
+    auto words_load = [&](BlockWords<RH> &w, int sidx) {
+      const int64_t k0 = (int64_t)(LOWER ? sidx : nb - 1 - sidx) * TB;
+      w.load(xw, n, nrhs, k0, (int)imin(TB, n - k0));
+    };
+    // one fold: block sidx's tile and words (in lvs, wds) into A, X[sidx & 1];
+    // block sidx + 2's requested into the same registers before the product
+    auto fold = [&](float(&lvs)[PER], BlockWords<RH> &wds, int sidx) {
       const int64_t k0 = (int64_t)(LOWER ? sidx : nb - 1 - sidx) * TB;
       const int kbk = (int)imin(TB, n - k0);
       const int h = sidx & 1;
-      wd.take(xw, n, nrhs, k0, kbk, epoch, X[h], err);
+      wds.take(xw, n, nrhs, k0, kbk, epoch, X[h], err);
 #pragma unroll
       for (int q = 0; q < PER; ++q) {
         const int e = tid + 256 * q;
-        A[h][e / TB][e % TB] = lv[q];
+        A[h][e / TB][e % TB] = lvs[q];
       }
-      if (sidx + 1 < nf) {
-        tile_load(lv, sidx + 1);
-        const int64_t k1 = (int64_t)(LOWER ? sidx + 1 : nb - 2 - sidx) * TB;
-        wd.load(xw, n, nrhs, k1, (int)imin(TB, n - k1));
+      if (sidx + 2 < nf) {
+        tile_load(lvs, sidx + 2);
+        words_load(wds, sidx + 2);
       }
       __syncthreads();  // (also: every thread is past the product that last read A[h], X[h])
-      block_product<RH>(acc, A[h], X[h], r, g);
+      block_product<RH>(acc, A[h], X[h], red, r, g);
+    };
+    float lv0[PER], lv1[PER];
+    BlockWords<RH> wd, wd1;
+    if (nf > 0) {
+      tile_load(lv0, 0);
+      words_load(wd, 0);
     }
+    if (nf > 1) {
+      tile_load(lv1, 1);
+      words_load(wd1, 1);
+    }
+    for (int sidx = 0; sidx < nf; sidx += 2) {
+      fold(lv0, wd, sidx);
+      if (sidx + 1 < nf) fold(lv1, wd1, sidx + 1);
+    }
+    // the coupled predecessors of an earlier cluster (d > rank: no push comes
+    // for them) are taken from their words into their unused push slots,
+    // Xp[d-1], furthest first; like the folds', their words are requested
+    // two ahead (the first two before the Dinv product)
+    const int nl = kc > rank ? kc - rank : 0;  // d = kc, kc - 1, ..., rank + 1
+    float cv[RH];                              // this block's solution
+    auto l2_load = [&](BlockWords<RH> &w, int i) {
+      const int64_t p0 = (int64_t)(LOWER ? b - (kc - i) : b + (kc - i)) * TB;
+      w.load(xw, n, nrhs, p0, (int)imin(TB, n - p0));
+    };
+    // (the next one's words, requested before this one's wait, are requested
+    // again where they came back stale: the nearest predecessors are published
+    // only about then)
+    auto l2_couple = [&](BlockWords<RH> &w, BlockWords<RH> &next, int i) {
+      const int d = kc - i;
+      const int64_t p0 = (int64_t)(LOWER ? b - d : b + d) * TB;
+      w.take(xw, n, nrhs, p0, (int)imin(TB, n - p0), epoch, Xp[d - 1], err);
+      if (i + 2 < nl) l2_load(w, i + 2);
+      if (i + 1 < nl) {
+        const int64_t p1 = (int64_t)(LOWER ? b - d + 1 : b + d - 1) * TB;
+        next.refresh(xw, n, nrhs, p1, (int)imin(TB, n - p1), epoch);
+      }
+      __syncthreads();
+      block_product<RH>(cv, Op[d], Xp[d - 1], red, r, g);
+    };
+    if (nl > 0) l2_load(wd, 0);
+    if (nl > 1) l2_load(wd1, 1);
     // c = Dinv acc: acc into X[0] as a 64 x (4 RH) operand
     __syncthreads();  // every thread is past the last fold's product
 #pragma unroll
     for (int c = 0; c < RH; ++c) X[0][r][g * RH + c] = acc[c];
     if (!__syncthreads_and(sm100::bounded_wait(&obar, 0u)) && tid == 0) atomicExch(err, 3);
-    float cv[RH];
 #pragma unroll
     for (int c = 0; c < RH; ++c) cv[c] = 0.f;
-    block_product<RH>(cv, Op[0], X[0], r, g);  // cv = -Dinv acc
+    block_product<RH>(cv, Op[0], X[0], red, r, g);  // cv = -Dinv acc
 #pragma unroll
     for (int c = 0; c < RH; ++c) cv[c] = -cv[c];
-    // the TNP predecessors, furthest first: x = c - sum_d C_d x_{t-d}, each
-    // from the push of its CTA (same cluster) or from its published words
-    // (an earlier cluster), into X[1] (the last fold read X[(nf-1)&1] and
-    // every thread is past that)
+    // x = c - sum_d C_d x_{t-d}: first the predecessors from words, then the
+    // pushed ones, furthest first
+    for (int i = 0; i < nl; i += 2) {
+      l2_couple(wd, wd1, i);
+      if (i + 1 < nl) l2_couple(wd1, wd, i + 1);
+    }
 #pragma unroll
     for (int d = TNP; d >= 1; --d) {
-      if (t < d) continue;
-      if (rank >= d) {
-        if (!__syncthreads_and(sm100::bounded_wait(&xbar[d - 1], 0u)) && tid == 0) atomicExch(err, 3);
-        block_product<RH>(cv, Op[d], Xp[d - 1], r, g);
-      } else {
-        const int64_t p0 = (int64_t)(LOWER ? b - d : b + d) * TB;
-        const int kbp = (int)imin(TB, n - p0);
-        __syncthreads();  // every thread is past the product that last read X[1]
-        wd.load(xw, n, nrhs, p0, kbp);
-        wd.take(xw, n, nrhs, p0, kbp, epoch, X[1], err);
-        __syncthreads();
-        block_product<RH>(cv, Op[d], X[1], r, g);
-      }
+      if (d > kc || d > rank) continue;
+      if (!__syncthreads_and(sm100::bounded_wait(&xbar[d - 1], 0u)) && tid == 0) atomicExch(err, 3);
+      block_product<RH>(cv, Op[d], Xp[d - 1], red, r, g);
     }
     // to the next TNP CTAs of the cluster (their Xp[d-1]): each thread stores
     // its row's values straight from registers (st.async, completing on the
