@@ -299,15 +299,18 @@ __device__ __forceinline__ void st_release(int32_t *p, int v) {
 // round trip.
 // Block blk at position t in solve order folds in the blocks solved before
 // its last TNP predecessors as they appear,
-//   acc -= T[blk, k] x_k              (tile and words of the next block in
-//                                      flight during this block's product)
+//   acc -= T[blk, k] x_k              (the tiles and words of the next two
+//                                      blocks in flight during a product)
 // and then, with c = Dinv acc formed before any predecessor is needed,
 //   x_blk = c - sum_{d=1..TNP} C_d x_{t-d},   C_d = Dinv T[blk, t-d]
-// (C_d precomputed per factorisation).  The chain between consecutive
-// blocks is then one 64 x 64 product and a push; a block's words on L2 are
-// needed TNP links after they are written.  Waits are bounded: on expiry
-// *err is set (the host fails the solve) and the CTA goes on, so that every
-// later wait still ends.
+// (C_d precomputed per factorisation, bulk-copied into shared memory with
+// Dinv at launch).  Predecessors pushed by the CTAs before it in the cluster
+// (d <= rank) enter from its shared memory; those of an earlier cluster from
+// their words, requested two ahead.  The chain between neighbours of a
+// cluster is then one 64 x 64 product and a push; only a cluster's first
+// block waits on an L2 round trip for the block before it.  Waits are
+// bounded: on expiry *err is set (the host fails the solve) and the CTA goes
+// on, so that every later wait still ends.
 constexpr int TCL = 8;  // blocks (CTAs) per cluster of the FP32 solve
 constexpr int TNP = 6;  // predecessors coupled through C_d
 
