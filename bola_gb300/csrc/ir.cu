@@ -484,6 +484,9 @@ constexpr size_t trsv_words_smem() {
   return sizeof(float) * ((size_t)(TNP + 1) * TB * TB + 2 * TB * TB + (2 + TNP) * TB * 4 * RH +
                           (RH == 4 ? 4 * 16 * TB : 0));
 }
+// one CTA per SM: dynamic plus static (barriers, ticket) within the 227 KB a CTA may hold
+static_assert(trsv_words_smem<4>() + 128 <= 227 * 1024, "trsv_words<RH = 4> shared memory");
+static_assert(trsv_words_smem<8>() + 128 <= 227 * 1024, "trsv_words<RH = 8> shared memory");
 
 template <bool LOWER, int RH>
 __global__ void __launch_bounds__(256)
