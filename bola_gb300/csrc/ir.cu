@@ -902,7 +902,8 @@ struct Workspace {
   bool split_kept = false;     // oz holds this call's A already (a solve handed on within one call)
   double *dscale = nullptr;    // its row scale D (W = D A D)
   void *dg = nullptr;          // scratch: the diagonal of L (8-byte elements)
-  float *Mc = nullptr;         // FP32 factors: Dinv times the coupling blocks (M lower, M upper, N lower, N upper)
+  float *Mc = nullptr;         // FP32 factors: the couplings C_1..C_TNP of every block, lower then upper
+  double *hpin = nullptr;      // pinned host staging of a sweep's norms and the wait-expiry flag
   TrsvSync ts;  // dataflow triangular solves
   MixedLU lu;
   OzMatrix oz;  // A's digit planes: the FP64-accurate products of the refinement
@@ -914,6 +915,8 @@ void ws_free(Workspace &w) {
                   (void *)w.V, (void *)w.Z, (void *)w.H, (void *)w.hn, (void *)w.ts.flags, (void *)w.ts.ticket,
                   (void *)w.dscale, w.dg, (void *)w.Mc, (void *)w.ts.xw})
     if (p) cudaFree(p);
+  if (w.hpin) cudaFreeHost(w.hpin);
+  w.hpin = nullptr;
   w.ts.flags = w.ts.ticket = w.ts.err = nullptr;
   w.lu.release(nullptr);
   w.oz.release();
@@ -952,6 +955,8 @@ int ws_reserve(Workspace &w, int64_t n, int64_t nrhs, int kind, cudaStream_t s) 
     BOLA_TRY(alloc(&w.r, sizeof(double) * n * nrhs));
     BOLA_TRY(alloc(&w.d, sizeof(double) * n * nrhs));
     BOLA_TRY(alloc(&w.norms, sizeof(double) * 6 * MAXRHS));
+    if (cudaMallocHost(reinterpret_cast<void **>(&w.hpin), sizeof(double) * (3 * MAXRHS + 2)) != cudaSuccess)
+      return fail(BOLA_ERR_CUDA, "mixed: out of pinned host memory");
     BOLA_TRY(alloc(&w.rowsum, sizeof(double) * n));
     BOLA_TRY(alloc(&w.dscale, sizeof(double) * n));
     BOLA_TRY(alloc(&w.dg, sizeof(double) * n));
@@ -1034,11 +1039,13 @@ int residual_berr(cudaStream_t s, Workspace &w, int64_t n, int nr, const double 
     col_absmax<<<nr, 256, 0, s>>>(n, x, ldx, nrm + nr);
   }
   BOLA_CHECK_LAUNCH();
-  std::vector<double> h(3 * nr + 1);
-  int32_t terr = 0;
-  BOLA_TRY_CUDA(cudaMemcpyAsync(h.data(), nrm, sizeof(double) * (3 * nr + 1), cudaMemcpyDeviceToHost, s));
-  BOLA_TRY_CUDA(cudaMemcpyAsync(&terr, w.ts.err, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  // through the workspace's pinned staging: both reads are truly asynchronous
+  const double *h = w.hpin;
+  int32_t *terr_h = reinterpret_cast<int32_t *>(w.hpin + 3 * MAXRHS + 1);
+  BOLA_TRY_CUDA(cudaMemcpyAsync(w.hpin, nrm, sizeof(double) * (3 * nr + 1), cudaMemcpyDeviceToHost, s));
+  BOLA_TRY_CUDA(cudaMemcpyAsync(terr_h, w.ts.err, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
   BOLA_TRY_CUDA(cudaStreamSynchronize(s));
+  const int32_t terr = *terr_h;
   if (terr != 0) {
     cudaMemsetAsync(w.ts.err, 0, sizeof(int32_t), s);
     return fail(BOLA_ERR_CUDA, "mixed: a bounded wait expired in the refinement (code %d)", terr);
