@@ -359,65 +359,92 @@ couple_blocks(int64_t n, const float *__restrict__ W, int64_t ldw, const float *
   }
 }
 
-// acc[c] (c < RH) -= sum_kk A[kk][r] X[kk][g RH + c].
+// Sums of products A X (A a 64 x 64 operand, A[kk][r] = A(r, kk); X a
+// 64 x (4 RH) block, X[kk][c]) formed in registers, then subtracted at once
+// from the outputs a thread owns (row r, right-hand sides g RH ..).
 // RH = 4 (16 right-hand sides): K is split in four; thread (ks, rg, cg) =
-// (tid / 64, tid % 16, tid / 16 % 4) forms the 4 x 4 partial product of rows
+// (tid / 64, tid % 16, tid / 16 % 4) accumulates the 4 x 4 tile of rows
 // 4 rg.., right-hand sides 4 cg.. over kk in [16 ks, 16 ks + 16) from two
-// 16-byte loads and 16 independent FMAs a step; the partials meet in red
-// (red[(ks 16 + c) 64 + r]) and thread (r, g) subtracts their sum, slices in
-// order.  Other RH: thread (r, g) runs the sum itself, two partial sums (even
-// and odd kk).  The caller has synchronised the CTA since red was last read.
+// 16-byte loads and 16 independent FMAs a step; subtract_from meets the
+// partials in red (red[(ks 16 + c) 64 + r], slices summed in order) behind
+// one barrier, so several products added in turn pay for one reduction.
+// Other RH: thread (r, g) runs the sums itself (two partial sums, even and
+// odd kk).
+template <int RH>
+struct ProductSums {
+  static constexpr int NP = RH == 4 ? 16 : RH;
+  float p[NP];
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int i = 0; i < NP; ++i) p[i] = 0.f;
+  }
+  __device__ __forceinline__ void add(const float (*A)[TB], const float (*X)[4 * RH], int r, int g) {
+    if constexpr (RH == 4) {
+      const int tid = threadIdx.x, ks = tid >> 6, rg = tid & 15, cg = (tid >> 4) & 3;
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        const int kk = ks * 16 + q;
+        const float4 a = *reinterpret_cast<const float4 *>(&A[kk][4 * rg]);
+        const float4 x = *reinterpret_cast<const float4 *>(&X[kk][4 * cg]);
+        const float av[4] = {a.x, a.y, a.z, a.w}, xv[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) p[4 * i + j] = fmaf(av[i], xv[j], p[4 * i + j]);
+      }
+    } else {
+      float q2[2][RH];
+#pragma unroll
+      for (int c = 0; c < RH; ++c) q2[0][c] = q2[1][c] = 0.f;
+#pragma unroll 8
+      for (int kk = 0; kk < TB; ++kk) {
+        const float a = A[kk][r];
+#pragma unroll
+        for (int c = 0; c < RH; c += 4) {
+          const float4 x = *reinterpret_cast<const float4 *>(&X[kk][g * RH + c]);
+          float *q = q2[kk & 1];
+          q[c] = fmaf(a, x.x, q[c]);
+          q[c + 1] = fmaf(a, x.y, q[c + 1]);
+          q[c + 2] = fmaf(a, x.z, q[c + 2]);
+          q[c + 3] = fmaf(a, x.w, q[c + 3]);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < RH; ++c) p[c] += q2[0][c] + q2[1][c];
+    }
+  }
+  // acc -= the sums added since zero(), which this also does again.  RH = 4:
+  // the caller has synchronised the CTA since red was last read.
+  __device__ __forceinline__ void subtract_from(float (&acc)[RH], float *red, int r, int g) {
+    if constexpr (RH == 4) {
+      const int tid = threadIdx.x, ks = tid >> 6, rg = tid & 15, cg = (tid >> 4) & 3;
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        *reinterpret_cast<float4 *>(&red[(ks * 16 + 4 * cg + j) * TB + 4 * rg]) =
+            make_float4(p[j], p[4 + j], p[8 + j], p[12 + j]);
+      __syncthreads();
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int col = 4 * g + c;
+        acc[c] -= ((red[col * TB + r] + red[(16 + col) * TB + r]) + red[(32 + col) * TB + r]) +
+                  red[(48 + col) * TB + r];
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < RH; ++c) acc[c] -= p[c];
+    }
+    zero();
+  }
+};
+
+// acc -= A X, one product (the caller has synchronised the CTA since red was last read)
 template <int RH>
 __device__ __forceinline__ void block_product(float (&acc)[RH], const float (*A)[TB], const float (*X)[4 * RH],
                                               float *red, int r, int g) {
-  if constexpr (RH == 4) {
-    const int tid = threadIdx.x, ks = tid >> 6, rg = tid & 15, cg = (tid >> 4) & 3;
-    float p[4][4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-      for (int j = 0; j < 4; ++j) p[i][j] = 0.f;
-#pragma unroll
-    for (int q = 0; q < 16; ++q) {
-      const int kk = ks * 16 + q;
-      const float4 a = *reinterpret_cast<const float4 *>(&A[kk][4 * rg]);
-      const float4 x = *reinterpret_cast<const float4 *>(&X[kk][4 * cg]);
-      const float av[4] = {a.x, a.y, a.z, a.w}, xv[4] = {x.x, x.y, x.z, x.w};
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) p[i][j] = fmaf(av[i], xv[j], p[i][j]);
-    }
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-      *reinterpret_cast<float4 *>(&red[(ks * 16 + 4 * cg + j) * TB + 4 * rg]) =
-          make_float4(p[0][j], p[1][j], p[2][j], p[3][j]);
-    __syncthreads();
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const int col = 4 * g + c;
-      acc[c] -= ((red[col * TB + r] + red[(16 + col) * TB + r]) + red[(32 + col) * TB + r]) + red[(48 + col) * TB + r];
-    }
-  } else {
-    float p[2][RH];
-#pragma unroll
-    for (int c = 0; c < RH; ++c) p[0][c] = p[1][c] = 0.f;
-#pragma unroll 8
-    for (int kk = 0; kk < TB; ++kk) {
-      const float a = A[kk][r];
-#pragma unroll
-      for (int c = 0; c < RH; c += 4) {
-        const float4 x = *reinterpret_cast<const float4 *>(&X[kk][g * RH + c]);
-        float *q = p[kk & 1];
-        q[c] = fmaf(a, x.x, q[c]);
-        q[c + 1] = fmaf(a, x.y, q[c + 1]);
-        q[c + 2] = fmaf(a, x.z, q[c + 2]);
-        q[c + 3] = fmaf(a, x.w, q[c + 3]);
-      }
-    }
-#pragma unroll
-    for (int c = 0; c < RH; ++c) acc[c] -= p[0][c] + p[1][c];
-  }
+  ProductSums<RH> s;
+  s.zero();
+  s.add(A, X, r, g);
+  s.subtract_from(acc, red, r, g);
 }
 
 // A thread's share of one published block's words (row tid % 64, the RH
@@ -600,6 +627,11 @@ trsv_words(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, const 
     // two ahead (the first two before the Dinv product)
     const int nl = kc > rank ? kc - rank : 0;  // d = kc, kc - 1, ..., rank + 1
     float cv[RH];                              // this block's solution
+    // sum_d C_d x_{t-d}, subtracted from cv after the last coupling (at most
+    // TNP products share one reduction; the folds, up to n/64 of them, each
+    // take their own, which keeps their FP32 sums short)
+    ProductSums<RH> csum;
+    csum.zero();
     auto l2_load = [&](BlockWords<RH> &w, int i) {
       const int64_t p0 = (int64_t)(LOWER ? b - (kc - i) : b + (kc - i)) * TB;
       w.load(xw, n, nrhs, p0, (int)imin(TB, n - p0));
@@ -617,7 +649,7 @@ trsv_words(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, const 
         next.refresh(xw, n, nrhs, p1, (int)imin(TB, n - p1), epoch);
       }
       __syncthreads();
-      block_product<RH>(cv, Op[d], Xp[d - 1], red, r, g);
+      csum.add(Op[d], Xp[d - 1], r, g);
     };
     if (nl > 0) l2_load(wd, 0);
     if (nl > 1) l2_load(wd1, 1);
@@ -641,8 +673,10 @@ trsv_words(int64_t n, int nrhs, const float *__restrict__ W, int64_t ldw, const 
     for (int d = TNP; d >= 1; --d) {
       if (d > kc || d > rank) continue;
       if (!__syncthreads_and(sm100::bounded_wait(&xbar[d - 1], 0u)) && tid == 0) atomicExch(err, 3);
-      block_product<RH>(cv, Op[d], Xp[d - 1], red, r, g);
+      csum.add(Op[d], Xp[d - 1], r, g);
     }
+    // (each coupling above passed a barrier after the Dinv product read red)
+    if (kc > 0) csum.subtract_from(cv, red, r, g);
     // to the next TNP CTAs of the cluster (their Xp[d-1]): each thread stores
     // its row's values straight from registers (st.async, completing on the
     // receiver's mbarrier); then the words, for the CTAs of later clusters
